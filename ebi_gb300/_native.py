@@ -1,0 +1,60 @@
+"""ctypes binding of libebi_gpu.so (include/ebi_gpu.h).
+
+The library is built in-tree by __graft_entry__.build() into ebi_gb300/_lib/.
+There is no fallback: importing the engine without the library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libebi_gpu.so"
+
+# Every symbol include/ebi_gpu.h declares.
+EXPORTS = [
+    "ebi_column_open", "ebi_column_close", "ebi_column_num_records", "ebi_column_num_chunks",
+    "ebi_column_scheme", "ebi_column_chunk_info", "ebi_column_set_precision", "ebi_materialize",
+    "ebi_filter", "ebi_filter_materialize", "ebi_sum", "ebi_min", "ebi_max", "ebi_filter_agg",
+    "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches",
+]
+
+
+class Predicate(C.Structure):
+    """ebi_predicate"""
+    _fields_ = [("kind", C.c_int32), ("start_kind", C.c_int32), ("end_kind", C.c_int32),
+                ("reserved", C.c_int32), ("value", C.c_double), ("start", C.c_double),
+                ("end", C.c_double)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() (no CPU fallback exists)")
+    L = C.CDLL(str(LIB_PATH))
+    vp, u64, i64, u64p, dp = C.c_void_p, C.c_uint64, C.c_int64, C.POINTER(C.c_uint64), C.POINTER(C.c_double)
+    PP = C.POINTER(Predicate)
+    L.ebi_column_open.argtypes = [C.c_char_p, u64, vp, C.POINTER(vp)]
+    L.ebi_column_close.argtypes = [vp]
+    for fn in (L.ebi_column_num_records, L.ebi_column_num_chunks):
+        fn.argtypes = [vp]
+        fn.restype = u64
+    L.ebi_column_scheme.argtypes = [vp]
+    L.ebi_column_chunk_info.argtypes = [vp, u64, u64p, u64p, u64p, u64p]
+    L.ebi_column_set_precision.argtypes = [vp, C.c_int32]
+    L.ebi_materialize.argtypes = [vp, vp, i64, vp, u64, u64p, vp]
+    L.ebi_filter.argtypes = [vp, PP, vp, i64, vp, vp]
+    L.ebi_filter_materialize.argtypes = [vp, PP, vp, i64, vp, u64, u64p, vp]
+    for fn in (L.ebi_sum, L.ebi_min, L.ebi_max):
+        fn.argtypes = [vp, vp, i64, dp, vp]
+    L.ebi_filter_agg.argtypes = [vp, PP, vp, i64, vp, dp, dp, dp, u64p, vp]
+    L.ebi_encode.argtypes = [dp, u64, C.c_int, C.c_int, u64, u64, C.POINTER(C.POINTER(C.c_uint8)), u64p]
+    L.ebi_free.argtypes = [vp]
+    L.ebi_last_error.restype = C.c_char_p
+    L.ebi_kernel_launches.restype = u64
+    _lib = L
+    return L

@@ -1,0 +1,287 @@
+"""Python mirror of ebi's public Decoder / Encoder API over the GB300 engine.
+
+Names, argument meaning and error behaviour follow the reference:
+  ebi/src/api/decoder.rs   Decoder::{new, materialize, filter, filter_materialize, sum, min, max,
+                           with_precision}, ChunkId
+  ebi/src/decoder/query.rs Predicate::{Eq, Ne, Range}, Range, RangeValue::{Inclusive, Exclusive, None}
+  ebi/src/decoder/error.rs DecoderError::{IO, ConversionError, UnexpectedEndOfChunk,
+                           PreconditionsNotMet, CudaError}
+Every call goes through the C ABI of include/ebi_gpu.h; device buffers are torch tensors.
+A bitmask is an int64 tensor of ceil(n_records / 64) words (bit r % 64 of word r // 64 = row r).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _native
+
+UNCOMPRESSED, RLE, BUFF, GORILLA, CHIMP, CHIMP128 = range(6)
+SCHEMES = {"uncompressed": UNCOMPRESSED, "rle": RLE, "buff": BUFF, "gorilla": GORILLA,
+           "chimp": CHIMP, "chimp128": CHIMP128}
+CHUNK_KINDS = {"full": 0, "record_count": 1, "byte_size": 2}
+
+
+# ---- errors (decoder/error.rs) -----------------------------------------------------------
+class DecoderError(RuntimeError):
+    code = -1
+
+    def __init__(self, msg: str, code: Optional[int] = None):
+        super().__init__(msg)
+        if code is not None:
+            self.code = code
+
+
+class IOError_(DecoderError): code = 1
+class ConversionError(DecoderError): code = 2
+class UnexpectedEndOfChunk(DecoderError): code = 3
+class PreconditionsNotMet(DecoderError): code = 4
+class CudaError(DecoderError): code = 5
+class CorruptChunk(DecoderError): code = 6
+class InvalidArgument(DecoderError): code = 7
+class OutOfMemory(DecoderError): code = 8
+class Unsupported(DecoderError): code = 9
+
+
+_ERRORS = {c.code: c for c in (IOError_, ConversionError, UnexpectedEndOfChunk, PreconditionsNotMet, CudaError,
+                               CorruptChunk, InvalidArgument, OutOfMemory, Unsupported)}
+
+
+def _check(code: int, what: str):
+    if code != 0:
+        msg = _native.lib().ebi_last_error().decode(errors="replace")
+        raise _ERRORS.get(code, DecoderError)(f"{what}: {msg}", code)
+
+
+# ---- predicates (decoder/query.rs:352-446) --------------------------------------------------
+@dataclass(frozen=True)
+class RangeValue:
+    kind: int  # 0 None, 1 Inclusive, 2 Exclusive
+    value: float = 0.0
+
+    @staticmethod
+    def inclusive(v: float) -> "RangeValue": return RangeValue(1, float(v))
+    @staticmethod
+    def exclusive(v: float) -> "RangeValue": return RangeValue(2, float(v))
+
+    def eval_start(self, x):
+        return x >= self.value if self.kind == 1 else x > self.value if self.kind == 2 else True
+
+    def eval_end(self, x):
+        return x <= self.value if self.kind == 1 else x < self.value if self.kind == 2 else True
+
+
+RangeValue.NONE = RangeValue(0, 0.0)
+
+
+@dataclass(frozen=True)
+class Range:
+    start: RangeValue
+    end: RangeValue
+
+    def eval(self, x) -> bool:  # RangeImpl::eval (query.rs:396-409)
+        return self.start.eval_start(x) and self.end.eval_end(x)
+
+
+@dataclass(frozen=True)
+class Predicate:
+    kind: int                 # 0 Eq, 1 Ne, 2 Range
+    value: float = 0.0
+    rng: Optional[Range] = None
+
+    @staticmethod
+    def eq(v: float) -> "Predicate": return Predicate(0, float(v))
+    @staticmethod
+    def ne(v: float) -> "Predicate": return Predicate(1, float(v))
+
+    @staticmethod
+    def range_(start: RangeValue, end: RangeValue) -> "Predicate":
+        return Predicate(2, 0.0, Range(start, end))
+
+    def eval(self, x) -> bool:  # PredicateImpl::eval (query.rs:431-437)
+        if self.kind == 0:
+            return x == self.value
+        if self.kind == 1:
+            return x != self.value
+        return self.rng.eval(x)
+
+    def to_c(self) -> _native.Predicate:
+        if self.kind == 2:
+            r = self.rng
+            return _native.Predicate(2, r.start.kind, r.end.kind, 0, 0.0, r.start.value, r.end.value)
+        return _native.Predicate(self.kind, 0, 0, 0, self.value, 0.0, 0.0)
+
+
+# Predicate.range(start, end) reads like the reference's Predicate::Range(Range::new(start, end)).
+Predicate.range = staticmethod(Predicate.range_)
+
+
+@dataclass(frozen=True)
+class ChunkId:
+    index: int
+
+
+def _cid(chunk_id) -> int:
+    if chunk_id is None:
+        return -1
+    return int(chunk_id.index if isinstance(chunk_id, ChunkId) else chunk_id)
+
+
+# ---- encoder (api/encoder.rs) ------------------------------------------------------------------
+def encode(values, scheme, chunk_option=("record_count", 8192), scale: int = 1) -> bytes:
+    """Encoder::new(input, output, chunk_option, config).encode(); returns the EBI1 bytes."""
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    kind, val = chunk_option if isinstance(chunk_option, tuple) else (chunk_option, 0)
+    out = C.POINTER(C.c_uint8)()
+    n = C.c_uint64()
+    L = _native.lib()
+    sch = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+    _check(L.ebi_encode(v.ctypes.data_as(C.POINTER(C.c_double)), len(v), sch, CHUNK_KINDS[kind], int(val),
+                        int(scale), C.byref(out), C.byref(n)), "Encoder::encode")
+    try:
+        return C.string_at(out, n.value)
+    finally:
+        L.ebi_free(out)
+
+
+# ---- decoder (api/decoder.rs) --------------------------------------------------------------------
+def _torch():
+    import torch
+    return torch
+
+
+class Decoder:
+    """Decoder::new over an in-memory EBI1 file; the file stays resident on the GPU."""
+
+    def __init__(self, data, device: str = "cuda:0", stream=None):
+        torch = _torch()
+        self.device = torch.device(device)
+        self._stream = stream
+        L = _native.lib()
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            if isinstance(data, torch.Tensor):  # host uint8 tensor (pinned for async copies)
+                assert data.dtype == torch.uint8 and not data.is_cuda
+                ptr, n = C.cast(data.data_ptr(), C.c_char_p), data.numel()
+                self._keep = data
+            else:
+                buf = bytes(data)
+                ptr, n = buf, len(buf)
+            _check(L.ebi_column_open(ptr, n, self._sp(), C.byref(h)), "Decoder::new")
+        self._h = h
+
+    def _sp(self):
+        torch = _torch()
+        s = self._stream if self._stream is not None else torch.cuda.current_stream(self.device)
+        return C.c_void_p(s.cuda_stream)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.lib().ebi_column_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- metadata --
+    @property
+    def n_records(self) -> int: return _native.lib().ebi_column_num_records(self._h)
+    @property
+    def n_chunks(self) -> int: return _native.lib().ebi_column_num_chunks(self._h)
+    @property
+    def scheme(self) -> int: return _native.lib().ebi_column_scheme(self._h)
+    @property
+    def mask_words(self) -> int: return max((self.n_records + 63) // 64, 1)
+
+    def chunk_info(self, i):
+        a, b, c, d = (C.c_uint64() for _ in range(4))
+        _check(_native.lib().ebi_column_chunk_info(self._h, i, C.byref(a), C.byref(b), C.byref(c), C.byref(d)),
+               "chunk_info")
+        return a.value, b.value, c.value, d.value
+
+    def with_precision(self, precision: int):
+        _check(_native.lib().ebi_column_set_precision(self._h, int(precision)), "Decoder::with_precision")
+
+    # -- buffers --
+    def _mask_in(self, bitmask):
+        if bitmask is None:
+            return None, None
+        torch = _torch()
+        if isinstance(bitmask, torch.Tensor):
+            t = bitmask.to(self.device, dtype=torch.int64).contiguous()
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(bitmask, dtype=np.uint64).view(np.int64)).to(self.device)
+        assert t.numel() >= self.mask_words, "bitmask shorter than ceil(n_records / 64) words"
+        return C.c_void_p(t.data_ptr()), t
+
+    def new_mask(self):
+        torch = _torch()
+        return torch.empty(self.mask_words, dtype=torch.int64, device=self.device)
+
+    # -- queries --
+    def materialize(self, bitmask=None, chunk_id=None, out=None):
+        torch = _torch()
+        mp, keep = self._mask_in(bitmask)
+        if out is None:
+            out = torch.empty(max(self.n_records, 1), dtype=torch.float64, device=self.device)
+        n = C.c_uint64()
+        _check(_native.lib().ebi_materialize(self._h, mp, _cid(chunk_id), C.c_void_p(out.data_ptr()), out.numel(),
+                                             C.byref(n), self._sp()), "Decoder::materialize")
+        return out[: n.value]
+
+    def filter(self, predicate: Predicate, bitmask=None, chunk_id=None, out=None):
+        mp, keep = self._mask_in(bitmask)
+        out = self.new_mask() if out is None else out
+        p = predicate.to_c()
+        _check(_native.lib().ebi_filter(self._h, C.byref(p), mp, _cid(chunk_id), C.c_void_p(out.data_ptr()),
+                                        self._sp()), "Decoder::filter")
+        return out
+
+    def filter_materialize(self, predicate: Predicate, bitmask=None, chunk_id=None, out=None):
+        torch = _torch()
+        mp, keep = self._mask_in(bitmask)
+        if out is None:
+            out = torch.empty(max(self.n_records, 1), dtype=torch.float64, device=self.device)
+        p = predicate.to_c()
+        n = C.c_uint64()
+        _check(_native.lib().ebi_filter_materialize(self._h, C.byref(p), mp, _cid(chunk_id), C.c_void_p(out.data_ptr()),
+                                                    out.numel(), C.byref(n), self._sp()), "Decoder::filter_materialize")
+        return out[: n.value]
+
+    def _agg(self, fn, bitmask, chunk_id, what):
+        mp, keep = self._mask_in(bitmask)
+        r = C.c_double()
+        _check(fn(self._h, mp, _cid(chunk_id), C.byref(r), self._sp()), what)
+        return r.value
+
+    def sum(self, bitmask=None, chunk_id=None) -> float:
+        return self._agg(_native.lib().ebi_sum, bitmask, chunk_id, "Decoder::sum")
+
+    def min(self, bitmask=None, chunk_id=None) -> float:
+        return self._agg(_native.lib().ebi_min, bitmask, chunk_id, "Decoder::min")
+
+    def max(self, bitmask=None, chunk_id=None) -> float:
+        return self._agg(_native.lib().ebi_max, bitmask, chunk_id, "Decoder::max")
+
+    def filter_agg(self, predicate: Predicate, bitmask=None, chunk_id=None, out=None, want_mask=True):
+        """Decoder::filter then Decoder::{sum, min, max} over its result, one pass."""
+        mp, keep = self._mask_in(bitmask)
+        if want_mask and out is None:
+            out = self.new_mask()
+        p = predicate.to_c()
+        s, a, b, n = C.c_double(), C.c_double(), C.c_double(), C.c_uint64()
+        _check(_native.lib().ebi_filter_agg(self._h, C.byref(p), mp, _cid(chunk_id),
+                                            C.c_void_p(out.data_ptr()) if want_mask else None,
+                                            C.byref(s), C.byref(a), C.byref(b), C.byref(n), self._sp()),
+               "Decoder::filter_agg")
+        return out, s.value, a.value, b.value, n.value
+
+
+def kernel_launches() -> int:
+    return _native.lib().ebi_kernel_launches()

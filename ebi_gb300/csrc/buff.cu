@@ -1,0 +1,447 @@
+// buff.cu -- BUFF (byte-sliced fixed point) chunks decoded and queried in place.
+//
+// Chunk layout (compressor/buff.rs:234-307): a 20-byte header (base as two
+// u32, row count, bit width `bits`, fractional bits `frac`), then bits/8 byte
+// planes, most significant first, each one byte per row and XOR 0x80
+// (`flip`), then a tail plane of bits%8 bits per row packed LSB-first.  A row
+// decodes to (base + delta) as f64 / 2^frac.
+//
+// Work split: one CTA of 256 threads per tile of 8192 rows; every thread owns
+// 32 consecutive rows, reads their 32 bytes of each plane with three aligned
+// 16-byte loads realigned in registers (the file sits in HBM unmodified, so
+// planes start at arbitrary byte addresses), and forms the 32 deltas.  The
+// range / equality predicates are compiled per chunk into the fixed-point
+// domain exactly as the reference's in-situ filters decide them
+// (buff/filter_cmp.rs:299-451, buff/filter_eq.rs:74-200), including their
+// shortcuts.  Sums are exact u64 sums of deltas (buff/sum.rs:60-119); min
+// and max are exact via the deltas (buff/min_max.rs).
+#include "internal.h"
+
+namespace ebi {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+__constant__ uint32_t c_precision_map[13] = {0, 5, 8, 11, 15, 18, 21, 25, 28, 31, 35, 38, 50};
+
+// into_fixed_representation_with_fractional_part_bits_length
+// (compression_common/buff.rs:11-51), with the reference's release-build
+// wrapping shift.
+__device__ int64_t buff_fixed(double value, int32_t frac) {
+    const uint64_t vb = static_cast<uint64_t>(__double_as_longlong(value));
+    const int32_t exp = static_cast<int32_t>((vb >> 52) & 0x7ff) - 1023;
+    if (exp < -frac) return 0;
+    const uint64_t sign = vb & 0x8000000000000000ull;
+    const int64_t s = 63 - static_cast<int64_t>(exp) - frac;
+    uint64_t fixed = s >= 64 ? 0 : (((vb << 11) | 0x8000000000000000ull) >> (static_cast<uint64_t>(s) & 63));
+    if (sign) fixed = ~(fixed - 1);
+    return static_cast<int64_t>(fixed);
+}
+
+__device__ __forceinline__ uint32_t bit_length(uint64_t x) { return x ? 64u - __clzll(static_cast<long long>(x)) : 0u; }
+
+enum : uint32_t { SIDE_ABSENT = 0, SIDE_ALL = 1, SIDE_NONE = 2, SIDE_CMP = 3 };
+
+// Per-chunk context, filled by thread 0 into shared memory.
+struct BuffCtx {
+    const uint8_t* planes;
+    const uint8_t* tail;
+    int64_t base;
+    uint64_t row_off;
+    double scale;       // 2^frac
+    double inv_scale;   // 2^-frac when exact (frac <= 1022), else 0
+    uint32_t n, bits, frac, np, tb;
+    uint32_t np_load, load_tail;  // planes / tail read when materializing
+    uint32_t ok;                  // selected and readable
+    uint32_t selected;
+    // predicate compiled into the delta domain
+    uint32_t lmode, rmode, lincl, rincl, emode;
+    uint64_t lthr, rthr, etgt;
+};
+
+__device__ void buff_setup(const QueryParams& q, uint32_t c, bool has_mask, BuffCtx& k) {
+    const ChunkDesc cd = q.chunks[c];
+    ChunkAcc* acc = q.acc + c;
+    k.ok = 0;
+    k.n = cd.n_rows;
+    k.row_off = cd.row_off;
+    k.selected = has_mask ? acc->selected : static_cast<uint32_t>(q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
+    if (!k.selected) return;
+    if (!has_mask && acc->selected == 0) acc->selected = 1;  // finalize folds selected chunks
+    if (cd.flags & kChunkBadGeometry) { set_status(acc, EBI_E_IO); return; }
+    if (cd.byte_len < 20) { set_status(acc, EBI_E_UNEXPECTED_END); return; }
+    const uint8_t* p = q.file + cd.byte_off;
+    k.base = static_cast<int64_t>(load_u64_unaligned(p));
+    const uint32_t n = load_u32_unaligned(p + 8);
+    k.bits = load_u32_unaligned(p + 12);
+    k.frac = load_u32_unaligned(p + 16);
+    if (k.bits > 64 || n != cd.n_rows) { set_status(acc, EBI_E_CORRUPT); return; }
+    k.np = k.bits / 8;
+    k.tb = k.bits % 8;
+    const uint64_t need = 20 + uint64_t(k.np) * n + (uint64_t(n) * k.tb + 7) / 8;
+    if (k.bits > 0 && need > cd.byte_len) { set_status(acc, EBI_E_UNEXPECTED_END); return; }
+    k.planes = p + 20;
+    k.tail = k.planes + uint64_t(k.np) * n;
+    k.scale = k.frac <= 1023 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 + k.frac) << 52))
+                             : __longlong_as_double(0x7ff0000000000000ll);
+    k.inv_scale = k.frac <= 1022 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 - k.frac) << 52)) : 0.0;
+
+    // controlled precision (buff/controlled_precision.rs:5-75)
+    k.np_load = k.np;
+    k.load_tail = k.tb > 0;
+    if (q.precision >= 0 && k.bits >= 8) {
+        const uint32_t cf = c_precision_map[q.precision];
+        const uint32_t unnecessary = k.frac > cf ? k.frac - cf : 0;
+        uint32_t rem = k.bits - 8;
+        uint32_t loaded = 1;
+        while (rem >= 8 && rem > unnecessary) { rem -= 8; ++loaded; }
+        k.np_load = loaded;
+        k.load_tail = rem > 0 && rem > unnecessary;
+    }
+
+    const ebi_predicate& pr = q.pred;
+    k.lmode = k.rmode = SIDE_ABSENT;
+    k.emode = SIDE_NONE;
+    if (pr.kind == EBI_PRED_RANGE) {
+        // left side: buff_simd256_cmp_filter::<true, INCL> (filter_cmp.rs:299-451)
+        if (pr.start_kind != EBI_BOUND_NONE) {
+            const bool incl = pr.start_kind == EBI_BOUND_INCLUSIVE;
+            const int64_t fp = buff_fixed(pr.start, static_cast<int32_t>(k.frac));
+            if (fp < k.base) k.lmode = SIDE_ALL;
+            else if (k.bits == 0) k.lmode = (incl ? k.base >= fp : k.base > fp) ? SIDE_ALL : SIDE_NONE;
+            else {
+                const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(k.base);
+                if (k.bits < bit_length(dp)) k.lmode = SIDE_NONE;
+                else { k.lmode = SIDE_CMP; k.lthr = dp; k.lincl = incl; }
+            }
+        }
+        // right side: buff_simd256_cmp_filter::<false, INCL>
+        if (pr.end_kind != EBI_BOUND_NONE) {
+            const bool incl = pr.end_kind == EBI_BOUND_INCLUSIVE;
+            const int64_t fp = buff_fixed(pr.end, static_cast<int32_t>(k.frac));
+            if (fp < k.base) k.rmode = SIDE_NONE;
+            else if (k.bits == 0) k.rmode = (incl ? k.base <= fp : k.base < fp) ? SIDE_ALL : SIDE_NONE;
+            else {
+                const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(k.base);
+                if (k.bits < bit_length(dp)) k.rmode = SIDE_ALL;
+                else { k.rmode = SIDE_CMP; k.rthr = dp; k.rincl = incl; }
+            }
+        }
+    } else {
+        // buff_simd256_equal_filter (filter_eq.rs:74-200)
+        const int64_t fp = buff_fixed(pr.value, static_cast<int32_t>(k.frac));
+        if (fp < k.base) k.emode = SIDE_NONE;
+        else if (k.bits == 0) k.emode = fp == k.base ? SIDE_ALL : SIDE_NONE;
+        else {
+            const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(k.base);
+            // Byte planes compare (u8)(dp >> shift) and the tail compares dp's low
+            // bits: together delta == dp mod 2^bits.  With neither byte planes
+            // nor an input bitmask the tail is compared with `dp as u8` (:190-196).
+            const uint64_t wmask = k.bits >= 64 ? ~0ull : ((1ull << k.bits) - 1);
+            k.emode = SIDE_CMP;
+            k.etgt = (k.np > 0 || has_mask) ? (dp & wmask) : (dp & 0xffull);
+        }
+    }
+    k.ok = 1;
+}
+
+// The 32 deltas of chunk rows [r0, r0 + 32); r0 is a multiple of 32.
+template <int TB, typename D>
+__device__ __forceinline__ void load_deltas(const BuffCtx& k, uint32_t r0, uint32_t np_load, uint32_t np_shift,
+                                            bool tail, D (&d)[32]) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) d[i] = 0;
+    for (uint32_t p = 0; p < np_load; ++p) {
+        uint32_t w[8];
+        load32(k.planes + uint64_t(p) * k.n + r0, w);
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            d[i] = (d[i] << 8) | static_cast<D>(((w[i >> 2] >> (8 * (i & 3))) & 0xffu) ^ 0x80u);
+    }
+    for (uint32_t p = np_load; p < np_shift; ++p) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) d[i] = static_cast<D>(d[i] << 8);
+    }
+    if constexpr (TB > 0) {
+        uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (tail) load32(k.tail + uint64_t(r0 / 8) * TB, w);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            constexpr uint32_t m = (1u << TB) - 1u;
+            const int pos = i * TB, wi = pos >> 5, sh = pos & 31;
+            uint32_t f;
+            if (sh + TB <= 32) f = w[wi] >> sh;
+            else f = __funnelshift_r(w[wi], w[wi + 1], sh);
+            d[i] = static_cast<D>((d[i] << TB) | static_cast<D>(f & m));
+        }
+    }
+}
+
+template <typename D>
+__device__ __forceinline__ uint32_t cmp_word(const D (&d)[32], uint64_t thr, bool greater, bool incl) {
+    uint32_t w = 0;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        const uint64_t x = d[i];
+        const bool s = greater ? (x > thr || (incl && x == thr)) : (x < thr || (incl && x == thr));
+        w |= static_cast<uint32_t>(s) << i;
+    }
+    return w;
+}
+
+template <typename D>
+__device__ __forceinline__ uint32_t eq_word(const D (&d)[32], uint64_t t) {
+    uint32_t w = 0;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) w |= static_cast<uint32_t>(static_cast<uint64_t>(d[i]) == t) << i;
+    return w;
+}
+
+struct BlockRed {
+    unsigned long long sum[kWarps], cnt[kWarps], mx[kWarps], mn[kWarps];
+};
+
+template <int TB, typename D>
+__device__ void buff_query_tile(const QueryParams& q, const BuffCtx& k, uint32_t c, uint32_t li, uint32_t tile_begin,
+                                BlockRed& red) {
+    const uint32_t r0 = tile_begin + threadIdx.x * 32;
+    const bool has_mask = q.in_mask != nullptr;
+    const bool want_agg = q.op == OP_FILTER_AGG || q.op == OP_AGG;
+    const bool in_chunk = r0 < k.n;
+    uint32_t sel = 0;
+    unsigned long long s = 0, mx = 0, mn = ~0ull;
+    if (in_chunk && k.ok) {
+        const uint32_t left = k.n - r0;
+        const uint32_t valid = left >= 32 ? ~0u : ((1u << left) - 1u);
+        const uint32_t m = has_mask ? (mask_word(q.in_mask, k.row_off + r0, q.n_records) & valid) : valid;
+        const bool need_deltas = k.lmode == SIDE_CMP || k.rmode == SIDE_CMP || k.emode == SIDE_CMP;
+        D d[32];
+        if (need_deltas || want_agg) load_deltas<TB, D>(k, r0, k.np, k.np, true, d);
+        if (q.op == OP_AGG) {
+            sel = m;
+        } else if (q.pred.kind == EBI_PRED_RANGE) {
+            const bool la = k.lmode == SIDE_ABSENT, ra = k.rmode == SIDE_ABSENT;
+            uint32_t L = 0, R = 0;
+            if (k.lmode == SIDE_ALL) L = valid;
+            else if (k.lmode == SIDE_CMP) L = cmp_word<D>(d, k.lthr, true, k.lincl) & m;
+            if (k.rmode == SIDE_ALL) R = valid;
+            else if (k.rmode == SIDE_CMP) R = cmp_word<D>(d, k.rthr, false, k.rincl) & m;
+            sel = (la && ra) ? m : la ? R : ra ? L : (L & R);
+        } else {
+            uint32_t e = 0;
+            if (k.emode == SIDE_ALL) e = valid;
+            else if (k.emode == SIDE_CMP) e = eq_word<D>(d, k.etgt) & m;
+            sel = q.pred.kind == EBI_PRED_EQ ? e : (m & ~e);
+        }
+        if (want_agg) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                if ((sel >> i) & 1u) {
+                    const unsigned long long x = static_cast<unsigned long long>(d[i]);
+                    s += x;
+                    mx = x > mx ? x : mx;
+                    mn = x < mn ? x : mn;
+                }
+            }
+        }
+    }
+    if ((q.op == OP_FILTER || q.op == OP_FILTER_AGG) && in_chunk && q.out_mask) {
+        if (!q.out_atomic || sel) store_mask_word(q.out_mask, k.row_off + r0, sel, q.out_atomic);
+    }
+    // block reduction of count (and sum / max / min)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned long long cnt = warp_sum<unsigned long long>(static_cast<unsigned long long>(__popc(sel)));
+    unsigned long long ws = 0, wmx = 0, wmn = ~0ull;
+    if (want_agg) { ws = warp_sum(s); wmx = warp_max_u64(mx); wmn = warp_min_u64(mn); }
+    if (lane == 0) { red.cnt[wid] = cnt; red.sum[wid] = ws; red.mx[wid] = wmx; red.mn[wid] = wmn; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long tc = 0, ts = 0, tmx = 0, tmn = ~0ull;
+        for (int w = 0; w < kWarps; ++w) {
+            tc += red.cnt[w]; ts += red.sum[w];
+            tmx = red.mx[w] > tmx ? red.mx[w] : tmx;
+            tmn = red.mn[w] < tmn ? red.mn[w] : tmn;
+        }
+        if (q.tile_counts) q.tile_counts[li] = tc;
+        if (want_agg && k.ok && tc) {
+            ChunkAcc* a = q.acc + c;
+            atomicAdd(&a->isum, ts);
+            atomicAdd(&a->count, tc);
+            atomicMax(&a->dmax, tmx);
+            atomicMin(&a->dmin, tmn);
+        }
+    }
+}
+
+template <typename D>
+__device__ void buff_query_dispatch(const QueryParams& q, const BuffCtx& k, uint32_t c, uint32_t li,
+                                    uint32_t begin, BlockRed& red) {
+    switch (k.ok ? k.tb : 0) {
+        case 0: buff_query_tile<0, D>(q, k, c, li, begin, red); break;
+        case 1: buff_query_tile<1, D>(q, k, c, li, begin, red); break;
+        case 2: buff_query_tile<2, D>(q, k, c, li, begin, red); break;
+        case 3: buff_query_tile<3, D>(q, k, c, li, begin, red); break;
+        case 4: buff_query_tile<4, D>(q, k, c, li, begin, red); break;
+        case 5: buff_query_tile<5, D>(q, k, c, li, begin, red); break;
+        case 6: buff_query_tile<6, D>(q, k, c, li, begin, red); break;
+        default: buff_query_tile<7, D>(q, k, c, li, begin, red); break;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) buff_query_kernel(QueryParams q, uint32_t tile_base) {
+    __shared__ BuffCtx k;
+    __shared__ BlockRed red;
+    const Tile t = q.tiles[tile_base + blockIdx.x];
+    if (threadIdx.x == 0) buff_setup(q, t.chunk, q.in_mask != nullptr, k);
+    __syncthreads();
+    if (k.ok && k.bits > 32) buff_query_dispatch<unsigned long long>(q, k, t.chunk, blockIdx.x, t.begin, red);
+    else buff_query_dispatch<uint32_t>(q, k, t.chunk, blockIdx.x, t.begin, red);
+}
+
+// Materialize pass 1: rows of the bitmask per tile.  A chunk is read (and its
+// header errors reported) only when the bitmask selects some of its rows.
+__global__ void __launch_bounds__(kThreads) buff_count_kernel(QueryParams q, uint32_t tile_base) {
+    __shared__ unsigned long long wsum[kWarps];
+    __shared__ BuffCtx k;
+    const Tile t = q.tiles[tile_base + blockIdx.x];
+    const ChunkDesc cd = q.chunks[t.chunk];
+    const uint32_t r0 = t.begin + threadIdx.x * 32;
+    uint32_t cnt = 0;
+    if (r0 < cd.n_rows) {
+        const uint32_t left = cd.n_rows - r0;
+        const uint32_t valid = left >= 32 ? ~0u : ((1u << left) - 1u);
+        cnt = __popc(mask_word(q.in_mask, cd.row_off + r0, q.n_records) & valid);
+    }
+    const unsigned long long w = warp_sum<unsigned long long>(cnt);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = w;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long tot = 0;
+        for (int i = 0; i < kWarps; ++i) tot += wsum[i];
+        q.tile_counts[blockIdx.x] = tot;
+        if (tot) buff_setup(q, t.chunk, false, k);
+    }
+}
+
+// Materialization: the decoded values of the selected rows, in row order.
+template <int TB, typename D>
+__device__ void buff_mat_tile(const QueryParams& q, const BuffCtx& k, uint32_t tile, uint32_t begin,
+                              const unsigned long long* tile_offsets, unsigned long long base_row,
+                              unsigned int* warp_tot) {
+    const uint32_t r0 = begin + threadIdx.x * 32;
+    const bool has_mask = q.in_mask != nullptr;
+    uint32_t sel = 0;
+    D d[32];
+    if (r0 < k.n && k.ok) {
+        const uint32_t left = k.n - r0;
+        const uint32_t valid = left >= 32 ? ~0u : ((1u << left) - 1u);
+        sel = has_mask ? (mask_word(q.in_mask, k.row_off + r0, q.n_records) & valid) : valid;
+        if (sel) load_deltas<TB, D>(k, r0, k.np_load, k.np, k.load_tail, d);
+    }
+    // block-exclusive prefix of the per-thread counts
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned int cnt = __popc(sel);
+    unsigned int inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_tot[wid] = inc;
+    __syncthreads();
+    unsigned int before = 0;
+    for (int w = 0; w < wid; ++w) before += warp_tot[w];
+    unsigned long long pos;
+    if (has_mask) pos = tile_offsets[blockIdx.x] + before + (inc - cnt);
+    else pos = k.row_off + r0 - base_row;
+    if (!sel) return;
+    for (int i = 0; i < 32; ++i) {
+        if (!((sel >> i) & 1u)) continue;
+        const long long fixed = static_cast<long long>(static_cast<unsigned long long>(k.base) + static_cast<unsigned long long>(d[i]));
+        const double v = k.inv_scale != 0.0 ? static_cast<double>(fixed) * k.inv_scale : static_cast<double>(fixed) / k.scale;
+        if (pos < q.out_cap) q.out_vals[pos] = v;
+        ++pos;
+    }
+}
+
+template <typename D>
+__device__ void buff_mat_dispatch(const QueryParams& q, const BuffCtx& k, uint32_t tile, uint32_t begin,
+                                  const unsigned long long* offs, unsigned long long base_row, unsigned int* wt) {
+    switch (k.ok ? k.tb : 0) {
+        case 0: buff_mat_tile<0, D>(q, k, tile, begin, offs, base_row, wt); break;
+        case 1: buff_mat_tile<1, D>(q, k, tile, begin, offs, base_row, wt); break;
+        case 2: buff_mat_tile<2, D>(q, k, tile, begin, offs, base_row, wt); break;
+        case 3: buff_mat_tile<3, D>(q, k, tile, begin, offs, base_row, wt); break;
+        case 4: buff_mat_tile<4, D>(q, k, tile, begin, offs, base_row, wt); break;
+        case 5: buff_mat_tile<5, D>(q, k, tile, begin, offs, base_row, wt); break;
+        case 6: buff_mat_tile<6, D>(q, k, tile, begin, offs, base_row, wt); break;
+        default: buff_mat_tile<7, D>(q, k, tile, begin, offs, base_row, wt); break;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) buff_materialize_kernel(QueryParams q, uint32_t tile_base,
+                                                                    const unsigned long long* tile_offsets,
+                                                                    unsigned long long base_row) {
+    __shared__ BuffCtx k;
+    __shared__ unsigned int warp_tot[kWarps];
+    const uint32_t tile = tile_base + blockIdx.x;
+    const Tile t = q.tiles[tile];
+    if (threadIdx.x == 0) {
+        // with a bitmask, tiles without selected rows were counted as 0 and
+        // their chunk may be unselected: only tiles that select rows read
+        buff_setup(q, t.chunk, false, k);
+        if (q.in_mask && tile_offsets[blockIdx.x + 1] == tile_offsets[blockIdx.x]) k.ok = 0;
+    }
+    __syncthreads();
+    if (k.ok && k.bits > 32) buff_mat_dispatch<unsigned long long>(q, k, tile, t.begin, tile_offsets, base_row, warp_tot);
+    else buff_mat_dispatch<uint32_t>(q, k, tile, t.begin, tile_offsets, base_row, warp_tot);
+}
+
+}  // namespace
+
+TileMap buff_tiles(const std::vector<ChunkDesc>& chunks) {
+    TileMap m;
+    m.first_tile.reserve(chunks.size() + 1);
+    for (uint32_t c = 0; c < chunks.size(); ++c) {
+        m.first_tile.push_back(static_cast<uint32_t>(m.tiles.size()));
+        const uint32_t n = chunks[c].n_rows;
+        uint32_t b = 0;
+        do { m.tiles.push_back(Tile{c, b}); b += kBuffTileRows; } while (b < n);
+    }
+    m.first_tile.push_back(static_cast<uint32_t>(m.tiles.size()));
+    return m;
+}
+
+cudaError_t launch_buff_query(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s) {
+    if (n_tiles == 0) return cudaSuccess;
+    buff_query_kernel<<<n_tiles, kThreads, 0, s>>>(q, tile_begin);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s) {
+    if (n_tiles == 0) return cudaSuccess;
+    buff_count_kernel<<<n_tiles, kThreads, 0, s>>>(q, tile_begin);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles,
+                                    const unsigned long long* tile_offsets, cudaStream_t s) {
+    if (n_tiles == 0) return cudaSuccess;
+    unsigned long long base_row = 0;
+    if (q.chunk_id >= 0) {
+        ChunkDesc cd;
+        cudaError_t e = cudaMemcpyAsync(&cd, q.chunks + q.chunk_id, sizeof cd, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        base_row = cd.row_off;
+    }
+    buff_materialize_kernel<<<n_tiles, kThreads, 0, s>>>(q, tile_begin, tile_offsets, base_row);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace ebi

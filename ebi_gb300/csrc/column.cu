@@ -1,0 +1,431 @@
+// column.cu -- host side of the engine: the EBI1 reader, the resident column
+// and the Decoder-shaped query entry points of include/ebi_gpu.h.
+//
+// Decoder::new (api/decoder.rs:136-156) becomes ebi_column_open: the header
+// and footer are parsed on the host exactly as FileReader::fetch_header /
+// fetch_footer do (decoder.rs:131-220, format/deserialize.rs:117-300), the
+// chunk table (GeneralChunkHandle geometry, decoder.rs:283-352) is built once,
+// and the unmodified file bytes are copied to HBM where they stay.  Every
+// query then runs the codec's kernel over the chunk table and one
+// finalize_kernel that folds the per-chunk results in chunk order.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace ebi {
+
+static std::atomic<uint64_t> g_launches{0};
+static thread_local std::string g_last_error;
+
+void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+static int fail(int code, const std::string& msg) {
+    set_last_error(msg);
+    return code;
+}
+static int cuda_fail(cudaError_t e, const char* what) {
+    return fail(EBI_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(expr)                                              \
+    do {                                                      \
+        cudaError_t _e = (expr);                              \
+        if (_e != cudaSuccess) return cuda_fail(_e, #expr);   \
+    } while (0)
+
+static uint32_t rd32(const uint8_t* p) {
+    return uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24);
+}
+static uint64_t rd64(const uint8_t* p) { return uint64_t(rd32(p)) | (uint64_t(rd32(p + 4)) << 32); }
+
+// The device's default stream-ordered pool keeps freed memory for reuse, so
+// reopening columns of similar size does not go back to the driver.
+static void tune_pool_once() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaMemPool_t pool;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+    });
+}
+
+}  // namespace ebi
+
+using namespace ebi;
+
+struct ebi_column {
+    cudaStream_t stream = nullptr;  // stream of open/close (allocation order)
+    int scheme = 0;
+    uint64_t n_records = 0, n_chunks = 0, file_len = 0, footer_off = 0;
+    std::vector<ChunkDesc> chunks;
+    TileMap tiles;
+    bool rows_aligned32 = true;
+    int32_t precision = -1;
+    uint8_t* d_file = nullptr;
+    ChunkDesc* d_chunks = nullptr;
+    Tile* d_tiles = nullptr;
+    ChunkAcc* d_acc = nullptr;
+    QueryResult* d_res = nullptr;
+    QueryResult* h_res = nullptr;
+    unsigned long long* d_tile_counts = nullptr;   // n_tiles
+    unsigned long long* d_tile_offsets = nullptr;  // n_tiles + 1
+    uint64_t* d_scratch_mask = nullptr;            // mask_words
+    uint64_t mask_words = 0;
+};
+
+namespace {
+
+// FileReader::fetch_header + fetch_footer (decoder.rs:131-220).
+int parse_file(const uint8_t* d, uint64_t len, ebi_column* c) {
+    if (len < 30) return fail(EBI_E_IO, "file shorter than the 30-byte FileHeader");
+    if (d[4] != 0) return fail(EBI_E_CONVERSION, "Failed to convert FieldType");
+    if (d[5] > 12) return fail(EBI_E_CONVERSION, "Failed to convert CompressionScheme");
+    if (d[6] > 2) return fail(EBI_E_CONVERSION, "Failed to convert ChunkOptionKind");
+    const int scheme = d[5];
+    const uint64_t fo = rd64(d + 14);
+    if (fo > len || len - fo < 16) return fail(EBI_E_IO, "footer offset past the end of the file");
+    const uint64_t nrec = rd64(d + fo), nch = rd64(d + fo + 8);
+    const uint64_t p = fo + 16;
+    if (nch > (len - p) / 16) return fail(EBI_E_IO, "chunk footers past the end of the file");
+    const uint64_t cf = p + nch * 16;
+    if (cf + 1 > len) return fail(EBI_E_IO, "compressor config past the end of the file");
+    const uint64_t csz = d[cf];
+    if (cf + 1 + csz > len) return fail(EBI_E_IO, "compressor config past the end of the file");
+    if (csz < 8) return fail(EBI_E_CORRUPT, "compressor config shorter than 8 bytes");
+    if (cf + 1 + csz + 164 > len) return fail(EBI_E_IO, "FileFooter3 past the end of the file");
+    if (scheme > EBI_CHIMP128) return fail(EBI_E_UNSUPPORTED, "compression scheme outside this engine");
+    if (nrec > 0xffffffffull) return fail(EBI_E_UNSUPPORTED, "more than 2^32 - 1 records (row ids are u32)");
+    c->scheme = scheme;
+    c->n_records = nrec;
+    c->n_chunks = nch;
+    c->footer_off = fo;
+    c->file_len = len;
+    c->chunks.resize(nch);
+    for (uint64_t i = 0; i < nch; ++i) {
+        const uint64_t phys = rd64(d + p + 16 * i), logi = rd64(d + p + 16 * i + 8);
+        const uint64_t nphys = i + 1 < nch ? rd64(d + p + 16 * (i + 1)) : fo;
+        const uint64_t nlogi = i + 1 < nch ? rd64(d + p + 16 * (i + 1) + 8) : nrec;
+        ChunkDesc cd{};
+        cd.byte_off = phys;
+        cd.byte_len = nphys - phys;
+        cd.row_off = logi;
+        cd.n_rows = static_cast<uint32_t>(nlogi - logi);
+        if (nphys < phys || phys > len || nphys > len) { cd.flags |= kChunkBadGeometry; cd.byte_len = 0; }
+        if (nlogi < logi || nlogi - logi > 0xffffffffull || nlogi > nrec) { cd.flags |= kChunkBadGeometry; cd.n_rows = 0; }
+        if (logi % 32) c->rows_aligned32 = false;
+        c->chunks[i] = cd;
+    }
+    return EBI_OK;
+}
+
+template <typename T>
+int dev_alloc(T** p, size_t count, cudaStream_t s) {
+    void* v = nullptr;
+    const cudaError_t e = cudaMallocAsync(&v, count ? count * sizeof(T) : 16, s);
+    if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? fail(EBI_E_OOM, "device allocation failed")
+                                                               : cuda_fail(e, "cudaMallocAsync");
+    *p = static_cast<T*>(v);
+    return EBI_OK;
+}
+
+QueryParams base_params(const ebi_column* c) {
+    QueryParams q{};
+    q.file = c->d_file;
+    q.chunks = c->d_chunks;
+    q.acc = c->d_acc;
+    q.tiles = c->d_tiles;
+    q.n_tiles = static_cast<uint32_t>(c->tiles.tiles.size());
+    q.n_chunks = static_cast<uint32_t>(c->n_chunks);
+    q.n_records = c->n_records;
+    q.chunk_id = -1;
+    q.precision = c->precision;
+    q.scheme = c->scheme;
+    return q;
+}
+
+int check_supported(const ebi_column* c) {
+    if (c->scheme != EBI_BUFF) return fail(EBI_E_UNSUPPORTED, "codec kernels not built for this scheme yet");
+    return EBI_OK;
+}
+
+// Tile range of the query: all tiles, or those of chunk_id (none when out of range).
+void tile_range(const ebi_column* c, int64_t chunk_id, uint32_t* begin, uint32_t* count) {
+    if (chunk_id < 0) { *begin = 0; *count = static_cast<uint32_t>(c->tiles.tiles.size()); return; }
+    if (static_cast<uint64_t>(chunk_id) >= c->n_chunks) { *begin = 0; *count = 0; return; }
+    *begin = c->tiles.first_tile[chunk_id];
+    *count = c->tiles.first_tile[chunk_id + 1] - *begin;
+}
+
+int ensure_scratch(ebi_column* c, cudaStream_t s) {
+    if (c->d_tile_counts) return EBI_OK;
+    const size_t nt = c->tiles.tiles.size();
+    int st = dev_alloc(&c->d_tile_counts, nt, s);
+    if (!st) st = dev_alloc(&c->d_tile_offsets, nt + 1, s);
+    if (!st) st = dev_alloc(&c->d_scratch_mask, c->mask_words, s);
+    return st;
+}
+
+// Enqueues finalize, copies the result back and waits.
+int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
+    CK(launch_finalize(q, c->d_res, s));
+    CK(cudaMemcpyAsync(c->h_res, c->d_res, sizeof(QueryResult), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (c->h_res->status) {
+        char buf[96];
+        std::snprintf(buf, sizeof buf, "chunk %u: status %u", c->h_res->bad_chunk, c->h_res->status);
+        return fail(static_cast<int>(c->h_res->status), buf);
+    }
+    return EBI_OK;
+}
+
+// Runs filter / filter+agg / agg over the column.
+int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
+             uint64_t* d_out_mask, unsigned long long* tile_counts, cudaStream_t s) {
+    QueryParams q = base_params(c);
+    q.op = op;
+    q.chunk_id = chunk_id;
+    q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
+    q.out_mask = reinterpret_cast<uint32_t*>(d_out_mask);
+    q.tile_counts = tile_counts;
+    if (pred) q.pred = *pred;
+    uint32_t tb, tn;
+    tile_range(c, chunk_id, &tb, &tn);
+    if (d_out_mask) {
+        // Words shared by two chunks, or words of chunks that are not read, need
+        // a zeroed output; otherwise every word is written by exactly one thread.
+        q.out_atomic = !c->rows_aligned32 || chunk_id >= 0;
+        if (q.out_atomic || tn == 0) CK(cudaMemsetAsync(d_out_mask, 0, c->mask_words * 8, s));
+        else if ((c->n_records + 31) / 32 % 2 == 1)  // last u32 of the last u64 word
+            CK(cudaMemsetAsync(reinterpret_cast<uint32_t*>(d_out_mask) + 2 * c->mask_words - 1, 0, 4, s));
+    }
+    if (d_mask) CK(launch_select_chunks(q, s));
+    if (c->scheme == EBI_BUFF) CK(launch_buff_query(q, tb, tn, s));
+    return EBI_OK;
+}
+
+int check_pred(const ebi_predicate* p) {
+    if (!p) return fail(EBI_E_INVALID, "predicate is null");
+    if (p->kind < EBI_PRED_EQ || p->kind > EBI_PRED_RANGE) return fail(EBI_E_INVALID, "bad predicate kind");
+    if (p->kind == EBI_PRED_RANGE && (p->start_kind < 0 || p->start_kind > 2 || p->end_kind < 0 || p->end_kind > 2))
+        return fail(EBI_E_INVALID, "bad range bound kind");
+    return EBI_OK;
+}
+
+// Materializes the rows of d_mask (all rows when null) into d_out.
+int run_materialize(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* d_out, uint64_t out_cap,
+                    uint64_t* n_out, cudaStream_t s, bool mask_is_scratch, const QueryParams* prior) {
+    QueryParams q = prior ? *prior : base_params(c);
+    q.op = OP_FILTER;  // only status is folded
+    q.chunk_id = chunk_id;
+    q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
+    q.out_mask = nullptr;
+    q.out_vals = d_out;
+    q.out_cap = out_cap;
+    uint32_t tb, tn;
+    tile_range(c, chunk_id, &tb, &tn);
+    uint64_t total = 0;
+    if (!d_mask) {
+        for (uint32_t t = tb; t < tb + tn; ++t) {
+            const Tile& tl = c->tiles.tiles[t];
+            const uint32_t n = c->chunks[tl.chunk].n_rows;
+            total += tl.begin < n ? std::min<uint64_t>(kBuffTileRows, n - tl.begin) : 0;
+        }
+        if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
+        q.tile_counts = nullptr;
+    } else {
+        q.tile_counts = c->d_tile_counts;
+        if (!mask_is_scratch) CK(launch_buff_count(q, tb, tn, s));
+        CK(launch_tile_scan(c->d_tile_counts, c->d_tile_offsets, tn, s));
+    }
+    CK(launch_buff_materialize(q, tb, tn, c->d_tile_offsets, s));
+    if (d_mask) CK(cudaMemcpyAsync(&c->h_res->count, c->d_tile_offsets + tn, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (d_mask) total = c->h_res->count;
+    int st = finish(c, q, s);
+    if (st) return st;
+    if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
+    if (n_out) *n_out = total;
+    return EBI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column** out) {
+    if (!out) return fail(EBI_E_INVALID, "out is null");
+    *out = nullptr;
+    if (!file && len) return fail(EBI_E_INVALID, "file is null");
+    tune_pool_once();
+    ebi_column* c = new (std::nothrow) ebi_column();
+    if (!c) return fail(EBI_E_OOM, "host allocation failed");
+    c->stream = static_cast<cudaStream_t>(stream);
+    int st = parse_file(file, len, c);
+    if (st) { delete c; return st; }
+    cudaStream_t s = c->stream;
+    if (c->scheme == EBI_BUFF) c->tiles = buff_tiles(c->chunks);
+    else c->tiles.first_tile.assign(c->n_chunks + 1, 0);
+    c->mask_words = (c->n_records + 63) / 64;
+    if (c->mask_words == 0) c->mask_words = 1;
+    st = dev_alloc(&c->d_file, len + kFilePad, s);
+    if (!st) st = dev_alloc(&c->d_chunks, c->n_chunks, s);
+    if (!st) st = dev_alloc(&c->d_tiles, c->tiles.tiles.size(), s);
+    if (!st) st = dev_alloc(&c->d_acc, c->n_chunks, s);
+    if (!st) st = dev_alloc(&c->d_res, 1, s);
+    if (!st && cudaMallocHost(&c->h_res, sizeof(QueryResult)) != cudaSuccess) st = fail(EBI_E_OOM, "pinned allocation failed");
+    if (!st) {
+        cudaError_t e = cudaMemcpyAsync(c->d_file, file, len, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->d_file + len, 0, kFilePad, s);
+        if (e == cudaSuccess && c->n_chunks)
+            e = cudaMemcpyAsync(c->d_chunks, c->chunks.data(), c->n_chunks * sizeof(ChunkDesc), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && !c->tiles.tiles.empty())
+            e = cudaMemcpyAsync(c->d_tiles, c->tiles.tiles.data(), c->tiles.tiles.size() * sizeof(Tile),
+                                cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
+        // host sources (chunk table, tiles) must stay alive until the copies ran
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = cuda_fail(e, "ebi_column_open upload");
+    }
+    if (st) { ebi_column_close(c); return st; }
+    *out = c;
+    return EBI_OK;
+}
+
+int ebi_column_close(ebi_column* c) {
+    if (!c) return EBI_OK;
+    cudaStream_t s = c->stream;
+    void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
+                    c->d_scratch_mask};
+    for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
+    if (c->h_res) cudaFreeHost(c->h_res);
+    delete c;
+    return EBI_OK;
+}
+
+uint64_t ebi_column_num_records(const ebi_column* c) { return c ? c->n_records : 0; }
+uint64_t ebi_column_num_chunks(const ebi_column* c) { return c ? c->n_chunks : 0; }
+int ebi_column_scheme(const ebi_column* c) { return c ? c->scheme : -1; }
+
+int ebi_column_chunk_info(const ebi_column* c, uint64_t i, uint64_t* phys, uint64_t* size, uint64_t* row,
+                          uint64_t* rows) {
+    if (!c || i >= c->n_chunks) return fail(EBI_E_INVALID, "chunk index out of range");
+    const ChunkDesc& cd = c->chunks[i];
+    if (phys) *phys = cd.byte_off;
+    if (size) *size = cd.byte_len;
+    if (row) *row = cd.row_off;
+    if (rows) *rows = cd.n_rows;
+    return EBI_OK;
+}
+
+int ebi_column_set_precision(ebi_column* c, int32_t precision) {
+    if (!c) return fail(EBI_E_INVALID, "column is null");
+    if (precision > 12) return fail(EBI_E_INVALID, "precision past PRECISION_MAP (0..12)");
+    c->precision = precision < 0 ? -1 : precision;
+    return EBI_OK;
+}
+
+int ebi_filter(ebi_column* c, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
+               uint64_t* d_out_mask, void* stream) {
+    if (!c || !d_out_mask) return fail(EBI_E_INVALID, "column or output is null");
+    int st = check_pred(pred);
+    if (!st) st = check_supported(c);
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    st = run_scan(c, OP_FILTER, pred, d_mask, chunk_id, d_out_mask, nullptr, s);
+    if (st) return st;
+    QueryParams q = base_params(c);
+    q.op = OP_FILTER;
+    q.chunk_id = chunk_id;
+    return finish(c, q, s);
+}
+
+int ebi_filter_agg(ebi_column* c, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
+                   uint64_t* d_out_mask, double* sum, double* mn, double* mx, uint64_t* n_selected, void* stream) {
+    if (!c) return fail(EBI_E_INVALID, "column is null");
+    int st = check_pred(pred);
+    if (!st) st = check_supported(c);
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    st = run_scan(c, OP_FILTER_AGG, pred, d_mask, chunk_id, d_out_mask, nullptr, s);
+    if (st) return st;
+    QueryParams q = base_params(c);
+    q.op = OP_FILTER_AGG;
+    q.chunk_id = chunk_id;
+    q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
+    st = finish(c, q, s);
+    if (st) return st;
+    if (sum) *sum = c->h_res->sum;
+    if (mn) *mn = c->h_res->min;
+    if (mx) *mx = c->h_res->max;
+    if (n_selected) *n_selected = c->h_res->count;
+    return EBI_OK;
+}
+
+static int agg_common(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, void* stream) {
+    if (!c) return fail(EBI_E_INVALID, "column is null");
+    int st = check_supported(c);
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    st = run_scan(c, OP_AGG, nullptr, d_mask, chunk_id, nullptr, nullptr, s);
+    if (st) return st;
+    QueryParams q = base_params(c);
+    q.op = OP_AGG;
+    q.chunk_id = chunk_id;
+    q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
+    return finish(c, q, s);
+}
+
+int ebi_sum(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream) {
+    const int st = agg_common(c, d_mask, chunk_id, stream);
+    if (!st && out) *out = c->h_res->sum;
+    return st;
+}
+int ebi_min(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream) {
+    const int st = agg_common(c, d_mask, chunk_id, stream);
+    if (!st && out) *out = c->h_res->min;
+    return st;
+}
+int ebi_max(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream) {
+    const int st = agg_common(c, d_mask, chunk_id, stream);
+    if (!st && out) *out = c->h_res->max;
+    return st;
+}
+
+int ebi_materialize(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* d_out, uint64_t out_cap,
+                    uint64_t* n_out, void* stream) {
+    if (!c || (!d_out && out_cap)) return fail(EBI_E_INVALID, "column or output is null");
+    int st = check_supported(c);
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (d_mask && (st = ensure_scratch(c, s))) return st;
+    return run_materialize(c, d_mask, chunk_id, d_out, out_cap, n_out, s, false, nullptr);
+}
+
+int ebi_filter_materialize(ebi_column* c, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
+                           double* d_out, uint64_t out_cap, uint64_t* n_out, void* stream) {
+    if (!c || (!d_out && out_cap)) return fail(EBI_E_INVALID, "column or output is null");
+    int st = check_pred(pred);
+    if (!st) st = check_supported(c);
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((st = ensure_scratch(c, s))) return st;
+    // filter into the scratch mask, counting per tile, then materialize it
+    st = run_scan(c, OP_FILTER, pred, d_mask, chunk_id, c->d_scratch_mask, c->d_tile_counts, s);
+    if (st) return st;
+    return run_materialize(c, c->d_scratch_mask, chunk_id, d_out, out_cap, n_out, s, true, nullptr);
+}
+
+const char* ebi_last_error(void) { return g_last_error.c_str(); }
+uint64_t ebi_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+}  // extern "C"

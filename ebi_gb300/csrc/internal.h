@@ -1,0 +1,47 @@
+// internal.h -- host-side interfaces between the engine's translation units.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace ebi {
+
+// Counts kernel launches (ebi_kernel_launches()).
+void count_launch(uint64_t n = 1);
+void set_last_error(const std::string& msg);
+
+// Tiles of a column: chunk c owns tiles [first_tile[c], first_tile[c + 1]).
+struct TileMap {
+    std::vector<Tile> tiles;
+    std::vector<uint32_t> first_tile;  // n_chunks + 1
+};
+
+// ---- BUFF (buff.cu) --------------------------------------------------------
+constexpr uint32_t kBuffTileRows = 8192;  // 256 threads x 32 rows
+TileMap buff_tiles(const std::vector<ChunkDesc>& chunks);
+// Filter / filter+agg / agg over tiles [tile_begin, tile_begin + n_tiles).
+cudaError_t launch_buff_query(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s);
+// Rows of the bitmask per tile into q.tile_counts[tile - tile_begin].
+cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s);
+// Writes the decoded values of the selected rows at tile_offsets[tile - tile_begin] + rank
+// (with a bitmask) or at their row - first row of the query (without).
+cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles,
+                                    const unsigned long long* tile_offsets, cudaStream_t s);
+
+// ---- shared kernels (query.cu) ---------------------------------------------
+// acc[c].selected = chunk passes chunk_id and intersects the mask (or no mask).
+cudaError_t launch_select_chunks(const QueryParams& q, cudaStream_t s);
+// Exclusive scan of n tile counts into offsets (n + 1 entries; offsets[n] = total).
+cudaError_t launch_tile_scan(const unsigned long long* counts, unsigned long long* offsets, uint32_t n,
+                             cudaStream_t s);
+// Folds the per-chunk partials in chunk order into *res and re-arms acc.
+cudaError_t launch_finalize(const QueryParams& q, QueryResult* res, cudaStream_t s);
+// Sets acc to its rest values (once, at open).
+cudaError_t launch_acc_init(ChunkAcc* acc, uint32_t n, cudaStream_t s);
+
+}  // namespace ebi

@@ -1,0 +1,152 @@
+/*
+ * ebi_gpu.h -- C ABI of the GB300 engine for lemolatoon/ebi's chunked
+ * decode-and-query path (EBI1 files; Gorilla, Chimp, Chimp128, BUFF, RLE and
+ * Uncompressed chunks).
+ *
+ * The entry points mirror ebi's public Decoder (ebi/src/api/decoder.rs) and
+ * Encoder (ebi/src/api/encoder.rs); each declaration cites the reference item
+ * it replaces.  A binding in the reference's own language is a thin `extern
+ * "C"` block over these functions (INTEGRATION.md shows it).
+ *
+ * Conventions
+ *  - Every function returns an ebi_status; 0 is success.  The codes mirror
+ *    DecoderError (ebi/src/decoder/error.rs:6-21).  When several chunks fail,
+ *    the status of the first failing chunk in chunk order is returned, as the
+ *    reference's sequential chunk loop would.
+ *  - A column keeps the whole EBI1 file resident in device memory from
+ *    ebi_column_open until ebi_column_close.
+ *  - Bitmasks are dense arrays of ceil(n_records / 64) little-endian uint64
+ *    words in DEVICE memory; bit (r % 64) of word (r / 64) is row r.  They
+ *    stand for the reference's RoaringBitmap of global u32 row ids.  NULL
+ *    means None.
+ *  - chunk_id < 0 means None (all chunks); otherwise only that chunk is read,
+ *    as Decoder::*(.., Some(ChunkId)) does.
+ *  - Bulk outputs (bitmasks, materialized values) are DEVICE pointers;
+ *    scalar outputs (sums, counts) are HOST pointers and the call waits for
+ *    its stream before returning them.
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream).  Calls on
+ *    one column must not overlap: a column owns one set of query scratch.
+ */
+#ifndef EBI_GPU_H
+#define EBI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    EBI_OK = 0,
+    EBI_E_IO = 1,             /* DecoderError::IO: the file is shorter than its own offsets say  */
+    EBI_E_CONVERSION = 2,     /* DecoderError::ConversionError: bad field type / scheme / option */
+    EBI_E_UNEXPECTED_END = 3, /* DecoderError::UnexpectedEndOfChunk                              */
+    EBI_E_PRECONDITION = 4,   /* DecoderError::PreconditionsNotMet                               */
+    EBI_E_CUDA = 5,           /* DecoderError::CudaError                                         */
+    EBI_E_CORRUPT = 6,        /* a stream breaks an invariant the reference asserts in debug     */
+    EBI_E_INVALID = 7,        /* bad argument (e.g. output buffer too small)                     */
+    EBI_E_OOM = 8,            /* device or host allocation failed                                */
+    EBI_E_UNSUPPORTED = 9     /* codec outside this engine (Elf, Sprintz, zstd, gzip, ...)       */
+} ebi_status;
+
+/* CompressionScheme (ebi/src/format.rs:185-199) */
+enum { EBI_UNCOMPRESSED = 0, EBI_RLE = 1, EBI_BUFF = 2, EBI_GORILLA = 3, EBI_CHIMP = 4, EBI_CHIMP128 = 5 };
+/* ChunkOptionKind (ebi/src/format.rs:174-180) */
+enum { EBI_CHUNK_FULL = 0, EBI_CHUNK_RECORD_COUNT = 1, EBI_CHUNK_BYTE_SIZE = 2 };
+/* Predicate / RangeValue kinds (ebi/src/decoder/query.rs:352-428) */
+enum { EBI_PRED_EQ = 0, EBI_PRED_NE = 1, EBI_PRED_RANGE = 2 };
+enum { EBI_BOUND_NONE = 0, EBI_BOUND_INCLUSIVE = 1, EBI_BOUND_EXCLUSIVE = 2 };
+
+/* Predicate = PredicateImpl<f64>::{Eq(v), Ne(v), Range{start, end}} (query.rs:422-437). */
+typedef struct {
+    int32_t kind;       /* EBI_PRED_*                          */
+    int32_t start_kind; /* EBI_BOUND_* of Range::start         */
+    int32_t end_kind;   /* EBI_BOUND_* of Range::end           */
+    int32_t reserved;   /* 0                                   */
+    double value;       /* operand of Eq / Ne                  */
+    double start;       /* RangeValue payload of Range::start  */
+    double end;         /* RangeValue payload of Range::end    */
+} ebi_predicate;
+
+typedef struct ebi_column ebi_column;
+
+/* ---- open / inspect ------------------------------------------------------ */
+
+/* Decoder::new (api/decoder.rs:136-156) over an in-memory EBI1 file: parses
+ * the header and footer (FileReader::fetch_header/fetch_footer,
+ * decoder.rs:131-220) and copies the file to device memory on `stream`.
+ * `file` may be pageable or pinned host memory; it is not used after return. */
+int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column** out);
+/* Drops the device copy (Decoder going out of scope). */
+int ebi_column_close(ebi_column* col);
+
+/* NativeFileFooter::{number_of_records, number_of_chunks} (format/native.rs:482-488) */
+uint64_t ebi_column_num_records(const ebi_column* col);
+uint64_t ebi_column_num_chunks(const ebi_column* col);
+/* NativeFileConfig::compression_scheme (format/native.rs:410-414) */
+int ebi_column_scheme(const ebi_column* col);
+/* GeneralChunkHandle::{physical_offset, chunk_size, logical_offset,
+ * number_of_records} (decoder.rs:283-328) */
+int ebi_column_chunk_info(const ebi_column* col, uint64_t chunk, uint64_t* physical_offset,
+                          uint64_t* size, uint64_t* logical_offset, uint64_t* n_records);
+/* Decoder::with_precision (api/decoder.rs:159-161): BUFF materialization keeps
+ * only the byte planes needed for `precision` decimal digits
+ * (buff/controlled_precision.rs:5-75).  precision < 0 restores full precision. */
+int ebi_column_set_precision(ebi_column* col, int32_t precision);
+
+/* ---- queries (Decoder methods, api/decoder.rs:202-439) -------------------- */
+
+/* Decoder::materialize: decoded values of the rows in `mask` (all rows when
+ * NULL), in row order, to d_out[0 .. *n_out).  Fails with EBI_E_INVALID and
+ * writes nothing past out_cap when more than out_cap values qualify. */
+int ebi_materialize(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* d_out,
+                    uint64_t out_cap, uint64_t* n_out, void* stream);
+
+/* Decoder::filter: rows (of `mask` when given) whose value satisfies `pred`,
+ * as a bitmask in d_out_mask (ceil(n_records/64) words, fully written). */
+int ebi_filter(ebi_column* col, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
+               uint64_t* d_out_mask, void* stream);
+
+/* Decoder::filter_materialize: the values of the rows ebi_filter selects. */
+int ebi_filter_materialize(ebi_column* col, const ebi_predicate* pred, const uint64_t* d_mask,
+                           int64_t chunk_id, double* d_out, uint64_t out_cap, uint64_t* n_out,
+                           void* stream);
+
+/* Decoder::sum / min / max over the rows of `mask` (all when NULL).  Sums of
+ * BUFF chunks are exact integer sums rounded once, as the reference computes
+ * them; sums of Gorilla/Chimp/Chimp128/RLE/Uncompressed chunks are
+ * compensated (double-double) sums whose relative difference to the
+ * reference's sequential f64 sum is below 1e-12 for the bench workloads. */
+int ebi_sum(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream);
+int ebi_min(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream);
+int ebi_max(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream);
+
+/* Fused Decoder::filter followed by Decoder::{sum,min,max}(Some(&result)),
+ * reading each chunk once.  Any output may be NULL.  n_selected receives the
+ * number of rows in the filter result. */
+int ebi_filter_agg(ebi_column* col, const ebi_predicate* pred, const uint64_t* d_mask,
+                   int64_t chunk_id, uint64_t* d_out_mask, double* sum, double* min, double* max,
+                   uint64_t* n_selected, void* stream);
+
+/* ---- encoder (host) -------------------------------------------------------- */
+
+/* Encoder::new(.., chunk_option, compressor_config).encode()
+ * (api/encoder.rs:121-178) on an in-memory f64 column.  `scale` is the BUFF
+ * scale (ignored by the other codecs).  The result is malloc'ed; release it
+ * with ebi_free.  The two timing fields of the footer are written as zero. */
+int ebi_encode(const double* values, uint64_t n, int scheme, int chunk_kind, uint64_t chunk_value,
+               uint64_t scale, uint8_t** out, uint64_t* out_len);
+void ebi_free(void* p);
+
+/* ---- diagnostics ------------------------------------------------------------ */
+
+/* Message of the last error raised on this thread (empty when none). */
+const char* ebi_last_error(void);
+/* Number of kernels this library launched since load (for launch accounting). */
+uint64_t ebi_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EBI_GPU_H */
