@@ -15,7 +15,8 @@ EXPORTS = [
     "ebi_column_open", "ebi_column_close", "ebi_column_num_records", "ebi_column_num_chunks",
     "ebi_column_scheme", "ebi_column_chunk_info", "ebi_column_set_precision", "ebi_materialize",
     "ebi_filter", "ebi_filter_materialize", "ebi_sum", "ebi_min", "ebi_max", "ebi_filter_agg",
-    "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches",
+    "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches", "ebi_column_set_timing",
+    "ebi_column_last_times",
 ]
 
 
@@ -24,6 +25,12 @@ class Predicate(C.Structure):
     _fields_ = [("kind", C.c_int32), ("start_kind", C.c_int32), ("end_kind", C.c_int32),
                 ("reserved", C.c_int32), ("value", C.c_double), ("start", C.c_double),
                 ("end", C.c_double)]
+
+
+class SegmentTimes(C.Structure):
+    """ebi_segment_times"""
+    _fields_ = [("scan_ms", C.c_double), ("finalize_ms", C.c_double), ("total_ms", C.c_double),
+                ("kernels", C.c_uint64)]
 
 
 _lib = None
@@ -56,5 +63,7 @@ def lib() -> C.CDLL:
     L.ebi_free.argtypes = [vp]
     L.ebi_last_error.restype = C.c_char_p
     L.ebi_kernel_launches.restype = u64
+    L.ebi_column_set_timing.argtypes = [vp, C.c_int]
+    L.ebi_column_last_times.argtypes = [vp, C.POINTER(SegmentTimes)]
     _lib = L
     return L

@@ -205,6 +205,15 @@ class Decoder:
                "chunk_info")
         return a.value, b.value, c.value, d.value
 
+    def set_timing(self, enable: bool = True):
+        _check(_native.lib().ebi_column_set_timing(self._h, int(enable)), "set_timing")
+
+    def segmented_execution_times(self) -> dict:
+        """Device time of the last query by segment (Decoder::segmented_execution_times)."""
+        t = _native.SegmentTimes()
+        _check(_native.lib().ebi_column_last_times(self._h, C.byref(t)), "segmented_execution_times")
+        return {"scan_ms": t.scan_ms, "finalize_ms": t.finalize_ms, "total_ms": t.total_ms, "kernels": t.kernels}
+
     def with_precision(self, precision: int):
         _check(_native.lib().ebi_column_set_precision(self._h, int(precision)), "Decoder::with_precision")
 

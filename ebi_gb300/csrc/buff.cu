@@ -428,17 +428,8 @@ cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_
 }
 
 cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles,
-                                    const unsigned long long* tile_offsets, cudaStream_t s) {
+                                    const unsigned long long* tile_offsets, uint64_t base_row, cudaStream_t s) {
     if (n_tiles == 0) return cudaSuccess;
-    unsigned long long base_row = 0;
-    if (q.chunk_id >= 0) {
-        ChunkDesc cd;
-        cudaError_t e = cudaMemcpyAsync(&cd, q.chunks + q.chunk_id, sizeof cd, cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess) return e;
-        e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return e;
-        base_row = cd.row_off;
-    }
     buff_materialize_kernel<<<n_tiles, kThreads, 0, s>>>(q, tile_begin, tile_offsets, base_row);
     count_launch();
     return cudaGetLastError();

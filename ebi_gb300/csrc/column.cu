@@ -81,6 +81,11 @@ struct ebi_column {
     unsigned long long* d_tile_offsets = nullptr;  // n_tiles + 1
     uint64_t* d_scratch_mask = nullptr;            // mask_words
     uint64_t mask_words = 0;
+    // segment timing (ebi_column_set_timing)
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // query start, scan end, finalize end
+    ebi_segment_times last{};
+    uint64_t launches_at_start = 0;
 };
 
 namespace {
@@ -175,11 +180,29 @@ int ensure_scratch(ebi_column* c, cudaStream_t s) {
     return st;
 }
 
+// Query timing: events around the codec kernels and the finalize fold.
+int begin_query(ebi_column* c, cudaStream_t s) {
+    c->launches_at_start = ebi_kernel_launches();
+    if (c->timing) CK(cudaEventRecord(c->ev[0], s));
+    return EBI_OK;
+}
+
 // Enqueues finalize, copies the result back and waits.
 int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
+    if (c->timing) CK(cudaEventRecord(c->ev[1], s));
     CK(launch_finalize(q, c->d_res, s));
+    if (c->timing) CK(cudaEventRecord(c->ev[2], s));
     CK(cudaMemcpyAsync(c->h_res, c->d_res, sizeof(QueryResult), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    c->last.kernels = ebi_kernel_launches() - c->launches_at_start;
+    if (c->timing) {
+        float a = 0.f, b = 0.f;
+        CK(cudaEventElapsedTime(&a, c->ev[0], c->ev[1]));
+        CK(cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
+        c->last.scan_ms = a;
+        c->last.finalize_ms = b;
+        c->last.total_ms = double(a) + double(b);
+    }
     if (c->h_res->status) {
         char buf[96];
         std::snprintf(buf, sizeof buf, "chunk %u: status %u", c->h_res->bad_chunk, c->h_res->status);
@@ -191,6 +214,7 @@ int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
 // Runs filter / filter+agg / agg over the column.
 int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
              uint64_t* d_out_mask, unsigned long long* tile_counts, cudaStream_t s) {
+    if (int st = begin_query(c, s)) return st;
     QueryParams q = base_params(c);
     q.op = op;
     q.chunk_id = chunk_id;
@@ -233,6 +257,9 @@ int run_materialize(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, dou
     q.out_cap = out_cap;
     uint32_t tb, tn;
     tile_range(c, chunk_id, &tb, &tn);
+    if (!mask_is_scratch) {
+        if (int st = begin_query(c, s)) return st;
+    }
     uint64_t total = 0;
     if (!d_mask) {
         for (uint32_t t = tb; t < tb + tn; ++t) {
@@ -247,7 +274,8 @@ int run_materialize(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, dou
         if (!mask_is_scratch) CK(launch_buff_count(q, tb, tn, s));
         CK(launch_tile_scan(c->d_tile_counts, c->d_tile_offsets, tn, s));
     }
-    CK(launch_buff_materialize(q, tb, tn, c->d_tile_offsets, s));
+    const uint64_t base_row = chunk_id >= 0 && static_cast<uint64_t>(chunk_id) < c->n_chunks ? c->chunks[chunk_id].row_off : 0;
+    CK(launch_buff_materialize(q, tb, tn, c->d_tile_offsets, base_row, s));
     if (d_mask) CK(cudaMemcpyAsync(&c->h_res->count, c->d_tile_offsets + tn, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (d_mask) total = c->h_res->count;
@@ -304,6 +332,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
 int ebi_column_close(ebi_column* c) {
     if (!c) return EBI_OK;
     cudaStream_t s = c->stream;
+    for (cudaEvent_t e : c->ev) if (e) cudaEventDestroy(e);
     void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
                     c->d_scratch_mask};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
@@ -423,6 +452,21 @@ int ebi_filter_materialize(ebi_column* c, const ebi_predicate* pred, const uint6
     st = run_scan(c, OP_FILTER, pred, d_mask, chunk_id, c->d_scratch_mask, c->d_tile_counts, s);
     if (st) return st;
     return run_materialize(c, c->d_scratch_mask, chunk_id, d_out, out_cap, n_out, s, true, nullptr);
+}
+
+int ebi_column_set_timing(ebi_column* c, int enable) {
+    if (!c) return fail(EBI_E_INVALID, "column is null");
+    if (enable && !c->ev[0]) {
+        for (cudaEvent_t& e : c->ev) CK(cudaEventCreate(&e));
+    }
+    c->timing = enable != 0;
+    return EBI_OK;
+}
+
+int ebi_column_last_times(const ebi_column* c, ebi_segment_times* out) {
+    if (!c || !out) return fail(EBI_E_INVALID, "column or output is null");
+    *out = c->last;
+    return EBI_OK;
 }
 
 const char* ebi_last_error(void) { return g_last_error.c_str(); }

@@ -31,7 +31,7 @@ cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_
 // Writes the decoded values of the selected rows at tile_offsets[tile - tile_begin] + rank
 // (with a bitmask) or at their row - first row of the query (without).
 cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles,
-                                    const unsigned long long* tile_offsets, cudaStream_t s);
+                                    const unsigned long long* tile_offsets, uint64_t base_row, cudaStream_t s);
 
 // ---- shared kernels (query.cu) ---------------------------------------------
 // acc[c].selected = chunk passes chunk_id and intersects the mask (or no mask).

@@ -141,6 +141,21 @@ void ebi_free(void* p);
 
 /* ---- diagnostics ------------------------------------------------------------ */
 
+/* Device time of the last query on a column, by segment, in milliseconds
+ * (the counterpart of Decoder::segmented_execution_times, api/decoder.rs:163-166,
+ * and SegmentKind, time.rs:11-22).  `scan` covers the codec kernels that read
+ * the chunks (decode, compare, aggregate: the reference's Xor / BitPacking /
+ * Decompression + CompareInsert + Sum segments), `finalize` the chunk-ordered
+ * fold.  Filled only while timing is enabled (CUDA events on the query's stream). */
+typedef struct {
+    double scan_ms;
+    double finalize_ms;
+    double total_ms;
+    uint64_t kernels;  /* kernels the query launched */
+} ebi_segment_times;
+int ebi_column_set_timing(ebi_column* col, int enable);
+int ebi_column_last_times(const ebi_column* col, ebi_segment_times* out);
+
 /* Message of the last error raised on this thread (empty when none). */
 const char* ebi_last_error(void);
 /* Number of kernels this library launched since load (for launch accounting). */
