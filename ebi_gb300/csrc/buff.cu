@@ -16,6 +16,7 @@
 // shortcuts.  Sums are exact u64 sums of deltas (buff/sum.rs:60-119); min
 // and max are exact via the deltas (buff/min_max.rs).
 #include "internal.h"
+#include "tma.cuh"
 
 namespace ebi {
 namespace {
@@ -60,6 +61,62 @@ struct BuffCtx {
     uint64_t lthr, rthr, etgt;
 };
 
+// Predicate compiled into the delta domain of one chunk, exactly as the
+// reference's in-situ filters decide it.
+struct BuffPred {
+    uint32_t lmode, rmode, lincl, rincl, emode;
+    uint64_t lthr, rthr, etgt;
+};
+
+__device__ void compile_pred(const ebi_predicate& pr, int64_t base, uint32_t bits, uint32_t frac, bool has_mask,
+                             BuffPred& k) {
+    k.lmode = k.rmode = SIDE_ABSENT;
+    k.emode = SIDE_NONE;
+    k.lincl = k.rincl = 0;
+    k.lthr = k.rthr = k.etgt = 0;
+    const uint32_t np = bits / 8;
+    if (pr.kind == EBI_PRED_RANGE) {
+        // left side: buff_simd256_cmp_filter::<true, INCL> (filter_cmp.rs:299-451)
+        if (pr.start_kind != EBI_BOUND_NONE) {
+            const bool incl = pr.start_kind == EBI_BOUND_INCLUSIVE;
+            const int64_t fp = buff_fixed(pr.start, static_cast<int32_t>(frac));
+            if (fp < base) k.lmode = SIDE_ALL;
+            else if (bits == 0) k.lmode = (incl ? base >= fp : base > fp) ? SIDE_ALL : SIDE_NONE;
+            else {
+                const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(base);
+                if (bits < bit_length(dp)) k.lmode = SIDE_NONE;
+                else { k.lmode = SIDE_CMP; k.lthr = dp; k.lincl = incl; }
+            }
+        }
+        // right side: buff_simd256_cmp_filter::<false, INCL>
+        if (pr.end_kind != EBI_BOUND_NONE) {
+            const bool incl = pr.end_kind == EBI_BOUND_INCLUSIVE;
+            const int64_t fp = buff_fixed(pr.end, static_cast<int32_t>(frac));
+            if (fp < base) k.rmode = SIDE_NONE;
+            else if (bits == 0) k.rmode = (incl ? base <= fp : base < fp) ? SIDE_ALL : SIDE_NONE;
+            else {
+                const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(base);
+                if (bits < bit_length(dp)) k.rmode = SIDE_ALL;
+                else { k.rmode = SIDE_CMP; k.rthr = dp; k.rincl = incl; }
+            }
+        }
+    } else {
+        // buff_simd256_equal_filter (filter_eq.rs:74-200)
+        const int64_t fp = buff_fixed(pr.value, static_cast<int32_t>(frac));
+        if (fp < base) k.emode = SIDE_NONE;
+        else if (bits == 0) k.emode = fp == base ? SIDE_ALL : SIDE_NONE;
+        else {
+            const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(base);
+            // Byte planes compare (u8)(dp >> shift) and the tail compares dp's low
+            // bits: together delta == dp mod 2^bits.  With neither byte planes
+            // nor an input bitmask the tail is compared with `dp as u8` (:190-196).
+            const uint64_t wmask = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
+            k.emode = SIDE_CMP;
+            k.etgt = (np > 0 || has_mask) ? (dp & wmask) : (dp & 0xffull);
+        }
+    }
+}
+
 __device__ void buff_setup(const QueryParams& q, uint32_t c, bool has_mask, BuffCtx& k) {
     const ChunkDesc cd = q.chunks[c];
     ChunkAcc* acc = q.acc + c;
@@ -100,49 +157,10 @@ __device__ void buff_setup(const QueryParams& q, uint32_t c, bool has_mask, Buff
         k.load_tail = rem > 0 && rem > unnecessary;
     }
 
-    const ebi_predicate& pr = q.pred;
-    k.lmode = k.rmode = SIDE_ABSENT;
-    k.emode = SIDE_NONE;
-    if (pr.kind == EBI_PRED_RANGE) {
-        // left side: buff_simd256_cmp_filter::<true, INCL> (filter_cmp.rs:299-451)
-        if (pr.start_kind != EBI_BOUND_NONE) {
-            const bool incl = pr.start_kind == EBI_BOUND_INCLUSIVE;
-            const int64_t fp = buff_fixed(pr.start, static_cast<int32_t>(k.frac));
-            if (fp < k.base) k.lmode = SIDE_ALL;
-            else if (k.bits == 0) k.lmode = (incl ? k.base >= fp : k.base > fp) ? SIDE_ALL : SIDE_NONE;
-            else {
-                const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(k.base);
-                if (k.bits < bit_length(dp)) k.lmode = SIDE_NONE;
-                else { k.lmode = SIDE_CMP; k.lthr = dp; k.lincl = incl; }
-            }
-        }
-        // right side: buff_simd256_cmp_filter::<false, INCL>
-        if (pr.end_kind != EBI_BOUND_NONE) {
-            const bool incl = pr.end_kind == EBI_BOUND_INCLUSIVE;
-            const int64_t fp = buff_fixed(pr.end, static_cast<int32_t>(k.frac));
-            if (fp < k.base) k.rmode = SIDE_NONE;
-            else if (k.bits == 0) k.rmode = (incl ? k.base <= fp : k.base < fp) ? SIDE_ALL : SIDE_NONE;
-            else {
-                const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(k.base);
-                if (k.bits < bit_length(dp)) k.rmode = SIDE_ALL;
-                else { k.rmode = SIDE_CMP; k.rthr = dp; k.rincl = incl; }
-            }
-        }
-    } else {
-        // buff_simd256_equal_filter (filter_eq.rs:74-200)
-        const int64_t fp = buff_fixed(pr.value, static_cast<int32_t>(k.frac));
-        if (fp < k.base) k.emode = SIDE_NONE;
-        else if (k.bits == 0) k.emode = fp == k.base ? SIDE_ALL : SIDE_NONE;
-        else {
-            const uint64_t dp = static_cast<uint64_t>(fp) - static_cast<uint64_t>(k.base);
-            // Byte planes compare (u8)(dp >> shift) and the tail compares dp's low
-            // bits: together delta == dp mod 2^bits.  With neither byte planes
-            // nor an input bitmask the tail is compared with `dp as u8` (:190-196).
-            const uint64_t wmask = k.bits >= 64 ? ~0ull : ((1ull << k.bits) - 1);
-            k.emode = SIDE_CMP;
-            k.etgt = (k.np > 0 || has_mask) ? (dp & wmask) : (dp & 0xffull);
-        }
-    }
+    BuffPred bp;
+    compile_pred(q.pred, k.base, k.bits, k.frac, has_mask, bp);
+    k.lmode = bp.lmode; k.rmode = bp.rmode; k.lincl = bp.lincl; k.rincl = bp.rincl; k.emode = bp.emode;
+    k.lthr = bp.lthr; k.rthr = bp.rthr; k.etgt = bp.etgt;
     k.ok = 1;
 }
 
@@ -398,6 +416,267 @@ __global__ void __launch_bounds__(kThreads) buff_materialize_kernel(QueryParams 
     else buff_mat_dispatch<uint32_t>(q, k, tile, t.begin, tile_offsets, base_row, warp_tot);
 }
 
+
+// ---------------------------------------------------------------------------
+// Pipelined scan: a persistent CTA streams its contiguous range of tiles
+// through a ring of shared-memory stages.  Warp 8 is the producer: for every
+// tile it reads the chunk's header facts, compiles the predicate and issues
+// one bulk copy (cp.async.bulk, the TMA unit) per byte plane plus one for
+// the tail plane, all completing on the stage's `full` mbarrier.  Warps 0-7
+// consume: each thread decodes 32 rows from shared memory, evaluates the
+// predicate, writes its 32-bit bitmask word and accumulates exact per-chunk
+// partials in registers, flushed with one atomic per warp when the chunk
+// changes.  Consumers release a stage through its `empty` mbarrier.
+// ---------------------------------------------------------------------------
+constexpr int kScanConsumers = 256;
+constexpr int kScanThreads = kScanConsumers + 32;
+
+struct ScanMeta {
+    uint64_t row0;      // global row of the tile's first row
+    uint32_t chunk, rows, ok, np, tb;
+    uint32_t mis[8];    // offset of the tile's first byte inside each plane slot
+    uint32_t mis_tail;  // offset of the tile's first tail byte inside the tail slot
+    BuffPred pred;
+};
+
+__device__ __forceinline__ uint4 lds16(const uint8_t* p) { return *reinterpret_cast<const uint4*>(p); }
+
+// 32 bytes at an arbitrary shared-memory address as 8 little-endian words.
+__device__ __forceinline__ void load32_smem(const uint8_t* p, uint32_t (&w)[8]) {
+    const uint32_t a = smem_addr(p);
+    const uint32_t s = a & 15;
+    const uint8_t* q = p - s;
+    uint4 x0 = lds16(q), x1 = lds16(q + 16), x2 = s ? lds16(q + 32) : make_uint4(0, 0, 0, 0);
+    uint32_t v[12] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x, x2.y, x2.z, x2.w};
+    const bool s8 = s & 8, s4 = s & 4;
+#pragma unroll
+    for (int j = 0; j < 10; ++j) v[j] = s8 ? v[j + 2] : v[j];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) v[j] = s4 ? v[j + 1] : v[j];
+    const uint32_t bs = (s & 3) * 8;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) w[j] = __funnelshift_r(v[j], v[j + 1], bs);
+}
+
+struct Partial {
+    unsigned long long sum, cnt, mx, mn;
+};
+
+__device__ __forceinline__ void flush_partial(const QueryParams& q, uint32_t chunk, Partial& p) {
+    const unsigned long long s = warp_sum(p.sum), c = warp_sum(p.cnt), mx = warp_max_u64(p.mx), mn = warp_min_u64(p.mn);
+    if ((threadIdx.x & 31) == 0 && c) {
+        ChunkAcc* a = q.acc + chunk;
+        atomicAdd(&a->isum, s);
+        atomicAdd(&a->count, c);
+        atomicMax(&a->dmax, mx);
+        atomicMin(&a->dmin, mn);
+    }
+    p.sum = 0; p.cnt = 0; p.mx = 0; p.mn = ~0ull;
+}
+
+template <int TB, typename D>
+__device__ __forceinline__ void scan_rows(const QueryParams& q, const ScanMeta& m, const uint8_t* stage,
+                                          const StageLayout& L, Partial& part) {
+    const uint32_t t = threadIdx.x;
+    const uint32_t lr = 32 * t;
+    const bool has_mask = q.in_mask != nullptr;
+    const bool want_agg = q.op == OP_FILTER_AGG || q.op == OP_AGG;
+    const bool in_tile = lr < m.rows;
+    uint32_t sel = 0;
+    if (in_tile && m.ok) {
+        const uint32_t left = m.rows - lr;
+        const uint32_t valid = left >= 32 ? ~0u : ((1u << left) - 1u);
+        const uint32_t mw = has_mask ? (mask_word(q.in_mask, m.row0 + lr, q.n_records) & valid) : valid;
+        D d[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) d[i] = 0;
+        for (uint32_t p = 0; p < m.np; ++p) {
+            uint32_t w[8];
+            load32_smem(stage + p * L.plane_stride + m.mis[p] + lr, w);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) w[j] ^= 0x80808080u;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) d[i] = (d[i] << 8) | static_cast<D>((w[i >> 2] >> (8 * (i & 3))) & 0xffu);
+        }
+        if constexpr (TB > 0) {
+            uint32_t w[8];
+            load32_smem(stage + L.np_max * L.plane_stride + m.mis_tail + 4 * TB * t, w);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                constexpr uint32_t msk = (1u << TB) - 1u;
+                const int pos = i * TB, wi = pos >> 5, sh = pos & 31;
+                const uint32_t f = (sh + TB <= 32) ? (w[wi] >> sh) : __funnelshift_r(w[wi], w[wi + 1], sh);
+                d[i] = static_cast<D>((d[i] << TB) | static_cast<D>(f & msk));
+            }
+        }
+        const BuffPred& k = m.pred;
+        if (q.op == OP_AGG) {
+            sel = mw;
+        } else if (q.pred.kind == EBI_PRED_RANGE) {
+            const bool la = k.lmode == SIDE_ABSENT, ra = k.rmode == SIDE_ABSENT;
+            uint32_t Lw = 0, Rw = 0;
+            if (k.lmode == SIDE_ALL) Lw = valid;
+            else if (k.lmode == SIDE_CMP) Lw = cmp_word<D>(d, k.lthr, true, k.lincl) & mw;
+            if (k.rmode == SIDE_ALL) Rw = valid;
+            else if (k.rmode == SIDE_CMP) Rw = cmp_word<D>(d, k.rthr, false, k.rincl) & mw;
+            sel = (la && ra) ? mw : la ? Rw : ra ? Lw : (Lw & Rw);
+        } else {
+            uint32_t e = 0;
+            if (k.emode == SIDE_ALL) e = valid;
+            else if (k.emode == SIDE_CMP) e = eq_word<D>(d, k.etgt) & mw;
+            sel = q.pred.kind == EBI_PRED_EQ ? e : (mw & ~e);
+        }
+        if (want_agg && sel) {
+            unsigned long long s64 = 0;
+            D mx = 0, mn = static_cast<D>(~D(0));
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                const bool on = (sel >> i) & 1u;
+                s64 += on ? static_cast<unsigned long long>(d[i]) : 0ull;
+                mx = (on && d[i] > mx) ? d[i] : mx;
+                mn = (on && d[i] < mn) ? d[i] : mn;
+            }
+            part.sum += s64;
+            part.cnt += __popc(sel);
+            part.mx = static_cast<unsigned long long>(mx) > part.mx ? static_cast<unsigned long long>(mx) : part.mx;
+            part.mn = static_cast<unsigned long long>(mn) < part.mn ? static_cast<unsigned long long>(mn) : part.mn;
+        }
+    }
+    if ((q.op == OP_FILTER || q.op == OP_FILTER_AGG) && in_tile && q.out_mask) {
+        if (!q.out_atomic || sel) store_mask_word(q.out_mask, m.row0 + lr, sel, q.out_atomic);
+    }
+}
+
+template <typename D>
+__device__ __forceinline__ void scan_dispatch(const QueryParams& q, const ScanMeta& m, const uint8_t* stage,
+                                              const StageLayout& L, Partial& part) {
+    switch (m.ok ? m.tb : 0) {
+        case 0: scan_rows<0, D>(q, m, stage, L, part); break;
+        case 1: scan_rows<1, D>(q, m, stage, L, part); break;
+        case 2: scan_rows<2, D>(q, m, stage, L, part); break;
+        case 3: scan_rows<3, D>(q, m, stage, L, part); break;
+        case 4: scan_rows<4, D>(q, m, stage, L, part); break;
+        case 5: scan_rows<5, D>(q, m, stage, L, part); break;
+        case 6: scan_rows<6, D>(q, m, stage, L, part); break;
+        default: scan_rows<7, D>(q, m, stage, L, part); break;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads, 2)
+buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, uint32_t n_tiles, StageLayout L) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+    uint64_t* empty = full + L.stages;
+    ScanMeta* meta = reinterpret_cast<ScanMeta*>(smem + 128);
+    uint8_t* stages = smem + L.data_offset;
+    // contiguous tile range of this CTA
+    const uint32_t t_first = static_cast<uint32_t>((uint64_t(n_tiles) * blockIdx.x) / gridDim.x);
+    const uint32_t t_end = static_cast<uint32_t>((uint64_t(n_tiles) * (blockIdx.x + 1)) / gridDim.x);
+    const uint32_t count = t_end - t_first;
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < L.stages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kScanConsumers / 32);
+        }
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool has_mask = q.in_mask != nullptr;
+
+    if (threadIdx.x >= kScanConsumers) {
+        // ---- producer warp (one lane issues) ----
+        if (threadIdx.x != kScanConsumers) return;
+        for (uint32_t i = 0; i < count; ++i) {
+            const uint32_t s = i % L.stages, k = i / L.stages;
+            if (k > 0 && !mbar_wait(&empty[s], (k - 1) & 1)) {
+                set_status(q.acc, EBI_E_CUDA);
+                return;  // consumers stopped; nothing of this stage is in flight
+            }
+            const Tile tl = q.tiles[tile_base + t_first + i];
+            const uint32_t c = tl.chunk;
+            const ChunkDesc cd = q.chunks[c];
+            const BuffChunkInfo ci = info[c];
+            ScanMeta& m = meta[s];
+            const bool selected = has_mask ? q.acc[c].selected != 0
+                                           : (q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
+            if (selected && tl.begin == 0) {
+                if (!has_mask) q.acc[c].selected = 1;
+                if (ci.status) set_status(q.acc + c, ci.status);
+            }
+            m.chunk = c;
+            m.row0 = cd.row_off + tl.begin;
+            m.rows = min(kBuffTileRows, cd.n_rows - tl.begin);
+            m.ok = selected && ci.status == 0;
+            uint32_t bytes = 0;
+            const uint8_t* file = q.file;
+            uint8_t* st = stages + size_t(s) * L.stage_bytes;
+            if (m.ok) {
+                m.np = ci.bits / 8;
+                m.tb = ci.bits % 8;
+                compile_pred(q.pred, ci.base, ci.bits, ci.frac, has_mask, m.pred);
+                for (uint32_t p = 0; p < m.np; ++p) {
+                    const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.planes + uint64_t(p) * ci.n + tl.begin);
+                    const uintptr_t a = src & ~uintptr_t(15);
+                    m.mis[p] = static_cast<uint32_t>(src - a);
+                    bytes += static_cast<uint32_t>(((src + m.rows + 15) & ~uintptr_t(15)) - a);
+                }
+                if (m.tb) {
+                    const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.tail + uint64_t(tl.begin / 8) * m.tb);
+                    const uintptr_t a = src & ~uintptr_t(15);
+                    m.mis_tail = static_cast<uint32_t>(src - a);
+                    bytes += static_cast<uint32_t>(((src + (uint64_t(m.rows) * m.tb + 7) / 8 + 15) & ~uintptr_t(15)) - a);
+                }
+            } else {
+                m.np = 0;
+                m.tb = 0;
+            }
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&full[s], bytes);
+            if (m.ok) {
+                for (uint32_t p = 0; p < m.np; ++p) {
+                    const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.planes + uint64_t(p) * ci.n + tl.begin);
+                    const uintptr_t a = src & ~uintptr_t(15);
+                    const uint32_t len = static_cast<uint32_t>(((src + m.rows + 15) & ~uintptr_t(15)) - a);
+                    bulk_g2s(st + p * L.plane_stride, reinterpret_cast<const void*>(a), len, &full[s]);
+                }
+                if (m.tb) {
+                    const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.tail + uint64_t(tl.begin / 8) * m.tb);
+                    const uintptr_t a = src & ~uintptr_t(15);
+                    const uint32_t len =
+                        static_cast<uint32_t>(((src + (uint64_t(m.rows) * m.tb + 7) / 8 + 15) & ~uintptr_t(15)) - a);
+                    bulk_g2s(st + L.np_max * L.plane_stride, reinterpret_cast<const void*>(a), len, &full[s]);
+                }
+            }
+        }
+        // drain: the last stages' copies complete before this lane leaves
+        for (uint32_t i = count > L.stages ? count - L.stages : 0; i < count; ++i)
+            if (!mbar_wait(&full[i % L.stages], (i / L.stages) & 1)) { set_status(q.acc, EBI_E_CUDA); break; }
+        return;
+    }
+
+    // ---- consumer warps ----
+    Partial part{0, 0, 0, ~0ull};
+    uint32_t cur = 0xffffffffu;
+    for (uint32_t i = 0; i < count; ++i) {
+        const uint32_t s = i % L.stages, k = i / L.stages;
+        if (!mbar_wait(&full[s], k & 1)) {
+            set_status(q.acc, EBI_E_CUDA);
+            break;
+        }
+        const ScanMeta& m = meta[s];
+        if (m.chunk != cur) {
+            if (cur != 0xffffffffu) flush_partial(q, cur, part);
+            cur = m.chunk;
+        }
+        const uint8_t* st = stages + size_t(s) * L.stage_bytes;
+        if (m.ok && m.np * 8 + m.tb > 32) scan_dispatch<unsigned long long>(q, m, st, L, part);
+        else scan_dispatch<uint32_t>(q, m, st, L, part);
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
+    }
+    if (cur != 0xffffffffu) flush_partial(q, cur, part);
+}
+
 }  // namespace
 
 TileMap buff_tiles(const std::vector<ChunkDesc>& chunks) {
@@ -416,6 +695,42 @@ TileMap buff_tiles(const std::vector<ChunkDesc>& chunks) {
 cudaError_t launch_buff_query(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s) {
     if (n_tiles == 0) return cudaSuccess;
     buff_query_kernel<<<n_tiles, kThreads, 0, s>>>(q, tile_begin);
+    count_launch();
+    return cudaGetLastError();
+}
+
+StageLayout buff_stage_layout(uint32_t np_max, uint32_t tb_max, uint32_t* ctas_per_sm) {
+    StageLayout L{};
+    L.plane_stride = kBuffTileRows + 32;
+    L.np_max = np_max;
+    L.tail_stride = ((kBuffTileRows / 8) * tb_max + 48 + 15) & ~15u;
+    L.stage_bytes = (np_max * L.plane_stride + L.tail_stride + 127) & ~127u;
+    const uint32_t meta = 128 + 8 * static_cast<uint32_t>(sizeof(ScanMeta));  // barriers + up to 8 stages
+    L.data_offset = (meta + 127) & ~127u;
+    const uint32_t budget2 = 110 * 1024, budget1 = 220 * 1024;
+    uint32_t st = (budget2 - L.data_offset) / L.stage_bytes;
+    *ctas_per_sm = 2;
+    if (st < 3) {
+        st = (budget1 - L.data_offset) / L.stage_bytes;
+        *ctas_per_sm = 1;
+    }
+    L.stages = st > 8 ? 8 : (st < 2 ? 2 : st);
+    if (L.stages > 4 && *ctas_per_sm == 2) L.stages = 4;
+    return L;
+}
+
+cudaError_t launch_buff_scan(const QueryParams& q, const BuffChunkInfo* info, uint32_t tile_begin, uint32_t n_tiles,
+                            const StageLayout& L, uint32_t grid, cudaStream_t s) {
+    if (n_tiles == 0) return cudaSuccess;
+    const size_t smem = L.data_offset + size_t(L.stages) * L.stage_bytes;
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(buff_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    buff_scan_kernel<<<grid < n_tiles ? grid : n_tiles, kScanThreads, smem, s>>>(q, info, tile_begin, n_tiles, L);
     count_launch();
     return cudaGetLastError();
 }

@@ -8,6 +8,7 @@
 // and the unmodified file bytes are copied to HBM where they stay.  Every
 // query then runs the codec's kernel over the chunk table and one
 // finalize_kernel that folds the per-chunk results in chunk order.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -81,6 +82,10 @@ struct ebi_column {
     unsigned long long* d_tile_offsets = nullptr;  // n_tiles + 1
     uint64_t* d_scratch_mask = nullptr;            // mask_words
     uint64_t mask_words = 0;
+    // BUFF: header facts per chunk and the scan's shared-memory ring
+    BuffChunkInfo* d_buff = nullptr;
+    StageLayout layout{};
+    uint32_t scan_grid = 0;
     // segment timing (ebi_column_set_timing)
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // query start, scan end, finalize end
@@ -131,6 +136,32 @@ int parse_file(const uint8_t* d, uint64_t len, ebi_column* c) {
         c->chunks[i] = cd;
     }
     return EBI_OK;
+}
+
+// BUFF chunk headers (decoder/chunk_reader/buff/decode.rs:5-17) and the
+// checks every reader of the chunk applies; a failing chunk keeps its status
+// and raises it only when a query reads the chunk.
+std::vector<BuffChunkInfo> parse_buff_headers(const uint8_t* file, const std::vector<ChunkDesc>& chunks) {
+    std::vector<BuffChunkInfo> out(chunks.size());
+    for (size_t i = 0; i < chunks.size(); ++i) {
+        const ChunkDesc& cd = chunks[i];
+        BuffChunkInfo b{};
+        if (cd.flags & kChunkBadGeometry) { b.status = EBI_E_IO; out[i] = b; continue; }
+        if (cd.byte_len < 20) { b.status = EBI_E_UNEXPECTED_END; out[i] = b; continue; }
+        const uint8_t* p = file + cd.byte_off;
+        b.base = static_cast<int64_t>(rd64(p));
+        b.n = rd32(p + 8);
+        b.bits = rd32(p + 12);
+        b.frac = rd32(p + 16);
+        if (b.bits > 64 || b.n != cd.n_rows) { b.status = EBI_E_CORRUPT; out[i] = b; continue; }
+        const uint64_t np = b.bits / 8, tb = b.bits % 8;
+        const uint64_t need = 20 + np * b.n + (uint64_t(b.n) * tb + 7) / 8;
+        if (b.bits > 0 && need > cd.byte_len) { b.status = EBI_E_UNEXPECTED_END; out[i] = b; continue; }
+        b.planes = cd.byte_off + 20;
+        b.tail = b.planes + np * b.n;
+        out[i] = b;
+    }
+    return out;
 }
 
 template <typename T>
@@ -233,7 +264,10 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
             CK(cudaMemsetAsync(reinterpret_cast<uint32_t*>(d_out_mask) + 2 * c->mask_words - 1, 0, 4, s));
     }
     if (d_mask) CK(launch_select_chunks(q, s));
-    if (c->scheme == EBI_BUFF) CK(launch_buff_query(q, tb, tn, s));
+    if (c->scheme == EBI_BUFF) {
+        if (tile_counts) CK(launch_buff_query(q, tb, tn, s));
+        else CK(launch_buff_scan(q, c->d_buff, tb, tn, c->layout, c->scan_grid, s));
+    }
     return EBI_OK;
 }
 
@@ -301,8 +335,22 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     int st = parse_file(file, len, c);
     if (st) { delete c; return st; }
     cudaStream_t s = c->stream;
-    if (c->scheme == EBI_BUFF) c->tiles = buff_tiles(c->chunks);
-    else c->tiles.first_tile.assign(c->n_chunks + 1, 0);
+    std::vector<BuffChunkInfo> binfo;
+    if (c->scheme == EBI_BUFF) {
+        c->tiles = buff_tiles(c->chunks);
+        binfo = parse_buff_headers(file, c->chunks);
+        uint32_t np_max = 0, tb_max = 0;
+        for (const BuffChunkInfo& b : binfo)
+            if (!b.status) { np_max = std::max(np_max, b.bits / 8); tb_max = std::max(tb_max, b.bits % 8); }
+        uint32_t per_sm = 1;
+        c->layout = buff_stage_layout(np_max, tb_max, &per_sm);
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        c->scan_grid = static_cast<uint32_t>(std::max(sms, 1)) * per_sm;
+    } else {
+        c->tiles.first_tile.assign(c->n_chunks + 1, 0);
+    }
     c->mask_words = (c->n_records + 63) / 64;
     if (c->mask_words == 0) c->mask_words = 1;
     st = dev_alloc(&c->d_file, len + kFilePad, s);
@@ -310,6 +358,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st) st = dev_alloc(&c->d_tiles, c->tiles.tiles.size(), s);
     if (!st) st = dev_alloc(&c->d_acc, c->n_chunks, s);
     if (!st) st = dev_alloc(&c->d_res, 1, s);
+    if (!st && !binfo.empty()) st = dev_alloc(&c->d_buff, binfo.size(), s);
     if (!st && cudaMallocHost(&c->h_res, sizeof(QueryResult)) != cudaSuccess) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st) {
         cudaError_t e = cudaMemcpyAsync(c->d_file, file, len, cudaMemcpyHostToDevice, s);
@@ -319,6 +368,8 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         if (e == cudaSuccess && !c->tiles.tiles.empty())
             e = cudaMemcpyAsync(c->d_tiles, c->tiles.tiles.data(), c->tiles.tiles.size() * sizeof(Tile),
                                 cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && !binfo.empty())
+            e = cudaMemcpyAsync(c->d_buff, binfo.data(), binfo.size() * sizeof(BuffChunkInfo), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
         // host sources (chunk table, tiles) must stay alive until the copies ran
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -334,7 +385,7 @@ int ebi_column_close(ebi_column* c) {
     cudaStream_t s = c->stream;
     for (cudaEvent_t e : c->ev) if (e) cudaEventDestroy(e);
     void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
-                    c->d_scratch_mask};
+                    c->d_scratch_mask, c->d_buff};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
     if (c->h_res) cudaFreeHost(c->h_res);
     delete c;

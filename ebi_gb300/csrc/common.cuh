@@ -31,6 +31,25 @@ struct ChunkDesc {
 };
 constexpr uint32_t kChunkBadGeometry = 1;
 
+// BUFF chunk header facts, parsed on the host at open (query independent).
+struct BuffChunkInfo {
+    uint64_t planes;   // file offset of the first byte plane
+    uint64_t tail;     // file offset of the tail plane
+    int64_t base;      // fixed-point base
+    uint32_t n, bits, frac;
+    uint32_t status;   // error to raise when the chunk is read (0: readable)
+};
+
+// Shared-memory ring of the pipelined BUFF scan.
+struct StageLayout {
+    uint32_t stages;        // ring depth
+    uint32_t plane_stride;  // bytes per plane slot
+    uint32_t np_max;        // plane slots per stage
+    uint32_t tail_stride;   // bytes of the tail slot
+    uint32_t stage_bytes;   // np_max * plane_stride + tail_stride
+    uint32_t data_offset;   // start of the stages (after barriers and per-stage metadata)
+};
+
 struct Tile {
     uint32_t chunk;
     uint32_t begin;  // first row (BUFF), first field (RLE) or first segment (XOR) of the tile

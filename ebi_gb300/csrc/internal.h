@@ -26,6 +26,13 @@ constexpr uint32_t kBuffTileRows = 8192;  // 256 threads x 32 rows
 TileMap buff_tiles(const std::vector<ChunkDesc>& chunks);
 // Filter / filter+agg / agg over tiles [tile_begin, tile_begin + n_tiles).
 cudaError_t launch_buff_query(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s);
+// Shared-memory ring for columns whose widest chunk has np_max byte planes
+// and tb_max tail bits; *ctas_per_sm receives the CTAs that fit one SM.
+StageLayout buff_stage_layout(uint32_t np_max, uint32_t tb_max, uint32_t* ctas_per_sm);
+// Pipelined scan (bulk copies into a shared-memory ring): filter without tile
+// counts, filter+agg and agg.  grid = persistent CTAs.
+cudaError_t launch_buff_scan(const QueryParams& q, const BuffChunkInfo* info, uint32_t tile_begin, uint32_t n_tiles,
+                            const StageLayout& L, uint32_t grid, cudaStream_t s);
 // Rows of the bitmask per tile into q.tile_counts[tile - tile_begin].
 cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s);
 // Writes the decoded values of the selected rows at tile_offsets[tile - tile_begin] + rank
