@@ -249,7 +249,7 @@ def main():
 
     def one_step(i):
         flush.fill_(i & 0xFF)  # evicts the column from L2 (not timed)
-        dec.filter_agg(qs[i % 3][1], out=mask)
+        dec.filter_agg(qs[i % 3][1], out=mask, aggregates=("sum",))
         return dec.segmented_execution_times()
 
     for i in range(args.warmup):
@@ -307,7 +307,7 @@ def main():
         ts = time.perf_counter()
         d2 = E.Decoder(host_file, device=str(dev))
         m2 = d2.new_mask()
-        _, s, mn, mx, cnt = d2.filter_agg(qs[i % 3][1], out=m2)
+        _, s, mn, mx, cnt = d2.filter_agg(qs[i % 3][1], out=m2, aggregates=("sum",))
         host_mask.copy_(m2, non_blocking=True)
         torch.cuda.synchronize(dev)
         d2.close()
@@ -327,12 +327,12 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 -> f64",
             "data": "synthetic (seeded numpy, the configuration's shape)",
             "config": {"workload": "BUFF 67,108,864 f64 U[-1000,1000] rounded to 3 dp, 65,536-row chunks, "
-                                   "scale 1000; fused filter+sum/min/max at 1%/10%/50% selectivity",
-                       "rows": N_ROWS, "chunk_rows": CHUNK, "column_bytes": len(data),
+                                   "scale 1000; fused filter (bitmask out) + sum at 1%/10%/50% selectivity",
+                       "rows": args.rows, "chunk_rows": CHUNK, "column_bytes": len(data),
                        "l2": "flushed before every step (256 MiB write)", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "kernel": "buff_query_kernel (fused decode + range filter + bitmask + sum/min/max)",
+                         "kernel": "buff_scan_kernel (fused decode + range filter + bitmask + sum)",
                          "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": round(1e3 * scan_avg_s, 5),
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s"},

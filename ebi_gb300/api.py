@@ -278,18 +278,23 @@ class Decoder:
     def max(self, bitmask=None, chunk_id=None) -> float:
         return self._agg(_native.lib().ebi_max, bitmask, chunk_id, "Decoder::max")
 
-    def filter_agg(self, predicate: Predicate, bitmask=None, chunk_id=None, out=None, want_mask=True):
-        """Decoder::filter then Decoder::{sum, min, max} over its result, one pass."""
+    def filter_agg(self, predicate: Predicate, bitmask=None, chunk_id=None, out=None, want_mask=True,
+                   aggregates=("sum", "min", "max")):
+        """Decoder::filter then Decoder::{sum, min, max} over its result, one pass.
+
+        Only the aggregates named in `aggregates` are computed; the others come back as None."""
         mp, keep = self._mask_in(bitmask)
         if want_mask and out is None:
             out = self.new_mask()
         p = predicate.to_c()
         s, a, b, n = C.c_double(), C.c_double(), C.c_double(), C.c_uint64()
+        ref = lambda x, name: C.byref(x) if name in aggregates else None
         _check(_native.lib().ebi_filter_agg(self._h, C.byref(p), mp, _cid(chunk_id),
                                             C.c_void_p(out.data_ptr()) if want_mask else None,
-                                            C.byref(s), C.byref(a), C.byref(b), C.byref(n), self._sp()),
+                                            ref(s, "sum"), ref(a, "min"), ref(b, "max"), C.byref(n), self._sp()),
                "Decoder::filter_agg")
-        return out, s.value, a.value, b.value, n.value
+        val = lambda x, name: x.value if name in aggregates else None
+        return out, val(s, "sum"), val(a, "min"), val(b, "max"), n.value
 
 
 def kernel_launches() -> int:

@@ -431,12 +431,54 @@ __global__ void __launch_bounds__(kThreads) buff_materialize_kernel(QueryParams 
 constexpr int kScanConsumers = 256;
 constexpr int kScanThreads = kScanConsumers + 32;
 
+// The query folded, per chunk, into one unsigned range test on the delta:
+//   sel = (negate ? ~cmp : cmp) & (use_mask ? bitmask : valid rows)
+// with cmp = lo <= delta <= hi (all rows when `full`, none when `empty`).
+// It reproduces the reference's in-situ decisions, including the shortcuts
+// that return all rows without looking at the input bitmask.
+struct RangeProg {
+    uint64_t lo, hi;
+    uint32_t empty, full, negate, use_mask;
+};
+
+__device__ RangeProg compile_prog(const QueryParams& q, const BuffPred& k, uint32_t bits, bool has_mask) {
+    RangeProg g{0, ~0ull, 0, 0, 0, 0};
+    const uint64_t dmax = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
+    if (q.op == OP_AGG) {  // no predicate: the rows of the bitmask (all rows without one)
+        g.full = 1;
+        g.use_mask = 1;
+        return g;
+    }
+    if (q.pred.kind == EBI_PRED_RANGE) {
+        const bool la = k.lmode == SIDE_ABSENT, ra = k.rmode == SIDE_ABSENT;
+        if (k.lmode == SIDE_NONE || k.rmode == SIDE_NONE) g.empty = 1;
+        if (k.lmode == SIDE_CMP) {
+            if (!k.lincl && k.lthr >= dmax) g.empty = 1;
+            else g.lo = k.lincl ? k.lthr : k.lthr + 1;
+        }
+        if (k.rmode == SIDE_CMP) {
+            if (!k.rincl && k.rthr == 0) g.empty = 1;
+            else g.hi = k.rincl ? k.rthr : k.rthr - 1;
+        }
+        if (!g.empty && g.lo > g.hi) g.empty = 1;
+        g.use_mask = k.lmode == SIDE_CMP || k.rmode == SIDE_CMP || (la && ra);
+    } else {
+        if (k.emode == SIDE_NONE) g.empty = 1;
+        else if (k.emode == SIDE_CMP) { g.lo = g.hi = k.etgt; g.use_mask = 1; }
+        if (q.pred.kind == EBI_PRED_NE) { g.negate = 1; g.use_mask = 1; }
+    }
+    g.full = !g.empty && g.lo == 0 && g.hi >= dmax;
+    g.use_mask = g.use_mask && has_mask;
+    return g;
+}
+
 struct ScanMeta {
     uint64_t row0;      // global row of the tile's first row
-    uint32_t chunk, rows, ok, np, tb;
+    uint32_t chunk, rows, ok, np, tb, bits;
     uint32_t mis[8];    // offset of the tile's first byte inside each plane slot
     uint32_t mis_tail;  // offset of the tile's first tail byte inside the tail slot
     BuffPred pred;
+    RangeProg prog;
 };
 
 __device__ __forceinline__ uint4 lds16(const uint8_t* p) { return *reinterpret_cast<const uint4*>(p); }
@@ -547,6 +589,117 @@ __device__ __forceinline__ void scan_rows(const QueryParams& q, const ScanMeta& 
     }
 }
 
+
+// Fast path for chunks of at most 32 bits.  Each lane handles quads of 4
+// consecutive rows; quad j * 256 + t of the tile belongs to thread t, so the
+// 32 lanes of a warp read consecutive words of every plane (no shared-memory
+// bank conflicts).  Deltas are u32; the predicate is one unsigned range test.
+template <int NP>
+__device__ __forceinline__ void scan_quads(const QueryParams& q, const ScanMeta& m, const uint8_t* stage,
+                                           const StageLayout& L, Partial& part) {
+    const uint32_t t = threadIdx.x, lane = t & 31;
+    const bool has_mask = q.in_mask != nullptr;
+    const bool want_count = q.op == OP_FILTER_AGG || q.op == OP_AGG;
+    const bool store = (q.op == OP_FILTER || q.op == OP_FILTER_AGG) && q.out_mask;
+    const RangeProg& g = m.prog;
+    const uint32_t tb = m.tb, fmask = (1u << tb) - 1u;
+    const uint32_t lo = static_cast<uint32_t>(g.lo), span = static_cast<uint32_t>(g.hi - g.lo);
+    const bool test = !(g.empty || g.full);
+    const bool need_d = test || (q.agg && want_count);
+    const uint32_t* slot[4];
+    uint32_t rsh[4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        const uint32_t mis = p < NP ? m.mis[p] : 0;
+        slot[p] = reinterpret_cast<const uint32_t*>(stage + p * L.plane_stride + (mis & ~3u));
+        rsh[p] = 8 * (mis & 3);
+    }
+    const uint32_t* tslot = reinterpret_cast<const uint32_t*>(stage + L.np_max * L.plane_stride);
+    const uint32_t tbit0 = 8 * m.mis_tail;
+    uint32_t s32 = 0, mx = 0, mn = ~0u, cnt = 0;
+    bool wide_sum = m.bits > 27;
+    unsigned long long s64 = 0;
+#pragma unroll 2
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t qd = j * kScanConsumers + t;  // quad index in the tile
+        const uint32_t r = 4 * qd;                   // first row of the quad in the tile
+        uint32_t nib = 0;
+        if (r < m.rows) {
+            const uint32_t left = m.rows - r;
+            const uint32_t valid = left >= 4 ? 0xfu : ((1u << left) - 1u);
+            uint32_t base_set = valid;
+            if (g.use_mask) base_set &= mask_word(q.in_mask, m.row0 + r, q.n_records) & 0xfu;
+            uint32_t d[4] = {0, 0, 0, 0};
+            if (need_d) {
+                uint32_t w[NP > 0 ? NP : 1];
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    const uint32_t x = slot[p][qd], y = slot[p][qd + 1];
+                    w[p] = __funnelshift_r(x, y, rsh[p]) ^ 0x80808080u;
+                }
+                uint32_t f = 0;
+                if (tb) {
+                    const uint32_t b = tbit0 + 4 * tb * qd;
+                    f = __funnelshift_r(tslot[b >> 5], tslot[(b >> 5) + 1], b & 31);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    uint32_t x = 0;
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) x = (x << 8) | ((w[p] >> (8 * k)) & 0xffu);
+                    d[k] = (x << tb) | ((f >> (tb * k)) & fmask);
+                }
+            }
+            uint32_t cw;
+            if (g.empty) cw = 0;
+            else if (g.full) cw = 0xfu;
+            else {
+                cw = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) cw |= static_cast<uint32_t>(d[k] - lo <= span) << k;
+            }
+            if (g.negate) cw = ~cw;
+            nib = cw & base_set;
+            if (want_count && nib) {
+                cnt += __popc(nib);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if ((nib >> k) & 1u) {
+                        if (wide_sum) s64 += d[k]; else s32 += d[k];
+                        mx = max(mx, d[k]);
+                        mn = min(mn, d[k]);
+                    }
+                }
+            }
+        }
+        if (store) {
+            // 8 lanes hold the 32 rows of one bitmask word: gather their nibbles
+            uint32_t v = nib << (4 * (lane & 7));
+            v |= __shfl_xor_sync(0xffffffffu, v, 1);
+            v |= __shfl_xor_sync(0xffffffffu, v, 2);
+            v |= __shfl_xor_sync(0xffffffffu, v, 4);
+            const uint32_t r0 = 4 * (j * kScanConsumers + (t & ~7u));  // first row of the word in the tile
+            if ((lane & 7) == 0 && r0 < m.rows && (!q.out_atomic || v))
+                store_mask_word(q.out_mask, m.row0 + r0, v, q.out_atomic);
+        }
+    }
+    part.cnt += cnt;
+    part.sum += wide_sum ? s64 : s32;
+    part.mx = mx > part.mx ? mx : part.mx;
+    part.mn = mn < part.mn ? mn : part.mn;
+}
+
+__device__ void scan_fast_dispatch(const QueryParams& q, const ScanMeta& m, const uint8_t* st, const StageLayout& L,
+                                   Partial& part) {
+    switch (m.np) {
+        case 0: scan_quads<0>(q, m, st, L, part); break;
+        case 1: scan_quads<1>(q, m, st, L, part); break;
+        case 2: scan_quads<2>(q, m, st, L, part); break;
+        case 3: scan_quads<3>(q, m, st, L, part); break;
+        default: scan_quads<4>(q, m, st, L, part); break;
+    }
+}
+
 template <typename D>
 __device__ __forceinline__ void scan_dispatch(const QueryParams& q, const ScanMeta& m, const uint8_t* stage,
                                               const StageLayout& L, Partial& part) {
@@ -613,7 +766,9 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
             if (m.ok) {
                 m.np = ci.bits / 8;
                 m.tb = ci.bits % 8;
+                m.bits = ci.bits;
                 compile_pred(q.pred, ci.base, ci.bits, ci.frac, has_mask, m.pred);
+                m.prog = compile_prog(q, m.pred, ci.bits, has_mask);
                 for (uint32_t p = 0; p < m.np; ++p) {
                     const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.planes + uint64_t(p) * ci.n + tl.begin);
                     const uintptr_t a = src & ~uintptr_t(15);
@@ -669,8 +824,9 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
             cur = m.chunk;
         }
         const uint8_t* st = stages + size_t(s) * L.stage_bytes;
-        if (m.ok && m.np * 8 + m.tb > 32) scan_dispatch<unsigned long long>(q, m, st, L, part);
-        else scan_dispatch<uint32_t>(q, m, st, L, part);
+        if (!m.ok) scan_dispatch<uint32_t>(q, m, st, L, part);  // writes zero words only
+        else if (m.bits > 32) scan_dispatch<unsigned long long>(q, m, st, L, part);
+        else scan_fast_dispatch(q, m, st, L, part);
         __syncwarp();
         if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
     }

@@ -186,6 +186,8 @@ QueryParams base_params(const ebi_column* c) {
     q.chunk_id = -1;
     q.precision = c->precision;
     q.scheme = c->scheme;
+    q.agg = AGG_ALL;
+    q.binfo = c->d_buff;
     return q;
 }
 
@@ -244,9 +246,10 @@ int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
 
 // Runs filter / filter+agg / agg over the column.
 int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
-             uint64_t* d_out_mask, unsigned long long* tile_counts, cudaStream_t s) {
+             uint64_t* d_out_mask, unsigned long long* tile_counts, cudaStream_t s, uint32_t agg = AGG_ALL) {
     if (int st = begin_query(c, s)) return st;
     QueryParams q = base_params(c);
+    q.agg = agg;
     q.op = op;
     q.chunk_id = chunk_id;
     q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
@@ -436,9 +439,11 @@ int ebi_filter_agg(ebi_column* c, const ebi_predicate* pred, const uint64_t* d_m
     if (!st) st = check_supported(c);
     if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    st = run_scan(c, OP_FILTER_AGG, pred, d_mask, chunk_id, d_out_mask, nullptr, s);
+    const uint32_t agg = (sum ? AGG_SUM : 0u) | (mn ? AGG_MIN : 0u) | (mx ? AGG_MAX : 0u);
+    st = run_scan(c, OP_FILTER_AGG, pred, d_mask, chunk_id, d_out_mask, nullptr, s, agg);
     if (st) return st;
     QueryParams q = base_params(c);
+    q.agg = agg;
     q.op = OP_FILTER_AGG;
     q.chunk_id = chunk_id;
     q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);

@@ -107,7 +107,11 @@ struct QueryParams {
     unsigned long long* tile_counts;  // per tile
     int32_t precision;         // BUFF controlled precision, < 0: full
     int scheme;
+    uint32_t agg;              // AGG_* aggregates the caller asked for (the count is always kept)
+    const BuffChunkInfo* binfo;  // BUFF: header facts per chunk
 };
+
+enum : uint32_t { AGG_SUM = 1, AGG_MIN = 2, AGG_MAX = 4, AGG_ALL = 7 };
 
 // ---------------------------------------------------------------------------
 // device helpers

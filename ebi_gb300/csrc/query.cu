@@ -2,6 +2,8 @@
 // the chunk-ordered fold of per-chunk results (Decoder's `result += chunk`,
 // `result = result.min(chunk)`, `result = result.max(chunk)`,
 // api/decoder.rs:323-439).
+#include <climits>
+
 #include "internal.h"
 
 namespace ebi {
@@ -80,179 +82,186 @@ __global__ void tile_scan_kernel(const unsigned long long* counts, unsigned long
     if (threadIdx.x == 0) offsets[n] = carry;
 }
 
-struct BuffHdr {
-    int64_t base;
-    uint32_t n, bits, frac;
-};
-__device__ BuffHdr read_buff_hdr(const QueryParams& q, uint32_t c) {
-    const uint8_t* p = q.file + q.chunks[c].byte_off;
-    BuffHdr h;
-    h.base = static_cast<int64_t>(load_u64_unaligned(p));
-    h.n = load_u32_unaligned(p + 8);
-    h.bits = load_u32_unaligned(p + 12);
-    h.frac = load_u32_unaligned(p + 16);
-    return h;
+__device__ __forceinline__ double pow2(int e) {  // 2^e for -1022 <= e <= 1023, exact
+    return __longlong_as_double(static_cast<long long>(uint64_t(1023 + e) << 52));
 }
-__device__ double pow2(uint32_t frac) {  // 2.0f64.powi(frac): exact, +inf past 1023
-    return frac <= 1023 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 + frac) << 52))
-                        : __longlong_as_double(0x7ff0000000000000ll);
+// (double)x / 2^frac exactly as `x as f64 / 2.0f64.powi(frac)` rounds it.
+__device__ __forceinline__ double scale_down(long long x, uint32_t frac) {
+    const double v = static_cast<double>(x);
+    if (frac <= 1022) return v * pow2(-static_cast<int>(frac));
+    return v / (frac <= 1023 ? pow2(1023) : __longlong_as_double(0x7ff0000000000000ll));
 }
 
-// One chunk's contribution, in the reference's arithmetic.
-struct ChunkVal {
-    double sum, mn, mx;
-    long long exact;       // BUFF: the sum as an integer multiple of 2^-frac, when exact
+// One BUFF chunk's contribution in exact integer form: every result of the
+// reference is (integer) as f64 / 2^frac (buff/sum.rs:116, buff/min_max.rs:273-276).
+struct BuffVal {
+    long long sum_fixed;  // sum_with_bitmask's integer before the f64 conversion
+    long long max_fixed, min_fixed;
     uint32_t frac;
-    bool exact_ok;         // |exact| < 2^53 and sum == exact * 2^-frac
-    bool included;
+    bool sum_exact;       // the chunk's f64 sum equals sum_fixed * 2^-frac exactly
 };
 
-__device__ ChunkVal chunk_value(const QueryParams& q, uint32_t c, const ChunkAcc& a) {
-    ChunkVal v;
-    v.included = q.op == OP_FILTER_AGG ? a.count > 0 : a.selected != 0;
-    v.sum = 0.0;
-    v.mn = __longlong_as_double(0x7ff0000000000000ll);
-    v.mx = -v.mn;
-    v.exact = 0; v.frac = 0; v.exact_ok = false;
-    if (!v.included || a.status) { v.included = false; return v; }
-    if (q.scheme == EBI_BUFF) {
-        const BuffHdr h = read_buff_hdr(q, c);
-        const double scale = pow2(h.frac);
-        v.frac = h.frac;
-        const double basev = static_cast<double>(h.base) / scale;
-        const bool has_mask = q.in_mask != nullptr || q.op == OP_FILTER_AGG;
-        if (h.bits == 0) {
-            // sum_with_bitmask: base / scale * number_of_records (buff/sum.rs:81-84)
-            v.sum = basev * static_cast<double>(h.n);
-            v.mn = v.mx = basev;
-            const __int128 p = static_cast<__int128>(h.base) * h.n;
-            v.exact_ok = p < (static_cast<__int128>(1) << 53) && p > -(static_cast<__int128>(1) << 53) &&
-                         h.base < (1ll << 53) && h.base > -(1ll << 53) && h.frac <= 1022;
-            v.exact = static_cast<long long>(p);
-        } else {
-            const unsigned long long cnt = a.count;
-            const long long s = static_cast<long long>(a.isum + static_cast<unsigned long long>(h.base) * cnt);
-            v.sum = static_cast<double>(s) / scale;
-            v.exact = s;
-            v.exact_ok = s < (1ll << 53) && s > -(1ll << 53) && h.frac <= 1022;
-            v.mx = static_cast<double>(static_cast<long long>(static_cast<unsigned long long>(h.base) + a.dmax)) / scale;
-            // min_without_bitmask returns base / scale (buff/min_max.rs:435-460)
-            v.mn = has_mask ? static_cast<double>(static_cast<long long>(static_cast<unsigned long long>(h.base) + a.dmin)) / scale
-                            : basev;
-        }
+__device__ BuffVal buff_value(const QueryParams& q, uint32_t c, const ChunkAcc& a) {
+    const BuffChunkInfo ci = q.binfo[c];
+    const bool has_mask = q.in_mask != nullptr || q.op == OP_FILTER_AGG;
+    BuffVal v;
+    v.frac = ci.frac;
+    constexpr long long kExact = 1ll << 53;
+    if (ci.bits == 0) {
+        // base / scale * number_of_records (buff/sum.rs:81-84)
+        const __int128 p = static_cast<__int128>(ci.base) * ci.n;
+        v.sum_fixed = static_cast<long long>(p);
+        v.sum_exact = p < kExact && p > -kExact && ci.base < kExact && ci.base > -kExact && ci.frac <= 1022;
+        v.max_fixed = v.min_fixed = ci.base;
     } else {
-        v.sum = a.fsum_hi;
-        v.mn = a.fmin;
-        v.mx = a.fmax;
+        v.sum_fixed = static_cast<long long>(a.isum + static_cast<unsigned long long>(ci.base) * a.count);
+        v.sum_exact = v.sum_fixed < kExact && v.sum_fixed > -kExact && ci.frac <= 1022;
+        v.max_fixed = static_cast<long long>(static_cast<unsigned long long>(ci.base) + a.dmax);
+        // min_without_bitmask returns base / scale (buff/min_max.rs:435-460)
+        v.min_fixed = has_mask ? static_cast<long long>(static_cast<unsigned long long>(ci.base) + a.dmin) : ci.base;
     }
     return v;
 }
+__device__ double buff_chunk_sum_f64(const BuffVal& v, uint32_t c, const QueryParams& q) {
+    const BuffChunkInfo ci = q.binfo[c];
+    if (ci.bits == 0) return scale_down(ci.base, ci.frac) * static_cast<double>(ci.n);
+    return scale_down(v.sum_fixed, v.frac);
+}
+
+__device__ __forceinline__ bool chunk_included(const QueryParams& q, const ChunkAcc& a) {
+    if (a.status) return false;
+    return q.op == OP_FILTER_AGG ? a.count > 0 : a.selected != 0;
+}
+
+template <typename T, typename F>
+__device__ __forceinline__ T block_reduce(T v, F op, T* sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < static_cast<int>(blockDim.x >> 5) ? sh[lane] : sh[0];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) sh[0] = v;
+    }
+    __syncthreads();
+    return sh[0];
+}
 
 __global__ void __launch_bounds__(kFinThreads) finalize_kernel(QueryParams q, QueryResult* res) {
-    __shared__ uint32_t s_bad[32];
-    __shared__ double s_mn[32], s_mx[32], s_hi[32], s_lo[32];
-    __shared__ unsigned long long s_cnt[32], s_abs[32];
-    __shared__ long long s_exact[32];
-    __shared__ uint32_t s_fracmin[32], s_fracmax[32], s_allexact[32];
+    __shared__ unsigned long long sh_u[32];
+    __shared__ long long sh_i[32];
+    __shared__ double sh_h[32], sh_l[32];
     const uint32_t nc = q.n_chunks;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
 
     uint32_t bad = 0xffffffffu;
+    unsigned long long cnt = 0;
+    // integer facts (BUFF)
+    long long ssum = 0, smax = LLONG_MIN, smin = LLONG_MAX;
+    unsigned long long sabs = 0;
+    uint32_t fracmin = 0xffffffffu, fracmax = 0, exact = 1, any = 0;
+    // floating facts (other codecs)
     double mn = inf, mx = -inf, hi = 0.0, lo = 0.0;
-    unsigned long long cnt = 0, sabs = 0;
-    long long sexact = 0;
-    uint32_t fracmin = 0xffffffffu, fracmax = 0, allexact = 1;
-    // Each thread folds a contiguous run of chunks in order; runs are then
-    // combined in thread order, so the combination order is fixed.
+    // each thread folds a contiguous run of chunks, runs combine in thread order
     const uint32_t per = (nc + kFinThreads - 1) / kFinThreads;
-    const uint32_t c0 = threadIdx.x * per, c1 = min(nc, c0 + per);
+    const uint32_t c0 = min(nc, threadIdx.x * per), c1 = min(nc, c0 + per);
     for (uint32_t c = c0; c < c1; ++c) {
         const ChunkAcc a = q.acc[c];
         if (a.status && bad == 0xffffffffu) bad = c;
-        const ChunkVal v = chunk_value(q, c, a);
-        if (!v.included) continue;
+        if (!chunk_included(q, a)) continue;
+        any = 1;
         cnt += a.count;
-        mn = fmin(mn, v.mn);
-        mx = fmax(mx, v.mx);
         if (q.scheme == EBI_BUFF) {
-            allexact &= v.exact_ok;
-            if (v.exact_ok) {
-                sexact += v.exact;
-                const unsigned long long ab = static_cast<unsigned long long>(v.exact < 0 ? -v.exact : v.exact);
-                sabs = sabs + ab < sabs || sabs + ab > (1ull << 62) ? (1ull << 62) : sabs + ab;
-            }
+            const BuffVal v = buff_value(q, c, a);
+            exact &= v.sum_exact;
+            ssum += v.sum_fixed;
+            const unsigned long long ab = static_cast<unsigned long long>(v.sum_fixed < 0 ? -v.sum_fixed : v.sum_fixed);
+            sabs = (sabs + ab < sabs || sabs + ab > (1ull << 62)) ? (1ull << 62) : sabs + ab;
+            smax = max(smax, v.max_fixed);
+            smin = min(smin, v.min_fixed);
             fracmin = min(fracmin, v.frac);
             fracmax = max(fracmax, v.frac);
         } else {
-            dd_add(hi, lo, q.acc[c].fsum_hi, q.acc[c].fsum_lo);
+            mn = fmin(mn, a.fmin);
+            mx = fmax(mx, a.fmax);
+            dd_add(hi, lo, a.fsum_hi, a.fsum_lo);
         }
     }
-    // warp reduction (lane order = chunk order)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        bad = min(bad, __shfl_xor_sync(0xffffffffu, bad, o));
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-        {
-            const unsigned long long x = __shfl_xor_sync(0xffffffffu, sabs, o);
-            sabs = sabs + x > (1ull << 62) ? (1ull << 62) : sabs + x;
-        }
-        sexact += __shfl_xor_sync(0xffffffffu, sexact, o);
-        fracmin = min(fracmin, __shfl_xor_sync(0xffffffffu, fracmin, o));
-        fracmax = max(fracmax, __shfl_xor_sync(0xffffffffu, fracmax, o));
-        allexact &= __shfl_xor_sync(0xffffffffu, allexact, o);
-    }
-    // double-double partial sums combined in a fixed tree over lanes
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const double oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
-        if ((lane & (2 * o - 1)) == 0) dd_add(hi, lo, oh, ol);
-    }
-    if (lane == 0) {
-        s_bad[wid] = bad; s_mn[wid] = mn; s_mx[wid] = mx; s_hi[wid] = hi; s_lo[wid] = lo;
-        s_cnt[wid] = cnt; s_abs[wid] = sabs; s_exact[wid] = sexact;
-        s_fracmin[wid] = fracmin; s_fracmax[wid] = fracmax; s_allexact[wid] = allexact;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        QueryResult r;
-        r.status = 0; r.bad_chunk = 0xffffffffu;
-        double tmn = inf, tmx = -inf, th = 0.0, tl = 0.0;
-        unsigned long long tc = 0, tabs = 0;
-        long long tex = 0;
-        uint32_t fmn = 0xffffffffu, fmx = 0, ae = 1;
-        for (int w = 0; w < kFinThreads / 32; ++w) {
-            if (s_bad[w] < r.bad_chunk) r.bad_chunk = s_bad[w];
-            tmn = fmin(tmn, s_mn[w]); tmx = fmax(tmx, s_mx[w]);
-            dd_add(th, tl, s_hi[w], s_lo[w]);
-            tc += s_cnt[w]; tex += s_exact[w];
-            tabs = tabs + s_abs[w] > (1ull << 62) ? (1ull << 62) : tabs + s_abs[w];
-            fmn = min(fmn, s_fracmin[w]); fmx = max(fmx, s_fracmax[w]); ae &= s_allexact[w];
-        }
-        if (r.bad_chunk != 0xffffffffu) r.status = q.acc[r.bad_chunk].status;
-        r.min = tmn; r.max = tmx; r.count = tc;
-        if (q.scheme == EBI_BUFF) {
-            if (tc == 0 && fmn == 0xffffffffu) {
-                r.sum = 0.0;
-            } else if (ae && fmn == fmx && tabs < (1ull << 53)) {
-                // Every chunk sum and every prefix of the chunk-ordered fold is an
-                // exact multiple of 2^-frac below 2^53 ulps: the sequential fold
-                // of the reference is exact, so it equals the exact total.
-                r.sum = static_cast<double>(tex) / pow2(fmn);
-            } else {
-                // the reference's sequential `result += chunk_sum`
-                double s = 0.0;
-                for (uint32_t c = 0; c < nc; ++c) {
-                    const ChunkVal v = chunk_value(q, c, q.acc[c]);
-                    if (v.included) s += v.sum;
+    bad = block_reduce<unsigned long long>(bad, [](unsigned long long x, unsigned long long y) { return x < y ? x : y; }, sh_u);
+    cnt = block_reduce<unsigned long long>(cnt, [](unsigned long long x, unsigned long long y) { return x + y; }, sh_u);
+    any = static_cast<uint32_t>(block_reduce<unsigned long long>(any, [](unsigned long long x, unsigned long long y) { return x | y; }, sh_u));
+    QueryResult r;
+    r.status = 0;
+    r.bad_chunk = static_cast<uint32_t>(bad);
+    r.count = cnt;
+    if (q.scheme == EBI_BUFF) {
+        ssum = block_reduce<long long>(ssum, [](long long x, long long y) { return x + y; }, sh_i);
+        smax = block_reduce<long long>(smax, [](long long x, long long y) { return x > y ? x : y; }, sh_i);
+        smin = block_reduce<long long>(smin, [](long long x, long long y) { return x < y ? x : y; }, sh_i);
+        sabs = block_reduce<unsigned long long>(sabs, [](unsigned long long x, unsigned long long y) {
+            return x + y > (1ull << 62) ? (1ull << 62) : x + y; }, sh_u);
+        exact = static_cast<uint32_t>(block_reduce<unsigned long long>(exact, [](unsigned long long x, unsigned long long y) { return x & y; }, sh_u));
+        fracmin = static_cast<uint32_t>(block_reduce<unsigned long long>(fracmin, [](unsigned long long x, unsigned long long y) { return x < y ? x : y; }, sh_u));
+        fracmax = static_cast<uint32_t>(block_reduce<unsigned long long>(fracmax, [](unsigned long long x, unsigned long long y) { return x > y ? x : y; }, sh_u));
+        if (threadIdx.x == 0) {
+            if (!any) {
+                r.sum = 0.0; r.min = inf; r.max = -inf;
+            } else if (fracmin == fracmax) {
+                // Every chunk value is integer * 2^-frac: min and max convert once.
+                r.max = scale_down(smax, fracmin);
+                r.min = scale_down(smin, fracmin);
+                if (exact && sabs < (1ull << 53)) {
+                    // Each chunk sum and every prefix of the chunk-ordered fold is
+                    // an exact multiple of 2^-frac below 2^53 of them, so the
+                    // reference's sequential f64 fold is exact: it equals the total.
+                    r.sum = scale_down(ssum, fracmin);
+                } else {
+                    double s = 0.0;  // the reference's sequential `result += chunk_sum`
+                    for (uint32_t c = 0; c < nc; ++c) {
+                        const ChunkAcc a = q.acc[c];
+                        if (chunk_included(q, a)) s += buff_chunk_sum_f64(buff_value(q, c, a), c, q);
+                    }
+                    r.sum = s;
                 }
-                r.sum = s;
+            } else {
+                double s = 0.0, a1 = inf, b1 = -inf;
+                for (uint32_t c = 0; c < nc; ++c) {
+                    const ChunkAcc a = q.acc[c];
+                    if (!chunk_included(q, a)) continue;
+                    const BuffVal v = buff_value(q, c, a);
+                    s += buff_chunk_sum_f64(v, c, q);
+                    a1 = fmin(a1, scale_down(v.min_fixed, v.frac));
+                    b1 = fmax(b1, scale_down(v.max_fixed, v.frac));
+                }
+                r.sum = s; r.min = a1; r.max = b1;
             }
-        } else {
-            r.sum = th + tl;
         }
+    } else {
+        mn = block_reduce<double>(mn, [](double x, double y) { return fmin(x, y); }, sh_h);
+        mx = block_reduce<double>(mx, [](double x, double y) { return fmax(x, y); }, sh_h);
+        // double-double partial sums in a fixed tree (lane order = chunk order)
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
+            if ((lane & (2 * o - 1)) == 0) dd_add(hi, lo, oh, ol);
+        }
+        if (lane == 0) { sh_h[wid] = hi; sh_l[wid] = lo; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double th = 0.0, tl = 0.0;
+            for (int w = 0; w < kFinThreads / 32; ++w) dd_add(th, tl, sh_h[w], sh_l[w]);
+            r.sum = th + tl;
+            r.min = mn;
+            r.max = mx;
+        }
+    }
+    if (threadIdx.x == 0) {
+        if (r.bad_chunk != 0xffffffffu) r.status = q.acc[r.bad_chunk].status;
         *res = r;
     }
     __syncthreads();
