@@ -446,7 +446,7 @@ __device__ RangeProg compile_prog(const QueryParams& q, const BuffPred& k, uint3
     const uint64_t dmax = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
     if (q.op == OP_AGG) {  // no predicate: the rows of the bitmask (all rows without one)
         g.full = 1;
-        g.use_mask = 1;
+        g.use_mask = has_mask;
         return g;
     }
     if (q.pred.kind == EBI_PRED_RANGE) {
@@ -628,7 +628,7 @@ __device__ __forceinline__ void scan_quads(const QueryParams& q, const ScanMeta&
             const uint32_t left = m.rows - r;
             const uint32_t valid = left >= 4 ? 0xfu : ((1u << left) - 1u);
             uint32_t base_set = valid;
-            if (g.use_mask) base_set &= mask_word(q.in_mask, m.row0 + r, q.n_records) & 0xfu;
+            if (g.use_mask && has_mask) base_set &= mask_word(q.in_mask, m.row0 + r, q.n_records) & 0xfu;
             uint32_t d[4] = {0, 0, 0, 0};
             if (need_d) {
                 uint32_t w[NP > 0 ? NP : 1];
