@@ -590,34 +590,36 @@ __device__ __forceinline__ void scan_rows(const QueryParams& q, const ScanMeta& 
 }
 
 
-// Fast path for chunks of at most 32 bits.  Each lane handles quads of 4
+// Fast path for chunks of 8 to 32 bits.  Each lane handles quads of 4
 // consecutive rows; quad j * 256 + t of the tile belongs to thread t, so the
 // 32 lanes of a warp read consecutive words of every plane (no shared-memory
-// bank conflicts).  Deltas are u32; the predicate is one unsigned range test.
-template <int NP>
+// bank conflicts).  Deltas are u32, assembled with byte permutes; the
+// predicate is one unsigned range test per row; the loop is straight-line.
+template <int NP, int TB, bool SUM, bool MINMAX>
 __device__ __forceinline__ void scan_quads(const QueryParams& q, const ScanMeta& m, const uint8_t* stage,
                                            const StageLayout& L, Partial& part) {
+    static_assert(NP >= 1 && NP <= 4 && NP * 8 + TB <= 32, "u32 deltas");
+    constexpr bool kSum32 = NP * 8 + TB <= 27;  // 32 rows of deltas fit a u32 sum
     const uint32_t t = threadIdx.x, lane = t & 31;
     const bool has_mask = q.in_mask != nullptr;
-    const bool want_count = q.op == OP_FILTER_AGG || q.op == OP_AGG;
     const bool store = (q.op == OP_FILTER || q.op == OP_FILTER_AGG) && q.out_mask;
     const RangeProg& g = m.prog;
-    const uint32_t tb = m.tb, fmask = (1u << tb) - 1u;
     const uint32_t lo = static_cast<uint32_t>(g.lo), span = static_cast<uint32_t>(g.hi - g.lo);
     const bool test = !(g.empty || g.full);
-    const bool need_d = test || (q.agg && want_count);
-    const uint32_t* slot[4];
-    uint32_t rsh[4];
+    const uint32_t fixed_cw = g.full ? 0xfu : 0u;
+    const uint32_t neg = g.negate ? 0xfu : 0u;
+    const bool use_mask = g.use_mask && has_mask;
+    const uint32_t* slot[NP];
+    uint32_t rsh[NP];
 #pragma unroll
-    for (int p = 0; p < 4; ++p) {
-        const uint32_t mis = p < NP ? m.mis[p] : 0;
-        slot[p] = reinterpret_cast<const uint32_t*>(stage + p * L.plane_stride + (mis & ~3u));
-        rsh[p] = 8 * (mis & 3);
+    for (int p = 0; p < NP; ++p) {
+        slot[p] = reinterpret_cast<const uint32_t*>(stage + p * L.plane_stride + (m.mis[p] & ~3u));
+        rsh[p] = 8 * (m.mis[p] & 3);
     }
     const uint32_t* tslot = reinterpret_cast<const uint32_t*>(stage + L.np_max * L.plane_stride);
     const uint32_t tbit0 = 8 * m.mis_tail;
-    uint32_t s32 = 0, mx = 0, mn = ~0u, cnt = 0;
-    bool wide_sum = m.bits > 27;
+    uint32_t cnt = 0, mx = 0, mn = ~0u;
+    uint32_t s32 = 0;
     unsigned long long s64 = 0;
 #pragma unroll 2
     for (int j = 0; j < 8; ++j) {
@@ -627,78 +629,102 @@ __device__ __forceinline__ void scan_quads(const QueryParams& q, const ScanMeta&
         if (r < m.rows) {
             const uint32_t left = m.rows - r;
             const uint32_t valid = left >= 4 ? 0xfu : ((1u << left) - 1u);
-            uint32_t base_set = valid;
-            if (g.use_mask && has_mask) base_set &= mask_word(q.in_mask, m.row0 + r, q.n_records) & 0xfu;
-            uint32_t d[4] = {0, 0, 0, 0};
-            if (need_d) {
-                uint32_t w[NP > 0 ? NP : 1];
+            uint32_t w[NP];
 #pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    const uint32_t x = slot[p][qd], y = slot[p][qd + 1];
-                    w[p] = __funnelshift_r(x, y, rsh[p]) ^ 0x80808080u;
-                }
-                uint32_t f = 0;
-                if (tb) {
-                    const uint32_t b = tbit0 + 4 * tb * qd;
-                    f = __funnelshift_r(tslot[b >> 5], tslot[(b >> 5) + 1], b & 31);
-                }
+            for (int p = 0; p < NP; ++p) w[p] = __funnelshift_r(slot[p][qd], slot[p][qd + 1], rsh[p]) ^ 0x80808080u;
+            uint32_t v[4];
+            if constexpr (NP == 1) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) v[k] = __byte_perm(w[0], 0u, 0x4440u | k);
+            } else if constexpr (NP == 2) {
+                const uint32_t P = __byte_perm(w[1], w[0], 0x5140u), Q = __byte_perm(w[1], w[0], 0x7362u);
+                v[0] = P & 0xffffu; v[1] = P >> 16; v[2] = Q & 0xffffu; v[3] = Q >> 16;
+            } else {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     uint32_t x = 0;
 #pragma unroll
                     for (int p = 0; p < NP; ++p) x = (x << 8) | ((w[p] >> (8 * k)) & 0xffu);
-                    d[k] = (x << tb) | ((f >> (tb * k)) & fmask);
+                    v[k] = x;
                 }
             }
-            uint32_t cw;
-            if (g.empty) cw = 0;
-            else if (g.full) cw = 0xfu;
-            else {
-                cw = 0;
+            uint32_t d[4];
+            if constexpr (TB > 0) {
+                const uint32_t b = tbit0 + 4 * TB * qd;
+                const uint32_t f = __funnelshift_r(tslot[b >> 5], tslot[(b >> 5) + 1], b & 31);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) d[k] = (v[k] << TB) | ((f >> (TB * k)) & ((1u << TB) - 1u));
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) d[k] = v[k];
+            }
+            uint32_t cw = fixed_cw;
+            if (test) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) cw |= static_cast<uint32_t>(d[k] - lo <= span) << k;
             }
-            if (g.negate) cw = ~cw;
-            nib = cw & base_set;
-            if (want_count && nib) {
-                cnt += __popc(nib);
+            uint32_t base_set = valid;
+            if (use_mask) base_set &= mask_word(q.in_mask, m.row0 + r, q.n_records);
+            nib = (cw ^ neg) & base_set;
+            cnt += __popc(nib);
+            if constexpr (SUM) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    if ((nib >> k) & 1u) {
-                        if (wide_sum) s64 += d[k]; else s32 += d[k];
-                        mx = max(mx, d[k]);
-                        mn = min(mn, d[k]);
-                    }
+                    const uint32_t x = ((nib >> k) & 1u) ? d[k] : 0u;
+                    if constexpr (kSum32) s32 += x; else s64 += x;
+                }
+            }
+            if constexpr (MINMAX) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const bool on = (nib >> k) & 1u;
+                    mx = max(mx, on ? d[k] : 0u);
+                    mn = min(mn, on ? d[k] : ~0u);
                 }
             }
         }
         if (store) {
             // 8 lanes hold the 32 rows of one bitmask word: gather their nibbles
-            uint32_t v = nib << (4 * (lane & 7));
-            v |= __shfl_xor_sync(0xffffffffu, v, 1);
-            v |= __shfl_xor_sync(0xffffffffu, v, 2);
-            v |= __shfl_xor_sync(0xffffffffu, v, 4);
+            uint32_t x = nib << (4 * (lane & 7));
+            x |= __shfl_xor_sync(0xffffffffu, x, 1);
+            x |= __shfl_xor_sync(0xffffffffu, x, 2);
+            x |= __shfl_xor_sync(0xffffffffu, x, 4);
             const uint32_t r0 = 4 * (j * kScanConsumers + (t & ~7u));  // first row of the word in the tile
-            if ((lane & 7) == 0 && r0 < m.rows && (!q.out_atomic || v))
-                store_mask_word(q.out_mask, m.row0 + r0, v, q.out_atomic);
+            if ((lane & 7) == 0 && r0 < m.rows && (!q.out_atomic || x))
+                store_mask_word(q.out_mask, m.row0 + r0, x, q.out_atomic);
         }
     }
-    part.cnt += cnt;
-    part.sum += wide_sum ? s64 : s32;
-    part.mx = mx > part.mx ? mx : part.mx;
-    part.mn = mn < part.mn ? mn : part.mn;
-}
-
-__device__ void scan_fast_dispatch(const QueryParams& q, const ScanMeta& m, const uint8_t* st, const StageLayout& L,
-                                   Partial& part) {
-    switch (m.np) {
-        case 0: scan_quads<0>(q, m, st, L, part); break;
-        case 1: scan_quads<1>(q, m, st, L, part); break;
-        case 2: scan_quads<2>(q, m, st, L, part); break;
-        case 3: scan_quads<3>(q, m, st, L, part); break;
-        default: scan_quads<4>(q, m, st, L, part); break;
+    if (q.op == OP_FILTER_AGG || q.op == OP_AGG) {
+        part.cnt += cnt;
+        part.sum += kSum32 ? s32 : s64;
+        part.mx = mx > part.mx ? mx : part.mx;
+        part.mn = mn < part.mn ? mn : part.mn;
     }
 }
+
+template <int NP, int TB>
+__device__ __forceinline__ void scan_quads_agg(const QueryParams& q, const ScanMeta& m, const uint8_t* st,
+                                               const StageLayout& L, Partial& part) {
+    const bool agg = q.op == OP_FILTER_AGG || q.op == OP_AGG;
+    const bool sum = agg && (q.agg & AGG_SUM), mm = agg && (q.agg & (AGG_MIN | AGG_MAX));
+    if (mm) scan_quads<NP, TB, true, true>(q, m, st, L, part);
+    else if (sum) scan_quads<NP, TB, true, false>(q, m, st, L, part);
+    else scan_quads<NP, TB, false, false>(q, m, st, L, part);
+}
+
+#define EBI_Q(NP, TB) case NP * 8 + TB: scan_quads_agg<NP, TB>(q, m, st, L, part); return true;
+// Chunks of 8..32 bits; false for the others (they take the generic path).
+__device__ bool scan_fast_dispatch(const QueryParams& q, const ScanMeta& m, const uint8_t* st, const StageLayout& L,
+                                   Partial& part) {
+    switch (m.bits) {
+        EBI_Q(1, 0) EBI_Q(1, 1) EBI_Q(1, 2) EBI_Q(1, 3) EBI_Q(1, 4) EBI_Q(1, 5) EBI_Q(1, 6) EBI_Q(1, 7)
+        EBI_Q(2, 0) EBI_Q(2, 1) EBI_Q(2, 2) EBI_Q(2, 3) EBI_Q(2, 4) EBI_Q(2, 5) EBI_Q(2, 6) EBI_Q(2, 7)
+        EBI_Q(3, 0) EBI_Q(3, 1) EBI_Q(3, 2) EBI_Q(3, 3) EBI_Q(3, 4) EBI_Q(3, 5) EBI_Q(3, 6) EBI_Q(3, 7)
+        EBI_Q(4, 0)
+        default: return false;
+    }
+}
+#undef EBI_Q
 
 template <typename D>
 __device__ __forceinline__ void scan_dispatch(const QueryParams& q, const ScanMeta& m, const uint8_t* stage,
@@ -826,7 +852,7 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
         const uint8_t* st = stages + size_t(s) * L.stage_bytes;
         if (!m.ok) scan_dispatch<uint32_t>(q, m, st, L, part);  // writes zero words only
         else if (m.bits > 32) scan_dispatch<unsigned long long>(q, m, st, L, part);
-        else scan_fast_dispatch(q, m, st, L, part);
+        else if (!scan_fast_dispatch(q, m, st, L, part)) scan_dispatch<uint32_t>(q, m, st, L, part);
         __syncwarp();
         if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
     }
