@@ -17,6 +17,8 @@
 // and max are exact via the deltas (buff/min_max.rs).
 #include "internal.h"
 #include "tma.cuh"
+#include "fold.cuh"
+#include <climits>
 
 namespace ebi {
 namespace {
@@ -473,6 +475,7 @@ __device__ RangeProg compile_prog(const QueryParams& q, const BuffPred& k, uint3
 }
 
 struct ScanMeta {
+    int64_t base;       // the chunk's fixed-point base
     uint64_t row0;      // global row of the tile's first row
     uint32_t chunk, rows, ok, np, tb, bits;
     uint32_t mis[8];    // offset of the tile's first byte inside each plane slot
@@ -504,7 +507,18 @@ struct Partial {
     unsigned long long sum, cnt, mx, mn;
 };
 
-__device__ __forceinline__ void flush_partial(const QueryParams& q, uint32_t chunk, Partial& p) {
+// Running query totals of one warp (kept by lane 0).
+struct WarpTot {
+    unsigned long long sum_fixed, count;
+    double abs_bound;
+    long long max_fixed, min_fixed;
+    unsigned int nonexact;
+};
+
+// Ends a warp's run over one chunk: per-chunk partials (for the chunk-ordered
+// fallback fold) and the warp's exact query totals.
+__device__ __forceinline__ void flush_partial(const QueryParams& q, uint32_t chunk, int64_t base, Partial& p,
+                                              WarpTot& wt) {
     const unsigned long long s = warp_sum(p.sum), c = warp_sum(p.cnt), mx = warp_max_u64(p.mx), mn = warp_min_u64(p.mn);
     if ((threadIdx.x & 31) == 0 && c) {
         ChunkAcc* a = q.acc + chunk;
@@ -512,6 +526,16 @@ __device__ __forceinline__ void flush_partial(const QueryParams& q, uint32_t chu
         atomicAdd(&a->count, c);
         atomicMax(&a->dmax, mx);
         atomicMin(&a->dmin, mn);
+        const __int128 piece = static_cast<__int128>(s) + static_cast<__int128>(base) * static_cast<__int128>(c);
+        const __int128 ap = piece < 0 ? -piece : piece;
+        wt.sum_fixed += static_cast<unsigned long long>(piece);
+        if (ap >= (static_cast<__int128>(1) << 53)) wt.nonexact = 1;
+        else wt.abs_bound += static_cast<double>(static_cast<long long>(ap));
+        wt.count += c;
+        const long long fmax = static_cast<long long>(static_cast<unsigned long long>(base) + mx);
+        const long long fmin = static_cast<long long>(static_cast<unsigned long long>(base) + mn);
+        wt.max_fixed = fmax > wt.max_fixed ? fmax : wt.max_fixed;
+        wt.min_fixed = fmin < wt.min_fixed ? fmin : wt.min_fixed;
     }
     p.sum = 0; p.cnt = 0; p.mx = 0; p.mn = ~0ull;
 }
@@ -595,7 +619,7 @@ __device__ __forceinline__ void scan_rows(const QueryParams& q, const ScanMeta& 
 // 32 lanes of a warp read consecutive words of every plane (no shared-memory
 // bank conflicts).  Deltas are u32, assembled with byte permutes; the
 // predicate is one unsigned range test per row; the loop is straight-line.
-template <int NP, int TB, bool SUM, bool MINMAX>
+template <int NP, int TB, bool SUM, bool MINMAX, bool FAST>
 __device__ __forceinline__ void scan_quads(const QueryParams& q, const ScanMeta& m, const uint8_t* stage,
                                            const StageLayout& L, Partial& part) {
     static_assert(NP >= 1 && NP <= 4 && NP * 8 + TB <= 32, "u32 deltas");
@@ -626,9 +650,9 @@ __device__ __forceinline__ void scan_quads(const QueryParams& q, const ScanMeta&
         const uint32_t qd = j * kScanConsumers + t;  // quad index in the tile
         const uint32_t r = 4 * qd;                   // first row of the quad in the tile
         uint32_t nib = 0;
-        if (r < m.rows) {
+        if (FAST || r < m.rows) {
             const uint32_t left = m.rows - r;
-            const uint32_t valid = left >= 4 ? 0xfu : ((1u << left) - 1u);
+            const uint32_t valid = FAST ? 0xfu : (left >= 4 ? 0xfu : ((1u << left) - 1u));
             uint32_t w[NP];
 #pragma unroll
             for (int p = 0; p < NP; ++p) w[p] = __funnelshift_r(slot[p][qd], slot[p][qd + 1], rsh[p]) ^ 0x80808080u;
@@ -658,6 +682,27 @@ __device__ __forceinline__ void scan_quads(const QueryParams& q, const ScanMeta&
 #pragma unroll
                 for (int k = 0; k < 4; ++k) d[k] = v[k];
             }
+            if constexpr (FAST) {
+                // full tile, no input bitmask, predicate not negated: the range
+                // test itself drives the bitmask bit and the accumulators
+                if (test) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const bool in = d[k] - lo <= span;
+                        nib |= static_cast<uint32_t>(in) << k;
+                        if constexpr (SUM) { if (in) { if constexpr (kSum32) s32 += d[k]; else s64 += d[k]; } }
+                        if constexpr (MINMAX) { if (in) { mx = max(mx, d[k]); mn = min(mn, d[k]); } }
+                    }
+                } else if (g.full) {
+                    nib = 0xfu;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if constexpr (SUM) { if constexpr (kSum32) s32 += d[k]; else s64 += d[k]; }
+                        if constexpr (MINMAX) { mx = max(mx, d[k]); mn = min(mn, d[k]); }
+                    }
+                }
+                cnt += __popc(nib);
+            } else {
             uint32_t cw = fixed_cw;
             if (test) {
 #pragma unroll
@@ -681,6 +726,7 @@ __device__ __forceinline__ void scan_quads(const QueryParams& q, const ScanMeta&
                     mx = max(mx, on ? d[k] : 0u);
                     mn = min(mn, on ? d[k] : ~0u);
                 }
+            }
             }
         }
         if (store) {
@@ -707,9 +753,16 @@ __device__ __forceinline__ void scan_quads_agg(const QueryParams& q, const ScanM
                                                const StageLayout& L, Partial& part) {
     const bool agg = q.op == OP_FILTER_AGG || q.op == OP_AGG;
     const bool sum = agg && (q.agg & AGG_SUM), mm = agg && (q.agg & (AGG_MIN | AGG_MAX));
-    if (mm) scan_quads<NP, TB, true, true>(q, m, st, L, part);
-    else if (sum) scan_quads<NP, TB, true, false>(q, m, st, L, part);
-    else scan_quads<NP, TB, false, false>(q, m, st, L, part);
+    const bool fast = m.rows == kBuffTileRows && !(m.prog.use_mask && q.in_mask) && !m.prog.negate;
+    if (fast) {
+        if (mm) scan_quads<NP, TB, true, true, true>(q, m, st, L, part);
+        else if (sum) scan_quads<NP, TB, true, false, true>(q, m, st, L, part);
+        else scan_quads<NP, TB, false, false, true>(q, m, st, L, part);
+    } else {
+        if (mm) scan_quads<NP, TB, true, true, false>(q, m, st, L, part);
+        else if (sum) scan_quads<NP, TB, true, false, false>(q, m, st, L, part);
+        else scan_quads<NP, TB, false, false, false>(q, m, st, L, part);
+    }
 }
 
 #define EBI_Q(NP, TB) case NP * 8 + TB: scan_quads_agg<NP, TB>(q, m, st, L, part); return true;
@@ -741,8 +794,55 @@ __device__ __forceinline__ void scan_dispatch(const QueryParams& q, const ScanMe
     }
 }
 
+__device__ __forceinline__ void chunk_error(const QueryParams& q, ScanTotals* T, uint32_t c, uint32_t code) {
+    set_status(q.acc + c, code);
+    atomicMin(&T->bad_chunk, c);
+}
+
+// The last CTA's fold of the query totals (chunk-ordered fallback when the
+// exact integer total does not apply).
+__device__ void scan_finalize(const QueryParams& q, const BuffChunkInfo* info, ScanTotals* T, QueryResult* res,
+                              uint32_t frac, bool fast_ok) {
+    __shared__ QueryResult r;
+    if (threadIdx.x == 0) {
+        const ScanTotals t = *T;
+        const double inf = __longlong_as_double(0x7ff0000000000000ll);
+        r.status = 0;
+        r.bad_chunk = t.bad_chunk;
+        if (t.bad_chunk != 0xffffffffu) r.status = q.acc[t.bad_chunk].status;
+        r.count = t.count;
+        r.sum = 0.0; r.min = inf; r.max = -inf;
+        if (fast_ok && !t.nonexact && t.abs_bound < 4503599627370496.0 /* 2^52 */) {
+            // Every chunk sum and every prefix of the chunk-ordered fold is an
+            // exact multiple of 2^-frac below 2^53 of them: the reference's
+            // sequential f64 fold is exact and equals the exact total.
+            if (t.count) {
+                r.sum = fold_scale(static_cast<long long>(t.sum_fixed), frac);
+                r.max = fold_scale(t.max_fixed, frac);
+                r.min = fold_scale(t.min_fixed, frac);
+            }
+        } else {
+            fold_buff_chunks(q, r);
+        }
+        *res = r;
+        T->sum_fixed = 0; T->abs_bound = 0.0; T->count = 0;
+        T->max_fixed = LLONG_MIN; T->min_fixed = LLONG_MAX;
+        T->done = 0; T->bad_chunk = 0xffffffffu; T->nonexact = 0;
+    }
+    __syncthreads();
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    for (uint32_t c = threadIdx.x; c < q.n_chunks; c += blockDim.x) {
+        ChunkAcc a = {};
+        a.dmin = ~0ull;
+        a.fmin = inf;
+        a.fmax = -inf;
+        q.acc[c] = a;
+    }
+}
+
 __global__ void __launch_bounds__(kScanThreads, 2)
-buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, uint32_t n_tiles, StageLayout L) {
+buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, uint32_t n_tiles, StageLayout L,
+                 ScanTotals* T, QueryResult* res, uint32_t frac, uint32_t fast_ok) {
     extern __shared__ __align__(128) uint8_t smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);
     uint64_t* empty = full + L.stages;
@@ -762,14 +862,13 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
     __syncthreads();
     const bool has_mask = q.in_mask != nullptr;
 
-    if (threadIdx.x >= kScanConsumers) {
-        // ---- producer warp (one lane issues) ----
-        if (threadIdx.x != kScanConsumers) return;
+    if (threadIdx.x == kScanConsumers) {
+        // ---- producer: one lane of warp 8 issues; the other lanes wait at the epilogue ----
         for (uint32_t i = 0; i < count; ++i) {
             const uint32_t s = i % L.stages, k = i / L.stages;
             if (k > 0 && !mbar_wait(&empty[s], (k - 1) & 1)) {
-                set_status(q.acc, EBI_E_CUDA);
-                return;  // consumers stopped; nothing of this stage is in flight
+                chunk_error(q, T, 0, EBI_E_CUDA);
+                break;  // consumers stopped; nothing of this stage is in flight
             }
             const Tile tl = q.tiles[tile_base + t_first + i];
             const uint32_t c = tl.chunk;
@@ -780,9 +879,10 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
                                            : (q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
             if (selected && tl.begin == 0) {
                 if (!has_mask) q.acc[c].selected = 1;
-                if (ci.status) set_status(q.acc + c, ci.status);
+                if (ci.status) chunk_error(q, T, c, ci.status);
             }
             m.chunk = c;
+            m.base = ci.base;
             m.row0 = cd.row_off + tl.begin;
             m.rows = min(kBuffTileRows, cd.n_rows - tl.begin);
             m.ok = selected && ci.status == 0;
@@ -831,23 +931,26 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
         }
         // drain: the last stages' copies complete before this lane leaves
         for (uint32_t i = count > L.stages ? count - L.stages : 0; i < count; ++i)
-            if (!mbar_wait(&full[i % L.stages], (i / L.stages) & 1)) { set_status(q.acc, EBI_E_CUDA); break; }
-        return;
+            if (!mbar_wait(&full[i % L.stages], (i / L.stages) & 1)) { chunk_error(q, T, 0, EBI_E_CUDA); break; }
     }
-
+    __shared__ WarpTot wtot[kScanConsumers / 32];
+    if (threadIdx.x < kScanConsumers) {
     // ---- consumer warps ----
     Partial part{0, 0, 0, ~0ull};
+    WarpTot wt{0, 0, 0.0, LLONG_MIN, LLONG_MAX, 0};
     uint32_t cur = 0xffffffffu;
+    int64_t cur_base = 0;
     for (uint32_t i = 0; i < count; ++i) {
         const uint32_t s = i % L.stages, k = i / L.stages;
         if (!mbar_wait(&full[s], k & 1)) {
-            set_status(q.acc, EBI_E_CUDA);
+            chunk_error(q, T, 0, EBI_E_CUDA);
             break;
         }
         const ScanMeta& m = meta[s];
         if (m.chunk != cur) {
-            if (cur != 0xffffffffu) flush_partial(q, cur, part);
+            if (cur != 0xffffffffu) flush_partial(q, cur, cur_base, part, wt);
             cur = m.chunk;
+            cur_base = m.base;
         }
         const uint8_t* st = stages + size_t(s) * L.stage_bytes;
         if (!m.ok) scan_dispatch<uint32_t>(q, m, st, L, part);  // writes zero words only
@@ -856,7 +959,37 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
         __syncwarp();
         if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
     }
-    if (cur != 0xffffffffu) flush_partial(q, cur, part);
+    if (cur != 0xffffffffu) flush_partial(q, cur, cur_base, part, wt);
+    if ((threadIdx.x & 31) == 0) wtot[threadIdx.x >> 5] = wt;
+    }
+    // ---- CTA totals, then the last CTA folds the query ----
+    __syncthreads();
+    __shared__ unsigned int s_last;
+    if (threadIdx.x == 0) {
+        WarpTot c{0, 0, 0.0, LLONG_MIN, LLONG_MAX, 0};
+        for (int w = 0; w < kScanConsumers / 32; ++w) {
+            c.sum_fixed += wtot[w].sum_fixed;
+            c.count += wtot[w].count;
+            c.abs_bound += wtot[w].abs_bound;
+            c.max_fixed = wtot[w].max_fixed > c.max_fixed ? wtot[w].max_fixed : c.max_fixed;
+            c.min_fixed = wtot[w].min_fixed < c.min_fixed ? wtot[w].min_fixed : c.min_fixed;
+            c.nonexact |= wtot[w].nonexact;
+        }
+        if (c.count) {
+            atomicAdd(&T->sum_fixed, c.sum_fixed);
+            atomicAdd(&T->count, c.count);
+            atomicAdd(&T->abs_bound, c.abs_bound);
+            atomicMax(&T->max_fixed, c.max_fixed);
+            atomicMin(&T->min_fixed, c.min_fixed);
+            if (c.nonexact) atomicOr(&T->nonexact, 1u);
+        }
+        __threadfence();
+        s_last = atomicAdd(&T->done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    scan_finalize(q, info, T, res, frac, fast_ok != 0);
 }
 
 }  // namespace
@@ -902,7 +1035,8 @@ StageLayout buff_stage_layout(uint32_t np_max, uint32_t tb_max, uint32_t* ctas_p
 }
 
 cudaError_t launch_buff_scan(const QueryParams& q, const BuffChunkInfo* info, uint32_t tile_begin, uint32_t n_tiles,
-                            const StageLayout& L, uint32_t grid, cudaStream_t s) {
+                            const StageLayout& L, uint32_t grid, ScanTotals* T, QueryResult* res, uint32_t frac,
+                            bool fast_ok, cudaStream_t s) {
     if (n_tiles == 0) return cudaSuccess;
     const size_t smem = L.data_offset + size_t(L.stages) * L.stage_bytes;
     static size_t configured = 0;
@@ -912,7 +1046,8 @@ cudaError_t launch_buff_scan(const QueryParams& q, const BuffChunkInfo* info, ui
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    buff_scan_kernel<<<grid < n_tiles ? grid : n_tiles, kScanThreads, smem, s>>>(q, info, tile_begin, n_tiles, L);
+    buff_scan_kernel<<<grid < n_tiles ? grid : n_tiles, kScanThreads, smem, s>>>(q, info, tile_begin, n_tiles, L, T,
+                                                                               res, frac, fast_ok ? 1u : 0u);
     count_launch();
     return cudaGetLastError();
 }

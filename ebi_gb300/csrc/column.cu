@@ -10,6 +10,7 @@
 // finalize_kernel that folds the per-chunk results in chunk order.
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -86,6 +87,10 @@ struct ebi_column {
     BuffChunkInfo* d_buff = nullptr;
     StageLayout layout{};
     uint32_t scan_grid = 0;
+    ScanTotals* d_tot = nullptr;
+    uint32_t buff_frac = 0;
+    bool buff_fast_ok = false;
+    bool fused_pending = false;  // the last query's kernel already folded into d_res
     // segment timing (ebi_column_set_timing)
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // query start, scan end, finalize end
@@ -220,10 +225,11 @@ int begin_query(ebi_column* c, cudaStream_t s) {
     return EBI_OK;
 }
 
-// Enqueues finalize, copies the result back and waits.
+// Enqueues finalize (unless the scan kernel already folded), copies the result back and waits.
 int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
     if (c->timing) CK(cudaEventRecord(c->ev[1], s));
-    CK(launch_finalize(q, c->d_res, s));
+    if (!c->fused_pending) CK(launch_finalize(q, c->d_res, s));
+    c->fused_pending = false;
     if (c->timing) CK(cudaEventRecord(c->ev[2], s));
     CK(cudaMemcpyAsync(c->h_res, c->d_res, sizeof(QueryResult), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -268,8 +274,13 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
     }
     if (d_mask) CK(launch_select_chunks(q, s));
     if (c->scheme == EBI_BUFF) {
-        if (tile_counts) CK(launch_buff_query(q, tb, tn, s));
-        else CK(launch_buff_scan(q, c->d_buff, tb, tn, c->layout, c->scan_grid, s));
+        if (tile_counts || tn == 0) {
+            CK(launch_buff_query(q, tb, tn, s));
+        } else {
+            CK(launch_buff_scan(q, c->d_buff, tb, tn, c->layout, c->scan_grid, c->d_tot, c->d_res, c->buff_frac,
+                                c->buff_fast_ok, s));
+            c->fused_pending = true;
+        }
     }
     return EBI_OK;
 }
@@ -343,8 +354,15 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         c->tiles = buff_tiles(c->chunks);
         binfo = parse_buff_headers(file, c->chunks);
         uint32_t np_max = 0, tb_max = 0;
-        for (const BuffChunkInfo& b : binfo)
-            if (!b.status) { np_max = std::max(np_max, b.bits / 8); tb_max = std::max(tb_max, b.bits % 8); }
+        bool first = true;
+        c->buff_fast_ok = true;
+        for (const BuffChunkInfo& b : binfo) {
+            if (b.status) continue;
+            np_max = std::max(np_max, b.bits / 8);
+            tb_max = std::max(tb_max, b.bits % 8);
+            if (first) { c->buff_frac = b.frac; first = false; }
+            if (b.frac != c->buff_frac || b.frac > 1022 || b.bits == 0) c->buff_fast_ok = false;
+        }
         uint32_t per_sm = 1;
         c->layout = buff_stage_layout(np_max, tb_max, &per_sm);
         int dev = 0, sms = 0;
@@ -362,6 +380,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st) st = dev_alloc(&c->d_acc, c->n_chunks, s);
     if (!st) st = dev_alloc(&c->d_res, 1, s);
     if (!st && !binfo.empty()) st = dev_alloc(&c->d_buff, binfo.size(), s);
+    if (!st) st = dev_alloc(&c->d_tot, 1, s);
     if (!st && cudaMallocHost(&c->h_res, sizeof(QueryResult)) != cudaSuccess) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st) {
         cudaError_t e = cudaMemcpyAsync(c->d_file, file, len, cudaMemcpyHostToDevice, s);
@@ -373,6 +392,8 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
                                 cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && !binfo.empty())
             e = cudaMemcpyAsync(c->d_buff, binfo.data(), binfo.size() * sizeof(BuffChunkInfo), cudaMemcpyHostToDevice, s);
+        static const ScanTotals kRest = {0, 0.0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_tot, &kRest, sizeof kRest, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
         // host sources (chunk table, tiles) must stay alive until the copies ran
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -388,7 +409,7 @@ int ebi_column_close(ebi_column* c) {
     cudaStream_t s = c->stream;
     for (cudaEvent_t e : c->ev) if (e) cudaEventDestroy(e);
     void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
-                    c->d_scratch_mask, c->d_buff};
+                    c->d_scratch_mask, c->d_buff, c->d_tot};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
     if (c->h_res) cudaFreeHost(c->h_res);
     delete c;

@@ -72,6 +72,20 @@ struct ChunkAcc {
     uint32_t pad;
 };
 
+// Query-wide totals of the fused BUFF scan, combined with one set of atomics
+// per CTA; the last CTA folds them.  At rest (re-armed by that CTA):
+// zeros, max_fixed = INT64_MIN, min_fixed = INT64_MAX, bad_chunk = ~0.
+struct ScanTotals {
+    unsigned long long sum_fixed;  // wrapping sum of every (CTA, chunk) piece of sum_with_bitmask's integer
+    double abs_bound;              // sum of |piece|: bounds every chunk total and their prefix sums
+    unsigned long long count;      // rows selected
+    long long max_fixed, min_fixed;
+    unsigned int done;             // CTAs finished
+    unsigned int bad_chunk;        // lowest chunk index that raised an error
+    unsigned int nonexact;         // a piece reached 2^53
+    unsigned int pad;
+};
+
 struct QueryResult {
     uint32_t status;       // status of the first failing chunk in chunk order
     uint32_t bad_chunk;    // its index

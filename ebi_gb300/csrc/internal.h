@@ -31,8 +31,12 @@ cudaError_t launch_buff_query(const QueryParams& q, uint32_t tile_begin, uint32_
 StageLayout buff_stage_layout(uint32_t np_max, uint32_t tb_max, uint32_t* ctas_per_sm);
 // Pipelined scan (bulk copies into a shared-memory ring): filter without tile
 // counts, filter+agg and agg.  grid = persistent CTAs.
+// The last CTA folds the query into *res (no finalize launch): exactly, from
+// integer totals, when fast_ok (one frac for every chunk, no constant chunk)
+// and the totals stay below 2^53 ulps; else in chunk order from acc.
 cudaError_t launch_buff_scan(const QueryParams& q, const BuffChunkInfo* info, uint32_t tile_begin, uint32_t n_tiles,
-                            const StageLayout& L, uint32_t grid, cudaStream_t s);
+                            const StageLayout& L, uint32_t grid, ScanTotals* T, QueryResult* res, uint32_t frac,
+                            bool fast_ok, cudaStream_t s);
 // Rows of the bitmask per tile into q.tile_counts[tile - tile_begin].
 cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s);
 // Writes the decoded values of the selected rows at tile_offsets[tile - tile_begin] + rank
