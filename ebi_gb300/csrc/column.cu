@@ -197,8 +197,18 @@ QueryParams base_params(const ebi_column* c) {
 }
 
 int check_supported(const ebi_column* c) {
-    if (c->scheme != EBI_BUFF) return fail(EBI_E_UNSUPPORTED, "codec kernels not built for this scheme yet");
+    if (c->scheme < EBI_UNCOMPRESSED || c->scheme > EBI_CHIMP128) return fail(EBI_E_UNSUPPORTED, "compression scheme outside this engine");
     return EBI_OK;
+}
+
+// The value codecs (everything but BUFF) run one CTA per chunk; their tiles are the chunks.
+cudaError_t launch_values(const ebi_column* c, const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
+                          const unsigned long long* chunk_offsets, cudaStream_t s) {
+    switch (c->scheme) {
+    case EBI_UNCOMPRESSED: return launch_raw(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
+    case EBI_RLE: return launch_rle(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
+    default: return launch_xor(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
+    }
 }
 
 // Tile range of the query: all tiles, or those of chunk_id (none when out of range).
@@ -262,8 +272,16 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
     q.out_mask = reinterpret_cast<uint32_t*>(d_out_mask);
     q.tile_counts = tile_counts;
     if (pred) q.pred = *pred;
+    q.pred_on = pred != nullptr;
     uint32_t tb, tn;
     tile_range(c, chunk_id, &tb, &tn);
+    if (c->scheme != EBI_BUFF) {
+        // value codecs OR their rows into a zeroed output (decoded runs may start on any row)
+        if (d_out_mask) CK(cudaMemsetAsync(d_out_mask, 0, c->mask_words * 8, s));
+        if (d_mask) CK(launch_select_chunks(q, s));
+        CK(launch_values(c, q, tb, tn, VAL_SCAN, nullptr, s));
+        return EBI_OK;
+    }
     if (d_out_mask) {
         // Words shared by two chunks, or words of chunks that are not read, need
         // a zeroed output; otherwise every word is written by exactly one thread.
@@ -290,6 +308,35 @@ int check_pred(const ebi_predicate* p) {
     if (p->kind < EBI_PRED_EQ || p->kind > EBI_PRED_RANGE) return fail(EBI_E_INVALID, "bad predicate kind");
     if (p->kind == EBI_PRED_RANGE && (p->start_kind < 0 || p->start_kind > 2 || p->end_kind < 0 || p->end_kind > 2))
         return fail(EBI_E_INVALID, "bad range bound kind");
+    return EBI_OK;
+}
+
+// Materialize / filter_materialize of a value codec: a count pass, a scan of
+// the per-chunk counts and a pass that writes every chunk's rows at its offset.
+int run_materialize_values(ebi_column* c, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
+                           double* d_out, uint64_t out_cap, uint64_t* n_out, cudaStream_t s) {
+    if (int st = begin_query(c, s)) return st;
+    QueryParams q = base_params(c);
+    q.op = OP_FILTER;  // only the status is folded
+    q.chunk_id = chunk_id;
+    q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
+    q.out_vals = d_out;
+    q.out_cap = out_cap;
+    q.tile_counts = c->d_tile_counts;
+    q.pred_on = pred != nullptr;
+    if (pred) q.pred = *pred;
+    uint32_t tb, tn;
+    tile_range(c, chunk_id, &tb, &tn);
+    CK(launch_values(c, q, tb, tn, VAL_COUNT, nullptr, s));
+    CK(launch_tile_scan(c->d_tile_counts, c->d_tile_offsets, tn, s));
+    CK(launch_values(c, q, tb, tn, VAL_MATERIALIZE, c->d_tile_offsets, s));
+    CK(cudaMemcpyAsync(&c->h_res->count, c->d_tile_offsets + tn, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const uint64_t total = c->h_res->count;
+    int st = finish(c, q, s);
+    if (st) return st;
+    if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
+    if (n_out) *n_out = total;
     return EBI_OK;
 }
 
@@ -370,7 +417,13 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         c->scan_grid = static_cast<uint32_t>(std::max(sms, 1)) * per_sm;
     } else {
-        c->tiles.first_tile.assign(c->n_chunks + 1, 0);
+        c->tiles.tiles.resize(c->n_chunks);
+        c->tiles.first_tile.resize(c->n_chunks + 1);
+        for (uint64_t i = 0; i < c->n_chunks; ++i) {
+            c->tiles.tiles[i] = Tile{static_cast<uint32_t>(i), 0};
+            c->tiles.first_tile[i] = static_cast<uint32_t>(i);
+        }
+        c->tiles.first_tile[c->n_chunks] = static_cast<uint32_t>(c->n_chunks);
     }
     c->mask_words = (c->n_records + 63) / 64;
     if (c->mask_words == 0) c->mask_words = 1;
@@ -513,6 +566,10 @@ int ebi_materialize(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, dou
     int st = check_supported(c);
     if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (c->scheme != EBI_BUFF) {
+        if ((st = ensure_scratch(c, s))) return st;
+        return run_materialize_values(c, nullptr, d_mask, chunk_id, d_out, out_cap, n_out, s);
+    }
     if (d_mask && (st = ensure_scratch(c, s))) return st;
     return run_materialize(c, d_mask, chunk_id, d_out, out_cap, n_out, s, false, nullptr);
 }
@@ -525,6 +582,7 @@ int ebi_filter_materialize(ebi_column* c, const ebi_predicate* pred, const uint6
     if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if ((st = ensure_scratch(c, s))) return st;
+    if (c->scheme != EBI_BUFF) return run_materialize_values(c, pred, d_mask, chunk_id, d_out, out_cap, n_out, s);
     // filter into the scratch mask, counting per tile, then materialize it
     st = run_scan(c, OP_FILTER, pred, d_mask, chunk_id, c->d_scratch_mask, c->d_tile_counts, s);
     if (st) return st;

@@ -123,7 +123,14 @@ struct QueryParams {
     int scheme;
     uint32_t agg;              // AGG_* aggregates the caller asked for (the count is always kept)
     const BuffChunkInfo* binfo;  // BUFF: header facts per chunk
+    int pred_on;               // value codecs: the predicate selects rows (filter, filter+agg, filter_materialize)
 };
+
+// Passes of the value-codec kernels (one CTA per chunk).
+//   VAL_SCAN         filter / filter+agg / agg into the output bitmask and acc
+//   VAL_COUNT        rows a materialize will write, per chunk (tile_counts)
+//   VAL_MATERIALIZE  writes those rows at chunk_offsets[chunk] onwards
+enum ValMode : int { VAL_SCAN = 0, VAL_COUNT = 1, VAL_MATERIALIZE = 2 };
 
 enum : uint32_t { AGG_SUM = 1, AGG_MIN = 2, AGG_MAX = 4, AGG_ALL = 7 };
 

@@ -44,6 +44,17 @@ cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_
 cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles,
                                     const unsigned long long* tile_offsets, uint64_t base_row, cudaStream_t s);
 
+// ---- value codecs: one CTA per chunk, modes of values.cuh (VAL_*) ----------
+// chunk_offsets[chunk - chunk_begin] (+1 entry) are the exclusive scan of a
+// VAL_COUNT pass; the count pass writes q.tile_counts[chunk - chunk_begin].
+cudaError_t launch_rle(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
+                       const unsigned long long* chunk_offsets, cudaStream_t s);
+cudaError_t launch_raw(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
+                       const unsigned long long* chunk_offsets, cudaStream_t s);
+// Gorilla, Chimp, Chimp128 (q.scheme selects the decoder).
+cudaError_t launch_xor(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
+                       const unsigned long long* chunk_offsets, cudaStream_t s);
+
 // ---- shared kernels (query.cu) ---------------------------------------------
 // acc[c].selected = chunk passes chunk_id and intersects the mask (or no mask).
 cudaError_t launch_select_chunks(const QueryParams& q, cudaStream_t s);

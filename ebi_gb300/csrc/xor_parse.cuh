@@ -1,0 +1,168 @@
+// xor_parse.cuh -- record parser of the Gorilla, Chimp and Chimp128 bitstreams,
+// shared by the decode kernel (xor.cu) and host-side checks of its segment
+// algorithm.  Host and device functions alike: the bit source is a functor
+// that returns the 64 stream bits starting at a bit position.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/ebi_gpu.h"
+
+#if defined(__CUDACC__)
+#define XOR_HD __host__ __device__ __forceinline__
+#else
+#define XOR_HD inline
+#endif
+
+namespace ebi {
+namespace xorp {
+
+constexpr uint32_t kNoRef = 0xffffu;     // Chimp128: value refers to an unset ring slot (0.0 bits)
+constexpr uint32_t kNoLead = 0xffu;      // Chimp: no leading-zero count stored yet
+
+enum : uint32_t { CODEC_GORILLA = EBI_GORILLA, CODEC_CHIMP = EBI_CHIMP, CODEC_CHIMP128 = EBI_CHIMP128 };
+
+// LEADING_REPR decode table [0, 8, 12, 16, 18, 20, 22, 24] (decoder/chunk_reader/chimp.rs), 5 bits per entry.
+XOR_HD uint32_t lead_decode(uint32_t t) {
+    constexpr uint64_t kTable = (0ull << 0) | (8ull << 5) | (12ull << 10) | (16ull << 15) | (18ull << 20) |
+                                (20ull << 25) | (22ull << 30) | (24ull << 35);
+    return static_cast<uint32_t>(kTable >> (5 * t)) & 31u;
+}
+
+// Parser state: bit position in the chunk and the inherited window
+// (Gorilla: lead | trail << 8; Chimp/Chimp128: stored leading zeros or kNoLead).
+struct PState {
+    uint64_t pos;
+    uint32_t win;
+};
+XOR_HD uint64_t pack_state(PState s) { return s.pos | (uint64_t(s.win) << 48); }
+XOR_HD PState unpack_state(uint64_t v) { return PState{v & ((1ull << 48) - 1), static_cast<uint32_t>(v >> 48)}; }
+
+// One decoded record: the value is value(ref) ^ delta, where ref is the
+// previous record (kRefPrev) or, for Chimp128's '00'/'01', a ring slot.
+constexpr uint32_t kRefPrev = 0xffffffffu;
+struct Rec {
+    uint64_t delta;
+    uint32_t ring;  // ring slot (Chimp128 '00'/'01') or kRefPrev
+    bool nan_ok;    // the reader checks this value against the NaN end marker
+};
+
+// Parses one record at s.pos; returns 0 or the error the reader raises there
+// (EBI_E_UNEXPECTED_END for a read past the chunk, EBI_E_CORRUPT for a
+// window the reader's u8/u32 arithmetic cannot represent).  B = chunk bits.
+template <int CODEC, typename Peek>
+XOR_HD uint32_t parse_rec(Peek peek, uint64_t B, PState& s, Rec& r) {
+    const uint64_t p = s.pos;
+    r.ring = kRefPrev;
+    r.nan_ok = true;
+    if (CODEC == CODEC_GORILLA) {
+        if (p + 1 > B) return EBI_E_UNEXPECTED_END;
+        const uint64_t x = peek(p);
+        if (!(x >> 63)) { s.pos = p + 1; r.delta = 0; return 0; }
+        if (p + 2 > B) return EBI_E_UNEXPECTED_END;
+        uint32_t lead = s.win & 0xffu, trail = s.win >> 8, n;
+        uint64_t q;
+        if (!((x >> 62) & 1)) {
+            n = 64 - lead - trail;
+            q = p + 2;
+        } else {
+            if (p + 13 > B) return EBI_E_UNEXPECTED_END;
+            const uint32_t l = static_cast<uint32_t>(x >> 57) & 31u, sg = (static_cast<uint32_t>(x >> 51) & 63u) + 1;
+            if (l + sg > 64) return EBI_E_CORRUPT;
+            lead = l;
+            trail = 64 - l - sg;
+            n = sg;
+            q = p + 13;
+        }
+        if (q + n > B) return EBI_E_UNEXPECTED_END;
+        r.delta = (peek(q) >> (64 - n)) << trail;
+        s.win = lead | (trail << 8);
+        s.pos = q + n;
+        return 0;
+    } else {
+        if (p + 2 > B) return EBI_E_UNEXPECTED_END;
+        const uint64_t x = peek(p);
+        const uint32_t flag = static_cast<uint32_t>(x >> 62);
+        if (flag == 0) {
+            r.delta = 0;
+            if (CODEC == CODEC_CHIMP128) {
+                if (p + 9 > B) return EBI_E_UNEXPECTED_END;
+                r.ring = static_cast<uint32_t>(x >> 55) & 127u;
+                r.nan_ok = false;  // chimp_n.rs: the '00' copy is not checked against NaN
+                s.pos = p + 9;
+            } else {
+                s.pos = p + 2;
+            }
+            return 0;
+        }
+        if (flag == 3 || flag == 2) {
+            uint32_t lead = s.win;
+            uint64_t q = p + 2;
+            if (flag == 3) {
+                if (p + 5 > B) return EBI_E_UNEXPECTED_END;
+                lead = lead_decode(static_cast<uint32_t>(x >> 59) & 7u);
+                q = p + 5;
+            } else if (lead > 64) {
+                return EBI_E_CORRUPT;  // '10' before any leading count was stored
+            }
+            const uint32_t n = 64 - lead;  // 40..64 bits
+            if (q + n > B) return EBI_E_UNEXPECTED_END;
+            r.delta = n == 64 ? peek(q) : peek(q) >> (64 - n);
+            s.win = lead;
+            s.pos = q + n;
+            return 0;
+        }
+        // flag 1
+        const uint32_t hdr = CODEC == CODEC_CHIMP128 ? 16u : 9u;
+        if (p + 2 + hdr > B) return EBI_E_UNEXPECTED_END;
+        const uint32_t t = static_cast<uint32_t>(x >> (62 - hdr)) & ((1u << hdr) - 1u);
+        if (CODEC == CODEC_CHIMP128) r.ring = (t >> 9) & 127u;
+        const uint32_t lead = lead_decode((t >> 6) & 7u);
+        uint32_t sig = t & 63u;
+        if (sig == 0) sig = 64;
+        if (sig + lead > 64) return EBI_E_CORRUPT;
+        const uint32_t trail = 64 - sig - lead;
+        const uint64_t q = p + 2 + hdr;
+        if (q + sig > B) return EBI_E_UNEXPECTED_END;
+        r.delta = (sig == 64 ? peek(q) : peek(q) >> (64 - sig)) << trail;
+        s.win = lead;
+        s.pos = q + sig;
+        return 0;
+    }
+}
+
+// Parses the records that start in [s.pos, end).  Counts the records before
+// the first failure (*fail = its error) and, when it fails, steps one bit and
+// goes on: a failing segment is either the true end of the stream or a
+// misaligned guess, and a misaligned parse should keep looking for the true
+// record boundaries.  The last segment fails at the end of the stream.
+template <int CODEC, typename Peek>
+XOR_HD PState parse_segment(Peek peek, uint64_t B, PState s, uint64_t end, bool last,
+                                                uint32_t* n_out, uint32_t* fail) {
+    uint32_t n = 0, f = 0;
+    Rec r;
+    while (s.pos < end) {
+        const uint32_t e = parse_rec<CODEC>(peek, B, s, r);
+        if (e) {
+            if (!f) f = e;
+            s.pos += 1;
+            continue;
+        }
+        n += f ? 0u : 1u;
+    }
+    if (last && !f) f = EBI_E_UNEXPECTED_END;
+    *n_out = n;
+    *fail = f;
+    return s;
+}
+
+// Ring slot -> record index: the latest record j < i with j % 128 == slot, or
+// kNoRef when the slot was never written (the ring starts zeroed).
+XOR_HD uint32_t ring_ref(uint32_t i, uint32_t slot) {
+    const int32_t j = static_cast<int32_t>(i) - 1 - static_cast<int32_t>((i - 1u - slot) & 127u);
+    return j < 0 ? kNoRef : static_cast<uint32_t>(j);
+}
+
+
+}  // namespace xorp
+}  // namespace ebi

@@ -1,0 +1,151 @@
+"""RLE, Uncompressed, Gorilla, Chimp and Chimp128 on the GPU against the oracle.
+
+Values, bitmasks and min/max are bit-exact; sums are compensated (double-double)
+and checked against the oracle's sequential sum (relative 1e-12 of the sum of
+magnitudes) and against math.fsum of the same values (2 ulps).
+"""
+import numpy as np
+import pytest
+
+import ebi_gb300 as E
+from oracle import oracle as O
+from tests.kat import KAT, chunk_option, round_at
+from tests.parity import check_query_suite, mask_np, random_mask, random_preds, same_f64, sum_ok
+
+pytestmark = pytest.mark.gpu
+
+VALUE_CODECS = ["uncompressed", "rle", "gorilla", "chimp", "chimp128"]
+KIND_NAMES = {O.CHUNK_RECORD_COUNT: "record_count", O.CHUNK_BYTE_SIZE: "byte_size", O.CHUNK_FULL: "full"}
+
+
+def to_pred(spec):
+    if spec[0] == "eq":
+        return E.Predicate.eq(spec[1])
+    if spec[0] == "ne":
+        return E.Predicate.ne(spec[1])
+    mk = {"none": lambda v: E.RangeValue.NONE, "incl": E.RangeValue.inclusive, "excl": E.RangeValue.exclusive}
+    (sk, sv), (ek, ev) = spec[1], spec[2]
+    return E.Predicate.range(mk[sk](sv), mk[ek](ev))
+
+
+@pytest.mark.parametrize("codec", VALUE_CODECS)
+@pytest.mark.parametrize("idx", range(len(KAT["filter_cases"])))
+def test_kat_filter_cases(codec, idx):
+    case = KAT["filter_cases"][idx]
+    kind, val = chunk_option(case["chunk"])
+    data = E.encode(case["values"], codec, (KIND_NAMES[kind], val))
+    d = E.Decoder(data)
+    mask = O.mask_from_rows(case["bitmask"], d.n_records) if "bitmask" in case else None
+    got = O.rows_from_mask(mask_np(d.filter(to_pred(case["pred"]), mask, case.get("chunk_id"))), d.n_records)
+    assert got == case["expect"], case["src"]
+    fm = d.filter_materialize(to_pred(case["pred"]), mask, case.get("chunk_id")).cpu().numpy()
+    assert same_f64(fm, np.asarray(case["values"], dtype=np.float64)[case["expect"]])
+    check_query_suite(data, [to_pred(case["pred"])], masks=(None, mask) if mask is not None else (None,),
+                      chunk_ids=(None, case.get("chunk_id")) if "chunk_id" in case else (None,))
+
+
+@pytest.mark.parametrize("codec", VALUE_CODECS)
+@pytest.mark.parametrize("idx", range(len(KAT["agg_cases"])))
+def test_kat_agg_cases(codec, idx):
+    case = KAT["agg_cases"][idx]
+    kind, val = chunk_option(case["chunk"])
+    data = E.encode(case["values"], codec, (KIND_NAMES[kind], val))
+    d = E.Decoder(data)
+    mask = O.mask_from_rows(case["bitmask"], d.n_records) if "bitmask" in case else None
+    got = getattr(d, case["op"])(mask)
+    assert round_at(got, 100) == round_at(case["expect"], 100), case["src"]
+
+
+def columns(rng, n):
+    walk = np.round(30 + np.cumsum(rng.normal(0, 0.5, n)), 2) + 0.0
+    i = np.arange(n)
+    sensor = np.round(20 + 10 * np.sin(2 * np.pi * i / 1440) + rng.normal(0, 0.1, n), 4) + 0.0
+    lens = rng.geometric(1 / 64, n)
+    steps = np.repeat(np.round(50 + np.cumsum(rng.integers(-5, 6, n) * 0.1), 1), lens)[:n] + 0.0
+    return {
+        "walk": walk,
+        "sensor": sensor,
+        "steps": steps,
+        "uniform": rng.uniform(-1e6, 1e6, n),
+        "few": rng.choice([-2.5, 0.0, 1.0, 7.25, 1e300], n),  # repeats, copies from the ring
+        "long_runs": np.repeat(rng.normal(0, 1, n // 600 + 1), 600)[:n],  # RLE runs past 255
+    }
+
+
+@pytest.mark.parametrize("codec", VALUE_CODECS)
+@pytest.mark.parametrize("kind", ["walk", "sensor", "steps", "uniform", "few", "long_runs"])
+@pytest.mark.parametrize("chunk", [("record_count", 8192), ("record_count", 1000), ("byte_size", 20000)])
+def test_random_columns(codec, kind, chunk):
+    rng = np.random.default_rng(abs(hash((codec, kind, chunk))) % 2**32)
+    n = 30_011
+    v = columns(rng, n)[kind]
+    data = E.encode(v, codec, chunk)
+    masks = (None, random_mask(n, 0.3, rng), random_mask(n, 0.001, rng), O.mask_from_rows([], n))
+    n_chunks = O.Decoder(data).n_chunks
+    check_query_suite(data, random_preds(v, rng), masks=masks,
+                      chunk_ids=(None, int(rng.integers(n_chunks)), n_chunks + 3))
+
+
+@pytest.mark.parametrize("codec", VALUE_CODECS)
+def test_full_chunk_sequential_path(codec):
+    # one chunk of 20,000 values: more records than the shared-memory decode holds
+    rng = np.random.default_rng(11)
+    v = np.round(30 + np.cumsum(rng.normal(0, 0.5, 20_000)), 2) + 0.0
+    data = E.encode(v, codec, ("full", 0))
+    check_query_suite(data, random_preds(v, rng, k=2), masks=(None, random_mask(len(v), 0.4, rng)))
+
+
+@pytest.mark.parametrize("codec", ["gorilla", "chimp", "chimp128"])
+def test_nan_truncates_stream(codec):
+    # the XOR readers stop at the first value whose bits equal f64::NAN (parity hazard kept on purpose)
+    v = np.round(np.random.default_rng(5).normal(10, 3, 5000), 2)
+    v[1234] = np.nan
+    v[4100] = np.nan
+    data = E.encode(v, codec, ("record_count", 1000))
+    check_query_suite(data, [E.Predicate.range(E.RangeValue.inclusive(5.0), E.RangeValue.exclusive(12.0))],
+                      masks=(None, random_mask(len(v), 0.5, np.random.default_rng(1))))
+
+
+@pytest.mark.parametrize("codec", VALUE_CODECS)
+def test_tiny_and_empty(codec):
+    for v in ([], [1.5], [0.0, -0.0, 0.0], [np.inf, -np.inf, 3.0], [5e-324, -5e-324, 1.0]):
+        data = E.encode(np.asarray(v, dtype=np.float64), codec, ("record_count", 2))
+        check_query_suite(data, [E.Predicate.eq(0.0), E.Predicate.ne(3.0),
+                                 E.Predicate.range(E.RangeValue.NONE, E.RangeValue.inclusive(1.0))])
+
+
+@pytest.mark.parametrize("codec", VALUE_CODECS)
+def test_corrupt_chunks_match_oracle(codec):
+    # flipped bits and truncated chunk payloads: same status (or same results) as the oracle
+    rng = np.random.default_rng(3)
+    v = np.round(30 + np.cumsum(rng.normal(0, 0.5, 6000)), 2) + 0.0
+    base = bytes(E.encode(v, codec, ("record_count", 1000)))
+    d = O.Decoder(base)
+    for trial in range(12):
+        data = bytearray(base)
+        c = int(rng.integers(d.n_chunks))
+        phys, size, _, _ = d.chunk_info(c)
+        for _ in range(1 + trial % 3):
+            k = phys + int(rng.integers(size))
+            data[k] ^= 1 << int(rng.integers(8))
+        check_query_suite(bytes(data), [E.Predicate.range(E.RangeValue.inclusive(25.0), E.RangeValue.NONE)],
+                          masks=(None,), chunk_ids=(None, c))
+
+
+@pytest.mark.parametrize("codec", VALUE_CODECS)
+def test_full_size_properties(codec):
+    # 1,048,576-value random walk in 8,192-value chunks: encode -> decode is the
+    # identity, the filter count and min/max equal numpy's, the sum is exact to 2 ulps
+    rng = np.random.default_rng(1)
+    v = np.round(30.0 + np.cumsum(rng.normal(0.0, 0.5, 1 << 20)), 2) + 0.0
+    d = E.Decoder(E.encode(v, codec, ("record_count", 8192)))
+    assert same_f64(d.materialize().cpu().numpy(), v)
+    p = E.Predicate.range(E.RangeValue.inclusive(10.0), E.RangeValue.inclusive(50.0))
+    sel = (v >= 10.0) & (v <= 50.0)
+    mask, s, mn, mx, cnt = d.filter_agg(p)
+    rows = np.nonzero(np.unpackbits(mask_np(mask).view(np.uint8), bitorder="little")[: len(v)])[0]
+    assert np.array_equal(rows, np.nonzero(sel)[0])
+    assert cnt == int(sel.sum())
+    assert mn == v[sel].min() and mx == v[sel].max()
+    assert sum_ok(s, float(np.sum(v[sel])), False, v[sel])
+    assert sum_ok(d.sum(), float(np.sum(v)), False, v)
