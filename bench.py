@@ -9,7 +9,13 @@ cycling through the 1 %, 10 % and 50 % selectivity ranges [-10, 10],
 every step.  value = GB/s of decoded f64 (8 B x rows per query / device time),
 the reference's throughput definition (uncompressed bytes / elapsed time).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
+
+--workload picks one of the other measured shapes instead of the headline
+BUFF column: "gorilla" (1,048,576-value random walk, 8,192-value chunks,
+filter 10 <= x <= 50 + sum/min/max), "chimp128" (16,777,216-value sensor
+series, filter 15 <= x <= 25 + max) and "rle" (16,777,216-value step series,
+filter over the middle 30 % of its values + max).
 
 Under torchrun every rank runs the same workload on its own GPU (replicas: the
 path has no cross-column exchange), and value sums the ranks' rows over the
@@ -48,23 +54,73 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
-def workload_bytes(n_rows=N_ROWS):
-    import ebi_gb300 as E
-    from ebi_gb300 import workloads as W
+class Workload:
+    """One measured shape: its column (EBI1 bytes) and the range queries a step cycles through."""
 
-    t = time.perf_counter()
-    v = W.buff_uniform(n_rows)
-    data = E.encode(v, "buff", ("record_count", CHUNK), SCALE)
-    log(f"workload: {n_rows} rows, {len(data)} B EBI1 ({time.perf_counter() - t:.1f} s to generate)")
-    return data
+    def __init__(self, name, rows):
+        from ebi_gb300 import workloads as W
+
+        self.name = name
+        self.rows = rows
+        if name == "buff":
+            self.codec, self.chunk, self.scale = "buff", CHUNK, SCALE
+            self.values = lambda: W.buff_uniform(rows)
+            self.ranges = [(k, -a, a) for k, a in W.BUFF_RANGES.items()]
+            self.aggregates = ("sum",)
+            self.describe = ("BUFF 67,108,864 f64 U[-1000,1000] rounded to 3 dp, 65,536-row chunks, scale 1000; "
+                             "fused filter (bitmask out) + sum at 1%/10%/50% selectivity")
+        elif name == "gorilla":
+            self.codec, self.chunk, self.scale = "gorilla", 8192, 1
+            self.values = lambda: W.gorilla_walk(rows)
+            self.ranges = [("10<=x<=50", 10.0, 50.0)]
+            self.aggregates = ("sum", "min", "max")
+            self.describe = ("Gorilla 1,048,576 f64 random walk x0=30, N(0,0.5) steps, 2 dp, 8,192-row chunks; "
+                             "fused filter 10<=x<=50 (bitmask out) + sum/min/max")
+        elif name == "chimp128":
+            self.codec, self.chunk, self.scale = "chimp128", 8192, 1
+            self.values = lambda: W.sensor(rows)
+            self.ranges = [("15<=x<=25", 15.0, 25.0)]
+            self.aggregates = ("max",)
+            self.describe = ("Chimp128 16,777,216 f64 sensor series 20+10sin(2pi i/1440)+N(0,0.1), 4 dp, "
+                             "8,192-row chunks; fused decode + filter 15<=x<=25 (bitmask out) + max")
+        elif name == "rle":
+            self.codec, self.chunk, self.scale = "rle", 8192, 1
+            self.values = lambda: W.steps(rows)
+            self.ranges = None  # the middle 30 % of the values, fixed once the column exists
+            self.aggregates = ("max",)
+            self.describe = ("RLE 16,777,216 f64 step series, Geometric(1/64) runs, 8,192-row chunks; "
+                             "fused decode + filter over the middle 30% of values (bitmask out) + max")
+        else:
+            raise SystemExit(f"unknown workload {name}")
+
+    def build(self):
+        import ebi_gb300 as E
+
+        t = time.perf_counter()
+        v = self.values()
+        if self.ranges is None:
+            lo, hi = np.quantile(v, [0.35, 0.65])
+            self.ranges = [(f"{lo:.1f}<=x<={hi:.1f}", float(lo), float(hi))]
+        data = E.encode(v, self.codec, ("record_count", self.chunk), self.scale)
+        log(f"workload {self.name}: {self.rows} rows, {len(data)} B EBI1 ({time.perf_counter() - t:.1f} s to generate)")
+        return data
+
+    def queries(self):
+        import ebi_gb300 as E
+
+        return [(k, E.Predicate.range(E.RangeValue.inclusive(a), E.RangeValue.inclusive(b))) for k, a, b in self.ranges]
+
+    def oracle_preds(self):
+        from oracle import oracle as O
+
+        return [O.rng(O.BOUND_INCLUSIVE, a, O.BOUND_INCLUSIVE, b) for _, a, b in self.ranges]
 
 
-def queries():
-    import ebi_gb300 as E
-    from ebi_gb300 import workloads as W
-
-    return [(name, E.Predicate.range(E.RangeValue.inclusive(-a), E.RangeValue.inclusive(a)))
-            for name, a in W.BUFF_RANGES.items()]
+DEFAULT_ROWS = {"buff": N_ROWS, "gorilla": 1_048_576, "chimp128": 16_777_216, "rle": 16_777_216}
+KERNELS = {"buff": "buff_scan_kernel (fused decode + range filter + bitmask + sum)",
+           "gorilla": "xor_kernel<Gorilla> (segment-parallel decode + filter + bitmask + sum/min/max)",
+           "chimp128": "xor_kernel<Chimp128> (segment-parallel decode + filter + bitmask + max)",
+           "rle": "rle_kernel (run expansion + filter + bitmask + max)"}
 
 
 class ClockSampler:
@@ -128,9 +184,9 @@ def measured_peak():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the filter+sum kernel from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "buff_filter_agg_64m.json"
+def ncu_traffic(workload="buff"):
+    """DRAM bytes per launch of the workload's dominant kernel from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / f"{workload}_traffic.json"
     if p.exists():
         try:
             return json.loads(p.read_text()).get("dram_bytes_per_launch")
@@ -139,25 +195,25 @@ def ncu_traffic():
     return None
 
 
-def cpu_baseline(data: bytes, threads: int, budget_s: float = 15.0):
+def cpu_baseline(data: bytes, threads: int, wl, budget_s: float = 15.0):
     """The oracle port timed on the host cores over a bounded sample of the same queries."""
     from oracle import oracle as O
 
     d = O.Decoder(data, threads=threads)
-    preds = [O.rng(O.BOUND_INCLUSIVE, -a, O.BOUND_INCLUSIVE, a) for a in (10.0, 100.0, 500.0)]
+    preds = wl.oracle_preds()
     rows = 0
     t0 = time.perf_counter()
     i = 0
     while True:
-        d.filter_agg(preds[i % 3])
+        d.filter_agg(preds[i % len(preds)])
         rows += d.n_records
         i += 1
         if time.perf_counter() - t0 > budget_s or i >= 9:
             break
     dt = time.perf_counter() - t0
     return {"value": round(8.0 * rows / dt / 1e9, 3), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{i} fused filter+sum queries (1%/10%/50% cycled) over the full {d.n_records}-row "
-                      f"column, chunk-parallel C restatement of ebi's Decoder, {threads} threads"}
+            "sample": f"{i} fused filter+aggregate queries ({', '.join(k for k, _, _ in wl.ranges)} cycled) over the "
+                      f"full {d.n_records}-row column, chunk-parallel C restatement of ebi's Decoder, {threads} threads"}
 
 
 def run_reference(args):
@@ -170,31 +226,31 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    import ebi_gb300 as E
-    from ebi_gb300 import workloads as W
     from oracle import oracle as O
 
-    sample_rows = N_ROWS // 8
-    data = E.encode(W.buff_uniform(N_ROWS)[:sample_rows], "buff", ("record_count", CHUNK), SCALE)
+    wl = Workload(args.workload, args.rows or DEFAULT_ROWS[args.workload])
+    full_rows = wl.rows
+    wl.rows = max(wl.chunk, min(wl.rows, N_ROWS // 8))  # bounded sample: the leading rows of the same series
+    data = wl.build()
+    sample_rows = wl.rows
     d = O.Decoder(data, threads=threads)
-    preds = [O.rng(O.BOUND_INCLUSIVE, -a, O.BOUND_INCLUSIVE, a) for a in (10.0, 100.0, 500.0)]
+    preds = wl.oracle_preds()
     for i in range(args.warmup):
-        d.filter_agg(preds[i % 3])
+        d.filter_agg(preds[i % len(preds)])
     t0 = time.perf_counter()
     for i in range(args.steps):
-        d.filter_agg(preds[i % 3])
+        d.filter_agg(preds[i % len(preds)])
     dt = time.perf_counter() - t0
     value = 8.0 * sample_rows * args.steps / dt / 1e9
-    sample = (f"per step one fused filter+sum (1%/10%/50% cycled) over the first {sample_rows} rows "
-              f"({d.n_chunks} chunks) of the workload column, chunk-parallel C restatement of ebi's CPU "
-              f"path on {threads} host threads (ebi is Rust; no Rust toolchain exists on this image)")
+    sample = (f"per step one fused filter+aggregate ({', '.join(k for k, _, _ in wl.ranges)}) over the first "
+              f"{sample_rows} of the workload's {full_rows} rows ({d.n_chunks} chunks), chunk-parallel C "
+              f"restatement of ebi's CPU path on {threads} host threads (ebi is Rust; no Rust toolchain exists "
+              f"on this image)")
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 -> f64",
             "data": "synthetic (seeded numpy, the configuration's shape)",
-            "config": {"workload": "BUFF 67,108,864 f64 U[-1000,1000] rounded to 3 dp, 65,536-row chunks, "
-                                   "scale 1000; fused filter+sum/min/max at 1%/10%/50% selectivity",
-                       "rows": N_ROWS, "chunk_rows": CHUNK},
+            "config": {"workload": wl.describe, "rows": full_rows, "chunk_rows": wl.chunk},
             "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -210,8 +266,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity-check", action="store_true")
-    ap.add_argument("--rows", type=int, default=N_ROWS, help="column length (profiling runs use smaller columns)")
+    ap.add_argument("--rows", type=int, default=0, help="column length (profiling runs use smaller columns)")
+    ap.add_argument("--workload", default="buff", choices=["buff", "gorilla", "chimp128", "rle"])
     args = ap.parse_args()
+    wl = None
     args.warmup = max(args.warmup, 3)
 
     if args.impl == "reference":
@@ -237,19 +295,21 @@ def main():
         torch.cuda.synchronize(dev)
 
     E.load_library()
-    data = workload_bytes(args.rows)
-    stream = torch.cuda.current_stream(dev)
+    wl = Workload(args.workload, args.rows or DEFAULT_ROWS[args.workload])
+    args.rows = wl.rows
+    data = wl.build()
     dec = E.Decoder(data, device=str(dev))
     dec.set_timing(True)
     n = dec.n_records
     mask = dec.new_mask()
-    qs = queries()
+    qs = wl.queries()
+    nq = len(qs)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MiB > 129 MB L2
     alg_bytes = sum(dec.chunk_info(c)[1] for c in range(dec.n_chunks)) + 8 * dec.mask_words
 
     def one_step(i):
         flush.fill_(i & 0xFF)  # evicts the column from L2 (not timed)
-        dec.filter_agg(qs[i % 3][1], out=mask, aggregates=("sum",))
+        dec.filter_agg(qs[i % nq][1], out=mask, aggregates=wl.aggregates)
         return dec.segmented_execution_times()
 
     for i in range(args.warmup):
@@ -285,18 +345,21 @@ def main():
     peak, peak_kind = measured_peak()
     scan_avg_s = statistics.mean(scan) / 1e3
     achieved = alg_bytes / scan_avg_s / 1e9
-    traffic = ncu_traffic()
+    traffic = ncu_traffic(wl.name)
 
     # parity spot check of the last query against the oracle (outside the timed region)
     check = None
     if rank == 0 and not args.no_parity_check:
         from oracle import oracle as O
-        name, p = qs[(args.steps - 1) % 3]
+        name, p = qs[(args.steps - 1) % nq]
         _, s, mn, mx, cnt = dec.filter_agg(p, out=mask)
         o = O.Decoder(data, threads=os.cpu_count() or 1)
         om, os_, omn, omx = o.filter_agg(O.rng(1, p.rng.start.value, 1, p.rng.end.value))
-        same = (np.array_equal(mask.cpu().numpy().view(np.uint64), om) and (s, mn, mx) == (os_, omn, omx))
-        check = {"query": name, "bitmask_and_aggregates_bit_exact": bool(same), "rows_selected": int(cnt)}
+        exact_sum = wl.codec == "buff"  # BUFF sums are exact; the others are compensated (1e-12 relative)
+        sum_same = s == os_ if exact_sum else abs(s - os_) <= 1e-12 * max(abs(os_), 1e-300)
+        same = np.array_equal(mask.cpu().numpy().view(np.uint64), om) and (mn, mx) == (omn, omx) and sum_same
+        check = {"query": name, "bitmask_min_max_bit_exact_sum_within_tolerance": bool(same),
+                 "sum_rel_diff": abs(s - os_) / max(abs(os_), 1e-300), "rows_selected": int(cnt)}
 
     # e2e: host file (pinned) -> open (H2D) -> fused query -> bitmask + scalars back to the host
     host_file = torch.frombuffer(bytearray(data), dtype=torch.uint8).pin_memory()
@@ -307,7 +370,7 @@ def main():
         ts = time.perf_counter()
         d2 = E.Decoder(host_file, device=str(dev))
         m2 = d2.new_mask()
-        _, s, mn, mx, cnt = d2.filter_agg(qs[i % 3][1], out=m2, aggregates=("sum",))
+        _, s, mn, mx, cnt = d2.filter_agg(qs[i % nq][1], out=m2, aggregates=wl.aggregates)
         host_mask.copy_(m2, non_blocking=True)
         torch.cuda.synchronize(dev)
         d2.close()
@@ -318,7 +381,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(data, os.cpu_count() or 1)
+        cpu = cpu_baseline(data, os.cpu_count() or 1, wl)
 
     if rank == 0:
         line = {
@@ -326,13 +389,12 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(1e3 * dev_s / args.steps, 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 -> f64",
             "data": "synthetic (seeded numpy, the configuration's shape)",
-            "config": {"workload": "BUFF 67,108,864 f64 U[-1000,1000] rounded to 3 dp, 65,536-row chunks, "
-                                   "scale 1000; fused filter (bitmask out) + sum at 1%/10%/50% selectivity",
-                       "rows": args.rows, "chunk_rows": CHUNK, "column_bytes": len(data),
+            "config": {"workload": wl.describe, "queries": [k for k, _, _ in wl.ranges],
+                       "rows": args.rows, "chunk_rows": wl.chunk, "column_bytes": len(data),
                        "l2": "flushed before every step (256 MiB write)", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "kernel": "buff_scan_kernel (fused decode + range filter + bitmask + sum)",
+                         "kernel": KERNELS[wl.name],
                          "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": round(1e3 * scan_avg_s, 5),
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s"},

@@ -237,11 +237,22 @@ class Decoder:
     def materialize(self, bitmask=None, chunk_id=None, out=None):
         torch = _torch()
         mp, keep = self._mask_in(bitmask)
+        call = lambda o, n: _native.lib().ebi_materialize(self._h, mp, _cid(chunk_id), C.c_void_p(o.data_ptr()),
+                                                          o.numel(), C.byref(n), self._sp())
+        return self._materialize(call, out, "Decoder::materialize")
+
+    def _materialize(self, call, out, what):
+        torch = _torch()
+        grow = out is None
         if out is None:
             out = torch.empty(max(self.n_records, 1), dtype=torch.float64, device=self.device)
         n = C.c_uint64()
-        _check(_native.lib().ebi_materialize(self._h, mp, _cid(chunk_id), C.c_void_p(out.data_ptr()), out.numel(),
-                                             C.byref(n), self._sp()), "Decoder::materialize")
+        rc = call(out, n)
+        if rc == InvalidArgument.code and grow and n.value > out.numel():
+            # the chunks decode to more values than the footer counts: retry at the size reported
+            out = torch.empty(n.value, dtype=torch.float64, device=self.device)
+            rc = call(out, n)
+        _check(rc, what)
         return out[: n.value]
 
     def filter(self, predicate: Predicate, bitmask=None, chunk_id=None, out=None):
@@ -255,13 +266,11 @@ class Decoder:
     def filter_materialize(self, predicate: Predicate, bitmask=None, chunk_id=None, out=None):
         torch = _torch()
         mp, keep = self._mask_in(bitmask)
-        if out is None:
-            out = torch.empty(max(self.n_records, 1), dtype=torch.float64, device=self.device)
         p = predicate.to_c()
-        n = C.c_uint64()
-        _check(_native.lib().ebi_filter_materialize(self._h, C.byref(p), mp, _cid(chunk_id), C.c_void_p(out.data_ptr()),
-                                                    out.numel(), C.byref(n), self._sp()), "Decoder::filter_materialize")
-        return out[: n.value]
+        call = lambda o, n: _native.lib().ebi_filter_materialize(self._h, C.byref(p), mp, _cid(chunk_id),
+                                                                 C.c_void_p(o.data_ptr()), o.numel(), C.byref(n),
+                                                                 self._sp())
+        return self._materialize(call, out, "Decoder::filter_materialize")
 
     def _agg(self, fn, bitmask, chunk_id, what):
         mp, keep = self._mask_in(bitmask)

@@ -335,8 +335,8 @@ int run_materialize_values(ebi_column* c, const ebi_predicate* pred, const uint6
     const uint64_t total = c->h_res->count;
     int st = finish(c, q, s);
     if (st) return st;
-    if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
     if (n_out) *n_out = total;
+    if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
     return EBI_OK;
 }
 
@@ -362,7 +362,10 @@ int run_materialize(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, dou
             const uint32_t n = c->chunks[tl.chunk].n_rows;
             total += tl.begin < n ? std::min<uint64_t>(kBuffTileRows, n - tl.begin) : 0;
         }
-        if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
+        if (total > out_cap) {
+            if (n_out) *n_out = total;
+            return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
+        }
         q.tile_counts = nullptr;
     } else {
         q.tile_counts = c->d_tile_counts;
@@ -376,8 +379,8 @@ int run_materialize(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, dou
     if (d_mask) total = c->h_res->count;
     int st = finish(c, q, s);
     if (st) return st;
-    if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
     if (n_out) *n_out = total;
+    if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
     return EBI_OK;
 }
 

@@ -227,10 +227,17 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
     const double bb = s - a;
     e = (a - (s - bb)) + (b - bb);
 }
-// (hi, lo) += (bh, bl) in double-double arithmetic.
+// (hi, lo) += (bh, bl) in double-double arithmetic.  Once the leading sum is
+// infinite or NaN the error terms are meaningless (inf - inf): the pair then
+// carries the plain IEEE sum, as the sequential f64 sum does.
 __device__ __forceinline__ void dd_add(double& hi, double& lo, double bh, double bl) {
     double s, e;
     two_sum(hi, bh, s, e);
+    if (!isfinite(s)) {
+        hi = s;
+        lo = 0.0;
+        return;
+    }
     e += lo + bl;
     hi = s + e;
     lo = e - (hi - s);

@@ -98,8 +98,10 @@ int ebi_column_set_precision(ebi_column* col, int32_t precision);
 /* ---- queries (Decoder methods, api/decoder.rs:202-439) -------------------- */
 
 /* Decoder::materialize: decoded values of the rows in `mask` (all rows when
- * NULL), in row order, to d_out[0 .. *n_out).  Fails with EBI_E_INVALID and
- * writes nothing past out_cap when more than out_cap values qualify. */
+ * NULL), in row order, to d_out[0 .. *n_out).  When more than out_cap values
+ * qualify it writes nothing past out_cap, sets *n_out to the number needed
+ * and fails with EBI_E_INVALID, so the caller can retry with a larger buffer
+ * (decoded chunks may hold more values than their footer's row count). */
 int ebi_materialize(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* d_out,
                     uint64_t out_cap, uint64_t* n_out, void* stream);
 
