@@ -51,6 +51,9 @@ cudaError_t launch_rle(const QueryParams& q, uint32_t chunk_begin, uint32_t n_ch
                        const unsigned long long* chunk_offsets, cudaStream_t s);
 cudaError_t launch_raw(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                        const unsigned long long* chunk_offsets, cudaStream_t s);
+// Gorilla: one warp per chunk following the stream several records per step.
+cudaError_t launch_gorilla(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
+                           const unsigned long long* chunk_offsets, cudaStream_t s);
 // Gorilla, Chimp, Chimp128 (q.scheme selects the decoder).
 cudaError_t launch_xor(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                        const unsigned long long* chunk_offsets, cudaStream_t s);

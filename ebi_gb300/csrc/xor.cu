@@ -13,8 +13,8 @@
 // for a '00' copy); a read past the chunk raises UnexpectedEndOfChunk first.
 //
 // Decoding is split in three parallel steps:
-//   1. control parse.  The chunk's bits (staged in shared memory) are cut into
-//      one segment per thread.  Thread 0 starts at the true first record;
+//   1. control parse.  The chunk's bits (read through L1 from the resident
+//      file) are cut into one segment per thread.  Thread 0 starts at the true first record;
 //      every other thread guesses a start and parses its segment.  Each round
 //      a thread whose start differs from its predecessor's end adopts that end
 //      and parses again.  The segments agree with the sequential parse once
@@ -30,10 +30,11 @@
 //      the references (ceil(log2 n) rounds).  The first NaN ends the chunk.
 // The query then runs row-parallel over the values in shared memory.
 //
-// A chunk with more records than kRcap or more bytes than the staging area
-// (only for chunks far above 8,192 values) is decoded by one thread in order.
+// A chunk with more records than kRcap (only for chunks far above 8,192
+// values) is decoded by one thread in order.
 #include "internal.h"
 #include "values.cuh"
+#include "bitstream.cuh"
 #include "xor_parse.cuh"
 
 namespace ebi {
@@ -43,26 +44,6 @@ using namespace xorp;
 
 constexpr int kThreads = 256;
 constexpr uint32_t kRcap = 8448;         // records (values) held in shared memory
-constexpr uint32_t kStageWords = 24576;  // 96 KB of staged bitstream
-__device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
-
-// 64 bits of the stream starting at bit q of a big-endian word array.
-__device__ __forceinline__ uint64_t peek64(const uint32_t* w, uint64_t q) {
-    const uint64_t i = q >> 5;
-    const uint32_t sh = static_cast<uint32_t>(q & 31);
-    const uint32_t a = w[i], b = w[i + 1], c = w[i + 2];
-    const uint32_t hi = __funnelshift_l(b, a, sh), lo = __funnelshift_l(c, b, sh);
-    return (uint64_t(hi) << 32) | lo;
-}
-// Same from little-endian file words (global memory, unstaged).
-__device__ __forceinline__ uint64_t peek64_file(const uint32_t* w, uint64_t q) {
-    const uint64_t i = q >> 5;
-    const uint32_t sh = static_cast<uint32_t>(q & 31);
-    const uint32_t a = bswap32(w[i]), b = bswap32(w[i + 1]), c = bswap32(w[i + 2]);
-    const uint32_t hi = __funnelshift_l(b, a, sh), lo = __funnelshift_l(c, b, sh);
-    return (uint64_t(hi) << 32) | lo;
-}
-
 __device__ __forceinline__ uint32_t block_min_u32(uint32_t v, uint32_t* sh) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -78,7 +59,6 @@ __device__ __forceinline__ uint32_t block_min_u32(uint32_t v, uint32_t* sh) {
 
 struct Smem {
     uint64_t* vals;   // kRcap: deltas, then values
-    uint32_t* stage;  // kStageWords: big-endian stream words
     uint16_t* refs;   // kRcap (Chimp128)
     uint32_t* nanok;  // kRcap / 32 (Chimp128)
 };
@@ -149,13 +129,12 @@ __device__ uint32_t decode_serial(const uint32_t* fw, uint64_t bit0, uint64_t B,
 }
 
 template <int CODEC>
-__global__ void __launch_bounds__(kThreads) xor_kernel(QueryParams q, uint32_t chunk_base, int mode,
+__global__ void __launch_bounds__(kThreads, 2) xor_kernel(QueryParams q, uint32_t chunk_base, int mode,
                                                        const unsigned long long* chunk_offsets) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     Smem sm;
     sm.vals = reinterpret_cast<uint64_t*>(smem_raw);
-    sm.stage = reinterpret_cast<uint32_t*>(sm.vals + kRcap);
-    sm.refs = reinterpret_cast<uint16_t*>(sm.stage + kStageWords);
+    sm.refs = reinterpret_cast<uint16_t*>(sm.vals + kRcap);
     sm.nanok = reinterpret_cast<uint32_t*>(sm.refs + kRcap);
     __shared__ uint64_t s_in[kThreads], s_out[kThreads];
     __shared__ uint32_t s_red[kThreads / 32];
@@ -197,19 +176,15 @@ __global__ void __launch_bounds__(kThreads) xor_kernel(QueryParams q, uint32_t c
     const bool pred_on = q.pred_on != 0;
     const bool store = mode == VAL_SCAN && pred_on && q.out_mask != nullptr;
     const uint64_t B = cd.byte_len * 8;
-    const uint64_t w0 = cd.byte_off >> 2;                       // first file word of the chunk
-    const uint64_t nwords = ((cd.byte_off + cd.byte_len + 3) >> 2) - w0 + 3;
-    const uint64_t bit0 = (cd.byte_off & 3) * 8;                // chunk start within the staged words
     const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
-    const bool parallel = nwords <= kStageWords && B >= 64;
+    const uint64_t bit0 = cd.byte_off * 8;
+    // well-formed chunks hold n_rows + 1 records (the end marker included)
+    const bool parallel = B >= 64 && cd.n_rows + 1 < kRcap;
 
     uint32_t end = 0;         // decoded values (the NaN end marker's index)
     bool serial = !parallel;
     if (parallel) {
-        // ---- stage the stream as big-endian words -------------------------
-        for (uint64_t i = tid; i < nwords; i += kThreads) sm.stage[i] = bswap32(fw[w0 + i]);
-        __syncthreads();
-        auto peek = [&sm, bit0](uint64_t p) { return peek64(sm.stage, bit0 + p); };
+        auto peek = [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); };
 
         // ---- 1. control parse: segments converge to the sequential parse ---
         const uint64_t span = B - 64;
@@ -290,36 +265,43 @@ __global__ void __launch_bounds__(kThreads) xor_kernel(QueryParams q, uint32_t c
             if (pre)
                 for (uint32_t i = b + lane; i < e; i += 32) sm.vals[i] ^= pre;
         } else {
-            // pointer jumping: value(i) = acc(i) ^ value(ref(i)), value(kNoRef) = 0
+            // pointer jumping: value(i) = acc(i) ^ value(ref(i)), value(kNoRef) = 0.
+            // Entries jump in groups; a group reads (acc, ref) pairs between two
+            // barriers and writes them between the next two, so every pair read
+            // is a consistent jump state and the invariant above holds throughout.
             constexpr int kPer = (kRcap + kThreads - 1) / kThreads;
+            constexpr int kGroup = 11;
             for (int round = 0; round < 20; ++round) {
-                uint64_t a[kPer];
-                uint16_t p[kPer];
                 bool any = false;
+                for (int g0 = 0; g0 < kPer; g0 += kGroup) {
+                    uint64_t a[kGroup];
+                    uint16_t p[kGroup];
 #pragma unroll
-                for (int k = 0; k < kPer; ++k) {
-                    const uint32_t i = tid + k * kThreads;
-                    p[k] = kNoRef;
-                    a[k] = 0;
-                    if (i < Rs) {
-                        const uint32_t r = sm.refs[i];
-                        if (r != kNoRef) {
-                            a[k] = sm.vals[r];
-                            p[k] = sm.refs[r];
-                            any = true;
+                    for (int k = 0; k < kGroup; ++k) {
+                        const uint32_t i = tid + (g0 + k) * kThreads;
+                        p[k] = kNoRef;
+                        a[k] = 0;
+                        if (g0 + k < kPer && i < Rs) {
+                            const uint32_t r = sm.refs[i];
+                            if (r != kNoRef) {
+                                a[k] = sm.vals[r];
+                                p[k] = sm.refs[r];
+                                any = true;
+                            }
                         }
                     }
+                    __syncthreads();
+#pragma unroll
+                    for (int k = 0; k < kGroup; ++k) {
+                        const uint32_t i = tid + (g0 + k) * kThreads;
+                        if (g0 + k < kPer && i < Rs && sm.refs[i] != kNoRef) {
+                            sm.vals[i] ^= a[k];
+                            sm.refs[i] = p[k];
+                        }
+                    }
+                    __syncthreads();
                 }
                 if (!__syncthreads_or(any)) break;
-#pragma unroll
-                for (int k = 0; k < kPer; ++k) {
-                    const uint32_t i = tid + k * kThreads;
-                    if (i < Rs && sm.refs[i] != kNoRef) {
-                        sm.vals[i] ^= a[k];
-                        sm.refs[i] = p[k];
-                    }
-                }
-                __syncthreads();
             }
         }
         __syncthreads();
@@ -346,7 +328,7 @@ __global__ void __launch_bounds__(kThreads) xor_kernel(QueryParams q, uint32_t c
         if (tid == 0) {
             SerialSink sink{&q, cd.row_off, mode, has_mask, pred_on, store, val_agg_init(),
                             mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull, 0, 0};
-            const uint32_t e = decode_serial<CODEC>(fw, cd.byte_off * 8, B, sm.vals, sink);
+            const uint32_t e = decode_serial<CODEC>(fw, bit0, B, sm.vals, sink);
             if (e) {
                 set_status(acc, e);
                 if (mode == VAL_COUNT) q.tile_counts[li] = 0;
@@ -390,7 +372,7 @@ __global__ void __launch_bounds__(kThreads) xor_kernel(QueryParams q, uint32_t c
 }
 
 constexpr size_t smem_bytes(int codec) {
-    return kRcap * 8 + kStageWords * 4 + (codec == CODEC_CHIMP128 ? kRcap * 2 + kRcap / 8 : 0);
+    return kRcap * 8 + (codec == CODEC_CHIMP128 ? kRcap * 2 + kRcap / 8 : 0);
 }
 
 template <int CODEC>
@@ -415,7 +397,7 @@ cudaError_t launch_xor(const QueryParams& q, uint32_t chunk_begin, uint32_t n_ch
                        const unsigned long long* chunk_offsets, cudaStream_t s) {
     if (n_chunks == 0) return cudaSuccess;
     switch (q.scheme) {
-    case EBI_GORILLA: return launch_codec<CODEC_GORILLA>(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
+    case EBI_GORILLA: return launch_gorilla(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
     case EBI_CHIMP: return launch_codec<CODEC_CHIMP>(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
     case EBI_CHIMP128: return launch_codec<CODEC_CHIMP128>(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
     default: return cudaErrorInvalidValue;

@@ -131,18 +131,50 @@ XOR_HD uint32_t parse_rec(Peek peek, uint64_t B, PState& s, Rec& r) {
     }
 }
 
+// Length-only step of one Chimp / Chimp128 record (the convergence rounds of
+// the segment parse need positions and windows, not payloads): selects
+// instead of branches, one 64-bit read.  Same errors as parse_rec.
+template <int CODEC, typename Peek>
+XOR_HD uint32_t step_len(Peek peek, uint64_t B, PState& s) {
+    const uint64_t p = s.pos;
+    if (p + 2 > B) return EBI_E_UNEXPECTED_END;
+    const uint64_t x = peek(p);
+    const uint32_t flag = static_cast<uint32_t>(x >> 62);
+    constexpr uint32_t hdr1 = CODEC == CODEC_CHIMP128 ? 16u : 9u;  // '01' header after the flag
+    const uint32_t t1 = static_cast<uint32_t>(x >> (62 - hdr1)) & ((1u << hdr1) - 1u);
+    const uint32_t lead1 = lead_decode((t1 >> 6) & 7u);
+    const uint32_t sig1 = (t1 & 63u) ? (t1 & 63u) : 64u;
+    const uint32_t lead3 = lead_decode(static_cast<uint32_t>(x >> 59) & 7u);
+    const uint32_t lead = s.win;
+    // header bits (flag included) and total length per flag
+    const uint32_t hdr = flag == 0 ? (CODEC == CODEC_CHIMP128 ? 9u : 2u) : flag == 1 ? 2 + hdr1 : flag == 2 ? 2u : 5u;
+    const uint32_t body = flag == 0 ? 0u : flag == 1 ? sig1 : flag == 2 ? 64u - (lead > 64 ? 0u : lead) : 64u - lead3;
+    const bool corrupt = (flag == 1 && sig1 + lead1 > 64) || (flag == 2 && lead > 64);
+    if (flag != 2 && p + hdr > B) return EBI_E_UNEXPECTED_END;
+    if (corrupt) return EBI_E_CORRUPT;
+    if (p + hdr + body > B) return EBI_E_UNEXPECTED_END;
+    s.win = flag == 1 ? lead1 : flag == 3 ? lead3 : lead;
+    s.pos = p + hdr + body;
+    return 0;
+}
+
 // Parses the records that start in [s.pos, end).  Counts the records before
 // the first failure (*fail = its error) and, when it fails, steps one bit and
 // goes on: a failing segment is either the true end of the stream or a
 // misaligned guess, and a misaligned parse should keep looking for the true
 // record boundaries.  The last segment fails at the end of the stream.
 template <int CODEC, typename Peek>
-XOR_HD PState parse_segment(Peek peek, uint64_t B, PState s, uint64_t end, bool last,
-                                                uint32_t* n_out, uint32_t* fail) {
+XOR_HD PState parse_segment(Peek peek, uint64_t B, PState s, uint64_t end, bool last, uint32_t* n_out,
+                            uint32_t* fail) {
     uint32_t n = 0, f = 0;
-    Rec r;
     while (s.pos < end) {
-        const uint32_t e = parse_rec<CODEC>(peek, B, s, r);
+        uint32_t e;
+        if (CODEC == CODEC_GORILLA) {
+            Rec r;
+            e = parse_rec<CODEC>(peek, B, s, r);
+        } else {
+            e = step_len<CODEC>(peek, B, s);
+        }
         if (e) {
             if (!f) f = e;
             s.pos += 1;
