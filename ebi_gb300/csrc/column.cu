@@ -91,6 +91,7 @@ struct ebi_column {
     uint32_t buff_frac = 0;
     bool buff_fast_ok = false;
     bool fused_pending = false;  // the last query's kernel already folded into d_res
+    uint32_t stage_bytes = 0;    // Gorilla: shared-memory staging per chunk
     // segment timing (ebi_column_set_timing)
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // query start, scan end, finalize end
@@ -193,6 +194,7 @@ QueryParams base_params(const ebi_column* c) {
     q.scheme = c->scheme;
     q.agg = AGG_ALL;
     q.binfo = c->d_buff;
+    q.stage_bytes = c->stage_bytes;
     return q;
 }
 
@@ -420,6 +422,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         c->scan_grid = static_cast<uint32_t>(std::max(sms, 1)) * per_sm;
     } else {
+        if (c->scheme == EBI_GORILLA) c->stage_bytes = gorilla_stage_bytes(c->chunks.data(), c->n_chunks);
         c->tiles.tiles.resize(c->n_chunks);
         c->tiles.first_tile.resize(c->n_chunks + 1);
         for (uint64_t i = 0; i < c->n_chunks; ++i) {

@@ -124,6 +124,7 @@ struct QueryParams {
     uint32_t agg;              // AGG_* aggregates the caller asked for (the count is always kept)
     const BuffChunkInfo* binfo;  // BUFF: header facts per chunk
     int pred_on;               // value codecs: the predicate selects rows (filter, filter+agg, filter_materialize)
+    uint32_t stage_bytes;      // Gorilla: shared-memory staging size per chunk (0: read through L1)
 };
 
 // Passes of the value-codec kernels (one CTA per chunk).

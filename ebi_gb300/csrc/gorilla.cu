@@ -19,15 +19,36 @@
 // windows, so an 8,192-value chunk takes a few hundred warp steps.  Each
 // step's values go straight to the query: NaN end check, bitmask ballot,
 // per-lane compensated sums, materialize positions from the ballot.
+//
+// Every step's read depends on the previous step's position, so the chunk is
+// first brought into shared memory by one bulk copy (cp.async.bulk, completed
+// on an mbarrier with a bounded wait); chunks above the staging size are read
+// through L1 from the resident file instead.
 #include "internal.h"
 #include "bitstream.cuh"
+#include "tma.cuh"
 #include "values.cuh"
 
 namespace ebi {
 namespace {
 
-constexpr int kWarpsPerCta = 4;
+constexpr int kWarpsPerCta = 1;  // one chunk (and its staged bytes) per CTA
 constexpr uint32_t kFull = 0xffffffffu;
+
+// 64 stream bits from little-endian words in shared memory.
+__device__ __forceinline__ uint64_t peek64_le_smem(const uint32_t* w, uint64_t q) {
+    const uint32_t i = static_cast<uint32_t>(q >> 5);
+    const uint32_t sh = static_cast<uint32_t>(q & 31);
+    const uint32_t a = bswap32(w[i]), b = bswap32(w[i + 1]), c = bswap32(w[i + 2]);
+    const uint32_t hi = __funnelshift_l(b, a, sh), lo = __funnelshift_l(c, b, sh);
+    return (uint64_t(hi) << 32) | lo;
+}
+
+// Bytes [byte_off & ~15, end) staged for a chunk: 16-byte aligned both ends
+// (bulk-copy rule) and 16 bytes past the chunk for the last read's over-read.
+__host__ __device__ __forceinline__ uint64_t stage_span(uint64_t byte_off, uint64_t byte_len) {
+    return ((byte_off + byte_len + 15) & ~uint64_t(15)) + 16 - (byte_off & ~uint64_t(15));
+}
 
 // Warp merge of per-lane partials in a fixed tree; the result is in lane 0.
 __device__ __forceinline__ ValAgg val_agg_warp(ValAgg a) {
@@ -45,45 +66,13 @@ __device__ __forceinline__ ValAgg val_agg_warp(ValAgg a) {
     return a;
 }
 
-__global__ void __launch_bounds__(kWarpsPerCta * 32) gorilla_kernel(QueryParams q, uint32_t chunk_base, uint32_t n_chunks,
-                                                                    int mode, const unsigned long long* chunk_offsets) {
+// Decodes chunk cd and runs the query over its values (one warp).
+template <typename Peek>
+__device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, ChunkAcc* acc, uint32_t li, int mode,
+                                     const unsigned long long* chunk_offsets, Peek peek) {
     const int lane = threadIdx.x & 31;
-    const uint32_t li = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
-    if (li >= n_chunks) return;  // whole warps; the kernel has no block barriers
-    const uint32_t c = chunk_base + li;
-    const ChunkDesc cd = q.chunks[c];
-    ChunkAcc* acc = q.acc + c;
     const bool has_mask = q.in_mask != nullptr;
-
-    int ok = 1;
-    if (lane == 0) {
-        if (mode == VAL_SCAN) {
-            ok = has_mask ? acc->selected != 0 : (q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
-            if (ok && !has_mask) acc->selected = 1;
-        } else if (mode == VAL_MATERIALIZE) {
-            ok = chunk_offsets[li + 1] != chunk_offsets[li];
-        } else if (has_mask) {
-            // the Decoder reads a chunk only when the bitmask meets its rows
-            uint32_t any = 0;
-            for (uint64_t r = 0; r < cd.n_rows && !any; r += 32) {
-                uint32_t w = mask_word(q.in_mask, cd.row_off + r, q.n_records);
-                if (cd.n_rows - r < 32) w &= (1u << (cd.n_rows - r)) - 1u;
-                any = w;
-            }
-            ok = any != 0;
-        }
-        if (ok && (cd.flags & kChunkBadGeometry)) {
-            set_status(acc, EBI_E_IO);
-            ok = 0;
-        }
-        if (!ok && mode == VAL_COUNT) q.tile_counts[li] = 0;
-    }
-    if (!__shfl_sync(kFull, ok, 0)) return;
-
-    const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
-    const uint64_t bit0 = cd.byte_off * 8;
     const uint64_t B = cd.byte_len * 8;
-    auto peek = [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); };
     const bool pred_on = q.pred_on != 0;
     const bool store = mode == VAL_SCAN && pred_on && q.out_mask != nullptr;
     ValAgg agg = val_agg_init();
@@ -202,13 +191,96 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) gorilla_kernel(QueryParams 
     else val_agg_store(acc, a);
 }
 
+__global__ void __launch_bounds__(kWarpsPerCta * 32) gorilla_kernel(QueryParams q, uint32_t chunk_base, uint32_t n_chunks,
+                                                                    int mode, const unsigned long long* chunk_offsets) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t li = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+    if (li >= n_chunks) return;  // whole warps; the kernel has no block barriers
+    const uint32_t c = chunk_base + li;
+    const ChunkDesc cd = q.chunks[c];
+    ChunkAcc* acc = q.acc + c;
+    const bool has_mask = q.in_mask != nullptr;
+
+    int ok = 1;
+    if (lane == 0) {
+        if (mode == VAL_SCAN) {
+            ok = has_mask ? acc->selected != 0 : (q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
+            if (ok && !has_mask) acc->selected = 1;
+        } else if (mode == VAL_MATERIALIZE) {
+            ok = chunk_offsets[li + 1] != chunk_offsets[li];
+        } else if (has_mask) {
+            // the Decoder reads a chunk only when the bitmask meets its rows
+            uint32_t any = 0;
+            for (uint64_t r = 0; r < cd.n_rows && !any; r += 32) {
+                uint32_t w = mask_word(q.in_mask, cd.row_off + r, q.n_records);
+                if (cd.n_rows - r < 32) w &= (1u << (cd.n_rows - r)) - 1u;
+                any = w;
+            }
+            ok = any != 0;
+        }
+        if (ok && (cd.flags & kChunkBadGeometry)) {
+            set_status(acc, EBI_E_IO);
+            ok = 0;
+        }
+        if (!ok && mode == VAL_COUNT) q.tile_counts[li] = 0;
+    }
+    if (!__shfl_sync(kFull, ok, 0)) return;
+
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+    const uint32_t* stage = reinterpret_cast<const uint32_t*>(smem + 16);
+    const uint64_t span = stage_span(cd.byte_off, cd.byte_len);
+    if (span <= q.stage_bytes) {
+        const uint8_t* src = q.file + (cd.byte_off & ~uint64_t(15));
+        if (lane == 0) {
+            mbar_init(bar, 1);
+            fence_mbar_init();
+            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(span));
+            bulk_g2s(smem + 16, src, static_cast<uint32_t>(span), bar);
+        }
+        __syncwarp();
+        bool arrived = mbar_wait(bar, 0);
+        if (!__all_sync(kFull, arrived)) {
+            // give the copy a second bounded wait before the CTA leaves, then report it
+            mbar_wait(bar, 0);
+            if (lane == 0) {
+                set_status(acc, EBI_E_CUDA);
+                if (mode == VAL_COUNT) q.tile_counts[li] = 0;
+            }
+            return;
+        }
+        const uint64_t bit0 = (cd.byte_off & 15) * 8;
+        walk(q, cd, acc, li, mode, chunk_offsets, [stage, bit0](uint64_t p) { return peek64_le_smem(stage, bit0 + p); });
+    } else {
+        const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
+        const uint64_t bit0 = cd.byte_off * 8;
+        walk(q, cd, acc, li, mode, chunk_offsets, [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); });
+    }
+}
+
 }  // namespace
+
+uint32_t gorilla_stage_bytes(const ChunkDesc* chunks, uint64_t n) {
+    uint64_t mx = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        if (chunks[i].flags & kChunkBadGeometry) continue;
+        const uint64_t sp = stage_span(chunks[i].byte_off, chunks[i].byte_len);
+        if (sp <= kGorillaStageCap && sp > mx) mx = sp;
+    }
+    return static_cast<uint32_t>(mx);
+}
 
 cudaError_t launch_gorilla(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                            const unsigned long long* chunk_offsets, cudaStream_t s) {
     if (n_chunks == 0) return cudaSuccess;
     const uint32_t grid = (n_chunks + kWarpsPerCta - 1) / kWarpsPerCta;
-    gorilla_kernel<<<grid, kWarpsPerCta * 32, 0, s>>>(q, chunk_begin, n_chunks, mode, chunk_offsets);
+    const size_t smem = q.stage_bytes ? 16 + size_t(q.stage_bytes) : 16;
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(gorilla_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    gorilla_kernel<<<grid, kWarpsPerCta * 32, smem, s>>>(q, chunk_begin, n_chunks, mode, chunk_offsets);
     count_launch();
     return cudaGetLastError();
 }

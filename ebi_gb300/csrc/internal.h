@@ -52,6 +52,10 @@ cudaError_t launch_rle(const QueryParams& q, uint32_t chunk_begin, uint32_t n_ch
 cudaError_t launch_raw(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                        const unsigned long long* chunk_offsets, cudaStream_t s);
 // Gorilla: one warp per chunk following the stream several records per step.
+// Chunks whose aligned byte span is at most kGorillaStageCap are staged in
+// shared memory; gorilla_stage_bytes is the per-CTA staging size of a column.
+constexpr uint32_t kGorillaStageCap = 100 * 1024;
+uint32_t gorilla_stage_bytes(const ChunkDesc* chunks, uint64_t n);
 cudaError_t launch_gorilla(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                            const unsigned long long* chunk_offsets, cudaStream_t s);
 // Gorilla, Chimp, Chimp128 (q.scheme selects the decoder).

@@ -185,6 +185,10 @@ __global__ void __launch_bounds__(kThreads, 2) xor_kernel(QueryParams q, uint32_
     bool serial = !parallel;
     if (parallel) {
         auto peek = [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); };
+        // The parse's reads depend on one another: bring the chunk into L2 first.
+        for (uint64_t a = (cd.byte_off & ~uint64_t(127)) + uint64_t(tid) * 128; a < cd.byte_off + cd.byte_len;
+             a += uint64_t(kThreads) * 128)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(q.file + a));
 
         // ---- 1. control parse: segments converge to the sequential parse ---
         const uint64_t span = B - 64;
