@@ -536,14 +536,15 @@ int ebi_filter_agg(ebi_column* c, const ebi_predicate* pred, const uint64_t* d_m
     return EBI_OK;
 }
 
-static int agg_common(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, void* stream) {
+static int agg_common(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, void* stream, uint32_t agg) {
     if (!c) return fail(EBI_E_INVALID, "column is null");
     int st = check_supported(c);
     if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    st = run_scan(c, OP_AGG, nullptr, d_mask, chunk_id, nullptr, nullptr, s);
+    st = run_scan(c, OP_AGG, nullptr, d_mask, chunk_id, nullptr, nullptr, s, agg);
     if (st) return st;
     QueryParams q = base_params(c);
+    q.agg = agg;
     q.op = OP_AGG;
     q.chunk_id = chunk_id;
     q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
@@ -551,17 +552,17 @@ static int agg_common(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, v
 }
 
 int ebi_sum(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream) {
-    const int st = agg_common(c, d_mask, chunk_id, stream);
+    const int st = agg_common(c, d_mask, chunk_id, stream, AGG_SUM);
     if (!st && out) *out = c->h_res->sum;
     return st;
 }
 int ebi_min(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream) {
-    const int st = agg_common(c, d_mask, chunk_id, stream);
+    const int st = agg_common(c, d_mask, chunk_id, stream, AGG_MIN);
     if (!st && out) *out = c->h_res->min;
     return st;
 }
 int ebi_max(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream) {
-    const int st = agg_common(c, d_mask, chunk_id, stream);
+    const int st = agg_common(c, d_mask, chunk_id, stream, AGG_MAX);
     if (!st && out) *out = c->h_res->max;
     return st;
 }

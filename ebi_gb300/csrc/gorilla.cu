@@ -50,22 +50,6 @@ __host__ __device__ __forceinline__ uint64_t stage_span(uint64_t byte_off, uint6
     return ((byte_off + byte_len + 15) & ~uint64_t(15)) + 16 - (byte_off & ~uint64_t(15));
 }
 
-// Warp merge of per-lane partials in a fixed tree; the result is in lane 0.
-__device__ __forceinline__ ValAgg val_agg_warp(ValAgg a) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        ValAgg b;
-        b.hi = __shfl_down_sync(kFull, a.hi, o);
-        b.lo = __shfl_down_sync(kFull, a.lo, o);
-        b.mn = __shfl_down_sync(kFull, a.mn, o);
-        b.mx = __shfl_down_sync(kFull, a.mx, o);
-        b.cnt = __shfl_down_sync(kFull, a.cnt, o);
-        if ((lane & (2 * o - 1)) == 0) val_agg_merge(a, b);
-    }
-    return a;
-}
-
 // Decodes chunk cd and runs the query over its values (one warp).
 template <typename Peek>
 __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, ChunkAcc* acc, uint32_t li, int mode,
@@ -75,7 +59,8 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
     const uint64_t B = cd.byte_len * 8;
     const bool pred_on = q.pred_on != 0;
     const bool store = mode == VAL_SCAN && pred_on && q.out_mask != nullptr;
-    ValAgg agg = val_agg_init();
+    const KeyPred kp = key_pred(q.pred);
+    ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
     unsigned long long out_pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull;
     uint64_t idx = 0;  // chunk row of the next value
 
@@ -89,14 +74,13 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
             ended = true;
         }
         const uint64_t g = cd.row_off + idx + lane;
-        const double v = __longlong_as_double(static_cast<long long>(vbits));
         const bool in = static_cast<uint32_t>(lane) < k && (!has_mask || mask_row(q.in_mask, q.n_records, g));
-        const bool pass = in && (!pred_on || pred_eval(q.pred, v));
+        const bool pass = in && (!pred_on || kp.pass(vbits));
         if (mode == VAL_MATERIALIZE) {
             const uint32_t bal = __ballot_sync(kFull, pass);
             if (pass) {
                 const unsigned long long pos = out_pos + __popc(bal & ((1u << lane) - 1u));
-                if (pos < q.out_cap) q.out_vals[pos] = v;
+                if (pos < q.out_cap) q.out_vals[pos] = __longlong_as_double(static_cast<long long>(vbits));
             }
             out_pos += __popc(bal);
         } else {
@@ -106,7 +90,7 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
             }
             if (pass) {
                 if (mode == VAL_COUNT) ++agg.cnt;
-                else val_agg_add(agg, v, 1);
+                else val_agg_add1(agg, vbits);
             }
         }
         idx += k;

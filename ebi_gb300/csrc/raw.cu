@@ -16,10 +16,9 @@ namespace {
 
 constexpr int kThreads = 512;
 
-__device__ __forceinline__ double raw_value(const uint64_t* w, uint32_t sh, uint64_t r) {
+__device__ __forceinline__ uint64_t raw_bits(const uint64_t* w, uint32_t sh, uint64_t r) {
     const uint64_t a = w[r];
-    const uint64_t v = sh ? (a >> sh) | (w[r + 1] << (64 - sh)) : a;
-    return __longlong_as_double(static_cast<long long>(v));
+    return sh ? (a >> sh) | (w[r + 1] << (64 - sh)) : a;
 }
 
 __global__ void __launch_bounds__(kThreads) raw_kernel(QueryParams q, uint32_t chunk_base, int mode,
@@ -59,7 +58,8 @@ __global__ void __launch_bounds__(kThreads) raw_kernel(QueryParams q, uint32_t c
     const uint32_t sh = static_cast<uint32_t>(addr & 7) * 8;
     const bool pred_on = q.pred_on != 0;
     const bool store = mode == VAL_SCAN && pred_on && q.out_mask != nullptr;
-    ValAgg agg = val_agg_init();
+    const KeyPred kp = key_pred(q.pred);
+    ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
     unsigned long long pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0;
     uint32_t count_in_mask = 0;  // count pass over an unreadable chunk: rows the bitmask selects
     for (uint64_t r0 = 0; r0 < cd.n_rows; r0 += kThreads) {
@@ -70,12 +70,12 @@ __global__ void __launch_bounds__(kThreads) raw_kernel(QueryParams q, uint32_t c
             count_in_mask += in;
             continue;
         }
-        const double v = in ? raw_value(words, sh, r) : 0.0;
-        const bool pass = in && (!pred_on || pred_eval(q.pred, v));
+        const uint64_t vb = in ? raw_bits(words, sh, r) : 0;
+        const bool pass = in && (!pred_on || kp.pass(vb));
         if (mode == VAL_MATERIALIZE) {
             uint32_t total;
             const uint32_t before = block_excl_scan_u32<kThreads>(pass, sh_scan, &total);
-            if (pass && pos + before < q.out_cap) q.out_vals[pos + before] = v;
+            if (pass && pos + before < q.out_cap) q.out_vals[pos + before] = __longlong_as_double(static_cast<long long>(vb));
             pos += total;
             continue;
         }
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kThreads) raw_kernel(QueryParams q, uint32_t c
             const uint32_t word = __ballot_sync(0xffffffffu, pass && g < q.n_records);
             if (lane == 0 && word) store_mask_word(q.out_mask, g, word, true);
         }
-        if (pass) val_agg_add(agg, v, 1);
+        if (pass) val_agg_add1(agg, vb);
     }
     if (mode == VAL_MATERIALIZE) return;
     const ValAgg a = val_agg_block(agg, sh_agg);

@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(kThreads) rle_kernel(QueryParams q, uint32_t c
     const uint8_t* fields = base + 8;
     const bool pred_on = q.pred_on != 0;
     const bool store = mode == VAL_SCAN && pred_on && q.out_mask;
-    ValAgg agg = val_agg_init();
+    const KeyPred kp = key_pred(q.pred);
+    ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
     unsigned long long out_pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0;
     uint64_t carry_row = 0;
     for (uint64_t b0 = 0; b0 < nf; b0 += kBatch) {
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(kThreads) rle_kernel(QueryParams q, uint32_t c
 #pragma unroll
         for (int k = 0; k < kPer; ++k) {
             const uint64_t g0 = cd.row_off + r;  // global rows [g0, g0 + run)
-            const bool pass = !pred_on || pred_eval(q.pred, val[k]);
+            const bool pass = !pred_on || kp.pass(static_cast<uint64_t>(__double_as_longlong(val[k])));
             uint32_t n_sel = 0;
             if (run[k] && pass) {
                 if (!has_mask) n_sel = run[k];

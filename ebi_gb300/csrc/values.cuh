@@ -4,60 +4,169 @@
 //
 // Per chunk, rows are judged as the default operators do: a row counts when
 // it is in the input bitmask (or there is none) and, for a filter, when the
-// predicate holds.  The chunk's sum is kept as a double-double (compensated)
-// value, min/max with fmin/fmax (NaN-ignoring, as f64::min/max).  Partial
-// results are combined in a fixed order, so a query returns the same bits on
-// every run and whatever else runs on the GPU.
+// predicate holds.  The chunk's sum is compensated, min/max are NaN-ignoring
+// (f64::min/max).  Partial results are combined in a fixed order, so a query
+// returns the same bits on every run and whatever else runs on the GPU.
 #pragma once
 
 #include "common.cuh"
 
 namespace ebi {
 
-struct ValAgg {
-    double hi, lo;   // double-double sum
-    double mn, mx;
-    unsigned long long cnt;
-};
+// ---- ordered keys ---------------------------------------------------------
+// order_key maps f64 bits to an unsigned key whose order is the IEEE total
+// order (-NaN < -inf < ... < -0 < +0 < ... < +inf < +NaN).  Predicates, min
+// and max compare keys on the integer pipes: GB300's FP64 pipe is a small
+// fraction of its integer throughput.
+constexpr uint64_t kAbsMask = 0x7fffffffffffffffull;
+constexpr uint64_t kSignBit = 0x8000000000000000ull;
+__host__ __device__ __forceinline__ constexpr uint64_t order_key(uint64_t b) { return (b >> 63) ? ~b : (b | kSignBit); }
+__host__ __device__ __forceinline__ constexpr uint64_t key_bits(uint64_t k) { return (k >> 63) ? (k & ~kSignBit) : ~k; }
+__device__ __forceinline__ bool is_nan_bits(uint64_t b) { return (b & kAbsMask) > 0x7ff0000000000000ull; }
+constexpr uint64_t kKeyPosInf = order_key(0x7ff0000000000000ull);
+constexpr uint64_t kKeyNegInf = order_key(0xfff0000000000000ull);
+// Key with -0 and +0 merged (they compare equal in IEEE predicates).
+__device__ __forceinline__ uint64_t cmp_key(uint64_t b) { return (b & kAbsMask) ? order_key(b) : kSignBit; }
 
-__device__ __forceinline__ ValAgg val_agg_init() {
-    const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    return ValAgg{0.0, 0.0, inf, -inf, 0};
+// A Predicate (decoder/query.rs:396-437) over keys: exactly the f64
+// comparisons of RangeImpl::eval / PredicateImpl::eval, NaN included (a NaN
+// operand fails every comparison, so NaN rows pass only Ne).
+struct KeyPred {
+    uint64_t lo, hi;  // cmp_key of the bounds (Eq / Ne: lo = the operand)
+    uint32_t kind;    // EBI_PRED_*
+    bool lo_on, lo_incl, hi_on, hi_incl, never;
+    __device__ __forceinline__ bool pass(uint64_t b) const {
+        if (is_nan_bits(b)) return kind == EBI_PRED_NE;
+        const uint64_t k = cmp_key(b);
+        if (kind != EBI_PRED_RANGE) return ((k == lo) && !never) != (kind == EBI_PRED_NE);
+        if (never) return false;
+        const bool a = !lo_on || (lo_incl ? k >= lo : k > lo);
+        const bool c = !hi_on || (hi_incl ? k <= hi : k < hi);
+        return a && c;
+    }
+};
+__device__ __forceinline__ KeyPred key_pred(const ebi_predicate& p) {
+    KeyPred kp{};
+    kp.kind = static_cast<uint32_t>(p.kind);
+    if (p.kind != EBI_PRED_RANGE) {
+        const uint64_t b = static_cast<uint64_t>(__double_as_longlong(p.value));
+        kp.never = is_nan_bits(b);  // x == NaN is false for every x
+        kp.lo = cmp_key(b);
+        return kp;
+    }
+    const uint64_t s = static_cast<uint64_t>(__double_as_longlong(p.start));
+    const uint64_t e = static_cast<uint64_t>(__double_as_longlong(p.end));
+    kp.lo_on = p.start_kind != EBI_BOUND_NONE;
+    kp.hi_on = p.end_kind != EBI_BOUND_NONE;
+    kp.lo_incl = p.start_kind == EBI_BOUND_INCLUSIVE;
+    kp.hi_incl = p.end_kind == EBI_BOUND_INCLUSIVE;
+    kp.never = (kp.lo_on && is_nan_bits(s)) || (kp.hi_on && is_nan_bits(e));
+    kp.lo = cmp_key(s);
+    kp.hi = cmp_key(e);
+    return kp;
 }
 
-// Adds k copies of v (v * k exactly, through an FMA product split).
+// ---- per-chunk aggregates --------------------------------------------------
+// The sum is compensated (Neumaier: a running sum plus the exact rounding
+// error of every addition), min/max are ordered keys with NaN skipped, as
+// f64::min / f64::max ignore a NaN operand.  `want` (AGG_* bits) switches off
+// what the caller did not ask for; the count is always kept.
+struct ValAgg {
+    double hi, lo;
+    unsigned long long mnk, mxk;
+    unsigned long long cnt;
+    uint32_t want;
+};
+
+__device__ __forceinline__ ValAgg val_agg_init(uint32_t want = AGG_ALL) {
+    return ValAgg{0.0, 0.0, kKeyPosInf, kKeyNegInf, 0, want};
+}
+
+// hi + lo += v (one FP64 add on the dependency chain through hi).  Once the
+// running sum leaves the finite range it carries the plain IEEE sum.
+__device__ __forceinline__ void neumaier_add(double& hi, double& lo, double v) {
+    const double s = hi + v;
+    const uint64_t sb = static_cast<uint64_t>(__double_as_longlong(s));
+    if ((sb & kAbsMask) < 0x7ff0000000000000ull) {
+        const uint64_t hb = static_cast<uint64_t>(__double_as_longlong(hi)) & kAbsMask;
+        const uint64_t vb = static_cast<uint64_t>(__double_as_longlong(v)) & kAbsMask;
+        lo += hb >= vb ? (hi - s) + v : (v - s) + hi;
+    }
+    hi = s;
+}
+__device__ __forceinline__ double neumaier_value(double hi, double lo) {
+    const uint64_t hb = static_cast<uint64_t>(__double_as_longlong(hi));
+    return (hb & kAbsMask) < 0x7ff0000000000000ull ? hi + lo : hi;
+}
+
+__device__ __forceinline__ void val_agg_minmax(ValAgg& a, uint64_t b) {
+    if ((a.want & (AGG_MIN | AGG_MAX)) && !is_nan_bits(b)) {
+        const uint64_t k = order_key(b);
+        a.mnk = k < a.mnk ? k : a.mnk;
+        a.mxk = k > a.mxk ? k : a.mxk;
+    }
+}
+
+// One value (bits).
+__device__ __forceinline__ void val_agg_add1(ValAgg& a, uint64_t b) {
+    ++a.cnt;
+    val_agg_minmax(a, b);
+    if (a.want & AGG_SUM) neumaier_add(a.hi, a.lo, __longlong_as_double(static_cast<long long>(b)));
+}
+
+// k copies of v (RLE runs): v * k split exactly into product and FMA error.
 __device__ __forceinline__ void val_agg_add(ValAgg& a, double v, uint32_t k) {
     if (!k) return;
-    const double kd = static_cast<double>(k);
-    const double p = v * kd;
-    const double e = fma(v, kd, -p);
-    dd_add(a.hi, a.lo, p, e);
-    a.mn = fmin(a.mn, v);
-    a.mx = fmax(a.mx, v);
     a.cnt += k;
+    const uint64_t b = static_cast<uint64_t>(__double_as_longlong(v));
+    val_agg_minmax(a, b);
+    if (a.want & AGG_SUM) {
+        const double kd = static_cast<double>(k);
+        const double p = v * kd;
+        neumaier_add(a.hi, a.lo, p);
+        const uint64_t pb = static_cast<uint64_t>(__double_as_longlong(p));
+        if ((pb & kAbsMask) < 0x7ff0000000000000ull) a.lo += fma(v, kd, -p);
+    }
 }
 
 __device__ __forceinline__ void val_agg_merge(ValAgg& a, const ValAgg& b) {
-    dd_add(a.hi, a.lo, b.hi, b.lo);
-    a.mn = fmin(a.mn, b.mn);
-    a.mx = fmax(a.mx, b.mx);
+    if (a.want & AGG_SUM) {
+        neumaier_add(a.hi, a.lo, b.hi);
+        const uint64_t hb = static_cast<uint64_t>(__double_as_longlong(a.hi));
+        if ((hb & kAbsMask) < 0x7ff0000000000000ull) a.lo += b.lo;
+    }
+    a.mnk = b.mnk < a.mnk ? b.mnk : a.mnk;
+    a.mxk = b.mxk > a.mxk ? b.mxk : a.mxk;
     a.cnt += b.cnt;
+}
+
+__device__ __forceinline__ ValAgg val_agg_shfl_down(const ValAgg& a, int o) {
+    ValAgg b;
+    b.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
+    b.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
+    b.mnk = __shfl_down_sync(0xffffffffu, a.mnk, o);
+    b.mxk = __shfl_down_sync(0xffffffffu, a.mxk, o);
+    b.cnt = __shfl_down_sync(0xffffffffu, a.cnt, o);
+    b.want = a.want;
+    return b;
+}
+
+// Warp merge in a fixed tree (lane order); the result is in lane 0.
+__device__ __forceinline__ ValAgg val_agg_warp(ValAgg a) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const ValAgg b = val_agg_shfl_down(a, o);
+        if ((lane & (2 * o - 1)) == 0) val_agg_merge(a, b);
+    }
+    return a;
 }
 
 // Block-wide merge in a fixed tree (lane order, then warp order); the result
 // is valid in thread 0.  `sh` holds one ValAgg per warp.
 __device__ inline ValAgg val_agg_block(ValAgg a, ValAgg* sh) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        ValAgg b;
-        b.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
-        b.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
-        b.mn = __shfl_down_sync(0xffffffffu, a.mn, o);
-        b.mx = __shfl_down_sync(0xffffffffu, a.mx, o);
-        b.cnt = __shfl_down_sync(0xffffffffu, a.cnt, o);
-        if ((lane & (2 * o - 1)) == 0 && lane + o < 32) val_agg_merge(a, b);
-    }
+    a = val_agg_warp(a);
     __syncthreads();
     if (lane == 0) sh[wid] = a;
     __syncthreads();
@@ -67,16 +176,13 @@ __device__ inline ValAgg val_agg_block(ValAgg a, ValAgg* sh) {
     return a;
 }
 
-// Adds a chunk's partial into its accumulator (one thread; chunks processed
-// by one CTA, so the order is fixed).
+// Stores a chunk's result in its accumulator (at rest before: one writer per chunk).
 __device__ __forceinline__ void val_agg_store(ChunkAcc* acc, const ValAgg& a) {
-    double hi = acc->fsum_hi, lo = acc->fsum_lo;
-    dd_add(hi, lo, a.hi, a.lo);
-    acc->fsum_hi = hi;
-    acc->fsum_lo = lo;
-    acc->fmin = fmin(acc->fmin, a.mn);
-    acc->fmax = fmax(acc->fmax, a.mx);
-    acc->count += a.cnt;
+    acc->fsum_hi = a.hi;
+    acc->fsum_lo = a.lo;
+    acc->fmin = __longlong_as_double(static_cast<long long>(key_bits(a.mnk)));
+    acc->fmax = __longlong_as_double(static_cast<long long>(key_bits(a.mxk)));
+    acc->count = a.cnt;
 }
 
 // Row g of the input bitmask (false past n_records, as RoaringBitmap::contains of a u32 row set).

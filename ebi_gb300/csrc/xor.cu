@@ -70,6 +70,7 @@ struct SerialSink {
     uint64_t row_off;
     int mode;
     bool has_mask, pred_on, store;
+    KeyPred kp;
     ValAgg agg;
     unsigned long long pos;
     uint64_t word_idx;
@@ -78,13 +79,13 @@ struct SerialSink {
         if (word) atomicOr(&q->out_mask[word_idx], word);
         word = 0;
     }
-    __device__ void row(uint64_t i, double v) {
+    __device__ void row(uint64_t i, uint64_t vb) {
         const uint64_t g = row_off + i;
         const bool in = !has_mask || mask_row(q->in_mask, q->n_records, g);
-        const bool pass = in && (!pred_on || pred_eval(q->pred, v));
+        const bool pass = in && (!pred_on || kp.pass(vb));
         if (!pass) return;
         if (mode == VAL_MATERIALIZE) {
-            if (pos < q->out_cap) q->out_vals[pos] = v;
+            if (pos < q->out_cap) q->out_vals[pos] = __longlong_as_double(static_cast<long long>(vb));
             ++pos;
             return;
         }
@@ -93,7 +94,7 @@ struct SerialSink {
             if ((g >> 5) != word_idx) { flush(); word_idx = g >> 5; }
             word |= 1u << (g & 31);
         }
-        val_agg_add(agg, v, 1);
+        val_agg_add1(agg, vb);
     }
 };
 
@@ -113,7 +114,7 @@ __device__ uint32_t decode_serial(const uint32_t* fw, uint64_t bit0, uint64_t B,
     bool check = true;
     for (uint64_t i = 0;; ++i) {
         if (check && v == kNanBits) return 0;
-        sink.row(i, __longlong_as_double(static_cast<long long>(v)));
+        sink.row(i, v);
         Rec r;
         const uint32_t e = parse_rec<CODEC>(peek, B, s, r);
         if (e) return e;
@@ -330,7 +331,8 @@ __global__ void __launch_bounds__(kThreads, 2) xor_kernel(QueryParams q, uint32_
     if (serial) {
         __syncthreads();
         if (tid == 0) {
-            SerialSink sink{&q, cd.row_off, mode, has_mask, pred_on, store, val_agg_init(),
+            SerialSink sink{&q, cd.row_off, mode, has_mask, pred_on, store, key_pred(q.pred),
+                            val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u),
                             mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull, 0, 0};
             const uint32_t e = decode_serial<CODEC>(fw, bit0, B, sm.vals, sink);
             if (e) {
@@ -347,18 +349,19 @@ __global__ void __launch_bounds__(kThreads, 2) xor_kernel(QueryParams q, uint32_
     }
 
     // ---- query over vals[0, end) ------------------------------------------
-    ValAgg agg = val_agg_init();
+    const KeyPred kp = key_pred(q.pred);
+    ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
     unsigned long long pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0;
     for (uint32_t r0 = 0; r0 < end; r0 += kThreads) {
         const uint32_t i = r0 + tid;
         const uint64_t g = cd.row_off + i;
         const bool in = i < end && (!has_mask || mask_row(q.in_mask, q.n_records, g));
-        const double v = in ? __longlong_as_double(static_cast<long long>(sm.vals[i])) : 0.0;
-        const bool pass = in && (!pred_on || pred_eval(q.pred, v));
+        const uint64_t vb = in ? sm.vals[i] : 0;
+        const bool pass = in && (!pred_on || kp.pass(vb));
         if (mode == VAL_MATERIALIZE) {
             uint32_t total;
             const uint32_t before = block_excl_scan_u32<kThreads>(pass, s_red, &total);
-            if (pass && pos + before < q.out_cap) q.out_vals[pos + before] = v;
+            if (pass && pos + before < q.out_cap) q.out_vals[pos + before] = __longlong_as_double(static_cast<long long>(vb));
             pos += total;
             continue;
         }
@@ -366,7 +369,7 @@ __global__ void __launch_bounds__(kThreads, 2) xor_kernel(QueryParams q, uint32_
             const uint32_t word = __ballot_sync(0xffffffffu, pass && g < q.n_records);
             if (lane == 0 && word) store_mask_word(q.out_mask, g, word, true);
         }
-        if (pass) val_agg_add(agg, v, 1);
+        if (pass) val_agg_add1(agg, vb);
     }
     if (mode == VAL_MATERIALIZE) return;
     const ValAgg a = val_agg_block(agg, sh_agg);
