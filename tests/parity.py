@@ -120,7 +120,9 @@ def check_query_suite(data: bytes, preds, masks=(None,), chunk_ids=(None,), exac
                     assert np.array_equal(mask_np(gmk)[: len(omk)], omk)
                     assert sum_ok(gs, os_, exact_sum, ofm), ("filter_agg sum", p, gs, os_)
                     assert same_scalar(gmn, omn) and same_scalar(gmx, omx), ("filter_agg min/max", p, gmn, omn, gmx, omx)
-                    assert gn == int(np.unpackbits(omk.view(np.uint8)).sum())
+                    # rows selected = values filter_materialize returns (decoded rows may overlap
+                    # the next chunk's in a corrupt file, so this is not always the bitmask's popcount)
+                    assert gn == len(ofm), ("filter_agg count", p, gn, len(ofm))
     finally:
         g.close()
         o.close()
