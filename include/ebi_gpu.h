@@ -6,7 +6,7 @@
  * The entry points mirror ebi's public Decoder (ebi/src/api/decoder.rs) and
  * Encoder (ebi/src/api/encoder.rs); each declaration cites the reference item
  * it replaces.  A binding in the reference's own language is a thin `extern
- * "C"` block over these functions (INTEGRATION.md shows it).
+ * "C"` block over these functions.
  *
  * Conventions
  *  - Every function returns an ebi_status; 0 is success.  The codes mirror
@@ -118,8 +118,8 @@ int ebi_filter_materialize(ebi_column* col, const ebi_predicate* pred, const uin
 /* Decoder::sum / min / max over the rows of `mask` (all when NULL).  Sums of
  * BUFF chunks are exact integer sums rounded once, as the reference computes
  * them; sums of Gorilla/Chimp/Chimp128/RLE/Uncompressed chunks are
- * compensated (double-double) sums whose relative difference to the
- * reference's sequential f64 sum is below 1e-12 for the bench workloads. */
+ * compensated (Neumaier) sums, within 1e-12 of the reference's sequential f64
+ * sum relative to the sum of magnitudes, and within 2 ulps of the exact sum. */
 int ebi_sum(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream);
 int ebi_min(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream);
 int ebi_max(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* out, void* stream);
