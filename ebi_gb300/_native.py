@@ -16,7 +16,7 @@ EXPORTS = [
     "ebi_column_scheme", "ebi_column_chunk_info", "ebi_column_set_precision", "ebi_materialize",
     "ebi_filter", "ebi_filter_materialize", "ebi_sum", "ebi_min", "ebi_max", "ebi_filter_agg",
     "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches", "ebi_column_set_timing",
-    "ebi_column_last_times",
+    "ebi_column_last_times", "ebi_materialize_static",
 ]
 
 
@@ -54,6 +54,7 @@ def lib() -> C.CDLL:
     L.ebi_column_chunk_info.argtypes = [vp, u64, u64p, u64p, u64p, u64p]
     L.ebi_column_set_precision.argtypes = [vp, C.c_int32]
     L.ebi_materialize.argtypes = [vp, vp, i64, vp, u64, u64p, vp]
+    L.ebi_materialize_static.argtypes = [vp, vp, i64, vp, u64, u64p, vp]
     L.ebi_filter.argtypes = [vp, PP, vp, i64, vp, vp]
     L.ebi_filter_materialize.argtypes = [vp, PP, vp, i64, vp, u64, u64p, vp]
     for fn in (L.ebi_sum, L.ebi_min, L.ebi_max):

@@ -596,6 +596,71 @@ int ebi_filter_materialize(ebi_column* c, const ebi_predicate* pred, const uint6
     return run_materialize(c, c->d_scratch_mask, chunk_id, d_out, out_cap, n_out, s, true, nullptr);
 }
 
+// Decoder::materialize without allocating: the per-tile counts and offsets go
+// to the fixed scratch of static_scratch.cu instead of the column's scratch.
+int ebi_materialize_static(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, double* d_out, uint64_t out_cap,
+                           uint64_t* n_out, void* stream) {
+    if (!c || (!d_out && out_cap)) return fail(EBI_E_INVALID, "column or output is null");
+    int st = check_supported(c);
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t tb, tn;
+    tile_range(c, chunk_id, &tb, &tn);
+    if (tn > kStaticTiles) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf,
+                      "ebi_materialize_static: the query covers %u tiles, the fixed scratch holds at most %u "
+                      "(use ebi_materialize)", tn, kStaticTiles);
+        return fail(EBI_E_INVALID, buf);
+    }
+    unsigned long long* counts = nullptr;
+    unsigned long long* offsets = nullptr;
+    CK(static_scratch(&counts, &offsets));
+    // Nothing here has to start at zero: the count pass writes the count of
+    // every tile in [0, tn) and the scan writes every offset it reads back.
+    if (int st2 = begin_query(c, s)) return st2;
+    QueryParams q = base_params(c);
+    q.op = OP_FILTER;  // only the status is folded
+    q.chunk_id = chunk_id;
+    q.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
+    q.out_vals = d_out;
+    q.out_cap = out_cap;
+    uint64_t total = 0;
+    if (c->scheme == EBI_BUFF && !d_mask) {
+        for (uint32_t t = tb; t < tb + tn; ++t) {
+            const Tile& tl = c->tiles.tiles[t];
+            const uint32_t n = c->chunks[tl.chunk].n_rows;
+            total += tl.begin < n ? std::min<uint64_t>(kBuffTileRows, n - tl.begin) : 0;
+        }
+        if (total > out_cap) {
+            if (n_out) *n_out = total;
+            return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
+        }
+        const uint64_t base_row = chunk_id >= 0 && static_cast<uint64_t>(chunk_id) < c->n_chunks ? c->chunks[chunk_id].row_off : 0;
+        CK(launch_buff_materialize(q, tb, tn, offsets, base_row, s));
+    } else {
+        q.tile_counts = counts;
+        if (c->scheme == EBI_BUFF) {
+            CK(launch_buff_count(q, tb, tn, s));
+            CK(launch_tile_scan(counts, offsets, tn, s));
+            const uint64_t base_row = chunk_id >= 0 && static_cast<uint64_t>(chunk_id) < c->n_chunks ? c->chunks[chunk_id].row_off : 0;
+            CK(launch_buff_materialize(q, tb, tn, offsets, base_row, s));
+        } else {
+            CK(launch_values(c, q, tb, tn, VAL_COUNT, nullptr, s));
+            CK(launch_tile_scan(counts, offsets, tn, s));
+            CK(launch_values(c, q, tb, tn, VAL_MATERIALIZE, offsets, s));
+        }
+        CK(cudaMemcpyAsync(&c->h_res->count, offsets + tn, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        total = c->h_res->count;
+    }
+    st = finish(c, q, s);
+    if (st) return st;
+    if (n_out) *n_out = total;
+    if (total > out_cap) return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
+    return EBI_OK;
+}
+
 int ebi_column_set_timing(ebi_column* c, int enable) {
     if (!c) return fail(EBI_E_INVALID, "column is null");
     if (enable && !c->ev[0]) {

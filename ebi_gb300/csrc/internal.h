@@ -62,6 +62,12 @@ cudaError_t launch_gorilla(const QueryParams& q, uint32_t chunk_begin, uint32_t 
 cudaError_t launch_xor(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                        const unsigned long long* chunk_offsets, cudaStream_t s);
 
+// ---- fixed scratch of ebi_materialize_static (static_scratch.cu) ----------
+constexpr uint32_t kStaticTiles = 16384;  // tiles per call: 2 x 128 KB of counts and offsets
+// Device addresses of the fixed per-tile counts (kStaticTiles entries) and
+// offsets (kStaticTiles + 1) for the current device; looked up on first use.
+cudaError_t static_scratch(unsigned long long** counts, unsigned long long** offsets);
+
 // ---- shared kernels (query.cu) ---------------------------------------------
 // acc[c].selected = chunk passes chunk_id and intersects the mask (or no mask).
 cudaError_t launch_select_chunks(const QueryParams& q, cudaStream_t s);

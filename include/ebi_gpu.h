@@ -105,6 +105,22 @@ int ebi_column_set_precision(ebi_column* col, int32_t precision);
 int ebi_materialize(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* d_out,
                     uint64_t out_cap, uint64_t* n_out, void* stream);
 
+/* ebi_materialize without any allocation (no reference counterpart: the
+ * reference's Decoder allocates freely).  Same arguments, results and errors
+ * as ebi_materialize, but its per-tile scratch lives in a fixed device array
+ * of 16,384 tiles (tiles are 8,192-row slices of a BUFF chunk, or whole chunks
+ * of the other codecs) instead of column memory allocated on first use; a
+ * query covering more tiles fails with EBI_E_INVALID before touching the GPU.
+ * It is for callers that must not allocate device memory, e.g. a serving
+ * thread whose latency must not include the allocator, or a process whose
+ * device memory is fully reserved by another allocator.  The first call on
+ * each device looks up the array's address (cudaGetSymbolAddress, with that
+ * device current); make that first call before any stream capture.  The array
+ * is shared by every column on a device: calls that overlap in time (other
+ * streams or host threads) race on it and must be serialised by the caller. */
+int ebi_materialize_static(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* d_out,
+                           uint64_t out_cap, uint64_t* n_out, void* stream);
+
 /* Decoder::filter: rows (of `mask` when given) whose value satisfies `pred`,
  * as a bitmask in d_out_mask (ceil(n_records/64) words, fully written). */
 int ebi_filter(ebi_column* col, const ebi_predicate* pred, const uint64_t* d_mask, int64_t chunk_id,
