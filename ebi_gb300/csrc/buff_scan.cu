@@ -540,6 +540,62 @@ __device__ void scan_finalize(const QueryParams& q, const BuffChunkInfo* info, S
     }
 }
 
+// A tile's metadata and copy plan, prepared by one producer lane.
+struct PreTile {
+    ScanMeta m;
+    uint64_t planes, tail;  // file offsets of the chunk's first plane and tail plane
+    uint32_t n, begin;      // plane length (rows of the chunk) and the tile's first row
+    uint32_t bytes;         // bytes the tile's copies deliver
+};
+
+__device__ __forceinline__ void prepare_tile(const QueryParams& q, const BuffChunkInfo* info, ScanTotals* T,
+                                             uint32_t tile, bool has_mask, PreTile& pt) {
+    const Tile tl = q.tiles[tile];
+    const uint32_t c = tl.chunk;
+    const ChunkDesc cd = q.chunks[c];
+    const BuffChunkInfo ci = info[c];
+    ScanMeta& m = pt.m;
+    const bool selected = has_mask ? q.acc[c].selected != 0
+                                   : (q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
+    if (selected && tl.begin == 0) {
+        if (!has_mask) q.acc[c].selected = 1;
+        if (ci.status) chunk_error(q, T, c, ci.status);
+    }
+    m.chunk = c;
+    m.base = ci.base;
+    m.row0 = cd.row_off + tl.begin;
+    m.rows = min(kBuffTileRows, cd.n_rows - tl.begin);
+    m.ok = selected && ci.status == 0;
+    pt.planes = ci.planes;
+    pt.tail = ci.tail;
+    pt.n = ci.n;
+    pt.begin = tl.begin;
+    uint32_t bytes = 0;
+    if (m.ok) {
+        m.np = ci.bits / 8;
+        m.tb = ci.bits % 8;
+        m.bits = ci.bits;
+        compile_pred(q.pred, ci.base, ci.bits, ci.frac, has_mask, m.pred);
+        m.prog = compile_prog(q, m.pred, ci.bits, has_mask);
+        for (uint32_t p = 0; p < m.np; ++p) {
+            const uintptr_t src = reinterpret_cast<uintptr_t>(q.file + ci.planes + uint64_t(p) * ci.n + tl.begin);
+            const uintptr_t a = src & ~uintptr_t(15);
+            m.mis[p] = static_cast<uint32_t>(src - a);
+            bytes += static_cast<uint32_t>(((src + m.rows + 15) & ~uintptr_t(15)) - a);
+        }
+        if (m.tb) {
+            const uintptr_t src = reinterpret_cast<uintptr_t>(q.file + ci.tail + uint64_t(tl.begin / 8) * m.tb);
+            const uintptr_t a = src & ~uintptr_t(15);
+            m.mis_tail = static_cast<uint32_t>(src - a);
+            bytes += static_cast<uint32_t>(((src + (uint64_t(m.rows) * m.tb + 7) / 8 + 15) & ~uintptr_t(15)) - a);
+        }
+    } else {
+        m.np = 0;
+        m.tb = 0;
+    }
+    pt.bytes = bytes;
+}
+
 __global__ void __launch_bounds__(kScanThreads, 2)
 buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, uint32_t n_tiles, StageLayout L,
                  ScanTotals* T, QueryResult* res, uint32_t frac, uint32_t fast_ok) {
@@ -562,76 +618,55 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
     __syncthreads();
     const bool has_mask = q.in_mask != nullptr;
 
-    if (threadIdx.x == kScanConsumers) {
-        // ---- producer: one lane of warp 8 issues; the other lanes wait at the epilogue ----
-        for (uint32_t i = 0; i < count; ++i) {
-            const uint32_t s = i % L.stages, k = i / L.stages;
-            if (k > 0 && !mbar_wait(&empty[s], (k - 1) & 1)) {
-                chunk_error(q, T, 0, EBI_E_CUDA);
-                break;  // consumers stopped; nothing of this stage is in flight
-            }
-            const Tile tl = q.tiles[tile_base + t_first + i];
-            const uint32_t c = tl.chunk;
-            const ChunkDesc cd = q.chunks[c];
-            const BuffChunkInfo ci = info[c];
-            ScanMeta& m = meta[s];
-            const bool selected = has_mask ? q.acc[c].selected != 0
-                                           : (q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
-            if (selected && tl.begin == 0) {
-                if (!has_mask) q.acc[c].selected = 1;
-                if (ci.status) chunk_error(q, T, c, ci.status);
-            }
-            m.chunk = c;
-            m.base = ci.base;
-            m.row0 = cd.row_off + tl.begin;
-            m.rows = min(kBuffTileRows, cd.n_rows - tl.begin);
-            m.ok = selected && ci.status == 0;
-            uint32_t bytes = 0;
-            const uint8_t* file = q.file;
-            uint8_t* st = stages + size_t(s) * L.stage_bytes;
-            if (m.ok) {
-                m.np = ci.bits / 8;
-                m.tb = ci.bits % 8;
-                m.bits = ci.bits;
-                compile_pred(q.pred, ci.base, ci.bits, ci.frac, has_mask, m.pred);
-                m.prog = compile_prog(q, m.pred, ci.bits, has_mask);
-                for (uint32_t p = 0; p < m.np; ++p) {
-                    const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.planes + uint64_t(p) * ci.n + tl.begin);
-                    const uintptr_t a = src & ~uintptr_t(15);
-                    m.mis[p] = static_cast<uint32_t>(src - a);
-                    bytes += static_cast<uint32_t>(((src + m.rows + 15) & ~uintptr_t(15)) - a);
-                }
-                if (m.tb) {
-                    const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.tail + uint64_t(tl.begin / 8) * m.tb);
-                    const uintptr_t a = src & ~uintptr_t(15);
-                    m.mis_tail = static_cast<uint32_t>(src - a);
-                    bytes += static_cast<uint32_t>(((src + (uint64_t(m.rows) * m.tb + 7) / 8 + 15) & ~uintptr_t(15)) - a);
-                }
-            } else {
-                m.np = 0;
-                m.tb = 0;
-            }
-            fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&full[s], bytes);
-            if (m.ok) {
-                for (uint32_t p = 0; p < m.np; ++p) {
-                    const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.planes + uint64_t(p) * ci.n + tl.begin);
-                    const uintptr_t a = src & ~uintptr_t(15);
-                    const uint32_t len = static_cast<uint32_t>(((src + m.rows + 15) & ~uintptr_t(15)) - a);
-                    bulk_g2s(st + p * L.plane_stride, reinterpret_cast<const void*>(a), len, &full[s]);
-                }
-                if (m.tb) {
-                    const uintptr_t src = reinterpret_cast<uintptr_t>(file + ci.tail + uint64_t(tl.begin / 8) * m.tb);
-                    const uintptr_t a = src & ~uintptr_t(15);
-                    const uint32_t len =
-                        static_cast<uint32_t>(((src + (uint64_t(m.rows) * m.tb + 7) / 8 + 15) & ~uintptr_t(15)) - a);
-                    bulk_g2s(st + L.np_max * L.plane_stride, reinterpret_cast<const void*>(a), len, &full[s]);
+    if (threadIdx.x >= kScanConsumers) {
+        // ---- producer warp.  Its lanes prepare the next 32 tiles' metadata in
+        // parallel (the chunk-table loads of different tiles overlap instead of
+        // queueing behind one lane); lane 0 then runs the ring in tile order:
+        // wait for a free stage, publish the tile's metadata, issue its copies.
+        const uint32_t lane = threadIdx.x - kScanConsumers;
+        __shared__ PreTile pre[32];
+        bool stop = false;
+        for (uint32_t i0 = 0; i0 < count && !stop; i0 += 32) {
+            const uint32_t nb = count - i0 < 32 ? count - i0 : 32u;
+            if (lane < nb) prepare_tile(q, info, T, tile_base + t_first + i0 + lane, has_mask, pre[lane]);
+            __syncwarp();
+            if (lane == 0) {
+                for (uint32_t j = 0; j < nb; ++j) {
+                    const uint32_t i = i0 + j, s = i % L.stages, k = i / L.stages;
+                    if (k > 0 && !mbar_wait(&empty[s], (k - 1) & 1)) {
+                        chunk_error(q, T, 0, EBI_E_CUDA);
+                        stop = true;  // consumers stopped; nothing of this stage is in flight
+                        break;
+                    }
+                    const PreTile& pt = pre[j];
+                    meta[s] = pt.m;
+                    uint8_t* st = stages + size_t(s) * L.stage_bytes;
+                    fence_proxy_async_smem();
+                    mbar_arrive_expect_tx(&full[s], pt.bytes);
+                    if (pt.m.ok) {
+                        for (uint32_t p = 0; p < pt.m.np; ++p) {
+                            const uintptr_t src = reinterpret_cast<uintptr_t>(q.file + pt.planes + uint64_t(p) * pt.n + pt.begin);
+                            const uintptr_t a = src & ~uintptr_t(15);
+                            const uint32_t len = static_cast<uint32_t>(((src + pt.m.rows + 15) & ~uintptr_t(15)) - a);
+                            bulk_g2s(st + p * L.plane_stride, reinterpret_cast<const void*>(a), len, &full[s]);
+                        }
+                        if (pt.m.tb) {
+                            const uintptr_t src = reinterpret_cast<uintptr_t>(q.file + pt.tail + uint64_t(pt.begin / 8) * pt.m.tb);
+                            const uintptr_t a = src & ~uintptr_t(15);
+                            const uint32_t len = static_cast<uint32_t>(
+                                ((src + (uint64_t(pt.m.rows) * pt.m.tb + 7) / 8 + 15) & ~uintptr_t(15)) - a);
+                            bulk_g2s(st + L.np_max * L.plane_stride, reinterpret_cast<const void*>(a), len, &full[s]);
+                        }
+                    }
                 }
             }
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+            __syncwarp();  // pre[] is rewritten only after lane 0 consumed it
         }
-        // drain: the last stages' copies complete before this lane leaves
-        for (uint32_t i = count > L.stages ? count - L.stages : 0; i < count; ++i)
-            if (!mbar_wait(&full[i % L.stages], (i / L.stages) & 1)) { chunk_error(q, T, 0, EBI_E_CUDA); break; }
+        // drain: the last stages' copies complete before this warp leaves
+        if (lane == 0)
+            for (uint32_t i = count > L.stages ? count - L.stages : 0; i < count; ++i)
+                if (!mbar_wait(&full[i % L.stages], (i / L.stages) & 1)) { chunk_error(q, T, 0, EBI_E_CUDA); break; }
     }
     __shared__ WarpTot wtot[kScanConsumers / 32];
     if (threadIdx.x < kScanConsumers) {
