@@ -7,7 +7,7 @@ engine is the C ABI of include/ebi_gpu.h (libebi_gpu.so); this package is its
 Python mirror of ebi's Decoder / Encoder API.
 """
 from . import _native
-from .api import (BUFF, CHIMP, CHIMP128, GORILLA, RLE, SCHEMES, UNCOMPRESSED, ChunkId, ConversionError,
+from .api import (BUFF, CHIMP, CHIMP128, GORILLA, RLE, SCHEMES, UNCOMPRESSED, Batch, ChunkId, ConversionError,
                   CorruptChunk, CudaError, Decoder, DecoderError, InvalidArgument, IOError_, OutOfMemory,
                   Predicate, PreconditionsNotMet, Range, RangeValue, UnexpectedEndOfChunk, Unsupported, encode,
                   kernel_launches)
@@ -19,7 +19,7 @@ def load_library():
 
 
 __all__ = [
-    "BUFF", "CHIMP", "CHIMP128", "GORILLA", "RLE", "SCHEMES", "UNCOMPRESSED", "ChunkId", "ConversionError",
+    "BUFF", "CHIMP", "CHIMP128", "GORILLA", "RLE", "SCHEMES", "UNCOMPRESSED", "Batch", "ChunkId", "ConversionError",
     "CorruptChunk", "CudaError", "Decoder", "DecoderError", "InvalidArgument", "IOError_", "OutOfMemory",
     "Predicate", "PreconditionsNotMet", "Range", "RangeValue", "UnexpectedEndOfChunk", "Unsupported", "encode",
     "kernel_launches", "load_library",

@@ -16,7 +16,8 @@ EXPORTS = [
     "ebi_column_scheme", "ebi_column_chunk_info", "ebi_column_set_precision", "ebi_materialize",
     "ebi_filter", "ebi_filter_materialize", "ebi_sum", "ebi_min", "ebi_max", "ebi_filter_agg",
     "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches", "ebi_column_set_timing",
-    "ebi_column_last_times", "ebi_materialize_static",
+    "ebi_column_last_times", "ebi_materialize_static", "ebi_batch_create", "ebi_batch_run",
+    "ebi_batch_get_info", "ebi_batch_destroy",
 ]
 
 
@@ -25,6 +26,24 @@ class Predicate(C.Structure):
     _fields_ = [("kind", C.c_int32), ("start_kind", C.c_int32), ("end_kind", C.c_int32),
                 ("reserved", C.c_int32), ("value", C.c_double), ("start", C.c_double),
                 ("end", C.c_double)]
+
+
+class BatchQuery(C.Structure):
+    """ebi_batch_query"""
+    _fields_ = [("col", C.c_void_p), ("pred", Predicate), ("aggregates", C.c_uint32), ("reserved", C.c_uint32),
+                ("d_out_mask", C.c_void_p)]
+
+
+class BatchResult(C.Structure):
+    """ebi_batch_result"""
+    _fields_ = [("sum", C.c_double), ("min", C.c_double), ("max", C.c_double), ("count", C.c_uint64),
+                ("status", C.c_int32), ("bad_chunk", C.c_uint32)]
+
+
+class BatchInfo(C.Structure):
+    """ebi_batch_info"""
+    _fields_ = [("queries", C.c_uint64), ("items", C.c_uint64), ("chunks", C.c_uint64), ("shape", C.c_int32),
+                ("ctas_per_sm", C.c_uint32), ("order", C.c_uint32), ("shape_ms", C.c_double * 4)]
 
 
 class SegmentTimes(C.Structure):
@@ -66,5 +85,9 @@ def lib() -> C.CDLL:
     L.ebi_kernel_launches.restype = u64
     L.ebi_column_set_timing.argtypes = [vp, C.c_int]
     L.ebi_column_last_times.argtypes = [vp, C.POINTER(SegmentTimes)]
+    L.ebi_batch_create.argtypes = [C.POINTER(BatchQuery), u64, vp, C.POINTER(vp)]
+    L.ebi_batch_run.argtypes = [vp, PP, C.POINTER(BatchResult), vp]
+    L.ebi_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+    L.ebi_batch_destroy.argtypes = [vp]
     _lib = L
     return L

@@ -306,5 +306,84 @@ class Decoder:
         return out, val(s, "sum"), val(a, "min"), val(b, "max"), n.value
 
 
+_AGG_BITS = {"sum": 1, "min": 2, "max": 4}
+
+
+class Batch:
+    """A fixed list of filter + aggregate queries over open Decoders (columns may
+    repeat and mix codecs), run as one persistent mixed-codec launch captured in
+    a CUDA graph (ebi_batch_* of the C ABI; no counterpart in the reference).
+
+    queries: sequence of (decoder, predicate) or (decoder, predicate, aggregates)."""
+
+    def __init__(self, queries, stream=None, want_masks=False):
+        torch = _torch()
+        if not queries:
+            raise InvalidArgument("a batch needs at least one query")
+        self.decoders = [q[0] for q in queries]
+        self.device = self.decoders[0].device
+        self._stream = stream
+        n = len(queries)
+        arr = (_native.BatchQuery * n)()
+        self.masks = []
+        for i, q in enumerate(queries):
+            d, p = q[0], q[1]
+            aggs = q[2] if len(q) > 2 else ("sum", "min", "max")
+            m = d.new_mask() if want_masks else None
+            self.masks.append(m)
+            arr[i].col = d._h
+            arr[i].pred = p.to_c()
+            arr[i].aggregates = sum(_AGG_BITS[a] for a in aggs)
+            arr[i].d_out_mask = m.data_ptr() if m is not None else None
+        self._aggs = [q[2] if len(q) > 2 else ("sum", "min", "max") for q in queries]
+        h = C.c_void_p()
+        _check(_native.lib().ebi_batch_create(arr, n, self._sp(), C.byref(h)), "Batch::new")
+        self._h = h
+        self._n = n
+        self._res = (_native.BatchResult * n)()
+
+    def _sp(self):
+        torch = _torch()
+        s = self._stream if self._stream is not None else torch.cuda.current_stream(self.device)
+        return C.c_void_p(s.cuda_stream)
+
+    def run(self, predicates=None):
+        """Runs every query; returns [(sum, min, max, count)] (None for aggregates not asked for)."""
+        preds = None
+        if predicates is not None:
+            assert len(predicates) == self._n
+            preds = (_native.Predicate * self._n)(*[p.to_c() for p in predicates])
+        rc = _native.lib().ebi_batch_run(self._h, preds, self._res, self._sp())
+        out = []
+        for i in range(self._n):
+            r = self._res[i]
+            a = self._aggs[i]
+            out.append((r.sum if "sum" in a else None, r.min if "min" in a else None,
+                        r.max if "max" in a else None, r.count))
+        _check(rc, "Batch::run")
+        return out
+
+    def statuses(self):
+        return [self._res[i].status for i in range(self._n)]
+
+    def info(self) -> dict:
+        inf = _native.BatchInfo()
+        _check(_native.lib().ebi_batch_get_info(self._h, C.byref(inf)), "Batch::info")
+        return {"queries": inf.queries, "items": inf.items, "chunks": inf.chunks, "shape": inf.shape,
+                "ctas_per_sm": inf.ctas_per_sm, "order": ["cost", "query"][inf.order] if inf.shape >= 0 else None,
+                "shape_ms": list(inf.shape_ms)}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.lib().ebi_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def kernel_launches() -> int:
     return _native.lib().ebi_kernel_launches()

@@ -1,0 +1,110 @@
+// batch.cu -- many queries over many columns of mixed codecs in one
+// persistent launch.
+//
+// A batch is a list of work items, each naming a query and a unit of one of
+// its columns: an 8,192-row BUFF tile, a whole Uncompressed / RLE / Chimp /
+// Chimp128 chunk, or a group of Gorilla chunks (one per warp).  A persistent
+// grid of 256-thread CTAs pulls items from a device counter, so columns of
+// very different lengths and codecs share the GPU without a launch per
+// column; each item runs the same per-chunk device code as the single-column
+// kernels and leaves its result in the query's own per-chunk accumulators.
+// A second launch folds every query (one CTA per query, chunk order).
+#include "internal.h"
+#include "buff_tile.cuh"
+#include "finalize.cuh"
+#include "gorilla_dev.cuh"
+#include "raw_dev.cuh"
+#include "rle_dev.cuh"
+#include "xor_dev.cuh"
+
+namespace ebi {
+namespace {
+
+constexpr int kBatchThreads = 256;
+static_assert(kBatchThreads == kXorThreads && kBatchThreads == kRleThreads, "codec CTA shapes");
+
+// One function per item kind, kept out of line so that each gets its own
+// register allocation (the kernel's is the largest, not the sum of all paths).
+__device__ __noinline__ void item_buff_tile(const QueryParams& q, const BatchItem& it, BuffCtx& k, BlockRed& red) {
+    const Tile t = q.tiles[it.unit];
+    if (threadIdx.x == 0) buff_setup(q, t.chunk, q.in_mask != nullptr, k);
+    __syncthreads();
+    if (k.ok && k.bits > 32) buff_query_dispatch<unsigned long long>(q, k, t.chunk, it.unit, t.begin, red);
+    else buff_query_dispatch<uint32_t>(q, k, t.chunk, it.unit, t.begin, red);
+}
+__device__ __noinline__ void item_raw(const QueryParams& q, const BatchItem& it) {
+    raw_chunk<kBatchThreads>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+}
+__device__ __noinline__ void item_rle(const QueryParams& q, const BatchItem& it) {
+    rle_chunk(q, it.unit, it.unit, VAL_SCAN, nullptr);
+}
+__device__ __noinline__ void item_gorilla(const QueryParams& q, const BatchItem& it) {
+    const uint32_t warp = threadIdx.x >> 5;
+    if (warp < it.count) gorilla_chunk_l1(q, it.unit + warp, it.unit + warp, VAL_SCAN, nullptr);
+}
+__device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_CHIMP>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+}
+__device__ __noinline__ void item_chimp128(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_CHIMP128>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+}
+
+__global__ void __launch_bounds__(kBatchThreads, 2)
+batch_kernel(const QueryParams* __restrict__ qp, const BatchItem* __restrict__ items, uint32_t n_items,
+             unsigned int* counter) {
+    __shared__ uint32_t s_item;
+    __shared__ BuffCtx s_k;
+    __shared__ BlockRed s_red;
+    for (;;) {
+        __syncthreads();  // every thread is done with the previous item's shared state
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t i = s_item;
+        if (i >= n_items) break;
+        const BatchItem it = items[i];
+        const QueryParams& q = qp[it.query];
+        switch (it.kind) {
+        case ITEM_BUFF_TILE: item_buff_tile(q, it, s_k, s_red); break;
+        case ITEM_RAW: item_raw(q, it); break;
+        case ITEM_RLE: item_rle(q, it); break;
+        case ITEM_GORILLA: item_gorilla(q, it); break;
+        case ITEM_CHIMP: item_chimp(q, it); break;
+        case ITEM_CHIMP128: item_chimp128(q, it); break;
+        default: break;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kFinThreads) batch_finalize_kernel(const QueryParams* __restrict__ qp,
+                                                                     QueryResult* res) {
+    finalize_chunks(qp[blockIdx.x], res + blockIdx.x);
+}
+
+}  // namespace
+
+size_t batch_smem_bytes() { return xor_smem_bytes(CODEC_CHIMP128); }
+
+cudaError_t prepare_batch_kernel() {
+    return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(batch_smem_bytes()));
+}
+
+cudaError_t launch_batch(const QueryParams* d_qp, const BatchItem* d_items, uint32_t n_items, unsigned int* d_counter,
+                         uint32_t grid, cudaStream_t s) {
+    if (n_items == 0) return cudaSuccess;
+    const size_t smem = batch_smem_bytes();
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    batch_kernel<<<grid, kBatchThreads, smem, s>>>(d_qp, d_items, n_items, d_counter);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_finalize(const QueryParams* d_qp, QueryResult* d_res, uint32_t n_queries, cudaStream_t s) {
+    if (n_queries == 0) return cudaSuccess;
+    batch_finalize_kernel<<<n_queries, kFinThreads, 0, s>>>(d_qp, d_res);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace ebi

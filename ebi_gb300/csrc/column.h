@@ -1,0 +1,50 @@
+// column.h -- the resident column (ebi_column of include/ebi_gpu.h), shared
+// by the single-query entry points (column.cu) and the batch / serving layer.
+#pragma once
+
+#include <vector>
+
+#include "internal.h"
+
+// internal header: the engine's own types, unqualified
+using namespace ebi;
+
+struct ebi_column {
+    cudaStream_t stream = nullptr;  // stream of open/close (allocation order)
+    int scheme = 0;
+    uint64_t n_records = 0, n_chunks = 0, file_len = 0, footer_off = 0;
+    std::vector<ChunkDesc> chunks;
+    TileMap tiles;
+    bool rows_aligned32 = true;
+    int32_t precision = -1;
+    uint8_t* d_file = nullptr;
+    ChunkDesc* d_chunks = nullptr;
+    Tile* d_tiles = nullptr;
+    ChunkAcc* d_acc = nullptr;
+    QueryResult* d_res = nullptr;
+    QueryResult* h_res = nullptr;
+    unsigned long long* d_tile_counts = nullptr;   // n_tiles
+    unsigned long long* d_tile_offsets = nullptr;  // n_tiles + 1
+    uint64_t* d_scratch_mask = nullptr;            // mask_words
+    uint64_t mask_words = 0;
+    // BUFF: header facts per chunk and the scan's shared-memory ring
+    BuffChunkInfo* d_buff = nullptr;
+    StageLayout layout{};
+    uint32_t scan_grid = 0;
+    ScanTotals* d_tot = nullptr;
+    uint32_t buff_frac = 0;
+    bool buff_fast_ok = false;
+    bool fused_pending = false;  // the last query's kernel already folded into d_res
+    uint32_t stage_bytes = 0;    // Gorilla: shared-memory staging per chunk
+    // segment timing (ebi_column_set_timing)
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // query start, scan end, finalize end
+    ebi_segment_times last{};
+    uint64_t launches_at_start = 0;
+};
+
+namespace ebi {
+// The column's query parameters with no query set (file, chunk table, tiles,
+// accumulators, BUFF facts, staging size).
+QueryParams column_params(const ebi_column* c);
+}  // namespace ebi

@@ -68,6 +68,32 @@ constexpr uint32_t kStaticTiles = 16384;  // tiles per call: 2 x 128 KB of count
 // offsets (kStaticTiles + 1) for the current device; looked up on first use.
 cudaError_t static_scratch(unsigned long long** counts, unsigned long long** offsets);
 
+// ---- batched queries (batch.cu) --------------------------------------------
+enum BatchItemKind : uint32_t {
+    ITEM_BUFF_TILE = 0,  // unit = tile index of the query's column
+    ITEM_RAW = 1,        // unit = chunk
+    ITEM_RLE = 2,
+    ITEM_GORILLA = 3,    // chunks [unit, unit + count), one warp each
+    ITEM_CHIMP = 4,
+    ITEM_CHIMP128 = 5,
+};
+struct BatchItem {
+    uint32_t query;  // index into the batch's QueryParams
+    uint32_t kind;   // BatchItemKind
+    uint32_t unit;
+    uint32_t count;
+};
+// Dynamic shared memory of the batch kernel; prepare_batch_kernel raises the
+// kernel's shared-memory limit to it (once per process, outside any capture).
+size_t batch_smem_bytes();
+cudaError_t prepare_batch_kernel();
+// Runs every item (persistent grid of `grid` CTAs pulling from *d_counter,
+// which the launch resets); each query's partials land in its own acc.
+cudaError_t launch_batch(const QueryParams* d_qp, const BatchItem* d_items, uint32_t n_items, unsigned int* d_counter,
+                         uint32_t grid, cudaStream_t s);
+// Folds query i into d_res[i] (one CTA per query) and re-arms its acc.
+cudaError_t launch_batch_finalize(const QueryParams* d_qp, QueryResult* d_res, uint32_t n_queries, cudaStream_t s);
+
 // ---- shared kernels (query.cu) ---------------------------------------------
 // acc[c].selected = chunk passes chunk_id and intersects the mask (or no mask).
 cudaError_t launch_select_chunks(const QueryParams& q, cudaStream_t s);

@@ -147,6 +147,43 @@ int ebi_filter_agg(ebi_column* col, const ebi_predicate* pred, const uint64_t* d
                    int64_t chunk_id, uint64_t* d_out_mask, double* sum, double* min, double* max,
                    uint64_t* n_selected, void* stream);
 
+/* ---- batched queries ------------------------------------------------------ */
+/* No reference counterpart: the reference answers one Decoder call at a time.
+ * A batch is a fixed list of filter + aggregate queries, each over one open
+ * column (columns may repeat and mix codecs).  Running it executes every
+ * query's chunks in one persistent mixed-codec launch followed by one fold
+ * launch, captured once into a CUDA graph and replayed; the first run also
+ * times a few launch shapes and keeps the fastest.  Results equal the
+ * single-column calls (ebi_filter_agg) bit for bit.  The columns must stay
+ * open while the batch exists; runs of one batch must not overlap. */
+enum { EBI_AGG_SUM = 1, EBI_AGG_MIN = 2, EBI_AGG_MAX = 4 };
+typedef struct {
+    ebi_column* col;
+    ebi_predicate pred;
+    uint32_t aggregates;   /* EBI_AGG_* bits; the selected-row count is always kept */
+    uint32_t reserved;
+    uint64_t* d_out_mask;  /* device bitmask of the filter result, or NULL */
+} ebi_batch_query;
+typedef struct {
+    double sum, min, max;
+    uint64_t count;        /* rows selected */
+    int32_t status;        /* ebi_status of this query (first failing chunk) */
+    uint32_t bad_chunk;
+} ebi_batch_result;
+typedef struct {
+    uint64_t queries, items, chunks;
+    int32_t shape;         /* launch shape chosen by the first run (-1 before) */
+    uint32_t ctas_per_sm, order;
+    double shape_ms[4];    /* device time of each candidate shape */
+} ebi_batch_info;
+typedef struct ebi_batch ebi_batch;
+int ebi_batch_create(const ebi_batch_query* queries, uint64_t n, void* stream, ebi_batch** out);
+/* preds (n entries, may be NULL) replace the queries' predicates for this and
+ * later runs; results (n entries, may be NULL) receive each query's result. */
+int ebi_batch_run(ebi_batch* batch, const ebi_predicate* preds, ebi_batch_result* results, void* stream);
+int ebi_batch_get_info(const ebi_batch* batch, ebi_batch_info* out);
+int ebi_batch_destroy(ebi_batch* batch);
+
 /* ---- encoder (host) -------------------------------------------------------- */
 
 /* Encoder::new(.., chunk_option, compressor_config).encode()

@@ -1,0 +1,86 @@
+"""ebi_batch (one persistent mixed-codec launch for many queries) against the
+single-column ebi_filter_agg: every query's bitmask, sum, min, max and count
+are bit-identical to the same query run alone."""
+import numpy as np
+import pytest
+
+import ebi_gb300 as E
+from tests.parity import mask_np, random_preds
+
+pytestmark = pytest.mark.gpu
+
+
+def make_columns(rng, n_cols):
+    cols = []
+    codecs = ["buff", "gorilla", "chimp128", "rle", "chimp", "uncompressed"]
+    for i in range(n_cols):
+        codec = codecs[i % len(codecs)]
+        n = int(rng.integers(1, 60_000)) if i % 5 else int(rng.integers(60_000, 300_000))
+        walk = np.round(30 + np.cumsum(rng.normal(0, 0.5, n)), 2) + 0.0
+        if codec == "buff":
+            v = np.round(rng.uniform(-1000, 1000, n), 3) + 0.0
+            data = E.encode(v, "buff", ("record_count", [65536, 8192, 1000][i % 3]), 1000)
+        elif codec == "rle":
+            v = np.repeat(np.round(rng.normal(0, 5, n // 30 + 1), 1), 30)[:n] + 0.0
+            data = E.encode(v, "rle", ("record_count", 8192))
+        else:
+            v = walk
+            data = E.encode(v, codec, ("record_count", [8192, 4096, 20000][i % 3]))
+        cols.append((E.Decoder(data), v))
+    return cols
+
+
+def alone(d, p, aggs):
+    m, s, mn, mx, n = d.filter_agg(p, aggregates=aggs)
+    return m, s, mn, mx, n
+
+
+def same(a, b):
+    return a is None and b is None or a == b or (np.isnan(a) and np.isnan(b))
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_batch_matches_single_queries(seed):
+    rng = np.random.default_rng(seed)
+    cols = make_columns(rng, 30)
+    queries, expect = [], []
+    for k in range(45):  # some columns appear in several queries
+        d, v = cols[k % len(cols)]
+        p = random_preds(v, rng, k=1)[int(rng.integers(4))]
+        aggs = [("sum", "min", "max"), ("sum",), ("max",)][k % 3]
+        queries.append((d, p, aggs))
+    b = E.Batch(queries, want_masks=True)
+    for rnd in range(2):
+        if rnd == 1:  # new predicates, same graph
+            preds = []
+            for k, (d, p, aggs) in enumerate(queries):
+                preds.append(random_preds(cols[k % len(cols)][1], rng, k=1)[0])
+            queries = [(d, p, a) for (d, _, a), p in zip(queries, preds)]
+            got = b.run(preds)
+        else:
+            got = b.run()
+        for k, (d, p, aggs) in enumerate(queries):
+            m, s, mn, mx, n = alone(d, p, aggs)
+            gs, gmn, gmx, gn = got[k]
+            assert gn == n, (k, gn, n)
+            assert same(gs, s) and same(gmn, mn) and same(gmx, mx), (k, gs, s, gmn, mn, gmx, mx)
+            assert np.array_equal(mask_np(b.masks[k]), mask_np(m)), k
+    info = b.info()
+    assert info["shape"] >= 0 and info["queries"] == 45
+    b.close()
+
+
+def test_batch_reports_a_failing_query():
+    rng = np.random.default_rng(4)
+    good = E.Decoder(E.encode(np.round(rng.normal(0, 1, 5000), 3), "gorilla", ("record_count", 1000)))
+    data = bytearray(E.encode(np.round(rng.uniform(-1, 1, 5000), 3), "buff", ("record_count", 1000), 1000))
+    phys, size, _, _ = E.Decoder(bytes(data)).chunk_info(2)
+    data[phys + 12] = 40  # the chunk's header claims more bits than its bytes hold
+    bad = E.Decoder(bytes(data))
+    p = E.Predicate.range(E.RangeValue.inclusive(-0.5), E.RangeValue.inclusive(0.5))
+    b = E.Batch([(good, p), (bad, p)])
+    with pytest.raises(E.UnexpectedEndOfChunk):
+        b.run()
+    st = b.statuses()
+    assert st[0] == 0 and st[1] == E.UnexpectedEndOfChunk.code
+    b.close()
