@@ -9,8 +9,8 @@ Python mirror of ebi's Decoder / Encoder API.
 from . import _native
 from .api import (BUFF, CHIMP, CHIMP128, GORILLA, RLE, SCHEMES, UNCOMPRESSED, Batch, ChunkId, ConversionError,
                   CorruptChunk, CudaError, Decoder, DecoderError, InvalidArgument, IOError_, OutOfMemory,
-                  Predicate, PreconditionsNotMet, Range, RangeValue, UnexpectedEndOfChunk, Unsupported, encode,
-                  kernel_launches)
+                  Predicate, PreconditionsNotMet, Range, RangeValue, Server, UnexpectedEndOfChunk, Unsupported,
+                  encode, kernel_launches, run_plain)
 
 
 def load_library():
@@ -22,5 +22,5 @@ __all__ = [
     "BUFF", "CHIMP", "CHIMP128", "GORILLA", "RLE", "SCHEMES", "UNCOMPRESSED", "Batch", "ChunkId", "ConversionError",
     "CorruptChunk", "CudaError", "Decoder", "DecoderError", "InvalidArgument", "IOError_", "OutOfMemory",
     "Predicate", "PreconditionsNotMet", "Range", "RangeValue", "UnexpectedEndOfChunk", "Unsupported", "encode",
-    "kernel_launches", "load_library",
+    "kernel_launches", "load_library", "Server", "run_plain",
 ]

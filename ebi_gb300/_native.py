@@ -17,7 +17,8 @@ EXPORTS = [
     "ebi_filter", "ebi_filter_materialize", "ebi_sum", "ebi_min", "ebi_max", "ebi_filter_agg",
     "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches", "ebi_column_set_timing",
     "ebi_column_last_times", "ebi_materialize_static", "ebi_batch_create", "ebi_batch_run",
-    "ebi_batch_get_info", "ebi_batch_destroy",
+    "ebi_batch_get_info", "ebi_batch_destroy", "ebi_server_create", "ebi_server_submit", "ebi_server_poll",
+    "ebi_server_replay", "ebi_server_get_stats", "ebi_server_destroy", "ebi_run_plain",
 ]
 
 
@@ -44,6 +45,31 @@ class BatchInfo(C.Structure):
     """ebi_batch_info"""
     _fields_ = [("queries", C.c_uint64), ("items", C.c_uint64), ("chunks", C.c_uint64), ("shape", C.c_int32),
                 ("ctas_per_sm", C.c_uint32), ("order", C.c_uint32), ("shape_ms", C.c_double * 4)]
+
+
+class Request(C.Structure):
+    """ebi_request"""
+    _fields_ = [("n_columns", C.c_uint32), ("columns", C.c_uint32 * 8), ("pred", Predicate),
+                ("aggregates", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Response(C.Structure):
+    """ebi_response"""
+    _fields_ = [("ticket", C.c_uint64), ("sum", C.c_double), ("min", C.c_double), ("max", C.c_double),
+                ("count", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_uint32),
+                ("submit_ns", C.c_uint64), ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64)]
+
+
+class ServerConfig(C.Structure):
+    """ebi_server_config"""
+    _fields_ = [("device", C.c_int32), ("slots", C.c_uint32), ("max_queries_per_batch", C.c_uint64),
+                ("max_chunks_per_batch", C.c_uint64), ("max_items_per_batch", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    """ebi_server_stats"""
+    _fields_ = [("batches", C.c_uint64), ("requests", C.c_uint64), ("max_in_flight", C.c_uint64),
+                ("pending", C.c_uint64)]
 
 
 class SegmentTimes(C.Structure):
@@ -89,5 +115,13 @@ def lib() -> C.CDLL:
     L.ebi_batch_run.argtypes = [vp, PP, C.POINTER(BatchResult), vp]
     L.ebi_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
     L.ebi_batch_destroy.argtypes = [vp]
+    RQ, RS = C.POINTER(Request), C.POINTER(Response)
+    L.ebi_server_create.argtypes = [C.POINTER(vp), C.c_uint32, C.POINTER(ServerConfig), C.POINTER(vp)]
+    L.ebi_server_submit.argtypes = [vp, RQ, u64p]
+    L.ebi_server_poll.argtypes = [vp, RS, C.c_uint32, C.POINTER(C.c_uint32)]
+    L.ebi_server_replay.argtypes = [vp, RQ, u64p, u64, RS]
+    L.ebi_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
+    L.ebi_server_destroy.argtypes = [vp]
+    L.ebi_run_plain.argtypes = [C.POINTER(vp), C.c_uint32, RQ, u64, RS, vp]
     _lib = L
     return L

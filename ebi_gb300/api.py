@@ -385,5 +385,90 @@ class Batch:
             pass
 
 
+def _requests(reqs):
+    """[(column ids, predicate, aggregates)] -> ebi_request array."""
+    arr = (_native.Request * len(reqs))()
+    for i, (cols, p, aggs) in enumerate(reqs):
+        if not 1 <= len(cols) <= 8:
+            raise InvalidArgument("a request reads 1..8 columns")
+        arr[i].n_columns = len(cols)
+        for k, c in enumerate(cols):
+            arr[i].columns[k] = int(c)
+        arr[i].pred = p.to_c()
+        arr[i].aggregates = sum(_AGG_BITS[a] for a in aggs)
+    return arr
+
+
+def _responses(arr):
+    return [{"sum": r.sum, "min": r.min, "max": r.max, "count": r.count, "status": r.status,
+             "submit_ns": r.submit_ns, "launch_ns": r.launch_ns, "done_ns": r.done_ns} for r in arr]
+
+
+class Server:
+    """Continuous-batching request loop over resident columns (ebi_server_* of
+    the C ABI; no counterpart in the reference).  Requests are
+    (column ids, predicate, aggregates) over 1..8 of the server's decoders."""
+
+    def __init__(self, decoders, slots=4, max_queries=1024, max_chunks=1 << 20, max_items=1 << 21, device=None):
+        self.decoders = list(decoders)
+        dev = self.decoders[0].device if device is None else _torch().device(device)
+        cfg = _native.ServerConfig(dev.index or 0, slots, max_queries, max_chunks, max_items)
+        cols = (C.c_void_p * len(self.decoders))(*[d._h.value for d in self.decoders])
+        h = C.c_void_p()
+        _check(_native.lib().ebi_server_create(cols, len(self.decoders), C.byref(cfg), C.byref(h)), "Server::new")
+        self._h = h
+
+    def submit(self, cols, predicate, aggregates=("sum", "min", "max")) -> int:
+        arr = _requests([(cols, predicate, aggregates)])
+        t = C.c_uint64()
+        _check(_native.lib().ebi_server_submit(self._h, arr, C.byref(t)), "Server::submit")
+        return t.value
+
+    def poll(self, max_n=1024):
+        buf = (_native.Response * max_n)()
+        n = C.c_uint32()
+        _check(_native.lib().ebi_server_poll(self._h, buf, max_n, C.byref(n)), "Server::poll")
+        return [dict(ticket=buf[i].ticket, **_responses([buf[i]])[0]) for i in range(n.value)]
+
+    def replay(self, requests, arrival_ns=None):
+        """Open-loop load (native): request i is submitted arrival_ns[i] after the start."""
+        arr = _requests(requests)
+        out = (_native.Response * len(requests))()
+        arrivals = None
+        if arrival_ns is not None:
+            arrivals = (C.c_uint64 * len(requests))(*[int(t) for t in arrival_ns])
+        _check(_native.lib().ebi_server_replay(self._h, arr, arrivals, len(requests), out), "Server::replay")
+        return _responses(out)
+
+    def stats(self) -> dict:
+        st = _native.ServerStats()
+        _check(_native.lib().ebi_server_get_stats(self._h, C.byref(st)), "Server::stats")
+        return {"batches": st.batches, "requests": st.requests, "max_in_flight": st.max_in_flight,
+                "pending": st.pending}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.lib().ebi_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_plain(decoders, requests, stream=None):
+    """The requests answered one at a time with per-column filter_agg calls (no batching)."""
+    torch = _torch()
+    cols = (C.c_void_p * len(decoders))(*[d._h.value for d in decoders])
+    arr = _requests(requests)
+    out = (_native.Response * len(requests))()
+    s = stream if stream is not None else torch.cuda.current_stream(decoders[0].device)
+    _check(_native.lib().ebi_run_plain(cols, len(decoders), arr, len(requests), out, C.c_void_p(s.cuda_stream)),
+           "run_plain")
+    return _responses(out)
+
+
 def kernel_launches() -> int:
     return _native.lib().ebi_kernel_launches()

@@ -184,6 +184,64 @@ int ebi_batch_run(ebi_batch* batch, const ebi_predicate* preds, ebi_batch_result
 int ebi_batch_get_info(const ebi_batch* batch, ebi_batch_info* out);
 int ebi_batch_destroy(ebi_batch* batch);
 
+/* ---- serving loop ----------------------------------------------------------- */
+/* No reference counterpart (the reference has no server).  A request is a
+ * predicate and the aggregates wanted over 1..8 columns of the server; its
+ * result combines the per-column filter_agg results in column order (sum of
+ * sums, min of mins, max of maxes, total count) and equals that combination
+ * computed one column at a time with ebi_filter_agg, bit for bit; aggregates
+ * not asked for come back as NaN.
+ *
+ * A dispatcher thread keeps `slots` batches in flight, each on its own stream.
+ * Whenever a slot is free it admits queued requests in arrival order while the
+ * slot's capacity lasts (queries, per-chunk accumulators and work items: a
+ * request's memory footprint), launches them as one mixed-codec batch, and
+ * hands back each request's result with its submit / launch / completion
+ * times.  Requests arriving while batches run go into the next free slot, so
+ * batches overlap on the device.  The columns must stay open while the server
+ * exists. */
+typedef struct {
+    uint32_t n_columns;     /* 1..8 */
+    uint32_t columns[8];    /* indices into the server's column list */
+    ebi_predicate pred;
+    uint32_t aggregates;    /* EBI_AGG_* bits */
+    uint32_t reserved;
+} ebi_request;
+typedef struct {
+    uint64_t ticket;        /* from ebi_server_submit (ebi_run_plain: the request index) */
+    double sum, min, max;
+    uint64_t count;
+    int32_t status;
+    uint32_t reserved;
+    uint64_t submit_ns, launch_ns, done_ns;  /* steady-clock times */
+} ebi_response;
+typedef struct {
+    int32_t device;
+    uint32_t slots;                  /* batches in flight (streams) */
+    uint64_t max_queries_per_batch;  /* column queries per batch */
+    uint64_t max_chunks_per_batch;   /* per-chunk accumulators per batch */
+    uint64_t max_items_per_batch;    /* work items per batch */
+} ebi_server_config;
+typedef struct {
+    uint64_t batches, requests, max_in_flight, pending;
+} ebi_server_stats;
+typedef struct ebi_server ebi_server;
+int ebi_server_create(ebi_column* const* columns, uint32_t n_columns, const ebi_server_config* config,
+                      ebi_server** out);
+int ebi_server_submit(ebi_server* server, const ebi_request* req, uint64_t* ticket);
+/* Moves up to `max` finished responses to out (any order); *n_out = how many. */
+int ebi_server_poll(ebi_server* server, ebi_response* out, uint32_t max, uint32_t* n_out);
+/* Open-loop load: submits reqs[i] at arrival_ns[i] nanoseconds after the call
+ * starts (NULL: all at once) and waits for every response; out[i] answers reqs[i]. */
+int ebi_server_replay(ebi_server* server, const ebi_request* reqs, const uint64_t* arrival_ns, uint64_t n,
+                      ebi_response* out);
+int ebi_server_get_stats(ebi_server* server, ebi_server_stats* out);
+int ebi_server_destroy(ebi_server* server);
+/* The same requests answered one at a time with ebi_filter_agg per column
+ * (plain per-query launches), on the calling thread. */
+int ebi_run_plain(ebi_column* const* columns, uint32_t n_columns, const ebi_request* reqs, uint64_t n,
+                  ebi_response* out, void* stream);
+
 /* ---- encoder (host) -------------------------------------------------------- */
 
 /* Encoder::new(.., chunk_option, compressor_config).encode()

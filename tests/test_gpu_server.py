@@ -1,0 +1,90 @@
+"""The continuous-batching server: every request's result, answered in the
+mix (batched with whatever arrived around it, batches overlapping on the
+device), equals the same request answered alone with plain per-column
+filter_agg calls, bit for bit."""
+import numpy as np
+import pytest
+
+import ebi_gb300 as E
+
+pytestmark = pytest.mark.gpu
+
+
+def columns(rng, n_cols):
+    out = []
+    codecs = ["buff", "gorilla", "chimp128", "rle"]
+    for i in range(n_cols):
+        codec = codecs[i % 4]
+        n = int(np.exp(rng.uniform(np.log(2_000), np.log(200_000))))
+        if codec == "buff":
+            v = np.round(rng.uniform(-1000, 1000, n), 3) + 0.0
+            out.append((E.Decoder(E.encode(v, "buff", ("record_count", 65536), 1000)), v))
+        elif codec == "rle":
+            v = np.repeat(np.round(50 + np.cumsum(rng.integers(-5, 6, n // 40 + 1) * 0.1), 1), 40)[:n] + 0.0
+            out.append((E.Decoder(E.encode(v, "rle", ("record_count", 8192))), v))
+        else:
+            v = np.round(30 + np.cumsum(rng.normal(0, 0.5, n)), 2) + 0.0
+            out.append((E.Decoder(E.encode(v, codec, ("record_count", 8192))), v))
+    return out
+
+
+def requests(rng, cols, n):
+    reqs = []
+    for _ in range(n):
+        k = int(rng.integers(1, 9))
+        ids = [int(x) for x in rng.choice(len(cols), size=k, replace=False)]
+        vals = np.concatenate([cols[i][1] for i in ids])
+        a, b = np.sort(rng.choice(vals, 2))
+        p = E.Predicate.range(E.RangeValue.inclusive(float(a)), E.RangeValue.inclusive(float(b)))
+        aggs = [("sum", "min", "max"), ("sum",), ("min",), ("max",)][int(rng.integers(4))]
+        reqs.append((ids, p, aggs))
+    return reqs
+
+
+def same(x, y):
+    return x == y or (np.isnan(x) and np.isnan(y))
+
+
+@pytest.mark.parametrize("rate", [5_000, 50_000, None])
+def test_results_equal_alone_and_in_the_mix(rate):
+    rng = np.random.default_rng(7)
+    cols = columns(rng, 24)
+    decs = [d for d, _ in cols]
+    reqs = requests(rng, cols, 400)
+    alone = E.run_plain(decs, reqs)
+    srv = E.Server(decs, slots=4, max_queries=512, max_chunks=1 << 16, max_items=1 << 17)
+    arrivals = None
+    if rate:
+        arrivals = np.cumsum(rng.exponential(1e9 / rate, len(reqs)))
+    mixed = srv.replay(reqs, arrivals)
+    st = srv.stats()
+    srv.close()
+    assert st["requests"] == len(reqs)
+    for i, (a, m) in enumerate(zip(alone, mixed)):
+        assert a["status"] == 0 and m["status"] == 0, i
+        assert a["count"] == m["count"], (i, a, m)
+        assert same(a["sum"], m["sum"]) and same(a["min"], m["min"]) and same(a["max"], m["max"]), (i, a, m)
+        assert m["done_ns"] >= m["launch_ns"] >= m["submit_ns"]
+    if rate is None:  # everything queued at once: requests share batches
+        assert st["batches"] < len(reqs)
+
+
+def test_poll_interface():
+    rng = np.random.default_rng(3)
+    cols = columns(rng, 6)
+    decs = [d for d, _ in cols]
+    srv = E.Server(decs, slots=2, max_queries=64, max_chunks=1 << 14, max_items=1 << 15)
+    reqs = requests(rng, cols, 20)
+    tickets = [srv.submit(*r) for r in reqs]
+    got = {}
+    import time
+    t0 = time.time()
+    while len(got) < len(reqs) and time.time() - t0 < 30:
+        for r in srv.poll():
+            got[r["ticket"]] = r
+    srv.close()
+    alone = E.run_plain(decs, reqs)
+    assert sorted(got) == sorted(tickets)
+    for t, a in zip(tickets, alone):
+        m = got[t]
+        assert a["count"] == m["count"] and same(a["sum"], m["sum"]) and same(a["min"], m["min"]) and same(a["max"], m["max"])
