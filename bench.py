@@ -257,6 +257,184 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+MIXED_CODECS = ("gorilla", "chimp128", "buff", "rle")
+
+
+def mixed_column(rng, codec, n, seed):
+    """One column of a mixed-codec configuration: the generator of its codec's measured shape."""
+    import ebi_gb300 as E
+    from ebi_gb300 import workloads as W
+
+    if codec == "buff":
+        v = W.round_dp(rng.uniform(-1000.0, 1000.0, n), 3)
+        return E.encode(v, "buff", ("record_count", CHUNK), SCALE)
+    if codec == "gorilla":
+        v = W.gorilla_walk(n, seed=seed)
+    elif codec == "chimp128":
+        v = W.sensor(n, seed=seed)
+    else:
+        v = W.steps(n, seed=seed)
+    return E.encode(v, codec, ("record_count", 8192))
+
+
+def build_mixed(n_cols, lo, hi, seed, dev):
+    """n_cols columns of log-uniform length in [lo, hi], codec drawn uniformly (seeded)."""
+    import ebi_gb300 as E
+
+    rng = np.random.default_rng(seed)
+    lens = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), n_cols))).astype(np.int64)
+    codecs = rng.integers(0, len(MIXED_CODECS), n_cols)
+    decs, meta = [], []
+    t = time.perf_counter()
+    for i in range(n_cols):
+        codec = MIXED_CODECS[codecs[i]]
+        data = mixed_column(rng, codec, int(lens[i]), seed * 100003 + i)
+        decs.append(E.Decoder(data, device=str(dev)))
+        meta.append((codec, int(lens[i]), len(data)))
+    log(f"built {n_cols} columns, {int(lens.sum())} rows, {sum(m[2] for m in meta)} B in {time.perf_counter() - t:.1f} s")
+    return decs, meta
+
+
+def column_range(codec, rng):
+    """A range predicate of about 10-50 % selectivity on a column of the codec's shape."""
+    import ebi_gb300 as E
+
+    if codec == "buff":
+        a = float(rng.uniform(-900, 0)); b = a + float(rng.uniform(200, 1000))
+    elif codec == "gorilla":
+        a = float(rng.uniform(-200, 0)); b = a + float(rng.uniform(50, 400))
+    elif codec == "chimp128":
+        a = float(rng.uniform(10, 20)); b = a + float(rng.uniform(2, 10))
+    else:
+        a = float(rng.uniform(0, 60)); b = a + float(rng.uniform(20, 80))
+    return E.Predicate.range(E.RangeValue.inclusive(a), E.RangeValue.inclusive(b))
+
+
+def run_batched(args):
+    """4,096 columns of log-uniform length 1K..4M, codec uniform over {Gorilla, Chimp128, BUFF, RLE};
+    one step = filter+sum on every column as one batch (persistent mixed-codec launch, graph replay)."""
+    import torch
+
+    import ebi_gb300 as E
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    E.load_library()
+    n_cols = max(1, int(round(4096 * args.scale)))
+    decs, meta = build_mixed(n_cols, 1024, 4_194_304, 5, dev)
+    rng = np.random.default_rng(55)
+    preds = [column_range(m[0], rng) for m in meta]
+    batch = E.Batch([(d, p, ("sum",)) for d, p in zip(decs, preds)])
+    stream = torch.cuda.current_stream(dev)
+    rows = sum(m[1] for m in meta)
+    col_bytes = sum(m[2] for m in meta)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for i in range(max(args.warmup, 3)):
+        batch.run()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = E.kernel_launches()
+    ts = []
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        ev0.record(stream)
+        batch.run()
+        ev1.record(stream)
+        ev1.synchronize()
+        ts.append(ev0.elapsed_time(ev1) / 1e3)
+    launches = E.kernel_launches() - launches0
+    # parity spot check: the batch against single-column queries on a few columns
+    got = batch.run()
+    ok = True
+    for k in list(range(0, n_cols, max(1, n_cols // 16)))[:16]:
+        _, s_, _, _, n_ = decs[k].filter_agg(preds[k], aggregates=("sum",), want_mask=False)
+        ok = ok and got[k][0] == s_ and got[k][3] == n_
+    info = batch.info()
+    t = statistics.median(ts)
+    peak, peak_kind = measured_peak()
+    by_codec = {c: sum(1 for m in meta if m[0] == c) for c in MIXED_CODECS}
+    line = {"metric": "batched filter+sum GB/s (decoded)", "value": round(8.0 * rows / t / 1e9, 3), "unit": "GB/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(1e3 * t, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "mixed -> f64",
+            "data": "synthetic (seeded numpy, the configuration's shape)",
+            "config": {"workload": "batched: columns of log-uniform length 1K..4M f64, codec uniform over "
+                                   "Gorilla/Chimp128/BUFF/RLE, filter+sum per column in one batch",
+                       "columns": n_cols, "scale": args.scale, "rows": rows, "column_bytes": col_bytes,
+                       "columns_by_codec": by_codec, "l2": "flushed before every step (256 MiB write)"},
+            "queries_per_s": round(n_cols / t, 1),
+            "roofline": {"bound": "hbm", "achieved": round(col_bytes / t / 1e9, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(col_bytes / t / 1e9 / peak, 4), "traffic": None,
+                         "kernel": "batch_kernel + batch_finalize_kernel (graph replay)", "peak_source": peak_kind},
+            "autotune": info, "gpu_launches": int(launches),
+            "parity_check": {"sum_and_count_equal_single_column_queries": bool(ok)}}
+    print(json.dumps(line), flush=True)
+    batch.close()
+
+
+def run_serving(args):
+    """512 resident columns of log-uniform length 256K..16M, mixed codecs; Poisson arrivals; each request a
+    random range plus one of sum/min/max over 1..8 columns.  Continuous batching vs plain per-query launches."""
+    import torch
+
+    import ebi_gb300 as E
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    E.load_library()
+    n_cols = max(8, int(round(512 * args.scale)))
+    decs, meta = build_mixed(n_cols, 262_144, 16_777_216, 6, dev)
+    rng = np.random.default_rng(66)
+
+    def make_requests(n):
+        reqs = []
+        for _ in range(n):
+            k = int(rng.integers(1, 9))
+            ids = [int(x) for x in rng.choice(n_cols, size=k, replace=False)]
+            p = column_range(meta[ids[0]][0], rng)
+            reqs.append((ids, p, (("sum",), ("min",), ("max",))[int(rng.integers(3))]))
+        return reqs
+
+    # plain per-query launches (closed loop, one request at a time)
+    plain_reqs = make_requests(max(20, args.steps))
+    E.run_plain(decs, plain_reqs[:5])
+    t0 = time.perf_counter()
+    plain = E.run_plain(decs, plain_reqs)
+    plain_qps = len(plain_reqs) / (time.perf_counter() - t0)
+    srv = E.Server(decs, slots=4, max_queries=4096, max_chunks=1 << 21, max_items=1 << 22)
+    srv.replay(plain_reqs[:50])  # warm-up
+    # the same requests in the mix, all at once: saturated throughput, and bit-equality with the plain answers
+    t0 = time.perf_counter()
+    mixed = srv.replay(plain_reqs)
+    sat_qps = len(plain_reqs) / (time.perf_counter() - t0)
+    equal = all((a["count"] == b["count"]) and all(
+        (a[f] == b[f]) or (np.isnan(a[f]) and np.isnan(b[f])) for f in ("sum", "min", "max"))
+        for a, b in zip(plain, mixed))
+    rates = []
+    for lam in (2_000, 5_000, 10_000, 20_000, 50_000):
+        n = int(min(4000, max(200, lam * 0.5)))
+        reqs = make_requests(n)
+        arr = np.cumsum(rng.exponential(1e9 / lam, n))
+        t0 = time.perf_counter()
+        res = srv.replay(reqs, arr)
+        wall = time.perf_counter() - t0
+        lat = np.array([(r["done_ns"] - r["submit_ns"]) / 1e6 for r in res])
+        rates.append({"offered_per_s": lam, "requests": n, "achieved_per_s": round(n / wall, 1),
+                      "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                      "errors": int(sum(1 for r in res if r["status"]))})
+    st = srv.stats()
+    srv.close()
+    line = {"metric": "serving queries/s (continuous batching) vs plain per-query launches", "value": round(sat_qps, 1),
+            "unit": "queries/s", "n_gpus": 1, "steps": len(plain_reqs), "warmup": 50, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "mixed -> f64",
+            "data": "synthetic (seeded numpy, the configuration's shape)",
+            "config": {"workload": "serving: resident columns of log-uniform length 256K..16M f64, codecs uniform over "
+                                   "Gorilla/Chimp128/BUFF/RLE; requests: random range + one of sum/min/max over 1..8 columns",
+                       "columns": n_cols, "scale": args.scale, "rows": sum(m[1] for m in meta),
+                       "column_bytes": sum(m[2] for m in meta), "slots": 4},
+            "plain_queries_per_s": round(plain_qps, 1), "speedup_vs_plain": round(sat_qps / plain_qps, 2),
+            "results_equal_alone_and_in_mix": bool(equal), "poisson": rates, "server_stats": st}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -267,9 +445,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity-check", action="store_true")
     ap.add_argument("--rows", type=int, default=0, help="column length (profiling runs use smaller columns)")
-    ap.add_argument("--workload", default="buff", choices=["buff", "gorilla", "chimp128", "rle"])
+    ap.add_argument("--workload", default="buff", choices=["buff", "gorilla", "chimp128", "rle", "batched", "serving"])
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="batched / serving: fraction of the configuration's columns to build")
     args = ap.parse_args()
     wl = None
+    if args.workload in ("batched", "serving"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "batched and serving shapes have no CPU reference path"}))
+            return
+        (run_batched if args.workload == "batched" else run_serving)(args)
+        return
     args.warmup = max(args.warmup, 3)
 
     if args.impl == "reference":

@@ -31,7 +31,7 @@ def columns(rng, n_cols):
 def requests(rng, cols, n):
     reqs = []
     for _ in range(n):
-        k = int(rng.integers(1, 9))
+        k = int(rng.integers(1, min(8, len(cols)) + 1))
         ids = [int(x) for x in rng.choice(len(cols), size=k, replace=False)]
         vals = np.concatenate([cols[i][1] for i in ids])
         a, b = np.sort(rng.choice(vals, 2))
