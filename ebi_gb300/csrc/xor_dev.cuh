@@ -188,10 +188,23 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
     bool serial = !parallel;
     if (parallel) {
         auto peek = [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); };
-        // The parse's reads depend on one another: bring the chunk into L2 first.
-        for (uint64_t a = (cd.byte_off & ~uint64_t(127)) + uint64_t(tid) * 128; a < cd.byte_off + cd.byte_len;
-             a += uint64_t(kXorThreads) * 128)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(q.file + a));
+        // The convergence rounds re-read the chunk and each read depends on the
+        // previous one: stage the chunk's words (big-endian) in the values
+        // array, unused until the extraction, when it fits; else warm L2.
+        const uint64_t w0 = cd.byte_off >> 2;
+        const uint64_t nwords = ((cd.byte_off + cd.byte_len + 3) >> 2) - w0 + 3;
+        const bool staged = nwords <= uint64_t(kRcap) * 2;
+        uint32_t* stage = reinterpret_cast<uint32_t*>(sm.vals);
+        if (staged) {
+            for (uint64_t i = tid; i < nwords; i += kXorThreads) stage[i] = bswap32(__ldg(fw + w0 + i));
+            __syncthreads();
+        } else {
+            for (uint64_t a = (cd.byte_off & ~uint64_t(127)) + uint64_t(tid) * 128; a < cd.byte_off + cd.byte_len;
+                 a += uint64_t(kXorThreads) * 128)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(q.file + a));
+        }
+        const uint64_t sbit0 = (cd.byte_off & 3) * 8;
+        auto peek_staged = [stage, sbit0](uint64_t p) { return peek64_be(stage, sbit0 + p); };
 
         // ---- 1. control parse: segments converge to the sequential parse ---
         const uint64_t span = B - 64;
@@ -201,7 +214,11 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
         const bool last = tid == kXorThreads - 1;
         PState in{tid == 0 ? 64 : (sbeg < B ? sbeg : B), CODEC == CODEC_GORILLA ? 0u : (tid == 0 ? kNoLead : 0u)};
         uint32_t n, fail;
-        PState out = parse_segment<CODEC>(peek, B, in, send, last, &n, &fail);
+        auto parse = [&](PState from, uint32_t* n_out, uint32_t* fail_out) {
+            return staged ? parse_segment<CODEC>(peek_staged, B, from, send, last, n_out, fail_out)
+                          : parse_segment<CODEC>(peek, B, from, send, last, n_out, fail_out);
+        };
+        PState out = parse(in, &n, &fail);
         s_in[tid] = pack_state(in);
         s_out[tid] = pack_state(out);
         uint32_t first_fail = kXorThreads;
@@ -213,11 +230,12 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
             if (!__syncthreads_or(stale && static_cast<uint32_t>(tid) <= first_fail)) break;
             if (stale) {
                 in = unpack_state(want);
-                out = parse_segment<CODEC>(peek, B, in, send, last, &n, &fail);
+                out = parse(in, &n, &fail);
                 s_in[tid] = want;
                 s_out[tid] = pack_state(out);
             }
         }
+        __syncthreads();  // the staged words are overwritten by the extraction
         // Segments past the first failure hold no records of the stream.
         if (static_cast<uint32_t>(tid) > first_fail) n = 0;
         uint32_t total;
