@@ -16,13 +16,14 @@
 #include "gorilla_dev.cuh"
 #include "raw_dev.cuh"
 #include "rle_dev.cuh"
+#include "xor_dev.cuh"
 #include "xor_lanes.cuh"
 
 namespace ebi {
 namespace {
 
 constexpr int kBatchThreads = 256;
-static_assert(kBatchThreads == kRleThreads && kBatchThreads == int(kLaneItemChunks), "codec CTA shapes");
+static_assert(kBatchThreads == kXorThreads && kBatchThreads == kRleThreads, "codec CTA shapes");
 
 // One function per item kind, kept out of line so that each gets its own
 // register allocation (the kernel's is the largest, not the sum of all paths).
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(kFinThreads) batch_finalize_kernel(const Query
 
 }  // namespace
 
-size_t batch_smem_bytes() { return 0; }  // the item paths use static shared memory only
+size_t batch_smem_bytes() { return xor_smem_bytes(CODEC_CHIMP128); }
 
 cudaError_t prepare_batch_kernel() {
     return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
