@@ -3,8 +3,7 @@
 //
 // A batch is a list of work items, each naming a query and a unit of one of
 // its columns: an 8,192-row BUFF tile, a whole Uncompressed / RLE / Chimp /
-// Chimp128 chunk, or a group of up to 256 Gorilla / Chimp / Chimp128 chunks
-// decoded one per thread (xor_lanes.cuh).  A persistent
+// Chimp128 chunk, or a group of Gorilla chunks (one per warp).  A persistent
 // grid of 256-thread CTAs pulls items from a device counter, so columns of
 // very different lengths and codecs share the GPU without a launch per
 // column; each item runs the same per-chunk device code as the single-column
@@ -17,7 +16,6 @@
 #include "raw_dev.cuh"
 #include "rle_dev.cuh"
 #include "xor_dev.cuh"
-#include "xor_lanes.cuh"
 
 namespace ebi {
 namespace {
@@ -40,10 +38,15 @@ __device__ __noinline__ void item_raw(const QueryParams& q, const BatchItem& it)
 __device__ __noinline__ void item_rle(const QueryParams& q, const BatchItem& it) {
     rle_chunk(q, it.unit, it.unit, VAL_SCAN, nullptr);
 }
-// Chunks [unit, unit + count) of an XOR-coded column, one per thread.
-template <int CODEC>
-__device__ __forceinline__ void item_xor_lanes(const QueryParams& q, const BatchItem& it) {
-    if (threadIdx.x < it.count) xor_lane_chunk<CODEC>(q, it.unit + threadIdx.x, it.unit + threadIdx.x, VAL_SCAN, nullptr);
+__device__ __noinline__ void item_gorilla(const QueryParams& q, const BatchItem& it) {
+    const uint32_t warp = threadIdx.x >> 5;
+    if (warp < it.count) gorilla_chunk_l1(q, it.unit + warp, it.unit + warp, VAL_SCAN, nullptr);
+}
+__device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_CHIMP>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+}
+__device__ __noinline__ void item_chimp128(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_CHIMP128>(q, it.unit, it.unit, VAL_SCAN, nullptr);
 }
 
 __global__ void __launch_bounds__(kBatchThreads, 2)
@@ -64,9 +67,9 @@ batch_kernel(const QueryParams* __restrict__ qp, const BatchItem* __restrict__ i
         case ITEM_BUFF_TILE: item_buff_tile(q, it, s_k, s_red); break;
         case ITEM_RAW: item_raw(q, it); break;
         case ITEM_RLE: item_rle(q, it); break;
-        case ITEM_GORILLA: item_xor_lanes<CODEC_GORILLA>(q, it); break;
-        case ITEM_CHIMP: item_xor_lanes<CODEC_CHIMP>(q, it); break;
-        case ITEM_CHIMP128: item_xor_lanes<CODEC_CHIMP128>(q, it); break;
+        case ITEM_GORILLA: item_gorilla(q, it); break;
+        case ITEM_CHIMP: item_chimp(q, it); break;
+        case ITEM_CHIMP128: item_chimp128(q, it); break;
         default: break;
         }
     }

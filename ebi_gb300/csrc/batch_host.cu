@@ -31,9 +31,9 @@ int bfail(int code, const std::string& msg) {
 // measured on the single-column kernels), for the cost-descending order.
 double item_cost(uint32_t kind, uint32_t count) {
     switch (kind) {
-    case ITEM_GORILLA:
-    case ITEM_CHIMP128:
-    case ITEM_CHIMP: return 1000.0 + count;  // a chunk's whole stream per thread: the longest items
+    case ITEM_GORILLA: return 40.0 * count;
+    case ITEM_CHIMP128: return 30.0;
+    case ITEM_CHIMP: return 25.0;
     case ITEM_BUFF_TILE: return 1.0;
     case ITEM_RLE: return 0.5;
     default: return 2.0;
@@ -194,16 +194,15 @@ int ebi_batch_create(const ebi_batch_query* queries, uint64_t n, void* stream, e
             for (uint32_t t = 0; t < c->tiles.tiles.size(); ++t) b->items_query.push_back({qi, ITEM_BUFF_TILE, t, 1});
             break;
         case EBI_GORILLA:
-        case EBI_CHIMP:
-        case EBI_CHIMP128: {
-            const uint32_t kind = c->scheme == EBI_GORILLA ? ITEM_GORILLA : c->scheme == EBI_CHIMP ? ITEM_CHIMP : ITEM_CHIMP128;
-            for (uint64_t k = 0; k < c->n_chunks; k += kLaneItemChunks)
-                b->items_query.push_back({qi, kind, static_cast<uint32_t>(k),
-                                          static_cast<uint32_t>(std::min<uint64_t>(kLaneItemChunks, c->n_chunks - k))});
+            for (uint64_t k = 0; k < c->n_chunks; k += 8)
+                b->items_query.push_back({qi, ITEM_GORILLA, static_cast<uint32_t>(k),
+                                          static_cast<uint32_t>(std::min<uint64_t>(8, c->n_chunks - k))});
             break;
-        }
         default: {
-            const uint32_t kind = c->scheme == EBI_UNCOMPRESSED ? ITEM_RAW : ITEM_RLE;
+            const uint32_t kind = c->scheme == EBI_UNCOMPRESSED ? ITEM_RAW
+                                : c->scheme == EBI_RLE         ? ITEM_RLE
+                                : c->scheme == EBI_CHIMP       ? ITEM_CHIMP
+                                                               : ITEM_CHIMP128;
             for (uint64_t k = 0; k < c->n_chunks; ++k) b->items_query.push_back({qi, kind, static_cast<uint32_t>(k), 1});
         }
         }

@@ -8,12 +8,11 @@
 //
 // The warp follows the stream exactly, several records per step:
 //   * a '0' run: the count of leading zero bits at the cursor is the number of
-//     consecutive repeats (up to 64 per step);
+//     consecutive repeats (up to 32 per step);
 //   * a '10' run: with the window fixed, records sit at a fixed stride of
-//     2 + significant bits.  Lane l checks that records 4l .. 4l + 3 of the
-//     stride still start with '10' and fit in the chunk; the warp minimum of
-//     the lanes' first failing record says how many (up to 128) are
-//     confirmed, each lane extracts its payloads and a lane-local plus
+//     2 + significant bits.  Lane i checks that record i of the stride still
+//     starts with '10' and fits in the chunk; the ballot's leading ones say how
+//     many records are confirmed, each lane extracts its payload and a
 //     warp-shuffle prefix XOR (seeded with the previous value) gives the values;
 //   * a '11' record (new window) is one step.
 // On the bench series over 99 % of the records are '10' in a handful of
@@ -52,16 +51,10 @@ __host__ __device__ __forceinline__ uint64_t stage_span(uint64_t byte_off, uint6
 }
 
 // Decodes chunk cd and runs the query over its values (one warp).
-constexpr uint32_t kPerLane = 4;                 // consecutive records per lane in a step
-constexpr uint32_t kStep = 32 * kPerLane;        // records a warp step can confirm
-struct LaneVals {
-    uint64_t v[kPerLane];
-};
-
 template <typename Peek>
 __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, ChunkAcc* acc, uint32_t li, int mode,
                                      const unsigned long long* chunk_offsets, Peek peek) {
-    const uint32_t lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31;
     const bool has_mask = q.in_mask != nullptr;
     const uint64_t B = cd.byte_len * 8;
     const bool pred_on = q.pred_on != 0;
@@ -69,60 +62,36 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
     const KeyPred kp = key_pred(q.pred);
     ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
     unsigned long long out_pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull;
-    uint64_t idx = 0;  // chunk row of the step's first record
+    uint64_t idx = 0;  // chunk row of the next value
 
-    // Record lane * kPerLane + r of the step (rows idx + that) has value bits
-    // v[r]; records at or past k are not part of the stream.  Applies the end
-    // marker and the query; returns true when the stream ended in this step.
-    auto emit = [&](uint32_t k, const LaneVals lv) -> bool {
-        const uint64_t* v = lv.v;
-        uint32_t first_nan = kStep;
-#pragma unroll
-        for (int r = kPerLane - 1; r >= 0; --r)
-            if (lane * kPerLane + r < k && v[r] == kNanBits) first_nan = lane * kPerLane + r;
-        first_nan = __reduce_min_sync(kFull, first_nan);
-        const bool ended = first_nan < k;
-        if (ended) k = first_nan;
-        uint32_t bits = 0;
-#pragma unroll
-        for (int r = 0; r < static_cast<int>(kPerLane); ++r) {
-            const uint32_t i = lane * kPerLane + r;
-            const uint64_t g = cd.row_off + idx + i;
-            const bool in = i < k && (!has_mask || mask_row(q.in_mask, q.n_records, g));
-            const bool pass = in && (!pred_on || kp.pass(v[r]));
-            if (pass) {
-                bits |= 1u << r;
-                if (mode == VAL_COUNT) ++agg.cnt;
-                else if (mode == VAL_SCAN) val_agg_add1(agg, v[r]);
-            }
+    // Lanes [0, k) hold the values (bits) of rows idx + lane.  Applies the end
+    // marker and the query; returns true when the stream ended here.
+    auto emit = [&](uint32_t k, uint64_t vbits) -> bool {
+        const uint32_t nanm = __ballot_sync(kFull, static_cast<uint32_t>(lane) < k && vbits == kNanBits);
+        bool ended = false;
+        if (nanm) {
+            k = __ffs(nanm) - 1;
+            ended = true;
         }
+        const uint64_t g = cd.row_off + idx + lane;
+        const bool in = static_cast<uint32_t>(lane) < k && (!has_mask || mask_row(q.in_mask, q.n_records, g));
+        const bool pass = in && (!pred_on || kp.pass(vbits));
         if (mode == VAL_MATERIALIZE) {
-            const uint32_t c = __popc(bits);
-            uint32_t incl = c;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(kFull, incl, o);
-                if (lane >= static_cast<uint32_t>(o)) incl += t;
+            const uint32_t bal = __ballot_sync(kFull, pass);
+            if (pass) {
+                const unsigned long long pos = out_pos + __popc(bal & ((1u << lane) - 1u));
+                if (pos < q.out_cap) q.out_vals[pos] = __longlong_as_double(static_cast<long long>(vbits));
             }
-            unsigned long long pos = out_pos + (incl - c);
-#pragma unroll
-            for (int r = 0; r < static_cast<int>(kPerLane); ++r)
-                if ((bits >> r) & 1u) {
-                    if (pos < q.out_cap) q.out_vals[pos] = __longlong_as_double(static_cast<long long>(v[r]));
-                    ++pos;
-                }
-            out_pos += __shfl_sync(kFull, incl, 31);
-        } else if (store) {
-            // rows >= n_records never enter a bitmask
-            uint32_t keep = 0;
-#pragma unroll
-            for (int r = 0; r < static_cast<int>(kPerLane); ++r)
-                keep |= (cd.row_off + idx + lane * kPerLane + r < q.n_records) ? (1u << r) : 0u;
-            uint32_t x = (bits & keep) << (kPerLane * (lane & 7));
-            x |= __shfl_xor_sync(kFull, x, 1);
-            x |= __shfl_xor_sync(kFull, x, 2);
-            x |= __shfl_xor_sync(kFull, x, 4);
-            if ((lane & 7) == 0 && x) store_mask_word(q.out_mask, cd.row_off + idx + kPerLane * lane, x, true);
+            out_pos += __popc(bal);
+        } else {
+            if (store) {
+                const uint32_t word = __ballot_sync(kFull, pass && g < q.n_records);
+                if (lane == 0 && word) store_mask_word(q.out_mask, cd.row_off + idx, word, true);
+            }
+            if (pass) {
+                if (mode == VAL_COUNT) ++agg.cnt;
+                else val_agg_add1(agg, vbits);
+            }
         }
         idx += k;
         return ended;
@@ -135,11 +104,7 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
         uint64_t carry = peek(0);  // the previous value
         uint64_t p = 64;
         uint32_t lead = 0, trail = 0;
-        LaneVals lv;
-        uint64_t* v = lv.v;
-#pragma unroll
-        for (int r = 0; r < static_cast<int>(kPerLane); ++r) v[r] = carry;
-        bool done = emit(1, lv);
+        bool done = emit(1, carry);
         while (!done) {
             if (p + 1 > B) { status = EBI_E_UNEXPECTED_END; break; }
             const uint64_t x = peek(p);
@@ -147,61 +112,40 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
                 // '0' run: one repeat per zero bit inside the chunk
                 uint64_t z = x ? static_cast<uint64_t>(__clzll(static_cast<long long>(x))) : 64;
                 if (z > B - p) z = B - p;
-                const uint32_t k = z < kStep ? static_cast<uint32_t>(z) : kStep;
-#pragma unroll
-                for (int r = 0; r < static_cast<int>(kPerLane); ++r) v[r] = carry;
-                done = emit(k, lv);
+                const uint32_t k = z < 32 ? static_cast<uint32_t>(z) : 32u;
+                done = emit(k, carry);
                 p += k;
                 continue;
             }
             if (p + 2 > B) { status = EBI_E_UNEXPECTED_END; break; }
             if (!((x >> 62) & 1)) {
-                // '10' run at stride 2 + sig: lane checks records lane * kPerLane + r
+                // '10' run at stride 2 + sig
                 const uint32_t sig = 64 - lead - trail;  // 1..64
                 const uint64_t L = 2 + sig;
-                uint64_t y[kPerLane];
-                uint32_t first_bad = kStep;
-#pragma unroll
-                for (int r = kPerLane - 1; r >= 0; --r) {
-                    const uint64_t qi = p + uint64_t(lane * kPerLane + r) * L;
-                    bool fits = qi + L <= B;
-                    y[r] = 0;
-                    if (fits) {
-                        y[r] = peek(qi);
-                        fits = (y[r] >> 62) == 2;
-                    }
-                    if (!fits) first_bad = lane * kPerLane + r;
+                const uint64_t qi = p + static_cast<uint64_t>(lane) * L;
+                bool fits = qi + L <= B;
+                uint64_t y = 0;
+                if (fits) {
+                    y = peek(qi);
+                    fits = (y >> 62) == 2;
                 }
-                const uint32_t k = __reduce_min_sync(kFull, first_bad);
+                const uint32_t m = __ballot_sync(kFull, fits);
+                const uint32_t k = ~m ? static_cast<uint32_t>(__ffs(~m) - 1) : 32u;
                 if (k == 0) { status = EBI_E_UNEXPECTED_END; break; }  // the record at p does not fit
-                uint64_t loc = 0;
-#pragma unroll
-                for (int r = 0; r < static_cast<int>(kPerLane); ++r) {
-                    const uint32_t i = lane * kPerLane + r;
-                    uint64_t d = 0;
-                    if (i < k) {
-                        const uint64_t w = sig <= 62 ? (y[r] << 2) : peek(p + uint64_t(i) * L + 2);
-                        d = (w >> (64 - sig)) << trail;
-                    }
-                    loc ^= d;
-                    v[r] = loc;  // XOR of the lane's deltas up to r
+                uint64_t d = 0;
+                if (static_cast<uint32_t>(lane) < k) {
+                    const uint64_t w = sig <= 62 ? (y << 2) : peek(qi + 2);
+                    d = (w >> (64 - sig)) << trail;
                 }
-                uint64_t pre = loc;  // inclusive warp XOR scan of the lane totals
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    const uint64_t t = __shfl_up_sync(kFull, pre, o);
-                    if (lane >= static_cast<uint32_t>(o)) pre ^= t;
+                    const uint64_t t = __shfl_up_sync(kFull, d, o);
+                    if (lane >= o) d ^= t;
                 }
-                const uint64_t base = carry ^ pre ^ loc;  // carry ^ lanes before this one
-#pragma unroll
-                for (int r = 0; r < static_cast<int>(kPerLane); ++r) v[r] ^= base;
-                const uint32_t last = k - 1;
-                uint64_t vl = v[0];
-#pragma unroll
-                for (int r = 1; r < static_cast<int>(kPerLane); ++r) vl = (last % kPerLane) == static_cast<uint32_t>(r) ? v[r] : vl;
-                carry = __shfl_sync(kFull, vl, last / kPerLane);
-                p += uint64_t(k) * L;
-                done = emit(k, lv);
+                const uint64_t v = carry ^ d;
+                carry = __shfl_sync(kFull, v, k - 1);
+                p += k * L;
+                done = emit(k, v);
                 continue;
             }
             // '11': a new window
@@ -214,9 +158,7 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
             trail = 64 - l - sg;
             carry ^= (peek(p + 13) >> (64 - sg)) << trail;
             p += 13 + sg;
-#pragma unroll
-            for (int r = 0; r < static_cast<int>(kPerLane); ++r) v[r] = carry;
-            done = emit(1, lv);
+            done = emit(1, carry);
         }
     }
     if (status) {

@@ -73,9 +73,9 @@ enum BatchItemKind : uint32_t {
     ITEM_BUFF_TILE = 0,  // unit = tile index of the query's column
     ITEM_RAW = 1,        // unit = chunk
     ITEM_RLE = 2,
-    ITEM_GORILLA = 3,    // chunks [unit, unit + count), count <= kLaneItemChunks, one thread each
-    ITEM_CHIMP = 4,      // same
-    ITEM_CHIMP128 = 5,   // same
+    ITEM_GORILLA = 3,    // chunks [unit, unit + count), one warp each
+    ITEM_CHIMP = 4,
+    ITEM_CHIMP128 = 5,
 };
 struct BatchItem {
     uint32_t query;  // index into the batch's QueryParams
@@ -83,7 +83,6 @@ struct BatchItem {
     uint32_t unit;
     uint32_t count;
 };
-constexpr uint32_t kLaneItemChunks = 256;  // XOR chunks per batch item (one per thread of a CTA)
 // Dynamic shared memory of the batch kernel; prepare_batch_kernel raises the
 // kernel's shared-memory limit to it (once per process, outside any capture).
 size_t batch_smem_bytes();

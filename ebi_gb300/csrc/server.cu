@@ -60,9 +60,9 @@ struct Slot {
 
 double item_cost(uint32_t kind, uint32_t count) {
     switch (kind) {
-    case ITEM_GORILLA:
-    case ITEM_CHIMP128:
-    case ITEM_CHIMP: return 1000.0 + count;  // a chunk's whole stream per thread: the longest items
+    case ITEM_GORILLA: return 40.0 * count;
+    case ITEM_CHIMP128: return 30.0;
+    case ITEM_CHIMP: return 25.0;
     case ITEM_BUFF_TILE: return 1.0;
     case ITEM_RLE: return 0.5;
     default: return 2.0;
@@ -98,9 +98,7 @@ void footprint(const ebi_server* s, const ebi_request& r, uint64_t* chunks, uint
         const ebi_column* col = s->cols[r.columns[k]];
         c += col->n_chunks;
         it += col->scheme == EBI_BUFF ? col->tiles.tiles.size()
-            : (col->scheme == EBI_GORILLA || col->scheme == EBI_CHIMP || col->scheme == EBI_CHIMP128)
-                ? (col->n_chunks + kLaneItemChunks - 1) / kLaneItemChunks
-                : col->n_chunks;
+            : col->scheme == EBI_GORILLA ? (col->n_chunks + 7) / 8 : col->n_chunks;
     }
     *chunks = c;
     *items = it;
@@ -127,13 +125,15 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
             sl.h_qp[nq] = q;
             if (c->scheme == EBI_BUFF) {
                 for (uint32_t t = 0; t < c->tiles.tiles.size(); ++t) items.push_back({nq, ITEM_BUFF_TILE, t, 1});
-            } else if (c->scheme == EBI_GORILLA || c->scheme == EBI_CHIMP || c->scheme == EBI_CHIMP128) {
-                const uint32_t kind = c->scheme == EBI_GORILLA ? ITEM_GORILLA : c->scheme == EBI_CHIMP ? ITEM_CHIMP : ITEM_CHIMP128;
-                for (uint64_t j = 0; j < c->n_chunks; j += kLaneItemChunks)
-                    items.push_back({nq, kind, static_cast<uint32_t>(j),
-                                     static_cast<uint32_t>(std::min<uint64_t>(kLaneItemChunks, c->n_chunks - j))});
+            } else if (c->scheme == EBI_GORILLA) {
+                for (uint64_t j = 0; j < c->n_chunks; j += 8)
+                    items.push_back({nq, ITEM_GORILLA, static_cast<uint32_t>(j),
+                                     static_cast<uint32_t>(std::min<uint64_t>(8, c->n_chunks - j))});
             } else {
-                const uint32_t kind = c->scheme == EBI_UNCOMPRESSED ? ITEM_RAW : ITEM_RLE;
+                const uint32_t kind = c->scheme == EBI_UNCOMPRESSED ? ITEM_RAW
+                                    : c->scheme == EBI_RLE         ? ITEM_RLE
+                                    : c->scheme == EBI_CHIMP       ? ITEM_CHIMP
+                                                                   : ITEM_CHIMP128;
                 for (uint64_t j = 0; j < c->n_chunks; ++j) items.push_back({nq, kind, static_cast<uint32_t>(j), 1});
             }
             ++nq;
