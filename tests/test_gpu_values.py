@@ -149,3 +149,33 @@ def test_full_size_properties(codec):
     assert mn == v[sel].min() and mx == v[sel].max()
     assert sum_ok(s, float(np.sum(v[sel])), False, v[sel])
     assert sum_ok(d.sum(), float(np.sum(v)), False, v)
+
+
+@pytest.mark.parametrize("codec", ["gorilla", "chimp", "chimp128"])
+@pytest.mark.parametrize("kind", ["walk", "sensor", "few"])
+def test_many_small_chunks(codec, kind):
+    # >= 1,024 chunks of 64 values: short streams, many CTAs
+    rng = np.random.default_rng(abs(hash((codec, kind, "lanes"))) % 2**32)
+    n = 80_000
+    v = columns(rng, n)[kind]
+    data = E.encode(v, codec, ("record_count", 64))
+    n_chunks = O.Decoder(data).n_chunks
+    assert n_chunks >= 1024
+    check_query_suite(data, random_preds(v, rng, k=2), masks=(None, random_mask(n, 0.3, rng)),
+                      chunk_ids=(None, int(rng.integers(n_chunks))))
+
+
+@pytest.mark.parametrize("codec", ["chimp", "chimp128"])
+def test_many_small_chunks_corrupt(codec):
+    rng = np.random.default_rng(9)
+    v = np.round(30 + np.cumsum(rng.normal(0, 0.5, 70_000)), 2) + 0.0
+    base = bytes(E.encode(v, codec, ("record_count", 64)))
+    d = O.Decoder(base)
+    for trial in range(4):
+        data = bytearray(base)
+        for _ in range(3):
+            c = int(rng.integers(d.n_chunks))
+            phys, size, _, _ = d.chunk_info(c)
+            data[phys + int(rng.integers(size))] ^= 1 << int(rng.integers(8))
+        check_query_suite(bytes(data), [E.Predicate.range(E.RangeValue.inclusive(25.0), E.RangeValue.NONE)],
+                          masks=(None,))
