@@ -10,7 +10,7 @@ from . import _native
 from .api import (BUFF, CHIMP, CHIMP128, GORILLA, RLE, SCHEMES, UNCOMPRESSED, Batch, ChunkId, ConversionError,
                   CorruptChunk, CudaError, Decoder, DecoderError, InvalidArgument, IOError_, OutOfMemory,
                   Predicate, PreconditionsNotMet, Range, RangeValue, Server, UnexpectedEndOfChunk, Unsupported,
-                  encode, kernel_launches, run_plain)
+                  encode, kernel_launches, mask_from_rows, rows_from_mask, run_plain)
 
 
 def load_library():
@@ -22,5 +22,5 @@ __all__ = [
     "BUFF", "CHIMP", "CHIMP128", "GORILLA", "RLE", "SCHEMES", "UNCOMPRESSED", "Batch", "ChunkId", "ConversionError",
     "CorruptChunk", "CudaError", "Decoder", "DecoderError", "InvalidArgument", "IOError_", "OutOfMemory",
     "Predicate", "PreconditionsNotMet", "Range", "RangeValue", "UnexpectedEndOfChunk", "Unsupported", "encode",
-    "kernel_launches", "load_library", "Server", "run_plain",
+    "kernel_launches", "load_library", "Server", "run_plain", "mask_from_rows", "rows_from_mask",
 ]

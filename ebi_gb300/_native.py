@@ -18,7 +18,8 @@ EXPORTS = [
     "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches", "ebi_column_set_timing",
     "ebi_column_last_times", "ebi_materialize_static", "ebi_batch_create", "ebi_batch_run",
     "ebi_batch_get_info", "ebi_batch_destroy", "ebi_server_create", "ebi_server_submit", "ebi_server_poll",
-    "ebi_server_replay", "ebi_server_get_stats", "ebi_server_destroy", "ebi_run_plain",
+    "ebi_server_replay", "ebi_server_get_stats", "ebi_server_destroy", "ebi_run_plain", "ebi_mask_from_rows",
+    "ebi_rows_from_mask",
 ]
 
 
@@ -122,6 +123,8 @@ def lib() -> C.CDLL:
     L.ebi_server_replay.argtypes = [vp, RQ, u64p, u64, RS]
     L.ebi_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
     L.ebi_server_destroy.argtypes = [vp]
+    L.ebi_mask_from_rows.argtypes = [vp, u64, u64, vp, vp]
+    L.ebi_rows_from_mask.argtypes = [vp, u64, vp, u64, u64p, vp]
     L.ebi_run_plain.argtypes = [C.POINTER(vp), C.c_uint32, RQ, u64, RS, vp]
     _lib = L
     return L

@@ -470,5 +470,35 @@ def run_plain(decoders, requests, stream=None):
     return _responses(out)
 
 
+def mask_from_rows(rows, n_records: int, device="cuda:0"):
+    """Dense device bitmask of a u32 row-id set (RoaringBitmap::iter order or any order)."""
+    torch = _torch()
+    dev = torch.device(device)
+    r = torch.as_tensor(np.ascontiguousarray(rows, dtype=np.uint32).view(np.int32), device=dev)
+    m = torch.empty(max((n_records + 63) // 64, 1), dtype=torch.int64, device=dev)
+    s = torch.cuda.current_stream(dev)
+    _check(_native.lib().ebi_mask_from_rows(C.c_void_p(r.data_ptr()), r.numel(), n_records, C.c_void_p(m.data_ptr()),
+                                            C.c_void_p(s.cuda_stream)), "mask_from_rows")
+    return m
+
+
+def rows_from_mask(mask, n_records: int):
+    """Ascending u32 row ids of a device bitmask (as RoaringBitmap::iter yields them)."""
+    torch = _torch()
+    dev = mask.device
+    s = torch.cuda.current_stream(dev)
+    n = C.c_uint64()
+    cap = 1 << 16
+    while True:
+        out = torch.empty(cap, dtype=torch.int32, device=dev)
+        rc = _native.lib().ebi_rows_from_mask(C.c_void_p(mask.data_ptr()), n_records, C.c_void_p(out.data_ptr()), cap,
+                                               C.byref(n), C.c_void_p(s.cuda_stream))
+        if rc == InvalidArgument.code and n.value > cap:
+            cap = n.value
+            continue
+        _check(rc, "rows_from_mask")
+        return out[: n.value]
+
+
 def kernel_launches() -> int:
     return _native.lib().ebi_kernel_launches()

@@ -147,6 +147,19 @@ int ebi_filter_agg(ebi_column* col, const ebi_predicate* pred, const uint64_t* d
                    int64_t chunk_id, uint64_t* d_out_mask, double* sum, double* min, double* max,
                    uint64_t* n_selected, void* stream);
 
+/* ---- row sets ------------------------------------------------------------- */
+/* The reference passes row sets as RoaringBitmap (ascending u32 row ids,
+ * decoder/query.rs:199-238); the engine takes dense device bitmasks.  These
+ * convert on the device, so a binding hands over RoaringBitmap::iter's ids:
+ * ebi_mask_from_rows sets the bit of every id (any order, duplicates allowed;
+ * ids >= n_records are dropped, as no chunk holds them) in a zeroed mask of
+ * ceil(n_records / 64) words; ebi_rows_from_mask writes the set rows in
+ * ascending order (RoaringBitmap::iter order) to d_rows[0 .. *n_out), or sets
+ * *n_out to the number needed and fails with EBI_E_INVALID when cap is short. */
+int ebi_mask_from_rows(const uint32_t* d_rows, uint64_t n_rows, uint64_t n_records, uint64_t* d_mask, void* stream);
+int ebi_rows_from_mask(const uint64_t* d_mask, uint64_t n_records, uint32_t* d_rows, uint64_t cap, uint64_t* n_out,
+                       void* stream);
+
 /* ---- batched queries ------------------------------------------------------ */
 /* No reference counterpart: the reference answers one Decoder call at a time.
  * A batch is a fixed list of filter + aggregate queries, each over one open
