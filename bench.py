@@ -54,6 +54,26 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def replica_throughput(local_s: float, local_rows: int, dist=None, device=None):
+    """Whole-job decoded GB/s of N replicas: every rank's rows over the slowest rank's time.
+
+    Returns (slowest rank's device seconds, GB/s of 8-byte values).  Without a process group
+    (one GPU) it is the local figure."""
+    import torch
+
+    t = local_s
+    rows = local_rows
+    if dist is not None and dist.is_initialized():
+        tt = torch.tensor([local_s, float(local_rows)], dtype=torch.float64,
+                          device=device if device is not None else "cpu")
+        mx = tt.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tt, op=dist.ReduceOp.SUM)
+        t = float(mx[0].item())
+        rows = int(tt[1].item())
+    return t, 8.0 * rows / t / 1e9
+
+
 class Workload:
     """One measured shape: its column (EBI1 bytes) and the range queries a step cycles through."""
 
@@ -519,13 +539,7 @@ def main():
     sampler.stop()
     clocks = sampler.summary(t0, t1)
 
-    dev_s = sum(total) / 1e3
-    if dist:
-        tt = torch.tensor([dev_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_s = float(tt.item())
-    rows_all = n * args.steps * world
-    value = 8.0 * rows_all / dev_s / 1e9
+    dev_s, value = replica_throughput(sum(total) / 1e3, n * args.steps, dist, dev)
 
     # roofline of the dominant kernel (the fused BUFF filter+sum kernel)
     peak, peak_kind = measured_peak()
