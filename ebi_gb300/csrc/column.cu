@@ -61,6 +61,35 @@ static void tune_pool_once() {
     });
 }
 
+// Pinned result slots: every column needs one small pinned QueryResult for
+// its scalar outputs.  cudaMallocHost / cudaFreeHost are slow, synchronizing
+// calls, so the slots come from pinned slabs allocated once and recycled.
+class PinnedSlots {
+  public:
+    QueryResult* take() {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (free_.empty()) {
+            constexpr size_t kSlab = 1024;
+            void* p = nullptr;
+            if (cudaMallocHost(&p, kSlab * sizeof(QueryResult)) != cudaSuccess) return nullptr;
+            QueryResult* q = static_cast<QueryResult*>(p);
+            for (size_t i = 0; i < kSlab; ++i) free_.push_back(q + i);
+        }
+        QueryResult* r = free_.back();
+        free_.pop_back();
+        return r;
+    }
+    void give(QueryResult* r) {
+        std::lock_guard<std::mutex> lk(mu_);
+        free_.push_back(r);
+    }
+
+  private:
+    std::mutex mu_;
+    std::vector<QueryResult*> free_;  // slabs are kept for the life of the process
+};
+static PinnedSlots g_pinned;
+
 }  // namespace ebi
 
 using namespace ebi;
@@ -409,7 +438,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st) st = dev_alloc(&c->d_res, 1, s);
     if (!st && !binfo.empty()) st = dev_alloc(&c->d_buff, binfo.size(), s);
     if (!st) st = dev_alloc(&c->d_tot, 1, s);
-    if (!st && cudaMallocHost(&c->h_res, sizeof(QueryResult)) != cudaSuccess) st = fail(EBI_E_OOM, "pinned allocation failed");
+    if (!st && !(c->h_res = g_pinned.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st) {
         cudaError_t e = cudaMemcpyAsync(c->d_file, file, len, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->d_file + len, 0, kFilePad, s);
@@ -439,7 +468,10 @@ int ebi_column_close(ebi_column* c) {
     void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
                     c->d_scratch_mask, c->d_buff, c->d_tot};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
-    if (c->h_res) cudaFreeHost(c->h_res);
+    if (c->h_res) {
+        cudaStreamSynchronize(s);  // no copy into the slot is pending when it is recycled
+        g_pinned.give(c->h_res);
+    }
     delete c;
     return EBI_OK;
 }
