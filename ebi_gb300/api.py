@@ -19,9 +19,9 @@ import numpy as np
 
 from . import _native
 
-UNCOMPRESSED, RLE, BUFF, GORILLA, CHIMP, CHIMP128 = range(6)
+UNCOMPRESSED, RLE, BUFF, GORILLA, CHIMP, CHIMP128, ELF_ON_CHIMP, ELF = range(8)
 SCHEMES = {"uncompressed": UNCOMPRESSED, "rle": RLE, "buff": BUFF, "gorilla": GORILLA,
-           "chimp": CHIMP, "chimp128": CHIMP128}
+           "chimp": CHIMP, "chimp128": CHIMP128, "elf_on_chimp": ELF_ON_CHIMP, "elf": ELF}
 CHUNK_KINDS = {"full": 0, "record_count": 1, "byte_size": 2}
 
 

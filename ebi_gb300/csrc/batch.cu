@@ -3,7 +3,7 @@
 //
 // A batch is a list of work items, each naming a query and a unit of one of
 // its columns: an 8,192-row BUFF tile, a whole Uncompressed / RLE / Chimp /
-// Chimp128 chunk, or a group of Gorilla chunks (one per warp).  A persistent
+// Chimp128 / Elf / ElfOnChimp chunk, or a group of Gorilla chunks (one per warp).  A persistent
 // grid of 256-thread CTAs pulls items from a device counter, so columns of
 // very different lengths and codecs share the GPU without a launch per
 // column; each item runs the same per-chunk device code as the single-column
@@ -48,6 +48,12 @@ __device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& i
 __device__ __noinline__ void item_chimp128(const QueryParams& q, const BatchItem& it) {
     xor_chunk<CODEC_CHIMP128>(q, it.unit, it.unit, VAL_SCAN, nullptr);
 }
+__device__ __noinline__ void item_elf_chimp(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_ELF_CHIMP>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+}
+__device__ __noinline__ void item_elf(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_ELF>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+}
 
 __global__ void __launch_bounds__(kBatchThreads, 2)
 batch_kernel(const QueryParams* __restrict__ qp, const BatchItem* __restrict__ items, uint32_t n_items,
@@ -70,6 +76,8 @@ batch_kernel(const QueryParams* __restrict__ qp, const BatchItem* __restrict__ i
         case ITEM_GORILLA: item_gorilla(q, it); break;
         case ITEM_CHIMP: item_chimp(q, it); break;
         case ITEM_CHIMP128: item_chimp128(q, it); break;
+        case ITEM_ELF_CHIMP: item_elf_chimp(q, it); break;
+        case ITEM_ELF: item_elf(q, it); break;
         default: break;
         }
     }
@@ -82,7 +90,45 @@ __global__ void __launch_bounds__(kFinThreads) batch_finalize_kernel(const Query
 
 }  // namespace
 
-size_t batch_smem_bytes() { return xor_smem_bytes(CODEC_CHIMP128); }
+size_t batch_smem_bytes() {
+    static_assert(xor_smem_bytes(CODEC_CHIMP128) >= xor_smem_bytes(CODEC_ELF), "largest codec body");
+    return xor_smem_bytes(CODEC_CHIMP128);
+}
+
+void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t query, std::vector<BatchItem>& out) {
+    switch (scheme) {
+    case EBI_BUFF:
+        for (uint32_t t = 0; t < n_tiles; ++t) out.push_back({query, ITEM_BUFF_TILE, t, 1});
+        return;
+    case EBI_GORILLA:
+        for (uint64_t k = 0; k < n_chunks; k += 8)
+            out.push_back({query, ITEM_GORILLA, static_cast<uint32_t>(k),
+                           static_cast<uint32_t>(n_chunks - k < 8 ? n_chunks - k : 8)});
+        return;
+    default: {
+        const uint32_t kind = scheme == EBI_UNCOMPRESSED ? ITEM_RAW
+                            : scheme == EBI_RLE          ? ITEM_RLE
+                            : scheme == EBI_CHIMP        ? ITEM_CHIMP
+                            : scheme == EBI_CHIMP128     ? ITEM_CHIMP128
+                            : scheme == EBI_ELF_ON_CHIMP ? ITEM_ELF_CHIMP
+                                                         : ITEM_ELF;
+        for (uint64_t k = 0; k < n_chunks; ++k) out.push_back({query, kind, static_cast<uint32_t>(k), 1});
+    }
+    }
+}
+
+double item_cost(uint32_t kind, uint32_t count) {
+    switch (kind) {
+    case ITEM_GORILLA: return 40.0 * count;
+    case ITEM_ELF: return 35.0;
+    case ITEM_ELF_CHIMP: return 35.0;
+    case ITEM_CHIMP128: return 30.0;
+    case ITEM_CHIMP: return 25.0;
+    case ITEM_BUFF_TILE: return 1.0;
+    case ITEM_RLE: return 0.5;
+    default: return 2.0;
+    }
+}
 
 cudaError_t prepare_batch_kernel() {
     return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -27,19 +27,6 @@ int bfail(int code, const std::string& msg) {
         if (_e != cudaSuccess) return bfail(EBI_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
     } while (0)
 
-// Relative cost of one item of each kind (device time of an 8,192-row unit
-// measured on the single-column kernels), for the cost-descending order.
-double item_cost(uint32_t kind, uint32_t count) {
-    switch (kind) {
-    case ITEM_GORILLA: return 40.0 * count;
-    case ITEM_CHIMP128: return 30.0;
-    case ITEM_CHIMP: return 25.0;
-    case ITEM_BUFF_TILE: return 1.0;
-    case ITEM_RLE: return 0.5;
-    default: return 2.0;
-    }
-}
-
 struct Shape {
     uint32_t ctas_per_sm;
     uint32_t order;  // 0: cost-descending, 1: query order
@@ -188,24 +175,8 @@ int ebi_batch_create(const ebi_batch_query* queries, uint64_t n, void* stream, e
         qp[i] = q;
         // work items of this query's column
         const ebi_column* c = bq.col;
-        const uint32_t qi = static_cast<uint32_t>(i);
-        switch (c->scheme) {
-        case EBI_BUFF:
-            for (uint32_t t = 0; t < c->tiles.tiles.size(); ++t) b->items_query.push_back({qi, ITEM_BUFF_TILE, t, 1});
-            break;
-        case EBI_GORILLA:
-            for (uint64_t k = 0; k < c->n_chunks; k += 8)
-                b->items_query.push_back({qi, ITEM_GORILLA, static_cast<uint32_t>(k),
-                                          static_cast<uint32_t>(std::min<uint64_t>(8, c->n_chunks - k))});
-            break;
-        default: {
-            const uint32_t kind = c->scheme == EBI_UNCOMPRESSED ? ITEM_RAW
-                                : c->scheme == EBI_RLE         ? ITEM_RLE
-                                : c->scheme == EBI_CHIMP       ? ITEM_CHIMP
-                                                               : ITEM_CHIMP128;
-            for (uint64_t k = 0; k < c->n_chunks; ++k) b->items_query.push_back({qi, kind, static_cast<uint32_t>(k), 1});
-        }
-        }
+        column_items(c->scheme, c->n_chunks, static_cast<uint32_t>(c->tiles.tiles.size()), static_cast<uint32_t>(i),
+                     b->items_query);
     }
     b->items_cost = b->items_query;
     std::stable_sort(b->items_cost.begin(), b->items_cost.end(), [](const BatchItem& x, const BatchItem& y) {

@@ -115,7 +115,7 @@ int parse_file(const uint8_t* d, uint64_t len, ebi_column* c) {
     if (cf + 1 + csz > len) return fail(EBI_E_IO, "compressor config past the end of the file");
     if (csz < 8) return fail(EBI_E_CORRUPT, "compressor config shorter than 8 bytes");
     if (cf + 1 + csz + 164 > len) return fail(EBI_E_IO, "FileFooter3 past the end of the file");
-    if (scheme > EBI_CHIMP128) return fail(EBI_E_UNSUPPORTED, "compression scheme outside this engine");
+    if (scheme > EBI_ELF) return fail(EBI_E_UNSUPPORTED, "compression scheme outside this engine");
     if (nrec > 0xffffffffull) return fail(EBI_E_UNSUPPORTED, "more than 2^32 - 1 records (row ids are u32)");
     c->scheme = scheme;
     c->n_records = nrec;
@@ -191,11 +191,12 @@ QueryParams base_params(const ebi_column* c) {
     q.agg = AGG_ALL;
     q.binfo = c->d_buff;
     q.stage_bytes = c->stage_bytes;
+    q.dec_tab = c->dec_tab;
     return q;
 }
 
 int check_supported(const ebi_column* c) {
-    if (c->scheme < EBI_UNCOMPRESSED || c->scheme > EBI_CHIMP128) return fail(EBI_E_UNSUPPORTED, "compression scheme outside this engine");
+    if (c->scheme < EBI_UNCOMPRESSED || c->scheme > EBI_ELF) return fail(EBI_E_UNSUPPORTED, "compression scheme outside this engine");
     return EBI_OK;
 }
 
@@ -421,6 +422,13 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         c->scan_grid = static_cast<uint32_t>(std::max(sms, 1)) * per_sm;
     } else {
         if (c->scheme == EBI_GORILLA) c->stage_bytes = gorilla_stage_bytes(c->chunks.data(), c->n_chunks);
+        if (c->scheme == EBI_ELF || c->scheme == EBI_ELF_ON_CHIMP) {
+            const cudaError_t e = elf_tables(&c->dec_tab);
+            if (e != cudaSuccess) {
+                delete c;
+                return fail(EBI_E_CUDA, std::string("Elf decimal tables: ") + cudaGetErrorString(e));
+            }
+        }
         c->tiles.tiles.resize(c->n_chunks);
         c->tiles.first_tile.resize(c->n_chunks + 1);
         for (uint64_t i = 0; i < c->n_chunks; ++i) {

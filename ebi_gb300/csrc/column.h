@@ -36,6 +36,7 @@ struct ebi_column {
     bool buff_fast_ok = false;
     bool fused_pending = false;  // the last query's kernel already folded into d_res
     uint32_t stage_bytes = 0;    // Gorilla: shared-memory staging per chunk
+    const double* dec_tab = nullptr;  // Elf / ElfOnChimp: the device's decimal tables
     // segment timing (ebi_column_set_timing)
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // query start, scan end, finalize end

@@ -125,6 +125,7 @@ struct QueryParams {
     const BuffChunkInfo* binfo;  // BUFF: header facts per chunk
     int pred_on;               // value codecs: the predicate selects rows (filter, filter+agg, filter_materialize)
     uint32_t stage_bytes;      // Gorilla: shared-memory staging size per chunk (0: read through L1)
+    const double* dec_tab;     // Elf / ElfOnChimp: decimal tables of elf_dev.cuh (device memory)
 };
 
 // Passes of the value-codec kernels (one CTA per chunk).

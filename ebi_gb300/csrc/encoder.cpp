@@ -3,7 +3,9 @@
 // encoders of the codecs this engine decodes:
 //   Uncompressed (compressor/uncompressed.rs), RLE (compressor/run_length.rs:49-117),
 //   Gorilla (compressor/gorilla.rs:248-380), Chimp (compressor/chimp.rs:51-146),
-//   Chimp128 (compressor/chimp_n.rs:126-258), BUFF (compressor/buff.rs:127-307).
+//   Chimp128 (compressor/chimp_n.rs:126-258), BUFF (compressor/buff.rs:127-307),
+//   Elf and ElfOnChimp (compressor/elf.rs: ElfEncoderWrapper over ElfXorEncoder
+//   or ChimpEncoder).
 // Output bytes equal the reference's except the two wall-clock timing fields
 // of FileFooter3, written here as zero.
 #include <algorithm>
@@ -15,6 +17,7 @@
 #include <vector>
 
 #include "../../include/ebi_gpu.h"
+#include "elf_host.h"
 
 namespace {
 
@@ -172,6 +175,125 @@ void chimp128(BitWriter& w, const double* v, uint64_t n) {
     w.bit(false);
 }
 
+// ChimpEncoder value by value (compressor/chimp.rs:51-146), the inner
+// stream of ElfOnChimp.
+struct ChimpStream {
+    uint64_t prev = 0;
+    uint32_t stored = 0xffffffffu;
+    bool first = true;
+    void add(BitWriter& w, uint64_t x) {
+        if (first) { first = false; prev = x; w.bits(x, 64); return; }
+        const uint64_t d = prev ^ x;
+        if (!d) {
+            w.bits(0, 2);
+            stored = 65;
+        } else {
+            const uint32_t lead = lead_round(lz64(d)), trail = uint32_t(tz64(d));
+            if (trail > 6) {
+                const uint32_t sig = 64 - lead - trail;
+                w.bits(1, 2);
+                w.bits(kRepr[lead], 3);
+                w.bits(sig, 6);
+                w.bits(d >> trail, sig);
+                stored = 65;
+            } else if (lead == stored) {
+                w.bits(2, 2);
+                w.bits(d, 64 - lead);
+            } else {
+                stored = lead;
+                w.bits(3, 2);
+                w.bits(kRepr[lead], 3);
+                w.bits(d, 64 - lead);
+            }
+        }
+        prev = x;
+    }
+};
+
+// ElfXorEncoder (compressor/elf.rs:164-262).
+struct ElfXorStream {
+    uint64_t prev = 0;
+    uint32_t lead = 0xffffffffu, trail = 0xffffffffu;
+    bool first = true;
+    void add(BitWriter& w, uint64_t x) {
+        if (first) {  // write_first: trailing zeros, then the bits above the lowest set one
+            first = false;
+            prev = x;
+            const uint32_t tz = uint32_t(tz64(x));
+            w.bits(tz, 7);
+            if (tz < 63) w.bits(x >> (tz + 1), 63 - tz);
+            return;
+        }
+        const uint64_t d = prev ^ x;
+        if (!d) { w.bits(1, 2); return; }  // '01': the same value
+        const uint32_t l = lead_round(lz64(d)), t = uint32_t(tz64(d));
+        if (l == lead && t >= trail) {  // '00': the stored window
+            w.bits(0, 2);
+            w.bits(d >> trail, 64 - lead - trail);
+        } else {
+            lead = l;
+            trail = t;
+            const uint32_t center = 64 - l - t;
+            if (center <= 16) {  // '10' + 3-bit leading code + 4-bit center
+                w.bits((((2u << 3) | kRepr[l]) << 4) | (center & 15u), 9);
+                if (center > 1) w.bits(d >> (t + 1), center - 1);
+            } else {             // '11' + 3-bit leading code + 6-bit center
+                w.bits((((3u << 3) | kRepr[l]) << 6) | (center & 63u), 11);
+                w.bits(d >> (t + 1), center - 1);
+            }
+        }
+        prev = x;
+    }
+};
+
+// ElfEncoderWrapper::add_value (compressor/elf.rs:92-158): values whose
+// decimal digits allow it lose their low mantissa bits (v'), which the
+// reader restores from beta*, the number of significant decimal digits.
+template <typename Inner>
+void elf(BitWriter& w, const double* v, uint64_t n) {
+    Inner inner;
+    int32_t last = INT32_MAX;
+    for (uint64_t i = 0; i < n; ++i) {
+        const double x = v[i];
+        const uint64_t b = bits_of(x);
+        uint64_t vp = b;
+        bool erased = false;
+        if (x == 0.0 || std::isinf(x)) {
+        } else if (x != x) {
+            vp = kNan;
+        } else {
+            bool pow10 = false;
+            const double a = std::fabs(x);
+            const int32_t sp = ebi::elf::sp_of(a, &pow10);
+            const int32_t beta = ebi::elf::significant(a, sp, last);
+            const uint32_t alpha = uint32_t(int64_t(beta) - sp - 1);
+            const int32_t beta_star = pow10 ? 0 : beta;
+            if (beta_star < 16) {
+                const uint32_t g = ebi::elf::f_alpha(alpha) + uint32_t((b >> 52) & 0x7ff) - 1023u;
+                const int32_t erase = 52 - int32_t(g);
+                if (erase > 4) {
+                    const uint64_t mask = ~0ull << (erase & 63);
+                    if (b & ~mask) {
+                        erased = true;
+                        vp = b & mask;
+                        if (beta_star == last) {
+                            w.bit(false);  // '0': the stored beta*
+                        } else {
+                            w.bits(uint32_t(beta_star) | 0x30u, 6);  // '11' + beta*
+                            last = beta_star;
+                        }
+                    }
+                }
+            }
+        }
+        if (!erased) w.bits(2, 2);  // '10': the value as is
+        inner.add(w, vp);
+    }
+    w.bits(2, 2);  // close: '10', the NaN end marker, one 0 bit
+    inner.add(w, kNan);
+    w.bit(false);
+}
+
 int64_t buff_fixed(double value, int32_t frac) {
     const uint64_t vb = bits_of(value);
     const int32_t exp = int32_t((vb >> 52) & 0x7ff) - 1023;
@@ -248,11 +370,13 @@ int chunk(Bytes& o, const double* v, uint64_t n, int scheme, uint64_t scale) {
         case EBI_UNCOMPRESSED: for (uint64_t i = 0; i < n; ++i) put64(o, bits_of(v[i])); return EBI_OK;
         case EBI_RLE: rle(o, v, n); return EBI_OK;
         case EBI_BUFF: return buff(o, v, n, scale);
-        case EBI_GORILLA: case EBI_CHIMP: case EBI_CHIMP128: {
+        case EBI_GORILLA: case EBI_CHIMP: case EBI_CHIMP128: case EBI_ELF_ON_CHIMP: case EBI_ELF: {
             BitWriter w;
             if (scheme == EBI_GORILLA) gorilla(w, v, n);
             else if (scheme == EBI_CHIMP) chimp(w, v, n);
-            else chimp128(w, v, n);
+            else if (scheme == EBI_CHIMP128) chimp128(w, v, n);
+            else if (scheme == EBI_ELF_ON_CHIMP) elf<ChimpStream>(w, v, n);
+            else elf<ElfXorStream>(w, v, n);
             o.insert(o.end(), w.out().begin(), w.out().end());
             return EBI_OK;
         }
@@ -264,7 +388,7 @@ int chunk(Bytes& o, const double* v, uint64_t n, int scheme, uint64_t scale) {
 
 extern "C" int ebi_encode(const double* v, uint64_t n, int scheme, int kind, uint64_t value, uint64_t scale,
                           uint8_t** out, uint64_t* out_len) {
-    if (!out || !out_len || (!v && n) || scheme < 0 || scheme > EBI_CHIMP128 || kind < 0 || kind > 2) return EBI_E_INVALID;
+    if (!out || !out_len || (!v && n) || scheme < 0 || scheme > EBI_ELF || kind < 0 || kind > 2) return EBI_E_INVALID;
     try {
         Bytes o;
         o.insert(o.end(), {'E', 'B', 'I', '1', 0, uint8_t(scheme), uint8_t(kind), 0});

@@ -58,9 +58,14 @@ constexpr uint32_t kGorillaStageCap = 100 * 1024;
 uint32_t gorilla_stage_bytes(const ChunkDesc* chunks, uint64_t n);
 cudaError_t launch_gorilla(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                            const unsigned long long* chunk_offsets, cudaStream_t s);
-// Gorilla, Chimp, Chimp128 (q.scheme selects the decoder).
+// Gorilla, Chimp, Chimp128, ElfOnChimp, Elf (q.scheme selects the decoder).
 cudaError_t launch_xor(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                        const unsigned long long* chunk_offsets, cudaStream_t s);
+
+// ---- Elf decimal tables (elf_tables.cu) ------------------------------------
+// Device address of the tables of elf_dev.cuh for the current device; built
+// and uploaded on first use per device (a synchronous copy).
+cudaError_t elf_tables(const double** out);
 
 // ---- fixed scratch of ebi_materialize_static (static_scratch.cu) ----------
 constexpr uint32_t kStaticTiles = 16384;  // tiles per call: 2 x 128 KB of counts and offsets
@@ -76,6 +81,8 @@ enum BatchItemKind : uint32_t {
     ITEM_GORILLA = 3,    // chunks [unit, unit + count), one warp each
     ITEM_CHIMP = 4,
     ITEM_CHIMP128 = 5,
+    ITEM_ELF_CHIMP = 6,  // unit = chunk
+    ITEM_ELF = 7,
 };
 struct BatchItem {
     uint32_t query;  // index into the batch's QueryParams
@@ -83,6 +90,11 @@ struct BatchItem {
     uint32_t unit;
     uint32_t count;
 };
+// Appends the items of one query over a column (scheme, chunks, BUFF tiles).
+void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t query, std::vector<BatchItem>& out);
+// Relative cost of one item of each kind (device time of an 8,192-row unit
+// measured on the single-column kernels), for the cost-descending order.
+double item_cost(uint32_t kind, uint32_t count);
 // Dynamic shared memory of the batch kernel; prepare_batch_kernel raises the
 // kernel's shared-memory limit to it (once per process, outside any capture).
 size_t batch_smem_bytes();

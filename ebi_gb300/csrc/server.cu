@@ -58,17 +58,6 @@ struct Slot {
     uint64_t launch_ns = 0;
 };
 
-double item_cost(uint32_t kind, uint32_t count) {
-    switch (kind) {
-    case ITEM_GORILLA: return 40.0 * count;
-    case ITEM_CHIMP128: return 30.0;
-    case ITEM_CHIMP: return 25.0;
-    case ITEM_BUFF_TILE: return 1.0;
-    case ITEM_RLE: return 0.5;
-    default: return 2.0;
-    }
-}
-
 }  // namespace
 
 struct ebi_server {
@@ -123,19 +112,7 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
             q.acc = sl.d_acc + acc_used;
             acc_used += c->n_chunks;
             sl.h_qp[nq] = q;
-            if (c->scheme == EBI_BUFF) {
-                for (uint32_t t = 0; t < c->tiles.tiles.size(); ++t) items.push_back({nq, ITEM_BUFF_TILE, t, 1});
-            } else if (c->scheme == EBI_GORILLA) {
-                for (uint64_t j = 0; j < c->n_chunks; j += 8)
-                    items.push_back({nq, ITEM_GORILLA, static_cast<uint32_t>(j),
-                                     static_cast<uint32_t>(std::min<uint64_t>(8, c->n_chunks - j))});
-            } else {
-                const uint32_t kind = c->scheme == EBI_UNCOMPRESSED ? ITEM_RAW
-                                    : c->scheme == EBI_RLE         ? ITEM_RLE
-                                    : c->scheme == EBI_CHIMP       ? ITEM_CHIMP
-                                                                   : ITEM_CHIMP128;
-                for (uint64_t j = 0; j < c->n_chunks; ++j) items.push_back({nq, kind, static_cast<uint32_t>(j), 1});
-            }
+            column_items(c->scheme, c->n_chunks, static_cast<uint32_t>(c->tiles.tiles.size()), nq, items);
             ++nq;
         }
     }

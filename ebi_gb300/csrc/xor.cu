@@ -1,4 +1,4 @@
-// xor.cu -- kernel and launchers of the Chimp / Chimp128 chunk pass (xor_dev.cuh).
+// xor.cu -- kernel and launchers of the Chimp / Chimp128 / Elf / ElfOnChimp chunk pass (xor_dev.cuh).
 #include "internal.h"
 #include "xor_dev.cuh"
 
@@ -36,6 +36,8 @@ cudaError_t launch_xor(const QueryParams& q, uint32_t chunk_begin, uint32_t n_ch
     case EBI_GORILLA: return launch_gorilla(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
     case EBI_CHIMP: return launch_codec<CODEC_CHIMP>(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
     case EBI_CHIMP128: return launch_codec<CODEC_CHIMP128>(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
+    case EBI_ELF_ON_CHIMP: return launch_codec<CODEC_ELF_CHIMP>(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
+    case EBI_ELF: return launch_codec<CODEC_ELF>(q, chunk_begin, n_chunks, mode, chunk_offsets, s);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -1,5 +1,6 @@
-// xor_dev.cuh -- Gorilla, Chimp and Chimp128 chunks: XOR bitstreams decoded on the
-// device and queried in the same kernel (one CTA per chunk).
+// xor_dev.cuh -- Gorilla, Chimp, Chimp128, Elf and ElfOnChimp chunks: XOR
+// bitstreams decoded on the device and queried in the same kernel (one CTA
+// per chunk).
 //
 // Formats (big-endian bit order, MSB of the first byte first):
 //   Gorilla   decoder/chunk_reader/gorilla.rs:215-296: 64 raw bits, then per
@@ -9,6 +10,11 @@
 //             a 3-bit leading code (LEADING_REPR) and 6 significant bits.
 //   Chimp128  decoder/chunk_reader/chimp_n.rs:544-646: as Chimp, but '00' and
 //             '01' name one of the last 128 values by a 7-bit ring index.
+//   Elf       decoder/chunk_reader/elf.rs: per value a wrapper prefix ('0'
+//             restore, '10' as is, '11' + 4-bit beta* and restore) and an
+//             ElfXor record; ElfOnChimp: the same prefix over Chimp records.
+//             The XOR chain runs over the erased values v'; a restored value
+//             is v' rounded up at the digits beta* names (elf_dev.cuh).
 // A stream ends at the first value equal to f64::NAN's bits (Chimp128: not
 // for a '00' copy); a read past the chunk raises UnexpectedEndOfChunk first.
 //
@@ -25,9 +31,11 @@
 //   2. extraction.  Record offsets come from a block scan of the segment
 //      record counts; each thread re-parses its segment and writes every
 //      record's XOR delta (and, for Chimp128, the record its value refers to).
-//   3. values.  Gorilla and Chimp values are the prefix XOR of the deltas
+//   3. values.  Gorilla, Chimp and Elf values are the prefix XOR of the deltas
 //      (warp-shuffle scans); Chimp128 values resolve by pointer jumping over
 //      the references (ceil(log2 n) rounds).  The first NaN ends the chunk.
+//      Elf: each record takes the beta* of the last '11' prefix at or before
+//      it (a block max-scan over record indices) and restores its value.
 // The query then runs row-parallel over the values in shared memory.
 //
 // A chunk with more records than kRcap (only for chunks far above 8,192
@@ -62,6 +70,7 @@ struct Smem {
     uint64_t* vals;   // kRcap: deltas, then values
     uint16_t* refs;   // kRcap (Chimp128)
     uint32_t* nanok;  // kRcap / 32 (Chimp128)
+    uint8_t* meta;    // kRcap (Elf): wrapper prefix flags and beta*
 };
 
 // Row sink of the query: one call per decoded row, in row order within the
@@ -104,6 +113,23 @@ struct SerialSink {
 template <int CODEC>
 __device__ uint32_t decode_serial(const uint32_t* fw, uint64_t bit0, uint64_t B, uint64_t* ring, SerialSink& sink) {
     auto peek = [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); };
+    if (is_elf(CODEC)) {
+        PState s{0, CODEC == CODEC_ELF ? kNoWin : kNoLead};
+        uint64_t v = 0;
+        int32_t beta = INT32_MAX;
+        for (uint64_t i = 0;; ++i) {
+            Rec r;
+            const uint32_t e = parse_rec<CODEC>(peek, B, s, r);
+            if (e) return e;
+            v ^= r.delta;
+            if (v == kNanBits) return 0;
+            if (r.meta & kElfBeta) beta = r.meta & 15;
+            const uint64_t out = (r.meta & kElfRestore)
+                ? static_cast<uint64_t>(__double_as_longlong(elf_recover(__longlong_as_double(static_cast<long long>(v)), beta, sink.q->dec_tab)))
+                : v;
+            sink.row(i, out);
+        }
+    }
     if (B < 64) return EBI_E_UNEXPECTED_END;
     uint64_t v = peek(0);
     PState s{64, CODEC == CODEC_GORILLA ? 0u : kNoLead};
@@ -130,6 +156,41 @@ __device__ uint32_t decode_serial(const uint32_t* fw, uint64_t bit0, uint64_t B,
     }
 }
 
+// Elf: vals[0, end) hold the erased values v'; each record flagged
+// kElfRestore is replaced by its decimal, with the beta* of the last record
+// at or before it that carries kElfBeta (i32::MAX when none does).  Thread t
+// takes a contiguous range of records; the block max-scan of "last beta
+// record + 1" over the ranges gives each thread the beta* it starts with.
+__device__ __noinline__ void elf_restore(Smem sm, uint32_t end, const double* __restrict__ tab, uint32_t* s_red) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t per = (end + kXorThreads - 1) / kXorThreads;
+    const uint32_t b = min(end, tid * per), e = min(end, b + per);
+    uint32_t last = 0;  // index + 1 of the range's last beta record
+    for (uint32_t i = b; i < e; ++i)
+        if (sm.meta[i] & kElfBeta) last = i + 1;
+    uint32_t inc = last;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc = max(inc, y);
+    }
+    __syncthreads();  // s_red's previous readers are done
+    if (lane == 31) s_red[wid] = inc;
+    __syncthreads();
+    uint32_t before = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) before = 0;
+    for (int w = 0; w < wid; ++w) before = max(before, s_red[w]);
+    int32_t beta = before ? (sm.meta[before - 1] & 15) : INT32_MAX;
+    for (uint32_t i = b; i < e; ++i) {
+        const uint8_t m = sm.meta[i];
+        if (m & kElfBeta) beta = m & 15;
+        if (m & kElfRestore)
+            sm.vals[i] = static_cast<uint64_t>(__double_as_longlong(
+                elf_recover(__longlong_as_double(static_cast<long long>(sm.vals[i])), beta, tab)));
+    }
+    __syncthreads();
+}
+
 // One Chimp / Chimp128 chunk c by a CTA of kXorThreads threads with
 // xor_smem_bytes(CODEC) bytes of dynamic shared memory; li indexes the pass's
 // per-chunk counts / offsets.
@@ -141,6 +202,7 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
     sm.vals = reinterpret_cast<uint64_t*>(smem_raw);
     sm.refs = reinterpret_cast<uint16_t*>(sm.vals + kRcap);
     sm.nanok = reinterpret_cast<uint32_t*>(sm.refs + kRcap);
+    sm.meta = reinterpret_cast<uint8_t*>(sm.vals + kRcap);  // Elf (no refs there)
     __shared__ uint64_t s_in[kXorThreads], s_out[kXorThreads];
     __shared__ uint32_t s_red[kXorThreads / 32];
     __shared__ uint64_t s_x[kXorThreads / 32];
@@ -182,7 +244,9 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
     const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
     const uint64_t bit0 = cd.byte_off * 8;
     // well-formed chunks hold n_rows + 1 records (the end marker included)
-    const bool parallel = B >= 64 && cd.n_rows + 1 < kRcap;
+    constexpr bool kElf = is_elf(CODEC);
+    constexpr uint64_t kFirst = kElf ? 0 : 64;  // bits before the first parsed record
+    const bool parallel = (kElf || B >= 64) && cd.n_rows + 1 < kRcap;
 
     uint32_t end = 0;         // decoded values (the NaN end marker's index)
     bool serial = !parallel;
@@ -207,12 +271,14 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
         auto peek_staged = [stage, sbit0](uint64_t p) { return peek64_be(stage, sbit0 + p); };
 
         // ---- 1. control parse: segments converge to the sequential parse ---
-        const uint64_t span = B - 64;
+        const uint64_t span = B - kFirst;
         const uint64_t seg = (span + kXorThreads - 1) / kXorThreads;
-        const uint64_t sbeg = 64 + seg * tid;
-        const uint64_t send = tid == kXorThreads - 1 ? B : (64 + seg * (tid + 1) < B ? 64 + seg * (tid + 1) : B);
+        const uint64_t sbeg = kFirst + seg * tid;
+        const uint64_t send =
+            tid == kXorThreads - 1 ? B : (kFirst + seg * (tid + 1) < B ? kFirst + seg * (tid + 1) : B);
         const bool last = tid == kXorThreads - 1;
-        PState in{tid == 0 ? 64 : (sbeg < B ? sbeg : B), CODEC == CODEC_GORILLA ? 0u : (tid == 0 ? kNoLead : 0u)};
+        const uint32_t win0 = CODEC == CODEC_GORILLA ? 0u : CODEC == CODEC_ELF ? kNoWin : kNoLead;
+        PState in{tid == 0 ? kFirst : (sbeg < B ? sbeg : B), tid == 0 ? win0 : 0u};
         uint32_t n, fail;
         auto parse = [&](PState from, uint32_t* n_out, uint32_t* fail_out) {
             return staged ? parse_segment<CODEC>(peek_staged, B, from, send, last, n_out, fail_out)
@@ -239,14 +305,15 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
         // Segments past the first failure hold no records of the stream.
         if (static_cast<uint32_t>(tid) > first_fail) n = 0;
         uint32_t total;
-        const uint32_t off = 1 + block_excl_scan_u32<kXorThreads>(n, s_red, &total);
-        const uint32_t R = 1 + total;  // records before the failure, the first value included
+        constexpr uint32_t kHead = kElf ? 0 : 1;  // the first value, outside the segments
+        const uint32_t off = kHead + block_excl_scan_u32<kXorThreads>(n, s_red, &total);
+        const uint32_t R = kHead + total;  // records before the failure, the first value included
         if (tid == static_cast<int>(first_fail)) s_status = fail;
         // ---- 2. extraction -------------------------------------------------
         if (CODEC == CODEC_CHIMP128)
             for (uint32_t i = tid; i < kRcap / 32; i += kXorThreads) sm.nanok[i] = 0;
         __syncthreads();
-        if (tid == 0) {
+        if (tid == 0 && !kElf) {
             sm.vals[0] = peek(0);
             if (CODEC == CODEC_CHIMP128) { sm.refs[0] = kNoRef; atomicOr(&sm.nanok[0], 1u); }
         }
@@ -257,6 +324,7 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
             for (uint32_t k = 0; k < n && idx < kRcap; ++k, ++idx) {
                 parse_rec<CODEC>(peek, B, s, r);  // succeeds: these records precede the failure
                 sm.vals[idx] = r.delta;
+                if (kElf) sm.meta[idx] = r.meta;
                 if (CODEC == CODEC_CHIMP128) {
                     sm.refs[idx] = static_cast<uint16_t>(r.ring == kRefPrev ? idx - 1 : ring_ref(idx, r.ring));
                     if (r.nan_ok) atomicOr(&sm.nanok[idx >> 5], 1u << (idx & 31));
@@ -339,6 +407,7 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
         nan_at = block_min_u32(nan_at, s_red);
         if (nan_at < Rs) {
             end = nan_at;
+            if (kElf) elf_restore(sm, end, q.dec_tab, s_red);
         } else if (R > kRcap) {
             serial = true;  // the end marker lies past the records held in shared memory
         } else {
@@ -399,7 +468,7 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
 }
 
 constexpr size_t xor_smem_bytes(int codec) {
-    return kRcap * 8 + (codec == CODEC_CHIMP128 ? kRcap * 2 + kRcap / 8 : 0);
+    return kRcap * 8 + (codec == CODEC_CHIMP128 ? kRcap * 2 + kRcap / 8 : is_elf(codec) ? kRcap : 0);
 }
 
 }  // namespace

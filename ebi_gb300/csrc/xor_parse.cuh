@@ -1,4 +1,4 @@
-// xor_parse.cuh -- record parser of the Gorilla, Chimp and Chimp128 bitstreams,
+// xor_parse.cuh -- record parser of the Gorilla, Chimp, Chimp128, Elf and ElfOnChimp bitstreams,
 // shared by the decode kernel (xor.cu) and host-side checks of its segment
 // algorithm.  Host and device functions alike: the bit source is a functor
 // that returns the 64 stream bits starting at a bit position.
@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "../../include/ebi_gpu.h"
+#include "elf_dev.cuh"
 
 #if defined(__CUDACC__)
 #define XOR_HD __host__ __device__ __forceinline__
@@ -20,7 +21,17 @@ namespace xorp {
 constexpr uint32_t kNoRef = 0xffffu;     // Chimp128: value refers to an unset ring slot (0.0 bits)
 constexpr uint32_t kNoLead = 0xffu;      // Chimp: no leading-zero count stored yet
 
-enum : uint32_t { CODEC_GORILLA = EBI_GORILLA, CODEC_CHIMP = EBI_CHIMP, CODEC_CHIMP128 = EBI_CHIMP128 };
+enum : uint32_t {
+    CODEC_GORILLA = EBI_GORILLA,
+    CODEC_CHIMP = EBI_CHIMP,
+    CODEC_CHIMP128 = EBI_CHIMP128,
+    CODEC_ELF_CHIMP = EBI_ELF_ON_CHIMP,
+    CODEC_ELF = EBI_ELF,
+};
+// Elf codecs: every record (the first included) is a wrapper prefix and a
+// record of the inner XOR stream; the first record starts at bit 0.
+XOR_HD constexpr bool is_elf(int codec) { return codec == CODEC_ELF || codec == CODEC_ELF_CHIMP; }
+constexpr uint32_t kNoWin = 0xffffu;  // ElfXor: leading and trailing counts not stored yet
 
 // LEADING_REPR decode table [0, 8, 12, 16, 18, 20, 22, 24] (decoder/chunk_reader/chimp.rs), 5 bits per entry.
 XOR_HD uint32_t lead_decode(uint32_t t) {
@@ -30,7 +41,8 @@ XOR_HD uint32_t lead_decode(uint32_t t) {
 }
 
 // Parser state: bit position in the chunk and the inherited window
-// (Gorilla: lead | trail << 8; Chimp/Chimp128: stored leading zeros or kNoLead).
+// (Gorilla: lead | trail << 8; Chimp/Chimp128/ElfOnChimp: stored leading zeros
+// or kNoLead; Elf: lead | trail << 8, kNoWin before any).
 struct PState {
     uint64_t pos;
     uint32_t win;
@@ -45,7 +57,23 @@ struct Rec {
     uint64_t delta;
     uint32_t ring;  // ring slot (Chimp128 '00'/'01') or kRefPrev
     bool nan_ok;    // the reader checks this value against the NaN end marker
+    uint8_t meta;   // Elf: kElfRestore | kElfBeta | beta* of the wrapper prefix
 };
+
+// payload of n <= 64 bits at q (0 for n == 0)
+template <typename Peek>
+XOR_HD uint64_t take_bits(Peek peek, uint64_t q, uint32_t n) {
+    return n ? peek(q) >> (64 - n) : 0;
+}
+
+// One Elf / ElfOnChimp record at s.pos (decoder/chunk_reader/elf.rs):
+// the wrapper prefix '0' (restore with the current beta*), '10' (as is) or
+// '11' + 4-bit beta* (restore), then the inner record -- at bit 0 the inner
+// stream's first value (ElfXor read_first :121-141: 7-bit trailing zeros
+// and the bits above the lowest set one; Chimp: 64 raw bits), else an
+// ElfXor record (decompress_float_inner :143-221) or a Chimp record.
+template <int CODEC, typename Peek>
+XOR_HD uint32_t parse_elf(Peek peek, uint64_t B, PState& s, Rec& r);
 
 // Parses one record at s.pos; returns 0 or the error the reader raises there
 // (EBI_E_UNEXPECTED_END for a read past the chunk, EBI_E_CORRUPT for a
@@ -55,7 +83,10 @@ XOR_HD uint32_t parse_rec(Peek peek, uint64_t B, PState& s, Rec& r) {
     const uint64_t p = s.pos;
     r.ring = kRefPrev;
     r.nan_ok = true;
-    if (CODEC == CODEC_GORILLA) {
+    r.meta = 0;
+    if (is_elf(CODEC)) {
+        return parse_elf<CODEC>(peek, B, s, r);
+    } else if (CODEC == CODEC_GORILLA) {
         if (p + 1 > B) return EBI_E_UNEXPECTED_END;
         const uint64_t x = peek(p);
         if (!(x >> 63)) { s.pos = p + 1; r.delta = 0; return 0; }
@@ -131,6 +162,94 @@ XOR_HD uint32_t parse_rec(Peek peek, uint64_t B, PState& s, Rec& r) {
     }
 }
 
+template <int CODEC, typename Peek>
+XOR_HD uint32_t parse_elf(Peek peek, uint64_t B, PState& s, Rec& r) {
+    const uint64_t p0 = s.pos;
+    if (p0 + 1 > B) return EBI_E_UNEXPECTED_END;
+    const uint64_t x = peek(p0);
+    uint64_t p;
+    if (!(x >> 63)) {
+        r.meta = kElfRestore;
+        p = p0 + 1;
+    } else {
+        if (p0 + 2 > B) return EBI_E_UNEXPECTED_END;
+        if (!((x >> 62) & 1)) {
+            r.meta = 0;
+            p = p0 + 2;
+        } else {
+            if (p0 + 6 > B) return EBI_E_UNEXPECTED_END;
+            r.meta = static_cast<uint8_t>(kElfRestore | kElfBeta | ((x >> 58) & 15u));
+            p = p0 + 6;
+        }
+    }
+    if (p0 == 0) {  // the first value of the inner stream
+        if (CODEC == CODEC_ELF_CHIMP) {
+            if (p + 64 > B) return EBI_E_UNEXPECTED_END;
+            r.delta = peek(p);
+            s.pos = p + 64;
+            s.win = kNoLead;
+            return 0;
+        }
+        if (p + 7 > B) return EBI_E_UNEXPECTED_END;
+        const uint32_t tz = static_cast<uint32_t>(peek(p) >> 57);
+        s.win = kNoWin;
+        if (tz >= 64) {
+            r.delta = 0;
+            s.pos = p + 7;
+            return 0;
+        }
+        const uint32_t n = 63 - tz;
+        if (p + 7 + n > B) return EBI_E_UNEXPECTED_END;
+        r.delta = ((take_bits(peek, p + 7, n) << 1) | 1u) << tz;
+        s.pos = p + 7 + n;
+        return 0;
+    }
+    if (CODEC == CODEC_ELF_CHIMP) {
+        const uint8_t meta = r.meta;
+        s.pos = p;
+        const uint32_t e = parse_rec<CODEC_CHIMP>(peek, B, s, r);
+        r.meta = meta;
+        return e;
+    }
+    if (p + 2 > B) return EBI_E_UNEXPECTED_END;
+    const uint64_t y = peek(p);
+    const uint32_t flag = static_cast<uint32_t>(y >> 62);
+    if (flag == 1) {  // '01': the previous value again
+        r.delta = 0;
+        s.pos = p + 2;
+        return 0;
+    }
+    if (flag == 0) {  // '00': payload in the stored window
+        const uint32_t lead = s.win & 0xffu, trail = s.win >> 8;
+        if (lead > 64 || trail > 64 || lead + trail > 64) return EBI_E_CORRUPT;
+        const uint32_t n = 64 - lead - trail;
+        if (p + 2 + n > B) return EBI_E_UNEXPECTED_END;
+        r.delta = n ? take_bits(peek, p + 2, n) << trail : 0;
+        s.pos = p + 2 + n;
+        return 0;
+    }
+    // '10': 3-bit leading code + 4-bit center; '11': 3-bit leading code + 6-bit center
+    const uint32_t hb = flag == 3 ? 9u : 7u, cb = flag == 3 ? 6u : 4u;
+    if (p + 2 + hb > B) return EBI_E_UNEXPECTED_END;
+    const uint32_t lc = static_cast<uint32_t>(y >> (62 - hb)) & ((1u << hb) - 1u);
+    const uint32_t lead = lead_decode(lc >> cb);
+    uint32_t center = lc & ((1u << cb) - 1u);
+    if (center == 0) center = 1u << cb;
+    if (lead + center > 64) return EBI_E_CORRUPT;
+    const uint32_t trail = 64 - lead - center;
+    const uint64_t q = p + 2 + hb;
+    if (flag == 2 && center == 1) {
+        r.delta = 1ull << trail;
+        s.pos = q;
+    } else {
+        if (q + center - 1 > B) return EBI_E_UNEXPECTED_END;
+        r.delta = ((take_bits(peek, q, center - 1) << 1) | 1u) << trail;
+        s.pos = q + center - 1;
+    }
+    s.win = lead | (trail << 8);
+    return 0;
+}
+
 // Length-only step of one Chimp / Chimp128 record (the convergence rounds of
 // the segment parse need positions and windows, not payloads): selects
 // instead of branches, one 64-bit read.  Same errors as parse_rec.
@@ -169,7 +288,7 @@ XOR_HD PState parse_segment(Peek peek, uint64_t B, PState s, uint64_t end, bool 
     uint32_t n = 0, f = 0;
     while (s.pos < end) {
         uint32_t e;
-        if (CODEC == CODEC_GORILLA) {
+        if (CODEC == CODEC_GORILLA || is_elf(CODEC)) {
             Rec r;
             e = parse_rec<CODEC>(peek, B, s, r);
         } else {

@@ -47,11 +47,12 @@ typedef enum {
     EBI_E_CORRUPT = 6,        /* a stream breaks an invariant the reference asserts in debug     */
     EBI_E_INVALID = 7,        /* bad argument (e.g. output buffer too small)                     */
     EBI_E_OOM = 8,            /* device or host allocation failed                                */
-    EBI_E_UNSUPPORTED = 9     /* codec outside this engine (Elf, Sprintz, zstd, gzip, ...)       */
+    EBI_E_UNSUPPORTED = 9     /* codec outside this engine (Sprintz, zstd, gzip, ...)            */
 } ebi_status;
 
 /* CompressionScheme (ebi/src/format.rs:185-199) */
-enum { EBI_UNCOMPRESSED = 0, EBI_RLE = 1, EBI_BUFF = 2, EBI_GORILLA = 3, EBI_CHIMP = 4, EBI_CHIMP128 = 5 };
+enum { EBI_UNCOMPRESSED = 0, EBI_RLE = 1, EBI_BUFF = 2, EBI_GORILLA = 3, EBI_CHIMP = 4, EBI_CHIMP128 = 5,
+       EBI_ELF_ON_CHIMP = 6, EBI_ELF = 7 };
 /* ChunkOptionKind (ebi/src/format.rs:174-180) */
 enum { EBI_CHUNK_FULL = 0, EBI_CHUNK_RECORD_COUNT = 1, EBI_CHUNK_BYTE_SIZE = 2 };
 /* Predicate / RangeValue kinds (ebi/src/decoder/query.rs:352-428) */

@@ -11,6 +11,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -267,6 +268,206 @@ static int chimp128_encode(bitw* w, const double* v, uint64_t n) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Elf decimal helpers (compression_common/elf.rs).  Rust's float -> int     */
+/* casts saturate (NaN -> 0); integer arithmetic wraps as in release builds.  */
+/* ------------------------------------------------------------------------ */
+static const uint32_t ELF_F[21] = {0, 4, 7, 10, 14, 17, 20, 24, 27, 30, 34, 37, 40, 44, 47, 50, 54, 57, 60, 64, 67};
+static int32_t sat_i32(double x) {
+    if (x != x) return 0;
+    if (x >= 2147483647.0) return INT32_MAX;
+    if (x <= -2147483648.0) return INT32_MIN;
+    return (int32_t)x;
+}
+static uint32_t sat_u32(double x) {
+    if (x != x || x <= 0.0) return 0;
+    if (x >= 4294967295.0) return UINT32_MAX;
+    return (uint32_t)x;
+}
+static int64_t sat_i64(double x) {
+    if (x != x) return 0;
+    if (x >= 9223372036854775807.0) return INT64_MAX;
+    if (x <= -9223372036854775808.0) return INT64_MIN;
+    return (int64_t)x;
+}
+/* get_10i_p / get_10i_n (:97-113): the table, else "1.0E{i}".parse::<f64>() */
+static const double ELF_10I_P[21] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9, 1e10,
+                                     1e11, 1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20};
+static const double ELF_10I_N[21] = {1e-0,  1e-1,  1e-2,  1e-3,  1e-4,  1e-5,  1e-6,  1e-7,  1e-8,  1e-9, 1e-10,
+                                     1e-11, 1e-12, 1e-13, 1e-14, 1e-15, 1e-16, 1e-17, 1e-18, 1e-19, 1e-20};
+static double elf_10i_p(uint32_t i) {
+    if (i < 21) return ELF_10I_P[i];
+    char b[32];
+    snprintf(b, sizeof b, "1.0E%u", i);
+    return strtod(b, NULL);
+}
+static double elf_10i_n(uint32_t i) {
+    if (i < 21) return ELF_10I_N[i];
+    char b[32];
+    snprintf(b, sizeof b, "1.0E-%u", i);
+    return strtod(b, NULL);
+}
+/* get_f_alpha (:33-39) */
+static uint32_t elf_f_alpha(uint32_t alpha) {
+    if (alpha < 21) return ELF_F[alpha];
+    return sat_u32(ceil((double)alpha * 3.321928094887362347870319429489390175864831393));
+}
+/* get_sp (:115-133) and get_sp_and_10i_n_flag (:135-155) */
+static int32_t elf_sp(double v, int* flag) {
+    static const double GT[10] = {1, 10, 100, 1000, 10000, 100000, 1000000, 10000000, 100000000, 1000000000};
+    static const double LT[11] = {1.0, 0.1, 0.01, 0.001, 0.0001, 0.00001, 0.000001, 0.0000001, 0.00000001,
+                                  0.000000001, 0.0000000001};
+    if (flag) *flag = 0;
+    if (v >= 1.0) {
+        for (int i = 0; i < 9; ++i) if (v < GT[i + 1]) return i;
+    } else {
+        for (int i = 1; i < 11; ++i)
+            if (v >= LT[i]) { if (flag) *flag = v == LT[i]; return -i; }
+    }
+    double l = log10(v);
+    if (flag) *flag = l == floor(l);
+    return sat_i32(floor(l));
+}
+/* round_up (:48-55) */
+static double elf_round_up(double v, uint32_t alpha) {
+    double scale = elf_10i_p(alpha);
+    return v < 0.0 ? floor(v * scale) / scale : ceil(v * scale) / scale;
+}
+/* get_significant_count (:57-95) */
+static int32_t elf_significant(double v, int32_t sp, int32_t last) {
+    int32_t i;
+    if (last != INT32_MAX && last != 0) { i = last - sp - 1; if (i < 1) i = 1; }
+    else if (last == INT32_MAX) i = 17 - sp - 1;
+    else if (sp >= 0) i = 1;
+    else i = -sp;
+    double temp = v * elf_10i_p((uint32_t)i);
+    int64_t ti = sat_i64(temp);
+    while ((double)ti != temp) {
+        i += 1;
+        temp = v * elf_10i_p((uint32_t)i);
+        if (isinf(temp)) return 17;
+        ti = sat_i64(temp);
+    }
+    if (temp / elf_10i_p((uint32_t)i) != v) return 17;
+    while (i > 0 && ti % 10 == 0) { i -= 1; ti /= 10; }
+    return sp + i + 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Elf / ElfOnChimp encoders (compressor/elf.rs)                             */
+/* ------------------------------------------------------------------------ */
+/* Chimp encoder as a stream of values (compressor/chimp.rs:51-146) */
+typedef struct { uint32_t stored_lead; uint64_t stored; int first; } chimp_enc;
+static void chimp_enc_add(bitw* w, chimp_enc* e, uint64_t val) {
+    if (e->first) { e->first = 0; e->stored = val; bw_bits(w, val, 64); return; }
+    uint64_t x = e->stored ^ val;
+    if (x == 0) {
+        bw_bit(w, 0); bw_bit(w, 0);
+        e->stored_lead = 65;
+    } else {
+        uint32_t lead = LEAD_ROUND[clz64(x)];
+        uint32_t trail = (uint32_t)ctz64(x);
+        if (trail > 6) {
+            uint32_t sig = 64 - lead - trail;
+            bw_bit(w, 0); bw_bit(w, 1);
+            bw_bits(w, LEAD_REPR[lead], 3);
+            bw_bits(w, sig, 6);
+            bw_bits(w, x >> trail, sig);
+            e->stored_lead = 65;
+        } else if (lead == e->stored_lead) {
+            bw_bit(w, 1); bw_bit(w, 0);
+            bw_bits(w, x, 64 - lead);
+        } else {
+            e->stored_lead = lead;
+            bw_bit(w, 1); bw_bit(w, 1);
+            bw_bits(w, LEAD_REPR[lead], 3);
+            bw_bits(w, x, 64 - lead);
+        }
+    }
+    e->stored = val;
+}
+/* ElfXorEncoder (compressor/elf.rs:164-262) */
+typedef struct { uint32_t lead, trail; uint64_t stored; int first; } elfx_enc;
+static void elfx_add(bitw* w, elfx_enc* e, uint64_t bits) {
+    if (e->first) {                                            /* write_first :192-206 */
+        e->first = 0;
+        e->stored = bits;
+        uint32_t tz = bits ? (uint32_t)ctz64(bits) : 64;
+        bw_bits(w, tz, 7);
+        if (tz < 63) bw_bits(w, bits >> (tz + 1), 63 - tz);    /* tz 63 writes no bits */
+        return;
+    }
+    uint64_t x = e->stored ^ bits;                             /* compress_float_inner :212-262 */
+    if (x == 0) { bw_bits(w, 1, 2); return; }                  /* case 01 */
+    uint32_t lead = LEAD_ROUND[clz64(x)];
+    uint32_t trail = (uint32_t)ctz64(x);
+    if (lead == e->lead && trail >= e->trail) {                /* case 00 */
+        uint32_t center = 64 - e->lead - e->trail;
+        bw_bits(w, 0, 2);
+        bw_bits(w, x >> e->trail, center);
+    } else {
+        e->lead = lead;
+        e->trail = trail;
+        uint32_t center = 64 - lead - trail;
+        uint32_t repr = LEAD_REPR[lead];
+        if (center <= 16) {                                     /* case 10 */
+            bw_bits(w, (((0x2u << 3) | repr) << 4) | (center & 0xf), 9);
+            if (center > 1) bw_bits(w, x >> (trail + 1), center - 1);
+        } else {                                                /* case 11 */
+            bw_bits(w, (((0x3u << 3) | repr) << 6) | (center & 0x3f), 11);
+            bw_bits(w, x >> (trail + 1), center - 1);
+        }
+    }
+    e->stored = bits;
+}
+/* ElfEncoderWrapper::add_value (:92-158) over ElfXorEncoder or ChimpEncoder */
+static void elf_encode(bitw* w, const double* v, uint64_t n, int on_chimp) {
+    elfx_enc ex = {0xffffffffu, 0xffffffffu, 0, 1};
+    chimp_enc ec = {0xffffffffu, 0, 1};
+    int32_t last = INT32_MAX;
+    for (uint64_t i = 0; i <= n; ++i) {
+        uint64_t vp;
+        if (i == n) {                                          /* close :61-66: case 10, then the XOR close */
+            bw_bits(w, 2, 2);
+            vp = NAN_BITS;
+        } else {
+            double x = v[i];
+            uint64_t vb = f2u(x);
+            if (x == 0.0 || isinf(x)) { bw_bits(w, 2, 2); vp = vb; }
+            else if (x != x) { bw_bits(w, 2, 2); vp = NAN_BITS; }
+            else {
+                int flag;
+                double ax = fabs(x);
+                int32_t sp = elf_sp(ax, &flag);                /* get_alpha_and_beta_star :41-47 */
+                int32_t beta = elf_significant(ax, sp, last);
+                uint32_t alpha = (uint32_t)((int64_t)beta - sp - 1);
+                int32_t beta_star = flag == 1 ? 0 : beta;
+                uint64_t mask = ~0ull;
+                uint64_t delta = 0;
+                int32_t erase = 0;
+                if (beta_star < 16) {
+                    uint64_t e = (vb >> 52) & 0x7ff;
+                    uint32_t g = elf_f_alpha(alpha) + (uint32_t)e - 1023u;
+                    erase = 52 - (int32_t)g;
+                    if (erase > 4) { mask = ~0ull << (erase & 63); delta = ~mask & vb; }
+                    else { mask = ~0ull; delta = 0; }
+                }
+                if (beta_star < 16 && erase > 4 && delta != 0) {
+                    if (beta_star == last) bw_bit(w, 0);           /* case 0 */
+                    else {                                         /* case 11 */
+                        bw_bits(w, (uint32_t)(beta_star | 0x30), 6);
+                        last = beta_star;
+                    }
+                    vp = mask & vb;
+                } else { bw_bits(w, 2, 2); vp = vb; }              /* case 10 */
+            }
+        }
+        if (on_chimp) chimp_enc_add(w, &ec, vp);
+        else elfx_add(w, &ex, vp);
+    }
+    bw_bit(w, 0);                                              /* the XOR encoder's closing bit */
+}
+
+/* ------------------------------------------------------------------------ */
 /* BUFF fixed-point helpers (compression_common/buff.rs:1-52)                */
 /* ------------------------------------------------------------------------ */
 static const uint64_t PRECISION_MAP[13] = {0, 5, 8, 11, 15, 18, 21, 25, 28, 31, 35, 38, 50};
@@ -386,12 +587,15 @@ static int encode_chunk(obuf* o, const double* v, uint64_t n, int scheme, uint64
         return buff_encode(o, v, n, scale);
     case ORA_GORILLA:
     case ORA_CHIMP:
-    case ORA_CHIMP128: {
+    case ORA_CHIMP128:
+    case ORA_ELF_ON_CHIMP:
+    case ORA_ELF: {
         int st = ORA_OK;
         bw_init(&w);
         if (scheme == ORA_GORILLA) gorilla_encode(&w, v, n);
         else if (scheme == ORA_CHIMP) chimp_encode(&w, v, n);
-        else st = chimp128_encode(&w, v, n);
+        else if (scheme == ORA_CHIMP128) st = chimp128_encode(&w, v, n);
+        else elf_encode(&w, v, n, scheme == ORA_ELF_ON_CHIMP);
         if (st == ORA_OK && !w.b.oom) ob_push(o, w.b.p, w.b.len);
         free(w.b.p);
         if (st != ORA_OK) return st;
@@ -420,7 +624,7 @@ int ora_encode_chunk(const double* v, uint64_t n, int scheme, uint64_t scale, ui
 /* ------------------------------------------------------------------------ */
 int ora_encode(const double* v, uint64_t n, int scheme, int chunk_kind, uint64_t chunk_value,
                uint64_t scale, uint8_t** out, uint64_t* out_len) {
-    if (scheme < 0 || scheme > ORA_CHIMP128 || chunk_kind < 0 || chunk_kind > 2) return ORA_E_INVALID;
+    if (scheme < 0 || scheme > ORA_ELF || chunk_kind < 0 || chunk_kind > 2) return ORA_E_INVALID;
     obuf o = {0};
     ob_push(&o, "EBI1", 4);
     ob_u8(&o, 0);
@@ -505,7 +709,7 @@ int ora_open(const uint8_t* d, uint64_t len, ora_file** out) {
     if (cf + 1 + csz > len) return ORA_E_IO;
     if (csz < 8) return ORA_E_CORRUPT;                /* from_le_bytes slices [..8] */
     if (cf + 1 + csz + 164 > len) return ORA_E_IO;    /* FileFooter3 */
-    if (scheme > ORA_CHIMP128) return ORA_E_INVALID;  /* codecs outside this path */
+    if (scheme > ORA_ELF) return ORA_E_INVALID;  /* codecs outside this path */
     ora_file* f = (ora_file*)calloc(1, sizeof *f);
     if (!f) return ORA_E_OOM;
     f->phys = (uint64_t*)malloc((nch ? nch : 1) * 8);
@@ -665,6 +869,129 @@ static int chimp128_decode(const uint8_t* c, uint64_t len, dvec* out) {
     }
 }
 
+/* Elf / ElfOnChimp readers (decoder/chunk_reader/elf.rs): the wrapper's
+ * prefix (0: restore with the current beta*, 10: value as is, 11: new 4-bit
+ * beta* then restore) before every value of the inner XOR stream; the inner
+ * stream ends at the NaN end marker. */
+typedef struct { uint64_t val; uint32_t lead; int first; } chimp_dec;      /* ChimpDecoder as a stream */
+static int chimp_dec_next(bitr* r, chimp_dec* d, uint64_t* out, int* end) {
+    uint64_t t;
+    *end = 0;
+    if (d->first) {
+        d->first = 0;
+        if (!br_bits(r, 64, &d->val)) return ORA_E_UNEXPECTED_END;
+    } else {
+        uint64_t flag;
+        if (!br_bits(r, 2, &flag)) return ORA_E_UNEXPECTED_END;
+        if (flag == 3) {
+            if (!br_bits(r, 3, &t)) return ORA_E_UNEXPECTED_END;
+            d->lead = LEAD_DECODE[t];
+            if (!br_bits(r, 64 - d->lead, &t)) return ORA_E_UNEXPECTED_END;
+            d->val ^= t;
+        } else if (flag == 2) {
+            if (d->lead > 64) return ORA_E_CORRUPT;
+            if (!br_bits(r, 64 - d->lead, &t)) return ORA_E_UNEXPECTED_END;
+            d->val ^= t;
+        } else if (flag == 1) {
+            uint64_t sig;
+            if (!br_bits(r, 3, &t)) return ORA_E_UNEXPECTED_END;
+            d->lead = LEAD_DECODE[t];
+            if (!br_bits(r, 6, &sig)) return ORA_E_UNEXPECTED_END;
+            if (sig == 0) sig = 64;
+            if (sig + d->lead > 64) return ORA_E_CORRUPT;
+            uint32_t trail = 64 - (uint32_t)sig - d->lead;
+            if (!br_bits(r, (unsigned)sig, &t)) return ORA_E_UNEXPECTED_END;
+            d->val ^= t << trail;
+        }
+    }
+    if (d->val == NAN_BITS) { *end = 1; return ORA_OK; }
+    *out = d->val;
+    return ORA_OK;
+}
+typedef struct { uint64_t val; uint32_t lead, trail; int first; } elfx_dec;  /* ElfXorDecoder (:104-258) */
+static int elfx_dec_next(bitr* r, elfx_dec* d, uint64_t* out, int* end) {
+    uint64_t t;
+    *end = 0;
+    if (d->first) {                                             /* read_first :121-141 */
+        d->first = 0;
+        if (!br_bits(r, 7, &t)) return ORA_E_UNEXPECTED_END;
+        uint32_t tz = (uint32_t)t;
+        if (tz < 64) {
+            uint64_t b;
+            if (!br_bits(r, 63 - tz, &b)) return ORA_E_UNEXPECTED_END;
+            d->val = ((b << 1) | 1) << tz;
+        } else d->val = 0;
+        if (d->val == NAN_BITS) { *end = 1; return ORA_OK; }
+        *out = d->val;
+        return ORA_OK;
+    }
+    uint64_t flag;
+    if (!br_bits(r, 2, &flag)) return ORA_E_UNEXPECTED_END;    /* decompress_float_inner :143-221 */
+    if (flag == 1) { *out = d->val; return ORA_OK; }           /* case 01: the same value */
+    uint64_t value;
+    if (flag == 3 || flag == 2) {
+        uint64_t lac;
+        unsigned hb = flag == 3 ? 9 : 7, cb = flag == 3 ? 6 : 4;
+        if (!br_bits(r, hb, &lac)) return ORA_E_UNEXPECTED_END;
+        d->lead = LEAD_DECODE[lac >> cb];
+        uint32_t center = (uint32_t)(lac & ((1u << cb) - 1));
+        if (center == 0) center = 1u << cb;
+        if (d->lead + center > 64) return ORA_E_CORRUPT;
+        d->trail = 64 - d->lead - center;
+        if (flag == 2 && center == 1) value = 1ull << d->trail;
+        else {
+            uint64_t b;
+            if (!br_bits(r, center - 1, &b)) return ORA_E_UNEXPECTED_END;
+            value = ((b << 1) | 1) << d->trail;
+        }
+    } else {                                                    /* case 00 */
+        if (d->lead > 64 || d->trail > 64 || d->lead + d->trail > 64) return ORA_E_CORRUPT;
+        uint32_t center = 64 - d->lead - d->trail;
+        uint64_t b;
+        if (!br_bits(r, center, &b)) return ORA_E_UNEXPECTED_END;
+        value = center ? b << d->trail : 0;
+    }
+    value ^= d->val;
+    if (value == NAN_BITS) { *end = 1; return ORA_OK; }
+    d->val = value;
+    *out = value;
+    return ORA_OK;
+}
+/* recover_v_by_beta_star (:68-84) */
+static double elf_recover(double vp, int32_t beta) {
+    int32_t sp = elf_sp(fabs(vp), NULL);
+    if (beta == 0) {
+        double v = elf_10i_n((uint32_t)(-(int64_t)sp - 1));
+        return vp < 0.0 ? -v : v;
+    }
+    return elf_round_up(vp, (uint32_t)((int64_t)beta - sp - 1));
+}
+static int elf_decode(const uint8_t* c, uint64_t len, int on_chimp, dvec* out) {
+    bitr r = {c, len, 0};
+    elfx_dec dx = {0, 0xffffffffu, 0xffffffffu, 1};
+    chimp_dec dc = {0, 0xffffffffu, 1};
+    int32_t beta = INT32_MAX;
+    for (;;) {
+        uint64_t b, vp = 0;
+        int restore, end = 0, st;
+        if (!br_bits(&r, 1, &b)) return ORA_E_UNEXPECTED_END;     /* next_value :42-64 */
+        if (!b) restore = 1;
+        else {
+            if (!br_bits(&r, 1, &b)) return ORA_E_UNEXPECTED_END;
+            if (!b) restore = 0;
+            else {
+                if (!br_bits(&r, 4, &b)) return ORA_E_UNEXPECTED_END;
+                beta = (int32_t)(uint32_t)b;
+                restore = 1;
+            }
+        }
+        st = on_chimp ? chimp_dec_next(&r, &dc, &vp, &end) : elfx_dec_next(&r, &dx, &vp, &end);
+        if (st) return st;
+        if (end) return ORA_OK;
+        PUSH(restore ? elf_recover(u2f(vp), beta) : u2f(vp));
+    }
+}
+
 /* RunLengthReaderImpl::decompress (decoder/chunk_reader/run_length.rs:314-337) */
 static int rle_decode(const uint8_t* c, uint64_t len, dvec* out) {
     if (len < 8) return ORA_E_IO;
@@ -758,6 +1085,8 @@ int ora_decode_chunk(const uint8_t* c, uint64_t len, int scheme, uint64_t n_rows
     case ORA_GORILLA: st = gorilla_decode(c, len, out); break;
     case ORA_CHIMP: st = chimp_decode(c, len, out); break;
     case ORA_CHIMP128: st = chimp128_decode(c, len, out); break;
+    case ORA_ELF_ON_CHIMP: st = elf_decode(c, len, 1, out); break;
+    case ORA_ELF: st = elf_decode(c, len, 0, out); break;
     default: st = ORA_E_INVALID;
     }
     if (st == ORA_OK) {
@@ -1073,6 +1402,8 @@ static int decode_any(const ora_file* f, const uint8_t* c, uint64_t len, uint64_
     case ORA_GORILLA: return gorilla_decode(c, len, out);
     case ORA_CHIMP: return chimp_decode(c, len, out);
     case ORA_CHIMP128: return chimp128_decode(c, len, out);
+    case ORA_ELF_ON_CHIMP: return elf_decode(c, len, 1, out);
+    case ORA_ELF: return elf_decode(c, len, 0, out);
     default: return ORA_E_INVALID;
     }
 }

@@ -41,7 +41,8 @@ enum {
     ORA_E_OOM = 8
 };
 
-enum { ORA_UNCOMPRESSED = 0, ORA_RLE = 1, ORA_BUFF = 2, ORA_GORILLA = 3, ORA_CHIMP = 4, ORA_CHIMP128 = 5 };
+enum { ORA_UNCOMPRESSED = 0, ORA_RLE = 1, ORA_BUFF = 2, ORA_GORILLA = 3, ORA_CHIMP = 4, ORA_CHIMP128 = 5,
+       ORA_ELF_ON_CHIMP = 6, ORA_ELF = 7 };
 enum { ORA_CHUNK_FULL = 0, ORA_CHUNK_RECORD_COUNT = 1, ORA_CHUNK_BYTE_SIZE = 2 };
 enum { ORA_PRED_EQ = 0, ORA_PRED_NE = 1, ORA_PRED_RANGE = 2 };
 enum { ORA_BOUND_NONE = 0, ORA_BOUND_INCLUSIVE = 1, ORA_BOUND_EXCLUSIVE = 2 };

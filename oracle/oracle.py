@@ -22,9 +22,9 @@ BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "libebi_oracle.so"
 SOURCES = [HERE / "ebi_oracle.c"]
 
-UNCOMPRESSED, RLE, BUFF, GORILLA, CHIMP, CHIMP128 = range(6)
+UNCOMPRESSED, RLE, BUFF, GORILLA, CHIMP, CHIMP128, ELF_ON_CHIMP, ELF = range(8)
 SCHEMES = {"uncompressed": UNCOMPRESSED, "rle": RLE, "buff": BUFF, "gorilla": GORILLA,
-           "chimp": CHIMP, "chimp128": CHIMP128}
+           "chimp": CHIMP, "chimp128": CHIMP128, "elf_on_chimp": ELF_ON_CHIMP, "elf": ELF}
 CHUNK_FULL, CHUNK_RECORD_COUNT, CHUNK_BYTE_SIZE = range(3)
 PRED_EQ, PRED_NE, PRED_RANGE = range(3)
 BOUND_NONE, BOUND_INCLUSIVE, BOUND_EXCLUSIVE = range(3)

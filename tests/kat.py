@@ -7,7 +7,7 @@ from oracle import oracle as O
 KAT = json.loads((Path(__file__).resolve().parent / "golden" / "kat.json").read_text())
 
 BOUND = {"none": O.BOUND_NONE, "incl": O.BOUND_INCLUSIVE, "excl": O.BOUND_EXCLUSIVE}
-CODECS = ["uncompressed", "rle", "gorilla", "chimp", "chimp128", "buff"]
+CODECS = ["uncompressed", "rle", "gorilla", "chimp", "chimp128", "elf_on_chimp", "elf", "buff"]
 
 
 def chunk_option(spec):

@@ -30,6 +30,21 @@ def test_library_exports_every_declared_symbol():
     assert sorted(_native.EXPORTS) == names
 
 
+def mixed_decimals(rng, n):
+    """Decimals of 0-9 digits over magnitudes 1e-14..1e14 with powers of ten,
+    zeros, infinities, subnormals and full-precision doubles mixed in."""
+    digits = rng.integers(0, 10, n)
+    mag = 10.0 ** rng.integers(-14, 15, n)
+    v = np.round(rng.uniform(-1, 1, n) * mag * 10.0 ** digits) / 10.0 ** digits
+    pick = rng.random(n)
+    v = np.where(pick < 0.05, 10.0 ** rng.integers(-320, 300, n).astype(np.float64), v)
+    v = np.where((pick >= 0.05) & (pick < 0.07), 0.0, v)
+    v = np.where((pick >= 0.07) & (pick < 0.08), rng.normal(0, 1, n), v)
+    v = np.where((pick >= 0.08) & (pick < 0.085), 5e-324 * rng.integers(1, 1 << 40, n), v)
+    v = np.where((pick >= 0.085) & (pick < 0.087), np.inf * np.sign(rng.normal(size=n)), v)
+    return v
+
+
 def gen(kind, n, seed):
     rng = np.random.default_rng(seed)
     if kind == "walk":
@@ -40,13 +55,15 @@ def gen(kind, n, seed):
         v = np.repeat(np.round(rng.normal(0, 5, n // 8 + 1), 1), 8)[:n]
     elif kind == "const":
         v = np.full(n, 3.25)
+    elif kind == "decimals":
+        v = mixed_decimals(rng, n)
     else:
         v = rng.normal(0, 1e6, n)
     return v + 0.0
 
 
-@pytest.mark.parametrize("codec", ["uncompressed", "rle", "gorilla", "chimp", "chimp128", "buff"])
-@pytest.mark.parametrize("kind", ["walk", "uniform", "steps", "const", "wide"])
+@pytest.mark.parametrize("codec", ["uncompressed", "rle", "gorilla", "chimp", "chimp128", "elf_on_chimp", "elf", "buff"])
+@pytest.mark.parametrize("kind", ["walk", "uniform", "steps", "const", "wide", "decimals"])
 @pytest.mark.parametrize("chunk", [("record_count", 1000), ("record_count", 4097), ("byte_size", 3000), ("full", 0)])
 def test_encoder_bytes_match_oracle(codec, kind, chunk):
     v = gen(kind, 5003, 11)

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 def make_columns(rng, n_cols):
     cols = []
-    codecs = ["buff", "gorilla", "chimp128", "rle", "chimp", "uncompressed"]
+    codecs = ["buff", "gorilla", "chimp128", "rle", "chimp", "uncompressed", "elf", "elf_on_chimp"]
     for i in range(n_cols):
         codec = codecs[i % len(codecs)]
         n = int(rng.integers(1, 60_000)) if i % 5 else int(rng.integers(60_000, 300_000))

@@ -12,9 +12,9 @@ pytestmark = pytest.mark.gpu
 
 def columns(rng, n_cols):
     out = []
-    codecs = ["buff", "gorilla", "chimp128", "rle"]
+    codecs = ["buff", "gorilla", "chimp128", "rle", "elf"]
     for i in range(n_cols):
-        codec = codecs[i % 4]
+        codec = codecs[i % len(codecs)]
         n = int(np.exp(rng.uniform(np.log(2_000), np.log(200_000))))
         if codec == "buff":
             v = np.round(rng.uniform(-1000, 1000, n), 3) + 0.0

@@ -1,4 +1,5 @@
-"""RLE, Uncompressed, Gorilla, Chimp and Chimp128 on the GPU against the oracle.
+"""RLE, Uncompressed, Gorilla, Chimp, Chimp128, Elf and ElfOnChimp on the GPU
+against the oracle.
 
 Values, bitmasks and min/max are bit-exact; sums are compensated (double-double)
 and checked against the oracle's sequential sum (relative 1e-12 of the sum of
@@ -14,7 +15,7 @@ from tests.parity import check_query_suite, mask_np, random_mask, random_preds, 
 
 pytestmark = pytest.mark.gpu
 
-VALUE_CODECS = ["uncompressed", "rle", "gorilla", "chimp", "chimp128"]
+VALUE_CODECS = ["uncompressed", "rle", "gorilla", "chimp", "chimp128", "elf_on_chimp", "elf"]
 KIND_NAMES = {O.CHUNK_RECORD_COUNT: "record_count", O.CHUNK_BYTE_SIZE: "byte_size", O.CHUNK_FULL: "full"}
 
 
@@ -95,7 +96,10 @@ def test_full_chunk_sequential_path(codec):
     check_query_suite(data, random_preds(v, rng, k=2), masks=(None, random_mask(len(v), 0.4, rng)))
 
 
-@pytest.mark.parametrize("codec", ["gorilla", "chimp", "chimp128"])
+XOR_CODECS = ["gorilla", "chimp", "chimp128", "elf_on_chimp", "elf"]
+
+
+@pytest.mark.parametrize("codec", XOR_CODECS)
 def test_nan_truncates_stream(codec):
     # the XOR readers stop at the first value whose bits equal f64::NAN (parity hazard kept on purpose)
     v = np.round(np.random.default_rng(5).normal(10, 3, 5000), 2)
@@ -151,7 +155,7 @@ def test_full_size_properties(codec):
     assert sum_ok(d.sum(), float(np.sum(v)), False, v)
 
 
-@pytest.mark.parametrize("codec", ["gorilla", "chimp", "chimp128"])
+@pytest.mark.parametrize("codec", XOR_CODECS)
 @pytest.mark.parametrize("kind", ["walk", "sensor", "few"])
 def test_many_small_chunks(codec, kind):
     # >= 1,024 chunks of 64 values: short streams, many CTAs
@@ -165,7 +169,7 @@ def test_many_small_chunks(codec, kind):
                       chunk_ids=(None, int(rng.integers(n_chunks))))
 
 
-@pytest.mark.parametrize("codec", ["chimp", "chimp128"])
+@pytest.mark.parametrize("codec", ["chimp", "chimp128", "elf_on_chimp", "elf"])
 def test_many_small_chunks_corrupt(codec):
     rng = np.random.default_rng(9)
     v = np.round(30 + np.cumsum(rng.normal(0, 0.5, 70_000)), 2) + 0.0
@@ -179,3 +183,31 @@ def test_many_small_chunks_corrupt(codec):
             data[phys + int(rng.integers(size))] ^= 1 << int(rng.integers(8))
         check_query_suite(bytes(data), [E.Predicate.range(E.RangeValue.inclusive(25.0), E.RangeValue.NONE)],
                           masks=(None,))
+
+
+def elf_edge_columns(rng, n):
+    from tests.test_cpu_abi import mixed_decimals
+    near = 10.0 ** rng.integers(-300, 300, n).astype(np.float64)
+    near = np.nextafter(near, np.where(rng.random(n) < 0.5, 0.0, np.inf))
+    return {
+        "decimals": mixed_decimals(rng, n),
+        # get_sp's log10 path and the power-of-ten flag (both sides of 10^k)
+        "near_powers": np.where(rng.random(n) < 0.5, near, np.round(rng.normal(0, 1, n), 2)),
+        "digits": np.round(rng.normal(0, 1e3, n), 1) * 10.0 ** rng.integers(-8, 8, n),
+    }
+
+
+@pytest.mark.parametrize("codec", ["elf_on_chimp", "elf"])
+@pytest.mark.parametrize("kind", ["decimals", "near_powers", "digits"])
+@pytest.mark.parametrize("chunk", [("record_count", 8192), ("record_count", 777)])
+def test_elf_decimal_restoration(codec, kind, chunk):
+    # restored values equal the oracle's bit for bit, including the values the
+    # reference's power-of-ten test turns into 10^k
+    rng = np.random.default_rng(abs(hash((codec, kind, chunk))) % 2**32)
+    n = 25_000
+    v = elf_edge_columns(rng, n)[kind]
+    data = E.encode(v, codec, chunk)
+    assert bytes(data) == O.encode(v, codec, O.CHUNK_RECORD_COUNT, chunk[1])
+    got = E.Decoder(data).materialize().cpu().numpy()
+    assert same_f64(got, O.Decoder(bytes(data)).materialize(None))
+    check_query_suite(data, random_preds(v[np.isfinite(v)], rng, k=2), masks=(None, random_mask(n, 0.3, rng)))
