@@ -14,8 +14,9 @@ the reference's throughput definition (uncompressed bytes / elapsed time).
 --workload picks one of the other measured shapes instead of the headline
 BUFF column: "gorilla" (1,048,576-value random walk, 8,192-value chunks,
 filter 10 <= x <= 50 + sum/min/max), "chimp128" (16,777,216-value sensor
-series, filter 15 <= x <= 25 + max) and "rle" (16,777,216-value step series,
-filter over the middle 30 % of its values + max).
+series, filter 15 <= x <= 25 + max), "elf" / "elf_on_chimp" (the same sensor
+series and query through the Elf codecs) and "rle" (16,777,216-value step
+series, filter over the middle 30 % of its values + max).
 
 Under torchrun every rank runs the same workload on its own GPU (replicas: the
 path has no cross-column exchange), and value sums the ranks' rows over the
@@ -103,6 +104,14 @@ class Workload:
             self.aggregates = ("max",)
             self.describe = ("Chimp128 16,777,216 f64 sensor series 20+10sin(2pi i/1440)+N(0,0.1), 4 dp, "
                              "8,192-row chunks; fused decode + filter 15<=x<=25 (bitmask out) + max")
+        elif name in ("elf", "elf_on_chimp"):
+            self.codec, self.chunk, self.scale = name, 8192, 1
+            self.values = lambda: W.sensor(rows)
+            self.ranges = [("15<=x<=25", 15.0, 25.0)]
+            self.aggregates = ("max",)
+            label = "Elf" if name == "elf" else "ElfOnChimp"
+            self.describe = (f"{label} 16,777,216 f64 sensor series 20+10sin(2pi i/1440)+N(0,0.1), 4 dp, "
+                             "8,192-row chunks; fused decode + decimal restore + filter 15<=x<=25 (bitmask out) + max")
         elif name == "rle":
             self.codec, self.chunk, self.scale = "rle", 8192, 1
             self.values = lambda: W.steps(rows)
@@ -136,10 +145,13 @@ class Workload:
         return [O.rng(O.BOUND_INCLUSIVE, a, O.BOUND_INCLUSIVE, b) for _, a, b in self.ranges]
 
 
-DEFAULT_ROWS = {"buff": N_ROWS, "gorilla": 1_048_576, "chimp128": 16_777_216, "rle": 16_777_216}
+DEFAULT_ROWS = {"buff": N_ROWS, "gorilla": 1_048_576, "chimp128": 16_777_216, "rle": 16_777_216,
+                "elf": 16_777_216, "elf_on_chimp": 16_777_216}
 KERNELS = {"buff": "buff_scan_kernel (fused decode + range filter + bitmask + sum)",
-           "gorilla": "xor_kernel<Gorilla> (segment-parallel decode + filter + bitmask + sum/min/max)",
+           "gorilla": "gorilla_kernel (one warp per chunk: decode + filter + bitmask + sum/min/max)",
            "chimp128": "xor_kernel<Chimp128> (segment-parallel decode + filter + bitmask + max)",
+           "elf": "xor_kernel<Elf> (segment-parallel decode + decimal restore + filter + bitmask + max)",
+           "elf_on_chimp": "xor_kernel<ElfOnChimp> (segment-parallel decode + decimal restore + filter + bitmask + max)",
            "rle": "rle_kernel (run expansion + filter + bitmask + max)"}
 
 
@@ -465,7 +477,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity-check", action="store_true")
     ap.add_argument("--rows", type=int, default=0, help="column length (profiling runs use smaller columns)")
-    ap.add_argument("--workload", default="buff", choices=["buff", "gorilla", "chimp128", "rle", "batched", "serving"])
+    ap.add_argument("--workload", default="buff", choices=["buff", "gorilla", "chimp128", "rle", "elf", "elf_on_chimp",
+                                                               "batched", "serving"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="batched / serving: fraction of the configuration's columns to build")
     args = ap.parse_args()
