@@ -528,6 +528,11 @@ def main():
 
     def one_step(i):
         flush.fill_(i & 0xFF)  # evicts the column from L2 (not timed)
+        # ~0.5 ms of device spin (not timed): the device is still busy when the
+        # host enqueues the query, so its events time device work, not the
+        # host's launch latency
+        if hasattr(torch.cuda, "_sleep"):
+            torch.cuda._sleep(1_000_000)
         dec.filter_agg(qs[i % nq][1], out=mask, aggregates=wl.aggregates)
         return dec.segmented_execution_times()
 

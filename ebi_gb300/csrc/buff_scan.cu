@@ -2,10 +2,8 @@
 // in one launch.  Bulk copies (cp.async.bulk) stream each tile's byte planes
 // into a ring of shared-memory stages; consumer warps decode and test 8 rows
 // per lane; the last CTA folds the query result.
-#include "buff_common.cuh"
+#include "buff_query_dev.cuh"
 #include "tma.cuh"
-#include "fold.cuh"
-#include <climits>
 
 namespace ebi {
 namespace {
@@ -24,47 +22,6 @@ using namespace buff;
 // ---------------------------------------------------------------------------
 constexpr int kScanConsumers = 256;
 constexpr int kScanThreads = kScanConsumers + 32;
-
-// The query folded, per chunk, into one unsigned range test on the delta:
-//   sel = (negate ? ~cmp : cmp) & (use_mask ? bitmask : valid rows)
-// with cmp = lo <= delta <= hi (all rows when `full`, none when `empty`).
-// It reproduces the reference's in-situ decisions, including the shortcuts
-// that return all rows without looking at the input bitmask.
-struct RangeProg {
-    uint64_t lo, hi;
-    uint32_t empty, full, negate, use_mask;
-};
-
-__device__ RangeProg compile_prog(const QueryParams& q, const BuffPred& k, uint32_t bits, bool has_mask) {
-    RangeProg g{0, ~0ull, 0, 0, 0, 0};
-    const uint64_t dmax = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
-    if (q.op == OP_AGG) {  // no predicate: the rows of the bitmask (all rows without one)
-        g.full = 1;
-        g.use_mask = has_mask;
-        return g;
-    }
-    if (q.pred.kind == EBI_PRED_RANGE) {
-        const bool la = k.lmode == SIDE_ABSENT, ra = k.rmode == SIDE_ABSENT;
-        if (k.lmode == SIDE_NONE || k.rmode == SIDE_NONE) g.empty = 1;
-        if (k.lmode == SIDE_CMP) {
-            if (!k.lincl && k.lthr >= dmax) g.empty = 1;
-            else g.lo = k.lincl ? k.lthr : k.lthr + 1;
-        }
-        if (k.rmode == SIDE_CMP) {
-            if (!k.rincl && k.rthr == 0) g.empty = 1;
-            else g.hi = k.rincl ? k.rthr : k.rthr - 1;
-        }
-        if (!g.empty && g.lo > g.hi) g.empty = 1;
-        g.use_mask = k.lmode == SIDE_CMP || k.rmode == SIDE_CMP || (la && ra);
-    } else {
-        if (k.emode == SIDE_NONE) g.empty = 1;
-        else if (k.emode == SIDE_CMP) { g.lo = g.hi = k.etgt; g.use_mask = 1; }
-        if (q.pred.kind == EBI_PRED_NE) { g.negate = 1; g.use_mask = 1; }
-    }
-    g.full = !g.empty && g.lo == 0 && g.hi >= dmax;
-    g.use_mask = g.use_mask && has_mask;
-    return g;
-}
 
 struct ScanMeta {
     int64_t base;       // the chunk's fixed-point base
@@ -93,43 +50,6 @@ __device__ __forceinline__ void load32_smem(const uint8_t* p, uint32_t (&w)[8]) 
     const uint32_t bs = (s & 3) * 8;
 #pragma unroll
     for (int j = 0; j < 8; ++j) w[j] = __funnelshift_r(v[j], v[j + 1], bs);
-}
-
-struct Partial {
-    unsigned long long sum, cnt, mx, mn;
-};
-
-// Running query totals of one warp (kept by lane 0).
-struct WarpTot {
-    unsigned long long sum_fixed, count;
-    double abs_bound;
-    long long max_fixed, min_fixed;
-    unsigned int nonexact;
-};
-
-// Ends a warp's run over one chunk: per-chunk partials (for the chunk-ordered
-// fallback fold) and the warp's exact query totals.
-__device__ __forceinline__ void flush_partial(const QueryParams& q, uint32_t chunk, int64_t base, Partial& p,
-                                              WarpTot& wt) {
-    const unsigned long long s = warp_sum(p.sum), c = warp_sum(p.cnt), mx = warp_max_u64(p.mx), mn = warp_min_u64(p.mn);
-    if ((threadIdx.x & 31) == 0 && c) {
-        ChunkAcc* a = q.acc + chunk;
-        atomicAdd(&a->isum, s);
-        atomicAdd(&a->count, c);
-        atomicMax(&a->dmax, mx);
-        atomicMin(&a->dmin, mn);
-        const __int128 piece = static_cast<__int128>(s) + static_cast<__int128>(base) * static_cast<__int128>(c);
-        const __int128 ap = piece < 0 ? -piece : piece;
-        wt.sum_fixed += static_cast<unsigned long long>(piece);
-        if (ap >= (static_cast<__int128>(1) << 53)) wt.nonexact = 1;
-        else wt.abs_bound += static_cast<double>(static_cast<long long>(ap));
-        wt.count += c;
-        const long long fmax = static_cast<long long>(static_cast<unsigned long long>(base) + mx);
-        const long long fmin = static_cast<long long>(static_cast<unsigned long long>(base) + mn);
-        wt.max_fixed = fmax > wt.max_fixed ? fmax : wt.max_fixed;
-        wt.min_fixed = fmin < wt.min_fixed ? fmin : wt.min_fixed;
-    }
-    p.sum = 0; p.cnt = 0; p.mx = 0; p.mn = ~0ull;
 }
 
 template <int TB, typename D>
@@ -494,57 +414,12 @@ __device__ __forceinline__ void scan_dispatch(const QueryParams& q, const ScanMe
     }
 }
 
-__device__ __forceinline__ void chunk_error(const QueryParams& q, ScanTotals* T, uint32_t c, uint32_t code) {
-    set_status(q.acc + c, code);
-    atomicMin(&T->bad_chunk, c);
-}
-
-// The last CTA's fold of the query totals (chunk-ordered fallback when the
-// exact integer total does not apply).
-__device__ void scan_finalize(const QueryParams& q, const BuffChunkInfo* info, ScanTotals* T, QueryResult* res,
-                              uint32_t frac, bool fast_ok) {
-    __shared__ QueryResult r;
-    if (threadIdx.x == 0) {
-        const ScanTotals t = *T;
-        const double inf = __longlong_as_double(0x7ff0000000000000ll);
-        r.status = 0;
-        r.bad_chunk = t.bad_chunk;
-        if (t.bad_chunk != 0xffffffffu) r.status = q.acc[t.bad_chunk].status;
-        r.count = t.count;
-        r.sum = 0.0; r.min = inf; r.max = -inf;
-        if (fast_ok && !t.nonexact && t.abs_bound < 4503599627370496.0 /* 2^52 */) {
-            // Every chunk sum and every prefix of the chunk-ordered fold is an
-            // exact multiple of 2^-frac below 2^53 of them: the reference's
-            // sequential f64 fold is exact and equals the exact total.
-            if (t.count) {
-                r.sum = fold_scale(static_cast<long long>(t.sum_fixed), frac);
-                r.max = fold_scale(t.max_fixed, frac);
-                r.min = fold_scale(t.min_fixed, frac);
-            }
-        } else {
-            fold_buff_chunks(q, r);
-        }
-        *res = r;
-        T->sum_fixed = 0; T->abs_bound = 0.0; T->count = 0;
-        T->max_fixed = LLONG_MIN; T->min_fixed = LLONG_MAX;
-        T->done = 0; T->bad_chunk = 0xffffffffu; T->nonexact = 0;
-    }
-    __syncthreads();
-    const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    for (uint32_t c = threadIdx.x; c < q.n_chunks; c += blockDim.x) {
-        ChunkAcc a = {};
-        a.dmin = ~0ull;
-        a.fmin = inf;
-        a.fmax = -inf;
-        q.acc[c] = a;
-    }
-}
-
 // A tile's metadata and copy plan, prepared by one producer lane.
 struct PreTile {
     ScanMeta m;
-    uint64_t planes, tail;  // file offsets of the chunk's first plane and tail plane
-    uint32_t n, begin;      // plane length (rows of the chunk) and the tile's first row
+    uint64_t planes, tail;  // device offsets of the chunk's first plane and tail plane
+    uint64_t stride;        // bytes from one plane to the next
+    uint32_t begin;         // the tile's first row
     uint32_t bytes;         // bytes the tile's copies deliver
 };
 
@@ -568,7 +443,7 @@ __device__ __forceinline__ void prepare_tile(const QueryParams& q, const BuffChu
     m.ok = selected && ci.status == 0;
     pt.planes = ci.planes;
     pt.tail = ci.tail;
-    pt.n = ci.n;
+    pt.stride = ci.stride;
     pt.begin = tl.begin;
     uint32_t bytes = 0;
     if (m.ok) {
@@ -578,7 +453,7 @@ __device__ __forceinline__ void prepare_tile(const QueryParams& q, const BuffChu
         compile_pred(q.pred, ci.base, ci.bits, ci.frac, has_mask, m.pred);
         m.prog = compile_prog(q, m.pred, ci.bits, has_mask);
         for (uint32_t p = 0; p < m.np; ++p) {
-            const uintptr_t src = reinterpret_cast<uintptr_t>(q.file + ci.planes + uint64_t(p) * ci.n + tl.begin);
+            const uintptr_t src = reinterpret_cast<uintptr_t>(q.file + ci.planes + uint64_t(p) * ci.stride + tl.begin);
             const uintptr_t a = src & ~uintptr_t(15);
             m.mis[p] = static_cast<uint32_t>(src - a);
             bytes += static_cast<uint32_t>(((src + m.rows + 15) & ~uintptr_t(15)) - a);
@@ -645,7 +520,7 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
                     mbar_arrive_expect_tx(&full[s], pt.bytes);
                     if (pt.m.ok) {
                         for (uint32_t p = 0; p < pt.m.np; ++p) {
-                            const uintptr_t src = reinterpret_cast<uintptr_t>(q.file + pt.planes + uint64_t(p) * pt.n + pt.begin);
+                            const uintptr_t src = reinterpret_cast<uintptr_t>(q.file + pt.planes + uint64_t(p) * pt.stride + pt.begin);
                             const uintptr_t a = src & ~uintptr_t(15);
                             const uint32_t len = static_cast<uint32_t>(((src + pt.m.rows + 15) & ~uintptr_t(15)) - a);
                             bulk_g2s(st + p * L.plane_stride, reinterpret_cast<const void*>(a), len, &full[s]);
@@ -697,34 +572,7 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
     if (cur != 0xffffffffu) flush_partial(q, cur, cur_base, part, wt);
     if ((threadIdx.x & 31) == 0) wtot[threadIdx.x >> 5] = wt;
     }
-    // ---- CTA totals, then the last CTA folds the query ----
-    __syncthreads();
-    __shared__ unsigned int s_last;
-    if (threadIdx.x == 0) {
-        WarpTot c{0, 0, 0.0, LLONG_MIN, LLONG_MAX, 0};
-        for (int w = 0; w < kScanConsumers / 32; ++w) {
-            c.sum_fixed += wtot[w].sum_fixed;
-            c.count += wtot[w].count;
-            c.abs_bound += wtot[w].abs_bound;
-            c.max_fixed = wtot[w].max_fixed > c.max_fixed ? wtot[w].max_fixed : c.max_fixed;
-            c.min_fixed = wtot[w].min_fixed < c.min_fixed ? wtot[w].min_fixed : c.min_fixed;
-            c.nonexact |= wtot[w].nonexact;
-        }
-        if (c.count) {
-            atomicAdd(&T->sum_fixed, c.sum_fixed);
-            atomicAdd(&T->count, c.count);
-            atomicAdd(&T->abs_bound, c.abs_bound);
-            atomicMax(&T->max_fixed, c.max_fixed);
-            atomicMin(&T->min_fixed, c.min_fixed);
-            if (c.nonexact) atomicOr(&T->nonexact, 1u);
-        }
-        __threadfence();
-        s_last = atomicAdd(&T->done, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    scan_finalize(q, info, T, res, frac, fast_ok != 0);
+    cta_finish(q, info, T, res, frac, fast_ok != 0, wtot, kScanConsumers / 32);
 }
 
 }  // namespace
@@ -761,6 +609,7 @@ cudaError_t launch_buff_scan(const QueryParams& q, const BuffChunkInfo* info, ui
         if (e != cudaSuccess) return e;
         configured = smem;
     }
+    if ((grid < n_tiles ? grid : n_tiles) > kScanSlots) return cudaErrorInvalidConfiguration;
     buff_scan_kernel<<<grid < n_tiles ? grid : n_tiles, kScanThreads, smem, s>>>(q, info, tile_begin, n_tiles, L, T,
                                                                                res, frac, fast_ok ? 1u : 0u);
     count_launch();

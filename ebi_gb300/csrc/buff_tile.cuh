@@ -19,6 +19,7 @@ __constant__ uint32_t c_precision_map[13] = {0, 5, 8, 11, 15, 18, 21, 25, 28, 31
 struct BuffCtx {
     const uint8_t* planes;
     const uint8_t* tail;
+    uint64_t stride;    // bytes from one byte plane to the next
     int64_t base;
     uint64_t row_off;
     double scale;       // 2^frac
@@ -41,20 +42,17 @@ __device__ void buff_setup(const QueryParams& q, uint32_t c, bool has_mask, Buff
     k.selected = has_mask ? acc->selected : static_cast<uint32_t>(q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
     if (!k.selected) return;
     if (!has_mask && acc->selected == 0) acc->selected = 1;  // finalize folds selected chunks
-    if (cd.flags & kChunkBadGeometry) { set_status(acc, EBI_E_IO); return; }
-    if (cd.byte_len < 20) { set_status(acc, EBI_E_UNEXPECTED_END); return; }
-    const uint8_t* p = q.file + cd.byte_off;
-    k.base = static_cast<int64_t>(load_u64_unaligned(p));
-    const uint32_t n = load_u32_unaligned(p + 8);
-    k.bits = load_u32_unaligned(p + 12);
-    k.frac = load_u32_unaligned(p + 16);
-    if (k.bits > 64 || n != cd.n_rows) { set_status(acc, EBI_E_CORRUPT); return; }
+    // the header facts were read and checked at open (the chunk's status)
+    const BuffChunkInfo ci = q.binfo[c];
+    if (ci.status) { set_status(acc, ci.status); return; }
+    k.base = ci.base;
+    k.bits = ci.bits;
+    k.frac = ci.frac;
     k.np = k.bits / 8;
     k.tb = k.bits % 8;
-    const uint64_t need = 20 + uint64_t(k.np) * n + (uint64_t(n) * k.tb + 7) / 8;
-    if (k.bits > 0 && need > cd.byte_len) { set_status(acc, EBI_E_UNEXPECTED_END); return; }
-    k.planes = p + 20;
-    k.tail = k.planes + uint64_t(k.np) * n;
+    k.planes = q.file + ci.planes;
+    k.tail = q.file + ci.tail;
+    k.stride = ci.stride;
     k.scale = k.frac <= 1023 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 + k.frac) << 52))
                              : __longlong_as_double(0x7ff0000000000000ll);
     k.inv_scale = k.frac <= 1022 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 - k.frac) << 52)) : 0.0;
@@ -87,7 +85,7 @@ __device__ __forceinline__ void load_deltas(const BuffCtx& k, uint32_t r0, uint3
     for (int i = 0; i < 32; ++i) d[i] = 0;
     for (uint32_t p = 0; p < np_load; ++p) {
         uint32_t w[8];
-        load32(k.planes + uint64_t(p) * k.n + r0, w);
+        load32(k.planes + uint64_t(p) * k.stride + r0, w);
 #pragma unroll
         for (int i = 0; i < 32; ++i)
             d[i] = (d[i] << 8) | static_cast<D>(((w[i >> 2] >> (8 * (i & 3))) & 0xffu) ^ 0x80u);

@@ -227,10 +227,18 @@ int ensure_scratch(ebi_column* c, cudaStream_t s) {
     return st;
 }
 
-// Query timing: events around the codec kernels and the finalize fold.
+// Query timing: events at the query's start, around the codec kernels and
+// after the finalize fold.  mark_scan re-records the scan start right before
+// the first codec kernel (after the query's memsets and chunk selection).
 int begin_query(ebi_column* c, cudaStream_t s) {
     c->launches_at_start = ebi_kernel_launches();
     if (c->timing) CK(cudaEventRecord(c->ev[0], s));
+    if (c->timing) CK(cudaEventRecord(c->ev[3], s));
+    return EBI_OK;
+}
+
+int mark_scan(ebi_column* c, cudaStream_t s) {
+    if (c->timing) CK(cudaEventRecord(c->ev[3], s));
     return EBI_OK;
 }
 
@@ -244,12 +252,13 @@ int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
     CK(cudaStreamSynchronize(s));
     c->last.kernels = ebi_kernel_launches() - c->launches_at_start;
     if (c->timing) {
-        float a = 0.f, b = 0.f;
-        CK(cudaEventElapsedTime(&a, c->ev[0], c->ev[1]));
+        float a = 0.f, b = 0.f, t = 0.f;
+        CK(cudaEventElapsedTime(&a, c->ev[3], c->ev[1]));
         CK(cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
+        CK(cudaEventElapsedTime(&t, c->ev[0], c->ev[2]));
         c->last.scan_ms = a;
         c->last.finalize_ms = b;
-        c->last.total_ms = double(a) + double(b);
+        c->last.total_ms = t;
     }
     if (c->h_res->status) {
         char buf[96];
@@ -278,6 +287,7 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
         // value codecs OR their rows into a zeroed output (decoded runs may start on any row)
         if (d_out_mask) CK(cudaMemsetAsync(d_out_mask, 0, c->mask_words * 8, s));
         if (d_mask) CK(launch_select_chunks(q, s));
+        if (int st = mark_scan(c, s)) return st;
         CK(launch_values(c, q, tb, tn, VAL_SCAN, nullptr, s));
         return EBI_OK;
     }
@@ -290,9 +300,17 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
             CK(cudaMemsetAsync(reinterpret_cast<uint32_t*>(d_out_mask) + 2 * c->mask_words - 1, 0, 4, s));
     }
     if (d_mask) CK(launch_select_chunks(q, s));
+    if (int st = mark_scan(c, s)) return st;
     if (c->scheme == EBI_BUFF) {
         if (tile_counts || tn == 0) {
             CK(launch_buff_query(q, tb, tn, s));
+        } else if (c->stream_ok) {
+            const uint32_t ub = chunk_id < 0 ? 0u : c->first_unit[chunk_id];
+            const uint32_t un = chunk_id < 0 ? c->first_unit.back() : c->first_unit[chunk_id + 1] - ub;
+            const uint32_t fold = (c->buff_fast_ok ? 1u : 0u) | (c->buff_exact ? 2u : 0u);
+            CK(launch_buff_stream(q, c->d_buff, c->d_units, ub, un, c->stream_bits, c->sms, c->d_tot, c->d_res,
+                                  c->buff_frac, fold, s));
+            c->fused_pending = true;
         } else {
             CK(launch_buff_scan(q, c->d_buff, tb, tn, c->layout, c->scan_grid, c->d_tot, c->d_res, c->buff_frac,
                                 c->buff_fast_ok, s));
@@ -401,25 +419,44 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (st) { delete c; return st; }
     cudaStream_t s = c->stream;
     std::vector<BuffChunkInfo> binfo;
+    std::vector<RepackSeg> segs;
+    uint64_t dev_len = len;  // bytes of the column in HBM
     if (c->scheme == EBI_BUFF) {
         c->tiles = buff_tiles(c->chunks);
         binfo = parse_buff_headers(file, c->chunks);
+        dev_len = buff_plan_layout(binfo, segs);
         uint32_t np_max = 0, tb_max = 0;
         bool first = true;
         c->buff_fast_ok = true;
+        c->stream_ok = true;
         for (const BuffChunkInfo& b : binfo) {
             if (b.status) continue;
+            if (b.bits < 8 || b.bits > 32) c->stream_ok = false;
             np_max = std::max(np_max, b.bits / 8);
             tb_max = std::max(tb_max, b.bits % 8);
             if (first) { c->buff_frac = b.frac; first = false; }
             if (b.frac != c->buff_frac || b.frac > 1022 || b.bits == 0) c->buff_fast_ok = false;
         }
+        // bound of sum |base + delta| over every readable row
+        long double bound = 0.0L;
+        for (const BuffChunkInfo& b : binfo) {
+            if (b.status) continue;
+            const long double lo = static_cast<long double>(b.base);
+            const long double hi = lo + (b.bits >= 64 ? 18446744073709551615.0L : static_cast<long double>((1ull << b.bits) - 1));
+            bound += static_cast<long double>(b.n) * std::max(lo < 0 ? -lo : lo, hi < 0 ? -hi : hi);
+        }
+        c->buff_exact = c->buff_fast_ok && bound < 4503599627370496.0L;  // 2^52
         uint32_t per_sm = 1;
         c->layout = buff_stage_layout(np_max, tb_max, &per_sm);
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         c->scan_grid = static_cast<uint32_t>(std::max(sms, 1)) * per_sm;
+        c->sms = static_cast<uint32_t>(std::max(sms, 1));
+        uint64_t rows_of[65] = {};
+        for (const BuffChunkInfo& b : binfo)
+            if (!b.status) rows_of[b.bits] += b.n;
+        c->stream_bits = static_cast<uint32_t>(std::max_element(rows_of + 8, rows_of + 33) - rows_of);
     } else {
         if (c->scheme == EBI_GORILLA) c->stage_bytes = gorilla_stage_bytes(c->chunks.data(), c->n_chunks);
         if (c->scheme == EBI_ELF || c->scheme == EBI_ELF_ON_CHIMP) {
@@ -439,17 +476,34 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     }
     c->mask_words = (c->n_records + 63) / 64;
     if (c->mask_words == 0) c->mask_words = 1;
-    st = dev_alloc(&c->d_file, len + kFilePad, s);
+    st = dev_alloc(&c->d_file, dev_len + kFilePad, s);
+    uint8_t* raw = nullptr;       // BUFF: the file as read, repacked into d_file
+    RepackSeg* d_segs = nullptr;
+    if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&raw, len + kFilePad, s);
+    if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&d_segs, segs.size(), s);
+    std::vector<uint2> units;
+    if (c->scheme == EBI_BUFF) units = buff_units(c->chunks, c->first_unit);
+    if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&c->d_units, units.size(), s);
     if (!st) st = dev_alloc(&c->d_chunks, c->n_chunks, s);
     if (!st) st = dev_alloc(&c->d_tiles, c->tiles.tiles.size(), s);
     if (!st) st = dev_alloc(&c->d_acc, c->n_chunks, s);
     if (!st) st = dev_alloc(&c->d_res, 1, s);
     if (!st && !binfo.empty()) st = dev_alloc(&c->d_buff, binfo.size(), s);
-    if (!st) st = dev_alloc(&c->d_tot, 1, s);
+    // the scan totals and, behind them, one slot per CTA of a scan launch
+    if (!st) st = dev_alloc(&c->d_tot, (kScanTotalsBytes + sizeof(ScanTotals) - 1) / sizeof(ScanTotals), s);
     if (!st && !(c->h_res = g_pinned.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st) {
-        cudaError_t e = cudaMemcpyAsync(c->d_file, file, len, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(c->d_file + len, 0, kFilePad, s);
+        uint8_t* dst = raw ? raw : c->d_file;
+        cudaError_t e = cudaMemcpyAsync(dst, file, len, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(dst + len, 0, kFilePad, s);
+        if (e == cudaSuccess && raw) {
+            e = cudaMemsetAsync(c->d_file + dev_len, 0, kFilePad, s);
+            if (e == cudaSuccess && !segs.empty())
+                e = cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(RepackSeg), cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = launch_buff_repack(raw, c->d_file, d_segs, static_cast<uint32_t>(segs.size()), s);
+            if (e == cudaSuccess && !units.empty())
+                e = cudaMemcpyAsync(c->d_units, units.data(), units.size() * sizeof(uint2), cudaMemcpyHostToDevice, s);
+        }
         if (e == cudaSuccess && c->n_chunks)
             e = cudaMemcpyAsync(c->d_chunks, c->chunks.data(), c->n_chunks * sizeof(ChunkDesc), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && !c->tiles.tiles.empty())
@@ -460,10 +514,12 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         static const ScanTotals kRest = {0, 0.0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0};
         if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_tot, &kRest, sizeof kRest, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
-        // host sources (chunk table, tiles) must stay alive until the copies ran
+        // host sources (chunk table, tiles, segments) must stay alive until the copies ran
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) st = cuda_fail(e, "ebi_column_open upload");
     }
+    if (raw) cudaFreeAsync(raw, s);
+    if (d_segs) cudaFreeAsync(d_segs, s);
     if (st) { ebi_column_close(c); return st; }
     *out = c;
     return EBI_OK;
@@ -474,7 +530,7 @@ int ebi_column_close(ebi_column* c) {
     cudaStream_t s = c->stream;
     for (cudaEvent_t e : c->ev) if (e) cudaEventDestroy(e);
     void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
-                    c->d_scratch_mask, c->d_buff, c->d_tot};
+                    c->d_scratch_mask, c->d_buff, c->d_tot, c->d_units};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
     if (c->h_res) {
         cudaStreamSynchronize(s);  // no copy into the slot is pending when it is recycled

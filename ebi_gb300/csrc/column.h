@@ -34,12 +34,20 @@ struct ebi_column {
     ScanTotals* d_tot = nullptr;
     uint32_t buff_frac = 0;
     bool buff_fast_ok = false;
+    bool buff_exact = false;     // fast_ok and sum |value| over all rows < 2^52: every query's totals exact
+    // register-streaming scan (every readable chunk 8..32 bits wide)
+    bool stream_ok = false;
+    uint2* d_units = nullptr;
+    std::vector<uint32_t> first_unit;  // n_chunks + 1
+    uint32_t stream_bits = 0;    // most common width of the readable chunks
+    uint32_t sms = 0;            // SMs of the column's device
     bool fused_pending = false;  // the last query's kernel already folded into d_res
     uint32_t stage_bytes = 0;    // Gorilla: shared-memory staging per chunk
     const double* dec_tab = nullptr;  // Elf / ElfOnChimp: the device's decimal tables
     // segment timing (ebi_column_set_timing)
     bool timing = false;
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // query start, scan end, finalize end
+    // query start, scan end, finalize end, scan start
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     ebi_segment_times last{};
     uint64_t launches_at_start = 0;
 };

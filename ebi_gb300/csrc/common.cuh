@@ -32,12 +32,16 @@ struct ChunkDesc {
 constexpr uint32_t kChunkBadGeometry = 1;
 
 // BUFF chunk header facts, parsed on the host at open (query independent).
+// BUFF chunks live in HBM in the column's plane layout (buff_layout.cu),
+// not at their file offsets: every byte plane and the tail plane start on a
+// 128-byte boundary, planes `stride` bytes apart.
 struct BuffChunkInfo {
-    uint64_t planes;   // file offset of the first byte plane
-    uint64_t tail;     // file offset of the tail plane
+    uint64_t planes;   // device-buffer offset of the first byte plane
+    uint64_t tail;     // device-buffer offset of the tail plane
     int64_t base;      // fixed-point base
     uint32_t n, bits, frac;
     uint32_t status;   // error to raise when the chunk is read (0: readable)
+    uint64_t stride;   // bytes from one byte plane to the next
 };
 
 // Shared-memory ring of the pipelined BUFF scan.
@@ -72,9 +76,11 @@ struct ChunkAcc {
     uint32_t pad;
 };
 
-// Query-wide totals of the fused BUFF scan, combined with one set of atomics
-// per CTA; the last CTA folds them.  At rest (re-armed by that CTA):
-// zeros, max_fixed = INT64_MIN, min_fixed = INT64_MAX, bad_chunk = ~0.
+// Query-wide totals of the fused BUFF scans.  Every CTA stores its totals in
+// its own slot (kScanSlots of them follow this struct in the same
+// allocation, from byte kSlotOffset) and counts itself in `done`; the last CTA reduces the slots and
+// folds.  At rest (re-armed by that CTA): zeros, max_fixed = INT64_MIN,
+// min_fixed = INT64_MAX, bad_chunk = ~0.
 struct ScanTotals {
     unsigned long long sum_fixed;  // wrapping sum of every (CTA, chunk) piece of sum_with_bitmask's integer
     double abs_bound;              // sum of |piece|: bounds every chunk total and their prefix sums
@@ -83,8 +89,27 @@ struct ScanTotals {
     unsigned int done;             // CTAs finished
     unsigned int bad_chunk;        // lowest chunk index that raised an error
     unsigned int nonexact;         // a piece reached 2^53
-    unsigned int pad;
+    unsigned int next;             // streaming scan: the next unit to hand out
 };
+constexpr uint32_t kScanSlots = 1024;  // CTAs of one scan launch, at most
+
+// Running query totals of one warp (kept by lane 0), and of one CTA in its slot.
+struct alignas(16) WarpTot {
+    unsigned long long sum_fixed, count;
+    double abs_bound;
+    long long max_fixed, min_fixed;
+    unsigned int nonexact;
+};
+// The CTA slots start 64 bytes into the scan-totals allocation (16-byte loads
+// and stores of whole slots stay aligned).
+constexpr size_t kSlotOffset = 64;
+static_assert(sizeof(ScanTotals) <= kSlotOffset, "slots follow the totals");
+static_assert(sizeof(WarpTot) % 16 == 0, "whole 16-byte words per slot");
+__host__ __device__ inline WarpTot* scan_slots(ScanTotals* T) {
+    return reinterpret_cast<WarpTot*>(reinterpret_cast<char*>(T) + kSlotOffset);
+}
+constexpr size_t kScanTotalsBytes = kSlotOffset + kScanSlots * sizeof(WarpTot);
+
 
 struct QueryResult {
     uint32_t status;       // status of the first failing chunk in chunk order

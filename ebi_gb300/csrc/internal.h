@@ -44,6 +44,36 @@ cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_
 cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles,
                                     const unsigned long long* tile_offsets, uint64_t base_row, cudaStream_t s);
 
+// ---- register-streaming BUFF scan (buff_stream.cu) -------------------------
+// Columns whose readable chunks are all 8..32 bits wide.  A unit is 2,048
+// rows of one chunk ({chunk, first row}); chunk c owns units
+// [first_unit[c], first_unit[c + 1]).
+constexpr uint32_t kBuffUnitRows = 2048;
+std::vector<uint2> buff_units(const std::vector<ChunkDesc>& chunks, std::vector<uint32_t>& first_unit);
+// Filter / filter+agg / agg over units [unit_base, unit_base + n_units) with
+// persistent CTAs, by the kernel built for chunks `bits` wide (the column's
+// most common width; other widths run a slower general path); the last CTA
+// folds the query into *res as launch_buff_scan does.  fold: bit 0 the exact
+// integer total may apply (fast_ok of launch_buff_scan), bit 1 it always
+// applies (no per-chunk accumulators).
+cudaError_t launch_buff_stream(const QueryParams& q, const BuffChunkInfo* info, const uint2* units, uint32_t unit_base,
+                               uint32_t n_units, uint32_t bits, uint32_t sms, ScanTotals* T, QueryResult* res,
+                               uint32_t frac, uint32_t fold, cudaStream_t s);
+
+// ---- BUFF plane layout (buff_layout.cu) ------------------------------------
+// One copy of the repack at column open: len bytes from src + src_off to
+// dst + dst_off (dst_off 16-byte aligned; whole 16-byte words are written).
+struct RepackSeg {
+    uint64_t src_off, dst_off, len;
+};
+// Plane layout of a BUFF file: fills every readable chunk's planes / tail /
+// stride in `info` (device offsets), appends its copies to `segs` and returns
+// the device buffer size (before padding).
+uint64_t buff_plan_layout(std::vector<BuffChunkInfo>& info, std::vector<RepackSeg>& segs);
+// Copies the segments from the raw file image `src` (device memory) into `dst`.
+cudaError_t launch_buff_repack(const uint8_t* src, uint8_t* dst, const RepackSeg* d_segs, uint32_t n_segs,
+                               cudaStream_t s);
+
 // ---- value codecs: one CTA per chunk, modes of values.cuh (VAL_*) ----------
 // chunk_offsets[chunk - chunk_begin] (+1 entry) are the exclusive scan of a
 // VAL_COUNT pass; the count pass writes q.tile_counts[chunk - chunk_begin].

@@ -273,7 +273,9 @@ void ebi_free(void* p);
  * and SegmentKind, time.rs:11-22).  `scan` covers the codec kernels that read
  * the chunks (decode, compare, aggregate: the reference's Xor / BitPacking /
  * Decompression + CompareInsert + Sum segments), `finalize` the chunk-ordered
- * fold.  Filled only while timing is enabled (CUDA events on the query's stream). */
+ * fold, `total` the whole query from its first enqueued operation (output
+ * clears and chunk selection included).  Filled only while timing is enabled
+ * (CUDA events on the query's stream). */
 typedef struct {
     double scan_ms;
     double finalize_ms;

@@ -85,6 +85,23 @@ def test_random_layouts(layout, chunk):
     check_query_suite(data, preds, masks=masks, chunk_ids=(None, int(rng.integers(n_chunks)), n_chunks + 3))
 
 
+@pytest.mark.parametrize("order", ["narrow_first", "wide_first"])
+def test_mixed_chunk_widths(order):
+    # chunks of 10, 14, 21 and 31 bits in one column: the scan kernel is built
+    # for the most common width and runs the others through its general path
+    rng = np.random.default_rng(7 if order == "narrow_first" else 8)
+    parts = [np.round(rng.uniform(0, 1, 12_000), 3), np.round(rng.uniform(0, 16, 8_192), 3),
+             np.round(rng.uniform(-1000, 1000, 30_000), 3), np.round(rng.uniform(-1e6, 1e6, 9_000), 3)]
+    if order == "wide_first":
+        parts = parts[::-1]
+    v = np.concatenate(parts) + 0.0
+    data = enc(v, ("record_count", 4096), 1000)
+    masks = (None, random_mask(len(v), 0.3, rng), random_mask(len(v), 0.01, rng))
+    n_chunks = O.Decoder(data).n_chunks
+    check_query_suite(data, random_preds(v, rng, k=6), masks=masks,
+                      chunk_ids=(None, 0, int(rng.integers(n_chunks)), n_chunks - 1))
+
+
 @pytest.mark.parametrize("scale", [1, 10, 100, 10000])
 def test_scales(scale):
     rng = np.random.default_rng(scale)
