@@ -477,9 +477,21 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     c->mask_words = (c->n_records + 63) / 64;
     if (c->mask_words == 0) c->mask_words = 1;
     st = dev_alloc(&c->d_file, dev_len + kFilePad, s);
+    // BUFF: the planes are repacked into d_file straight from the caller's
+    // buffer when the device can read it (pinned host memory: one pass over
+    // the host link), else from a device copy of the file
+    const uint8_t* src = nullptr;
+    if (c->scheme == EBI_BUFF) {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, file) == cudaSuccess &&
+            (pa.type == cudaMemoryTypeHost || pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged) &&
+            pa.devicePointer)
+            src = static_cast<const uint8_t*>(pa.devicePointer);
+        cudaGetLastError();  // a pageable pointer is not an error here
+    }
     uint8_t* raw = nullptr;       // BUFF: the file as read, repacked into d_file
     RepackSeg* d_segs = nullptr;
-    if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&raw, len + kFilePad, s);
+    if (!st && c->scheme == EBI_BUFF && !src) st = dev_alloc(&raw, len + kFilePad, s);
     if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&d_segs, segs.size(), s);
     std::vector<uint2> units;
     if (c->scheme == EBI_BUFF) units = buff_units(c->chunks, c->first_unit);
@@ -493,14 +505,19 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st) st = dev_alloc(&c->d_tot, (kScanTotalsBytes + sizeof(ScanTotals) - 1) / sizeof(ScanTotals), s);
     if (!st && !(c->h_res = g_pinned.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st) {
-        uint8_t* dst = raw ? raw : c->d_file;
-        cudaError_t e = cudaMemcpyAsync(dst, file, len, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(dst + len, 0, kFilePad, s);
-        if (e == cudaSuccess && raw) {
+        cudaError_t e = cudaSuccess;
+        if (!src) {
+            uint8_t* dst = raw ? raw : c->d_file;
+            e = cudaMemcpyAsync(dst, file, len, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(dst + len, 0, kFilePad, s);
+            if (raw) src = raw;
+        }
+        // the small tables first: a copy from pageable memory may hold the
+        // host until the stream reaches it, which must not wait for the repack
+        if (e == cudaSuccess && c->scheme == EBI_BUFF) {
             e = cudaMemsetAsync(c->d_file + dev_len, 0, kFilePad, s);
             if (e == cudaSuccess && !segs.empty())
                 e = cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(RepackSeg), cudaMemcpyHostToDevice, s);
-            if (e == cudaSuccess) e = launch_buff_repack(raw, c->d_file, d_segs, static_cast<uint32_t>(segs.size()), s);
             if (e == cudaSuccess && !units.empty())
                 e = cudaMemcpyAsync(c->d_units, units.data(), units.size() * sizeof(uint2), cudaMemcpyHostToDevice, s);
         }
@@ -514,6 +531,8 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         static const ScanTotals kRest = {0, 0.0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0};
         if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_tot, &kRest, sizeof kRest, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
+        if (e == cudaSuccess && c->scheme == EBI_BUFF)
+            e = launch_buff_repack(src, c->d_file, d_segs, static_cast<uint32_t>(segs.size()), s);
         // host sources (chunk table, tiles, segments) must stay alive until the copies ran
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) st = cuda_fail(e, "ebi_column_open upload");

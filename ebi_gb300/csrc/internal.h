@@ -61,14 +61,14 @@ cudaError_t launch_buff_stream(const QueryParams& q, const BuffChunkInfo* info, 
                                uint32_t frac, uint32_t fold, cudaStream_t s);
 
 // ---- BUFF plane layout (buff_layout.cu) ------------------------------------
-// One copy of the repack at column open: len bytes from src + src_off to
-// dst + dst_off (dst_off 16-byte aligned; whole 16-byte words are written).
+// One block of the repack at column open: `len` 16-byte words from
+// src + src_off to dst + dst_off (dst_off 16-byte aligned).
 struct RepackSeg {
     uint64_t src_off, dst_off, len;
 };
 // Plane layout of a BUFF file: fills every readable chunk's planes / tail /
-// stride in `info` (device offsets), appends its copies to `segs` and returns
-// the device buffer size (before padding).
+// stride in `info` (device offsets), appends its copies (as blocks of at most
+// 64 KB) to `segs` and returns the device buffer size (before padding).
 uint64_t buff_plan_layout(std::vector<BuffChunkInfo>& info, std::vector<RepackSeg>& segs);
 // Copies the segments from the raw file image `src` (device memory) into `dst`.
 cudaError_t launch_buff_repack(const uint8_t* src, uint8_t* dst, const RepackSeg* d_segs, uint32_t n_segs,

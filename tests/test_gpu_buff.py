@@ -102,6 +102,26 @@ def test_mixed_chunk_widths(order):
                       chunk_ids=(None, 0, int(rng.integers(n_chunks)), n_chunks - 1))
 
 
+@pytest.mark.parametrize("chunk", [("record_count", 65536), ("record_count", 1000), ("byte_size", 30000)])
+def test_open_from_pinned_host_memory(chunk):
+    # a pinned file is repacked by the device straight from host memory; the
+    # result equals opening the same bytes from pageable memory
+    import torch
+    rng = np.random.default_rng(5)
+    v = np.concatenate([np.round(rng.uniform(-1000, 1000, 50_003), 3), np.round(rng.uniform(0, 1, 7_000), 3)]) + 0.0
+    data = bytes(enc(v, chunk, 1000))
+    for offset in (0, 3, 8):  # the caller's buffer at several alignments
+        pinned = torch.zeros(len(data) + offset, dtype=torch.uint8).pin_memory()
+        pinned[offset:] = torch.frombuffer(bytearray(data), dtype=torch.uint8)
+        a = E.Decoder(pinned[offset:])
+        b = E.Decoder(data)
+        assert same_f64(a.materialize().cpu().numpy(), b.materialize().cpu().numpy())
+        p = E.Predicate.range(E.RangeValue.inclusive(-10.0), E.RangeValue.exclusive(600.0))
+        ma, sa, mna, mxa, na = a.filter_agg(p)
+        mb, sb, mnb, mxb, nb = b.filter_agg(p)
+        assert np.array_equal(mask_np(ma), mask_np(mb)) and (sa, mna, mxa, na) == (sb, mnb, mxb, nb)
+
+
 @pytest.mark.parametrize("scale", [1, 10, 100, 10000])
 def test_scales(scale):
     rng = np.random.default_rng(scale)
