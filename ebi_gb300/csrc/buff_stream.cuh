@@ -237,8 +237,13 @@ __device__ __forceinline__ uint32_t run_chunk(const QueryParams& q, const Stream
             add_group(part, o);
             if (store) {
                 const uint64_t row = k.row_off + g0;
-                if (!q.out_atomic || o.w0) store_mask_word(q.out_mask, row, o.w0, q.out_atomic);
-                if (left > 32 && (!q.out_atomic || o.w1)) store_mask_word(q.out_mask, row + 32, o.w1, q.out_atomic);
+                if (!q.out_atomic && left >= 64 && (row & 63) == 0) {
+                    // one 8-byte store: a warp's 64 words go out as one coalesced 256-byte store
+                    *reinterpret_cast<uint2*>(q.out_mask + (row >> 5)) = make_uint2(o.w0, o.w1);
+                } else {
+                    if (!q.out_atomic || o.w0) store_mask_word(q.out_mask, row, o.w0, q.out_atomic);
+                    if (left > 32 && (!q.out_atomic || o.w1)) store_mask_word(q.out_mask, row + 32, o.w1, q.out_atomic);
+                }
             }
         }
     }
@@ -314,7 +319,7 @@ __device__ __forceinline__ uint32_t run_chunk_any(const QueryParams& q, const St
 template <int NP, int TB>
 __global__ void __launch_bounds__(kStreamThreads, NP <= 2 ? 3 : 2)
 buff_stream_kernel(QueryParams q, const BuffChunkInfo* info, const uint2* __restrict__ units, uint32_t unit_base,
-                   uint32_t n_units, ScanTotals* T, QueryResult* res, uint32_t frac, uint32_t fold) {
+                   uint32_t n_units, uint32_t upc, ScanTotals* T, QueryResult* res, uint32_t frac, uint32_t fold) {
     __shared__ WarpTot wtot[kStreamWarps];
     const bool exact = (fold & 2u) != 0;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -338,7 +343,10 @@ buff_stream_kernel(QueryParams q, const BuffChunkInfo* info, const uint2* __rest
         if (u >= n_units) break;
         const uint32_t ue = u + kStreamBatch < n_units ? u + kStreamBatch : n_units;
         while (u < ue) {
-            const uint2 un = units[unit_base + u];
+            // (chunk, first row) of unit u: by arithmetic when every chunk but
+            // the last holds upc units, else from the unit table
+            const uint2 un = upc ? make_uint2(unit_base / upc + u / upc, (u % upc) * kBuffUnitRows)
+                                 : units[unit_base + u];
             if (un.x != k.chunk) {
                 if (k.chunk != 0xffffffffu) {
                     Partial p64{part.sum, part.cnt, part.mx, part.cnt ? part.mn : ~0ull};
@@ -372,9 +380,10 @@ buff_stream_kernel(QueryParams q, const BuffChunkInfo* info, const uint2* __rest
 // Launch of the kernel for widths NP * 8 + TB (instantiated by buff_stream_np{1,2,3,4}.cu).
 template <int NP, int TB>
 cudaError_t launch_stream_kernel(const QueryParams& q, const BuffChunkInfo* info, const uint2* units, uint32_t unit_base,
-                                 uint32_t n_units, uint32_t grid, ScanTotals* T, QueryResult* res, uint32_t frac,
-                                 uint32_t fold, cudaStream_t s) {
-    buff_stream_kernel<NP, TB><<<grid, kStreamThreads, 0, s>>>(q, info, units, unit_base, n_units, T, res, frac, fold);
+                                 uint32_t n_units, uint32_t upc, uint32_t grid, ScanTotals* T, QueryResult* res,
+                                 uint32_t frac, uint32_t fold, cudaStream_t s) {
+    buff_stream_kernel<NP, TB><<<grid, kStreamThreads, 0, s>>>(q, info, units, unit_base, n_units, upc, T, res, frac,
+                                                               fold);
     count_launch();
     return cudaGetLastError();
 }

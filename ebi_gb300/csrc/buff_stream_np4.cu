@@ -5,10 +5,10 @@
 namespace ebi {
 
 cudaError_t launch_buff_stream_np4(uint32_t tb, const QueryParams& q, const BuffChunkInfo* info, const uint2* units,
-                                   uint32_t unit_base, uint32_t n_units, uint32_t grid, ScanTotals* T,
+                                   uint32_t unit_base, uint32_t n_units, uint32_t upc, uint32_t grid, ScanTotals* T,
                                    QueryResult* res, uint32_t frac, uint32_t fold, cudaStream_t s) {
     switch (tb) {
-    case 0: return launch_stream_kernel<4, 0>(q, info, units, unit_base, n_units, grid, T, res, frac, fold, s);
+    case 0: return launch_stream_kernel<4, 0>(q, info, units, unit_base, n_units, upc, grid, T, res, frac, fold, s);
     default: return cudaErrorInvalidValue;
     }
 }

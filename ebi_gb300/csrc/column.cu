@@ -308,7 +308,7 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
             const uint32_t ub = chunk_id < 0 ? 0u : c->first_unit[chunk_id];
             const uint32_t un = chunk_id < 0 ? c->first_unit.back() : c->first_unit[chunk_id + 1] - ub;
             const uint32_t fold = (c->buff_fast_ok ? 1u : 0u) | (c->buff_exact ? 2u : 0u);
-            CK(launch_buff_stream(q, c->d_buff, c->d_units, ub, un, c->stream_bits, c->sms, c->d_tot, c->d_res,
+            CK(launch_buff_stream(q, c->d_buff, c->d_units, ub, un, c->units_per_chunk, c->stream_bits, c->sms, c->d_tot, c->d_res,
                                   c->buff_frac, fold, s));
             c->fused_pending = true;
         } else {
@@ -494,7 +494,10 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st && c->scheme == EBI_BUFF && !src) st = dev_alloc(&raw, len + kFilePad, s);
     if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&d_segs, segs.size(), s);
     std::vector<uint2> units;
-    if (c->scheme == EBI_BUFF) units = buff_units(c->chunks, c->first_unit);
+    if (c->scheme == EBI_BUFF) {
+        units = buff_units(c->chunks, c->first_unit);
+        c->units_per_chunk = buff_uniform_units(c->first_unit);
+    }
     if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&c->d_units, units.size(), s);
     if (!st) st = dev_alloc(&c->d_chunks, c->n_chunks, s);
     if (!st) st = dev_alloc(&c->d_tiles, c->tiles.tiles.size(), s);
@@ -528,7 +531,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
                                 cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && !binfo.empty())
             e = cudaMemcpyAsync(c->d_buff, binfo.data(), binfo.size() * sizeof(BuffChunkInfo), cudaMemcpyHostToDevice, s);
-        static const ScanTotals kRest = {0, 0.0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0};
+        static const ScanTotals kRest = {0, 0.0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0, 0};
         if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_tot, &kRest, sizeof kRest, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
         if (e == cudaSuccess && c->scheme == EBI_BUFF)

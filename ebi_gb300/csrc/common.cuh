@@ -89,7 +89,8 @@ struct ScanTotals {
     unsigned int done;             // CTAs finished
     unsigned int bad_chunk;        // lowest chunk index that raised an error
     unsigned int nonexact;         // a piece reached 2^53
-    unsigned int next;             // streaming scan: the next unit to hand out
+    unsigned int next;             // streaming scan: the next batch of units to hand out
+    unsigned int pad;
 };
 constexpr uint32_t kScanSlots = 1024;  // CTAs of one scan launch, at most
 

@@ -50,15 +50,20 @@ cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, u
 // [first_unit[c], first_unit[c + 1]).
 constexpr uint32_t kBuffUnitRows = 2048;
 std::vector<uint2> buff_units(const std::vector<ChunkDesc>& chunks, std::vector<uint32_t>& first_unit);
+// Units per chunk when every chunk but the last holds the same number of units
+// and the last no more, else 0.
+uint32_t buff_uniform_units(const std::vector<uint32_t>& first_unit);
 // Filter / filter+agg / agg over units [unit_base, unit_base + n_units) with
 // persistent CTAs, by the kernel built for chunks `bits` wide (the column's
 // most common width; other widths run a slower general path); the last CTA
 // folds the query into *res as launch_buff_scan does.  fold: bit 0 the exact
 // integer total may apply (fast_ok of launch_buff_scan), bit 1 it always
 // applies (no per-chunk accumulators).
+// upc: units per chunk when every chunk but the last holds exactly upc units
+// (and the last at most upc; unit_base a multiple of upc), else 0.
 cudaError_t launch_buff_stream(const QueryParams& q, const BuffChunkInfo* info, const uint2* units, uint32_t unit_base,
-                               uint32_t n_units, uint32_t bits, uint32_t sms, ScanTotals* T, QueryResult* res,
-                               uint32_t frac, uint32_t fold, cudaStream_t s);
+                               uint32_t n_units, uint32_t upc, uint32_t bits, uint32_t sms, ScanTotals* T,
+                               QueryResult* res, uint32_t frac, uint32_t fold, cudaStream_t s);
 
 // ---- BUFF plane layout (buff_layout.cu) ------------------------------------
 // One block of the repack at column open: `len` 16-byte words from
