@@ -104,7 +104,7 @@ int parse_file(const uint8_t* d, uint64_t len, ebi_column* c) {
     if (d[5] > 12) return fail(EBI_E_CONVERSION, "Failed to convert CompressionScheme");
     if (d[6] > 2) return fail(EBI_E_CONVERSION, "Failed to convert ChunkOptionKind");
     const int scheme = d[5];
-    const uint64_t fo = rd64(d + 14);
+    const uint64_t fo = rd64(d + 16);  // FileHeader::footer_offset (format.rs:143-151)
     if (fo > len || len - fo < 16) return fail(EBI_E_IO, "footer offset past the end of the file");
     const uint64_t nrec = rd64(d + fo), nch = rd64(d + fo + 8);
     const uint64_t p = fo + 16;

@@ -414,7 +414,7 @@ extern "C" int ebi_encode(const double* v, uint64_t n, int scheme, int kind, uin
         o.push_back(8);
         put64(o, scheme == EBI_BUFF ? scale : 8192);
         o.resize(o.size() + 16 + 9 * 16 + 4, 0);
-        for (int i = 0; i < 8; ++i) o[14 + i] = uint8_t(footer >> (8 * i));
+        for (int i = 0; i < 8; ++i) o[16 + i] = uint8_t(footer >> (8 * i));  // offset_of!(FileHeader, footer_offset)
         uint8_t* m = static_cast<uint8_t*>(std::malloc(o.size() ? o.size() : 1));
         if (!m) return EBI_E_OOM;
         std::memcpy(m, o.data(), o.size());

@@ -668,7 +668,7 @@ int ora_encode(const double* v, uint64_t n, int scheme, int chunk_kind, uint64_t
     ob_zero(&o, 16 + 9 * 16 + 4);          /* FileFooter3 */
     free(foot);
     if (o.oom) { free(o.p); return ORA_E_OOM; }
-    for (int i = 0; i < 8; ++i) o.p[14 + i] = (uint8_t)(footer_off >> (8 * i));
+    for (int i = 0; i < 8; ++i) o.p[16 + i] = (uint8_t)(footer_off >> (8 * i));  /* offset_of!(FileHeader, footer_offset) */
     *out = o.p; *out_len = o.len;
     return ORA_OK;
 }
@@ -698,7 +698,7 @@ int ora_open(const uint8_t* d, uint64_t len, ora_file** out) {
     if (d[5] > 12) return ORA_E_CONVERSION;          /* CompressionScheme */
     if (d[6] > 2) return ORA_E_CONVERSION;           /* ChunkOptionKind */
     int scheme = d[5];
-    uint64_t fo = rd_u64le(d + 14);
+    uint64_t fo = rd_u64le(d + 16);                  /* FileHeader::footer_offset (format.rs:143-151) */
     if (fo > len || len - fo < 16) return ORA_E_IO;
     uint64_t nrec = rd_u64le(d + fo), nch = rd_u64le(d + fo + 8);
     uint64_t p = fo + 16;

@@ -81,3 +81,27 @@ def test_encoder_empty_column():
 def test_encoder_rejects_bad_arguments():
     with pytest.raises(E.InvalidArgument):
         E.encode(np.ones(4), 99)
+
+
+@pytest.mark.parametrize("codec", ["uncompressed", "rle", "gorilla", "chimp", "chimp128", "elf_on_chimp", "elf", "buff"])
+@pytest.mark.parametrize("chunk", [("record_count", 1000), ("byte_size", 3000), ("full", 0)])
+def test_file_header_layout(codec, chunk):
+    # FileHeader (format.rs:143-172), repr(C, packed(1)): magic [u8; 4], FileConfig
+    # {field_type u8, compression_scheme u8, ChunkOption {kind u8, reserved u8,
+    # value u64}}, footer_offset u64 (byte 16, encoder.rs:126-128), version [u16; 3]
+    import struct
+    v = gen("walk", 5003, 3)
+    for data in (E.encode(v, codec, chunk, 1000 if codec == "buff" else 1),
+                 O.encode(v, codec, {"record_count": 1, "byte_size": 2, "full": 0}[chunk[0]], chunk[1],
+                          1000 if codec == "buff" else 1)):
+        magic, ftype, scheme, kind, reserved, value, footer, v0, v1, v2 = struct.unpack_from("<4sBBBBQQHHH", data, 0)
+        assert magic == b"EBI1" and ftype == 0 and reserved == 0
+        assert scheme == E.SCHEMES[codec] and kind == {"full": 0, "record_count": 1, "byte_size": 2}[chunk[0]]
+        assert value == (0 if chunk[0] == "full" else chunk[1])
+        assert (v0, v1, v2) == (0, 1, 14)
+        # FileFooter0 {number_of_records, number_of_chunks} at the footer offset
+        nrec, nch = struct.unpack_from("<QQ", data, footer)
+        assert nrec == len(v) and nch == O.Decoder(data).n_chunks
+        # the chunks fill the bytes between the 30-byte header and the footer
+        first_chunk, first_row = struct.unpack_from("<QQ", data, footer + 16)
+        assert first_chunk == 30 and first_row == 0
