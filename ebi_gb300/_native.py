@@ -12,7 +12,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libebi_gpu.so"
 
 # Every symbol include/ebi_gpu.h declares.
 EXPORTS = [
-    "ebi_column_open", "ebi_column_close", "ebi_column_num_records", "ebi_column_num_chunks",
+    "ebi_column_open", "ebi_column_open_file", "ebi_column_close", "ebi_column_num_records", "ebi_column_num_chunks",
     "ebi_column_scheme", "ebi_column_chunk_info", "ebi_column_set_precision", "ebi_materialize",
     "ebi_filter", "ebi_filter_materialize", "ebi_sum", "ebi_min", "ebi_max", "ebi_filter_agg",
     "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches", "ebi_column_set_timing",
@@ -92,6 +92,7 @@ def lib() -> C.CDLL:
     vp, u64, i64, u64p, dp = C.c_void_p, C.c_uint64, C.c_int64, C.POINTER(C.c_uint64), C.POINTER(C.c_double)
     PP = C.POINTER(Predicate)
     L.ebi_column_open.argtypes = [C.c_char_p, u64, vp, C.POINTER(vp)]
+    L.ebi_column_open_file.argtypes = [C.c_char_p, vp, C.POINTER(vp)]
     L.ebi_column_close.argtypes = [vp]
     for fn in (L.ebi_column_num_records, L.ebi_column_num_chunks):
         fn.argtypes = [vp]

@@ -12,6 +12,7 @@ A bitmask is an int64 tensor of ceil(n_records / 64) words (bit r % 64 of word r
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 from typing import Optional
 
@@ -154,15 +155,20 @@ def _torch():
 
 
 class Decoder:
-    """Decoder::new over an in-memory EBI1 file; the file stays resident on the GPU."""
+    """Decoder::new over an in-memory EBI1 file (bytes, or a host uint8 tensor;
+    Decoder.from_file reads a path); the column stays resident on the GPU."""
 
-    def __init__(self, data, device: str = "cuda:0", stream=None):
+    def __init__(self, data, device: str = "cuda:0", stream=None, _path=None):
         torch = _torch()
         self.device = torch.device(device)
         self._stream = stream
         L = _native.lib()
         h = C.c_void_p()
         with torch.cuda.device(self.device):
+            if _path is not None:  # Decoder::new(DecoderInput::from_file(path))
+                _check(L.ebi_column_open_file(os.fsencode(_path), self._sp(), C.byref(h)), "Decoder::new")
+                self._h = h
+                return
             if isinstance(data, torch.Tensor):  # host uint8 tensor (pinned for async copies)
                 assert data.dtype == torch.uint8 and not data.is_cuda
                 ptr, n = C.cast(data.data_ptr(), C.c_char_p), data.numel()
@@ -172,6 +178,12 @@ class Decoder:
                 ptr, n = buf, len(buf)
             _check(L.ebi_column_open(ptr, n, self._sp(), C.byref(h)), "Decoder::new")
         self._h = h
+
+    @classmethod
+    def from_file(cls, path, device: str = "cuda:0", stream=None):
+        """Decoder::new(DecoderInput::from_file(path)): the file is read into
+        pinned host memory and moved to HBM (BUFF planes in one device pass)."""
+        return cls(None, device=device, stream=stream, _path=path)
 
     def _sp(self):
         torch = _torch()

@@ -547,6 +547,44 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     return EBI_OK;
 }
 
+// The staging buffer of ebi_column_open_file: pinned, grown on demand, kept.
+namespace {
+std::mutex g_file_mu;
+uint8_t* g_file_buf = nullptr;
+uint64_t g_file_cap = 0;
+}  // namespace
+
+int ebi_column_open_file(const char* path, void* stream, ebi_column** out) {
+    if (!path || !out) return fail(EBI_E_INVALID, "path or out is null");
+    *out = nullptr;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(EBI_E_IO, std::string("cannot open ") + path);
+    uint64_t len = 0;
+    if (std::fseek(f, 0, SEEK_END) == 0) {
+        const long n = std::ftell(f);
+        len = n > 0 ? static_cast<uint64_t>(n) : 0;
+    }
+    std::rewind(f);
+    std::lock_guard<std::mutex> lock(g_file_mu);
+    if (len > g_file_cap) {
+        if (g_file_buf) cudaFreeHost(g_file_buf);
+        g_file_buf = nullptr;
+        g_file_cap = 0;
+        void* p = nullptr;
+        if (cudaHostAlloc(&p, len, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            std::fclose(f);
+            return fail(EBI_E_OOM, "pinned staging allocation failed");
+        }
+        g_file_buf = static_cast<uint8_t*>(p);
+        g_file_cap = len;
+    }
+    const uint64_t got = len ? std::fread(g_file_buf, 1, len, f) : 0;
+    std::fclose(f);
+    if (got != len) return fail(EBI_E_IO, std::string("short read of ") + path);
+    return ebi_column_open(g_file_buf, len, stream, out);
+}
+
 int ebi_column_close(ebi_column* c) {
     if (!c) return EBI_OK;
     cudaStream_t s = c->stream;

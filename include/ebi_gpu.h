@@ -79,6 +79,13 @@ typedef struct ebi_column ebi_column;
  * decoder.rs:131-220) and copies the file to device memory on `stream`.
  * `file` may be pageable or pinned host memory; it is not used after return. */
 int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column** out);
+/* Decoder::new(DecoderInput::from_file(path)) (api/decoder.rs:136-156,
+ * DecoderInput::from_file :66-79): reads the EBI1 file at `path` into a
+ * process-wide pinned staging buffer and opens it as ebi_column_open does
+ * (BUFF planes go from that buffer to HBM in one device pass).  A file that
+ * cannot be opened or read is EBI_E_IO.  Opens from several threads take
+ * turns on the staging buffer. */
+int ebi_column_open_file(const char* path, void* stream, ebi_column** out);
 /* Drops the device copy (Decoder going out of scope). */
 int ebi_column_close(ebi_column* col);
 

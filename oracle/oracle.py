@@ -193,6 +193,12 @@ class Decoder:
         except Exception:
             pass
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     @property
     def n_records(self): return lib().ora_num_records(self._h)
     @property
