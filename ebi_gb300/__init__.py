@@ -8,7 +8,7 @@ engine is the C ABI of include/ebi_gpu.h (libebi_gpu.so); this package is its
 Python mirror of ebi's Decoder / Encoder API.
 """
 from . import _native
-from .api import (BUFF, CHIMP, CHIMP128, ELF, ELF_ON_CHIMP, GORILLA, RLE, SCHEMES, UNCOMPRESSED, Batch, ChunkId,
+from .api import (BUFF, CHIMP, Aggregation, AggregationKind, Expr, Op, CHIMP128, ELF, ELF_ON_CHIMP, GORILLA, RLE, SCHEMES, UNCOMPRESSED, Batch, ChunkId,
                   ConversionError,
                   CorruptChunk, CudaError, Decoder, DecoderError, InvalidArgument, IOError_, OutOfMemory,
                   Predicate, PreconditionsNotMet, Range, RangeValue, Server, UnexpectedEndOfChunk, Unsupported,
@@ -25,4 +25,5 @@ __all__ = [
     "CorruptChunk", "CudaError", "Decoder", "DecoderError", "InvalidArgument", "IOError_", "OutOfMemory",
     "Predicate", "PreconditionsNotMet", "Range", "RangeValue", "UnexpectedEndOfChunk", "Unsupported", "encode",
     "kernel_launches", "load_library", "Server", "run_plain", "mask_from_rows", "rows_from_mask",
+    "Aggregation", "AggregationKind", "Expr", "Op",
 ]

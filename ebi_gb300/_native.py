@@ -19,7 +19,7 @@ EXPORTS = [
     "ebi_column_last_times", "ebi_materialize_static", "ebi_batch_create", "ebi_batch_run",
     "ebi_batch_get_info", "ebi_batch_destroy", "ebi_server_create", "ebi_server_submit", "ebi_server_poll",
     "ebi_server_replay", "ebi_server_get_stats", "ebi_server_destroy", "ebi_run_plain", "ebi_mask_from_rows",
-    "ebi_rows_from_mask",
+    "ebi_rows_from_mask", "ebi_aggregate",
 ]
 
 
@@ -79,6 +79,17 @@ class SegmentTimes(C.Structure):
                 ("kernels", C.c_uint64)]
 
 
+class ExprNode(C.Structure):
+    """ebi_expr_node"""
+    _fields_ = [("kind", C.c_int32), ("index", C.c_uint32), ("literal", C.c_double)]
+
+
+class Aggregation(C.Structure):
+    """ebi_aggregation"""
+    _fields_ = [("kind", C.c_int32), ("n_nodes", C.c_uint32), ("nodes", C.POINTER(ExprNode)),
+                ("d_array", C.c_void_p), ("array_cap", C.c_uint64), ("scalar", C.c_double), ("n_array", C.c_uint64)]
+
+
 _lib = None
 
 
@@ -93,6 +104,7 @@ def lib() -> C.CDLL:
     PP = C.POINTER(Predicate)
     L.ebi_column_open.argtypes = [C.c_char_p, u64, vp, C.POINTER(vp)]
     L.ebi_column_open_file.argtypes = [C.c_char_p, vp, C.POINTER(vp)]
+    L.ebi_aggregate.argtypes = [C.POINTER(vp), C.c_uint32, C.POINTER(Aggregation), C.c_uint32, vp, vp]
     L.ebi_column_close.argtypes = [vp]
     for fn in (L.ebi_column_num_records, L.ebi_column_num_chunks):
         fn.argtypes = [vp]

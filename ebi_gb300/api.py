@@ -318,6 +318,145 @@ class Decoder:
         return out, val(s, "sum"), val(a, "min"), val(b, "max"), n.value
 
 
+# ---- multi-column aggregation (api/decoder.rs:755-917, decoder/expr.rs) ----------
+class Op:
+    """Op (decoder/expr.rs:11-29): one IEEE f64 operation."""
+    Add, Sub, Mul, Div = 2, 3, 4, 5
+
+
+class Expr:
+    """Expr (decoder/expr.rs:31-40): Expr.Index(i) is the decoders[i] column,
+    Expr.Literal(x) a constant, Expr.Binary(op, lhs, rhs) lhs OP rhs.  The
+    arithmetic operators build Binary nodes: (Expr.Index(0) * (1.0 - Expr.Index(1)))."""
+
+    __slots__ = ("kind", "index", "value", "op", "lhs", "rhs")
+
+    def __init__(self, kind, index=0, value=0.0, op=None, lhs=None, rhs=None):
+        self.kind, self.index, self.value, self.op, self.lhs, self.rhs = kind, index, value, op, lhs, rhs
+
+    @staticmethod
+    def Index(i: int) -> "Expr": return Expr("index", index=int(i))
+    @staticmethod
+    def Literal(x: float) -> "Expr": return Expr("literal", value=float(x))
+    @staticmethod
+    def Binary(op: int, lhs: "Expr", rhs: "Expr") -> "Expr": return Expr("binary", op=int(op), lhs=lhs, rhs=rhs)
+
+    @staticmethod
+    def _wrap(x) -> "Expr": return x if isinstance(x, Expr) else Expr.Literal(x)
+    def __add__(self, o): return Expr.Binary(Op.Add, self, Expr._wrap(o))
+    def __radd__(self, o): return Expr.Binary(Op.Add, Expr._wrap(o), self)
+    def __sub__(self, o): return Expr.Binary(Op.Sub, self, Expr._wrap(o))
+    def __rsub__(self, o): return Expr.Binary(Op.Sub, Expr._wrap(o), self)
+    def __mul__(self, o): return Expr.Binary(Op.Mul, self, Expr._wrap(o))
+    def __rmul__(self, o): return Expr.Binary(Op.Mul, Expr._wrap(o), self)
+    def __truediv__(self, o): return Expr.Binary(Op.Div, self, Expr._wrap(o))
+    def __rtruediv__(self, o): return Expr.Binary(Op.Div, Expr._wrap(o), self)
+
+    def max_chunk_reader_index(self):
+        """Expr::max_chunk_reader_index (expr.rs:43-58)."""
+        if self.kind == "literal":
+            return None
+        if self.kind == "index":
+            return self.index
+        ids = [i for i in (self.lhs.max_chunk_reader_index(), self.rhs.max_chunk_reader_index()) if i is not None]
+        return max(ids) if ids else None
+
+    def postfix(self):
+        """[(EBI_EXPR_* kind, index, literal), ...] in postfix order."""
+        if self.kind == "index":
+            return [(0, self.index, 0.0)]
+        if self.kind == "literal":
+            return [(1, 0, self.value)]
+        return self.lhs.postfix() + self.rhs.postfix() + [(self.op, 0, 0.0)]
+
+    def __repr__(self):
+        if self.kind == "index":
+            return f"Index({self.index})"
+        if self.kind == "literal":
+            return f"Literal({self.value!r})"
+        return f"({self.lhs!r} {'+-*/'[self.op - 2]} {self.rhs!r})"
+
+
+class AggregationKind:
+    """AggregationKind (api/decoder.rs:755-761)."""
+    NONE, MAX, MIN, SUM = 0, 1, 2, 3
+
+
+class Aggregation:
+    """Aggregation { kind, expr } (api/decoder.rs:840-917) over resident
+    columns: compute() returns a float (Max / Min / Sum) or, for
+    AggregationKind.NONE, the device tensor of the values (the reference's
+    AggregationResult::Array)."""
+
+    def __init__(self, kind: int, expr: Expr):
+        self.kind, self.expr = int(kind), expr
+
+    @classmethod
+    def new(cls, kind, expr): return cls(kind, expr)
+    @classmethod
+    def sum(cls, expr): return cls(AggregationKind.SUM, expr)
+    @classmethod
+    def min(cls, expr): return cls(AggregationKind.MIN, expr)
+    @classmethod
+    def max(cls, expr): return cls(AggregationKind.MAX, expr)
+    @classmethod
+    def none(cls, expr): return cls(AggregationKind.NONE, expr)
+
+    def compute(self, decoders, bitmask=None):
+        """Aggregation::compute (api/decoder.rs:858-879)."""
+        return Aggregation.compute_multiple([self], decoders, bitmask)[0]
+
+    @staticmethod
+    def compute_multiple(aggregations, decoders, bitmask=None):
+        """Aggregation::compute_multiple (api/decoder.rs:881-916)."""
+        torch = _torch()
+        if not decoders:
+            raise InvalidArgument("Aggregation::compute: no decoders", InvalidArgument.code)
+        d0 = decoders[0]
+        hs = (C.c_void_p * len(decoders))(*[d._h for d in decoders])
+        mask_ptr, keep = None, None
+        if bitmask is not None:
+            words = max(max(d.mask_words for d in decoders), 1)
+            if isinstance(bitmask, torch.Tensor):
+                keep = bitmask.to(d0.device, dtype=torch.int64).contiguous()
+            else:
+                keep = torch.from_numpy(np.ascontiguousarray(bitmask, dtype=np.uint64).view(np.int64)).to(d0.device)
+            if keep.numel() < words:
+                keep = torch.cat([keep, keep.new_zeros(words - keep.numel())])
+            mask_ptr = C.c_void_p(keep.data_ptr())
+        n = len(aggregations)
+        arr = (_native.Aggregation * max(n, 1))()
+        node_bufs, outs = [], []
+        for i, g in enumerate(aggregations):
+            pf = g.expr.postfix()
+            nodes = (_native.ExprNode * len(pf))(*[_native.ExprNode(k, ix, float(x)) for k, ix, x in pf])
+            node_bufs.append(nodes)
+            arr[i].kind = g.kind
+            arr[i].n_nodes = len(pf)
+            arr[i].nodes = nodes
+            out = None
+            if g.kind == AggregationKind.NONE:
+                cap = max(d.n_records for d in decoders)
+                out = torch.empty(max(cap, 1), dtype=torch.float64, device=d0.device)
+                arr[i].d_array = C.c_void_p(out.data_ptr())
+                arr[i].array_cap = cap
+            outs.append(out)
+        with torch.cuda.device(d0.device):
+            rc = _native.lib().ebi_aggregate(hs, len(decoders), arr, n, mask_ptr, d0._sp())
+            if rc == InvalidArgument.code and any(
+                    g.kind == AggregationKind.NONE and arr[i].n_array > arr[i].array_cap
+                    for i, g in enumerate(aggregations)):
+                for i, g in enumerate(aggregations):  # decoded chunks held more values than their row counts
+                    if g.kind == AggregationKind.NONE:
+                        outs[i] = torch.empty(max(arr[i].n_array, 1), dtype=torch.float64, device=d0.device)
+                        arr[i].d_array = C.c_void_p(outs[i].data_ptr())
+                        arr[i].array_cap = arr[i].n_array
+                rc = _native.lib().ebi_aggregate(hs, len(decoders), arr, n, mask_ptr, d0._sp())
+            _check(rc, "Aggregation::compute_multiple")
+        return [outs[i][: arr[i].n_array] if g.kind == AggregationKind.NONE else arr[i].scalar
+                for i, g in enumerate(aggregations)]
+
+
 _AGG_BITS = {"sum": 1, "min": 2, "max": 4}
 
 

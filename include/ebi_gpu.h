@@ -263,6 +263,58 @@ int ebi_server_destroy(ebi_server* server);
 int ebi_run_plain(ebi_column* const* columns, uint32_t n_columns, const ebi_request* reqs, uint64_t n,
                   ebi_response* out, void* stream);
 
+/* ---- multi-column aggregation ---------------------------------------------- */
+
+/* Expr (decoder/expr.rs:31-40) in postfix order: an EBI_EXPR_INDEX node
+ * (column `index` of the call's column list) or an EBI_EXPR_LITERAL node
+ * pushes a value; an operator node pops rhs, then lhs, and pushes lhs OP rhs
+ * (Op::doit, expr.rs:19-28: one IEEE f64 operation, never fused). */
+enum { EBI_EXPR_INDEX = 0, EBI_EXPR_LITERAL = 1, EBI_EXPR_ADD = 2, EBI_EXPR_SUB = 3, EBI_EXPR_MUL = 4,
+       EBI_EXPR_DIV = 5 };
+#define EBI_EXPR_MAX_NODES 64
+typedef struct {
+    int32_t kind;     /* EBI_EXPR_*              */
+    uint32_t index;   /* EBI_EXPR_INDEX: column  */
+    double literal;   /* EBI_EXPR_LITERAL: value */
+} ebi_expr_node;
+
+/* AggregationKind (api/decoder.rs:755-761) */
+enum { EBI_AGGR_NONE = 0, EBI_AGGR_MAX = 1, EBI_AGGR_MIN = 2, EBI_AGGR_SUM = 3 };
+
+/* Aggregation { kind, expr } (api/decoder.rs:840-856) with its result:
+ * AggregationResult::Scalar in `scalar`, or for EBI_AGGR_NONE the
+ * AggregationResult::Array written to the DEVICE buffer d_array (array_cap
+ * values; n_array is the count, set even when the buffer is too small). */
+typedef struct {
+    int32_t kind;                 /* EBI_AGGR_*                                */
+    uint32_t n_nodes;             /* 1 .. EBI_EXPR_MAX_NODES                   */
+    const ebi_expr_node* nodes;   /* host, postfix                             */
+    double* d_array;              /* EBI_AGGR_NONE: device output              */
+    uint64_t array_cap;
+    double scalar;                /* out: Max / Min / Sum                      */
+    uint64_t n_array;             /* out: EBI_AGGR_NONE                        */
+} ebi_aggregation;
+
+/* Aggregation::compute_multiple (api/decoder.rs:881-916); n_aggs = 1 is
+ * Aggregation::compute (:858-879).  An aggregation whose expression is a bare
+ * Index runs that column's own sum / min / max (in-situ, as
+ * AggregationKind::dispatch does); the others are evaluated chunk by chunk
+ * over cols[0]'s chunk count: in chunk i every Index leaf stands for the
+ * values of its column's chunk i selected by the mask, the operands of an
+ * operator are zipped to the shorter one (Expr::compute_chunk,
+ * expr.rs:67-135), and the chunk results combine in chunk order
+ * (AggregationResult::concat).  Sums are compensated (Neumaier), within 1e-12
+ * of the reference's per-chunk sequential sums relative to the sum of
+ * magnitudes; min / max ignore NaN operands as f64::min / f64::max do.
+ * d_mask (device, NULL = None) covers the rows of every column read.
+ * Errors: EBI_E_PRECONDITION for a Literal root or an operator over two
+ * literals (when cols[0] has chunks); EBI_E_INVALID where the reference
+ * panics (an index past n_cols, a column with fewer chunks than cols[0]) or
+ * for a malformed program; EBI_E_UNSUPPORTED for EBI_AGGR_NONE over a bare
+ * Index (the reference's todo!()). */
+int ebi_aggregate(ebi_column* const* cols, uint32_t n_cols, ebi_aggregation* aggs, uint32_t n_aggs,
+                  const uint64_t* d_mask, void* stream);
+
 /* ---- encoder (host) -------------------------------------------------------- */
 
 /* Encoder::new(.., chunk_option, compressor_config).encode()

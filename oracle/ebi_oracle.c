@@ -1719,3 +1719,139 @@ int ora_filter_agg(ora_file* f, const ora_pred* p, const uint64_t* mask, int64_t
     free_job(&j);
     return st;
 }
+
+/* ------------------------------------------------------------------------ */
+/* multi-column aggregation (api/decoder.rs:755-917, decoder/expr.rs:11-135) */
+/* ------------------------------------------------------------------------ */
+typedef struct { int32_t kind; uint32_t index; double lit; int32_t lhs, rhs; } enode;
+
+/* Postfix nodes -> tree (children by index); returns the root or -1. */
+static int32_t expr_tree(const ora_expr_node* nodes, uint32_t n, enode* t) {
+    int32_t* st = (int32_t*)malloc((n ? n : 1) * sizeof(int32_t));
+    if (!st) return -1;
+    uint32_t sp = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        t[i].kind = nodes[i].kind; t[i].index = nodes[i].index; t[i].lit = nodes[i].literal;
+        t[i].lhs = t[i].rhs = -1;
+        if (nodes[i].kind == ORA_EXPR_INDEX || nodes[i].kind == ORA_EXPR_LITERAL) { st[sp++] = (int32_t)i; continue; }
+        if (nodes[i].kind < ORA_EXPR_ADD || nodes[i].kind > ORA_EXPR_DIV || sp < 2) { free(st); return -1; }
+        t[i].rhs = st[--sp];
+        t[i].lhs = st[--sp];
+        st[sp++] = (int32_t)i;
+    }
+    int32_t root = sp == 1 ? st[0] : -1;
+    free(st);
+    return root;
+}
+
+/* Op::doit (expr.rs:19-28) */
+static inline double op_doit(int32_t op, double l, double r) {
+    switch (op) {
+    case ORA_EXPR_ADD: return l + r;
+    case ORA_EXPR_SUB: return l - r;
+    case ORA_EXPR_MUL: return l * r;
+    default: return l / r;
+    }
+}
+
+/* The selected values of one chunk (GeneralChunkReader::materialize with the
+ * bitmask; an empty intersection materializes nothing). */
+static int chunk_vals(ora_file* f, const uint64_t* mask, uint64_t c, dvec* out) {
+    job_t j = {0};
+    j.f = f; j.op = OP_MATERIALIZE; j.mask = mask;
+    int st = run_job(&j, (int64_t)c, 1);
+    out->v = NULL; out->n = out->cap = 0;
+    if (!st && j.nsel == 1) { *out = j.res[0].vals; j.res[0].vals.v = NULL; j.res[0].vals.n = 0; }
+    free_job(&j);
+    return st;
+}
+
+/* Expr::compute_chunk (expr.rs:67-135) */
+static int expr_chunk(ora_file* const* files, const enode* t, int32_t k, const uint64_t* mask, uint64_t c,
+                      dvec* out) {
+    const enode* e = &t[k];
+    if (e->kind == ORA_EXPR_LITERAL) return ORA_E_PRECONDITION;
+    if (e->kind == ORA_EXPR_INDEX) return chunk_vals(files[e->index], mask, c, out);
+    const enode *L = &t[e->lhs], *R = &t[e->rhs];
+    const int ll = L->kind == ORA_EXPR_LITERAL, rl = R->kind == ORA_EXPR_LITERAL;
+    if (ll && rl) return ORA_E_PRECONDITION;
+    if (!ll && !rl) {
+        dvec a, b;
+        int st = expr_chunk(files, t, e->lhs, mask, c, &a);
+        if (st) return st;
+        st = expr_chunk(files, t, e->rhs, mask, c, &b);
+        if (st) { free(a.v); return st; }
+        const uint64_t n = a.n < b.n ? a.n : b.n;  /* zip stops at the shorter */
+        for (uint64_t i = 0; i < n; ++i) a.v[i] = op_doit(e->kind, a.v[i], b.v[i]);
+        a.n = n;
+        free(b.v);
+        *out = a;
+        return ORA_OK;
+    }
+    int st = expr_chunk(files, t, ll ? e->rhs : e->lhs, mask, c, out);
+    if (st) return st;
+    for (uint64_t i = 0; i < out->n; ++i)
+        out->v[i] = ll ? op_doit(e->kind, L->lit, out->v[i]) : op_doit(e->kind, out->v[i], R->lit);
+    return ORA_OK;
+}
+
+int ora_aggregate(ora_file* const* files, uint32_t n_files, int kind, const ora_expr_node* nodes,
+                  uint32_t n_nodes, const uint64_t* mask, double* scalar, double* array, uint64_t cap,
+                  uint64_t* n_array) {
+    if (!files || n_files == 0 || !nodes || kind < ORA_AGGR_NONE || kind > ORA_AGGR_SUM) return ORA_E_INVALID;
+    enode* t = (enode*)malloc((n_nodes ? n_nodes : 1) * sizeof(enode));
+    if (!t) return ORA_E_OOM;
+    const int32_t root = expr_tree(nodes, n_nodes, t);
+    int st = root < 0 ? ORA_E_INVALID : ORA_OK;
+    for (uint32_t i = 0; !st && i < n_nodes; ++i)
+        if (t[i].kind == ORA_EXPR_INDEX && t[i].index >= n_files) st = ORA_E_INVALID;  /* decoders[i] panics */
+    if (st) { free(t); return st; }
+    if (n_array) *n_array = 0;
+    if (t[root].kind == ORA_EXPR_INDEX) {
+        /* in-situ dispatch (AggregationKind::dispatch, api/decoder.rs:816-828) */
+        free(t);
+        ora_file* f = files[nodes[root].index];
+        if (kind == ORA_AGGR_NONE) return ORA_E_INVALID;  /* todo!() */
+        if (kind == ORA_AGGR_SUM) return ora_sum(f, mask, -1, scalar, 1);
+        if (kind == ORA_AGGR_MIN) return ora_min(f, mask, -1, scalar, 1);
+        return ora_max(f, mask, -1, scalar, 1);
+    }
+    /* AggregationResult::zero (api/decoder.rs:773-780) */
+    double r = kind == ORA_AGGR_MAX ? -INFINITY : kind == ORA_AGGR_MIN ? INFINITY : 0.0;
+    uint64_t na = 0;
+    const uint64_t nc = files[0]->n_chunks;
+    for (uint64_t c = 0; !st && c < nc; ++c) {
+        for (uint32_t d = 0; d < n_files; ++d)
+            if (c >= files[d]->n_chunks) st = ORA_E_INVALID;  /* chunk_handles[i] panics */
+        if (st) break;
+        dvec v;
+        st = expr_chunk(files, t, root, mask, c, &v);
+        if (st) break;
+        /* dispatch_on_vec (api/decoder.rs:830-837), then concat (:791-808) */
+        if (kind == ORA_AGGR_NONE) {
+            if (array && na + v.n <= cap && v.n) memcpy(array + na, v.v, v.n * 8);
+            na += v.n;
+        } else if (kind == ORA_AGGR_SUM) {
+            double s = -0.0;  /* <f64 as Sum>: a sequential fold */
+            for (uint64_t i = 0; i < v.n; ++i) s += v.v[i];
+            r += s;
+        } else if (kind == ORA_AGGR_MAX) {
+            double m = -INFINITY;
+            for (uint64_t i = 0; i < v.n; ++i) m = fmax(m, v.v[i]);
+            r = fmax(r, m);
+        } else {
+            double m = INFINITY;
+            for (uint64_t i = 0; i < v.n; ++i) m = fmin(m, v.v[i]);
+            r = fmin(r, m);
+        }
+        free(v.v);
+    }
+    free(t);
+    if (st) return st;
+    if (kind == ORA_AGGR_NONE) {
+        if (n_array) *n_array = na;
+        return na > cap ? ORA_E_INVALID : ORA_OK;
+    }
+    if (scalar) *scalar = r;
+    return ORA_OK;
+}

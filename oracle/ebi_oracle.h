@@ -96,6 +96,30 @@ int ora_max(ora_file* f, const uint64_t* mask, int64_t chunk_id, double* out, in
 int ora_filter_agg(ora_file* f, const ora_pred* p, const uint64_t* mask, int64_t chunk_id,
                    uint64_t* out_mask, double* sum, double* mn, double* mx, int threads);
 
+/* ---- multi-column aggregation (api/decoder.rs:755-917, decoder/expr.rs) ---
+ * Expr (expr.rs:31-40) in postfix order: INDEX and LITERAL nodes push a
+ * value, an operator node pops rhs, then lhs, and pushes lhs OP rhs
+ * (Op::doit, expr.rs:19-28). */
+enum { ORA_EXPR_INDEX = 0, ORA_EXPR_LITERAL = 1, ORA_EXPR_ADD = 2, ORA_EXPR_SUB = 3, ORA_EXPR_MUL = 4,
+       ORA_EXPR_DIV = 5 };
+typedef struct { int32_t kind; uint32_t index; double literal; } ora_expr_node;
+/* AggregationKind (api/decoder.rs:755-761) */
+enum { ORA_AGGR_NONE = 0, ORA_AGGR_MAX = 1, ORA_AGGR_MIN = 2, ORA_AGGR_SUM = 3 };
+/* Aggregation::compute (api/decoder.rs:858-879): an Index expression runs
+ * that decoder's sum / min / max; any other expression is evaluated chunk by
+ * chunk over files[0]'s chunk count (Expr::compute_chunk, expr.rs:67-135:
+ * each Index leaf materializes its file's chunk under the mask, operands are
+ * zipped to the shorter one), aggregated per chunk (dispatch_on_vec) and
+ * combined in chunk order (AggregationResult::concat).  NONE writes the
+ * concatenated values to array (cap values; *n_array is set even when cap is
+ * too small, which fails with ORA_E_INVALID).  Errors: PRECONDITION for a
+ * Literal root or an operator over two literals, INVALID where the reference
+ * panics (index out of range, a file with fewer chunks than files[0]) or
+ * reaches todo!() (NONE over an Index root). */
+int ora_aggregate(ora_file* const* files, uint32_t n_files, int kind, const ora_expr_node* nodes,
+                  uint32_t n_nodes, const uint64_t* mask, double* scalar, double* array, uint64_t cap,
+                  uint64_t* n_array);
+
 /* ---- building blocks exposed for known-answer tests ---------------------- */
 /* BufferedBitReader::read_bits over buf (io/bit_read.rs:293-318); returns 1
  * and the value, or 0 when fewer than n bits remain.  *bitpos advances. */

@@ -49,6 +49,15 @@ def eq(v): return Pred(PRED_EQ, 0, 0, 0, float(v), 0.0, 0.0)
 def ne(v): return Pred(PRED_NE, 0, 0, 0, float(v), 0.0, 0.0)
 
 
+class ExprNode(C.Structure):
+    """ora_expr_node: one postfix node of an Expr (kind EXPR_*, column index, literal)."""
+    _fields_ = [("kind", C.c_int32), ("index", C.c_uint32), ("literal", C.c_double)]
+
+
+EXPR_INDEX, EXPR_LITERAL, EXPR_ADD, EXPR_SUB, EXPR_MUL, EXPR_DIV = range(6)
+AGGR_NONE, AGGR_MAX, AGGR_MIN, AGGR_SUM = range(4)
+
+
 def rng(start_kind=BOUND_NONE, start=0.0, end_kind=BOUND_NONE, end=0.0):
     return Pred(PRED_RANGE, start_kind, end_kind, 0, 0.0, float(start), float(end))
 
@@ -59,7 +68,7 @@ def build(force: bool = False) -> Path:
     newest = max(p.stat().st_mtime for p in SOURCES + [HERE / "ebi_oracle.h"])
     if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < newest:
         tmp = LIB_PATH.with_suffix(f".{os.getpid()}.tmp")
-        subprocess.run(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-o", str(tmp),
+        subprocess.run(["gcc", "-O3", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(tmp),
                         *map(str, SOURCES), "-lpthread", "-lm"], check=True)
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -102,6 +111,8 @@ def lib():
         L.ora_buff_fixed.restype = C.c_int64
         L.ora_buff_precision.argtypes = [C.c_uint64]
         L.ora_buff_precision.restype = C.c_int32
+        L.ora_aggregate.argtypes = [C.POINTER(C.c_void_p), C.c_uint32, C.c_int, C.POINTER(ExprNode), C.c_uint32,
+                                    C.c_void_p, dp, dp, C.c_uint64, u64p]
         _lib = L
     return _lib
 
@@ -279,3 +290,32 @@ def rows_from_mask(mask, n_records=None):
     if n_records is not None:
         rows = rows[rows < n_records]
     return rows.tolist()
+
+
+def aggregate(decoders, kind, postfix, bitmask=None):
+    """Aggregation::new(kind, expr).compute(decoders, bitmask) over oracle
+    Decoders; postfix = [(EXPR_*, index, literal), ...].  Returns a float, or
+    the concatenated values (numpy) for AGGR_NONE."""
+    hs = (C.c_void_p * len(decoders))(*[d._h.value if isinstance(d._h, C.c_void_p) else d._h for d in decoders])
+    nodes = (ExprNode * max(len(postfix), 1))(*[ExprNode(k, i, float(x)) for k, i, x in postfix])
+    keep = None
+    mp = None
+    if bitmask is not None:
+        keep = np.ascontiguousarray(bitmask, dtype=np.uint64)
+        mp = keep.ctypes.data_as(C.c_void_p)
+    out = C.c_double()
+    n = C.c_uint64()
+    if kind != AGGR_NONE:
+        _check(lib().ora_aggregate(hs, len(decoders), kind, nodes, len(postfix), mp, C.byref(out), None, 0,
+                                   C.byref(n)), "Aggregation::compute")
+        return out.value
+    cap = 0
+    while True:
+        arr = np.empty(max(cap, 1), dtype=np.float64)
+        rc = lib().ora_aggregate(hs, len(decoders), kind, nodes, len(postfix), mp, C.byref(out), _dptr(arr), cap,
+                                 C.byref(n))
+        if rc == 7 and n.value > cap:
+            cap = n.value
+            continue
+        _check(rc, "Aggregation::compute")
+        return arr[: n.value]

@@ -150,6 +150,49 @@ BUFF_PRECISION = {"src": "ebi/src/compression_common/buff.rs:36",
                   "scale_to_precision": [[1, 0], [10, 1], [100, 2], [1000, 3], [10000, 4]]}
 
 
+# --- Aggregation / Expr (ebi/tests/aggregation.rs:471-754) -----------------------------
+# Every column is encoded Uncompressed with RecordCount(3) (helper::decoder,
+# ebi/tests/aggregation.rs:172-188).  expr: ["index", i] | ["lit", x] |
+# [op, lhs, rhs] with op in add/sub/mul/div; kind: sum/min/max; bitmask: row ids.
+_I = lambda i: ["index", i]
+EXPR_CASES = [
+    {"src": "ebi/tests/aggregation.rs:471-479", "columns": [[0.0, 2.0, 3.0, 4.0, 5.0]],
+     "aggs": [{"kind": "sum", "expr": _I(0), "expect": 14.0}]},
+    {"src": "ebi/tests/aggregation.rs:485-509", "columns": [[0.0, 2.0, -3.0, 4.0, 7.0], [1.0, 2.0, 3.0, 4.0, 5.0]],
+     "aggs": [{"kind": "sum", "expr": ["add", ["mul", _I(0), _I(1)], _I(1)], "expect": 61.0}]},
+    {"src": "ebi/tests/aggregation.rs:512-519", "columns": [[0.0, 2.0, 3.0, 4.0, 5.0]],
+     "aggs": [{"kind": "sum", "expr": _I(0), "expect": 14.0}]},
+    {"src": "ebi/tests/aggregation.rs:522-543", "columns": [[0.0, 2.0, -3.0, 4.0, 7.0], [1.0, 2.0, 3.0, 4.0, 5.0]],
+     "aggs": [{"kind": "sum", "expr": ["add", ["mul", _I(0), _I(1)], _I(1)], "expect": 61.0}]},
+    {"src": "ebi/tests/aggregation.rs:547-554", "columns": [[1.0, 5.0, 2.0, 4.0]],
+     "aggs": [{"kind": "max", "expr": _I(0), "expect": 5.0}]},
+    {"src": "ebi/tests/aggregation.rs:557-571", "columns": [[1.0, 2.0, 3.0], [2.0, 1.0, 4.0]],
+     "aggs": [{"kind": "max", "expr": ["mul", _I(0), _I(1)], "expect": 12.0}]},
+    {"src": "ebi/tests/aggregation.rs:575-582", "columns": [[1.0, 5.0, 2.0, 4.0]],
+     "aggs": [{"kind": "min", "expr": _I(0), "expect": 1.0}]},
+    {"src": "ebi/tests/aggregation.rs:585-599", "columns": [[3.0, 1.0, 4.0], [2.0, 2.0, 1.0]],
+     "aggs": [{"kind": "min", "expr": ["sub", _I(0), _I(1)], "expect": -1.0}]},
+    {"src": "ebi/tests/aggregation.rs:603-614", "columns": [[0.0, 0.8, 0.3], [1.0, 1.0, 20.0]], "bitmask": [0, 1],
+     "aggs": [{"kind": "sum", "expr": _I(0), "expect": 0.8}]},
+    {"src": "ebi/tests/aggregation.rs:617-633", "columns": [[1.0, 2.2, 5.0, 4.0]], "bitmask": [0, 2],
+     "aggs": [{"kind": "sum", "expr": _I(0), "expect": 6.0}]},
+    {"src": "ebi/tests/aggregation.rs:636-663", "columns": [[1.0, 2.0, 3.0], [10.0, 20.0, 30.0]],
+     "aggs": [{"kind": "sum", "expr": _I(0), "expect": 6.0},
+              {"kind": "sum", "expr": ["add", _I(0), _I(1)], "expect": 66.0}]},
+    {"src": "ebi/tests/aggregation.rs:666-693", "columns": [[3.0, 8.0, 5.0], [2.0, 1.0, 7.0]],
+     "aggs": [{"kind": "max", "expr": _I(1), "expect": 7.0},
+              {"kind": "max", "expr": ["mul", _I(0), _I(1)], "expect": 35.0}]},
+    {"src": "ebi/tests/aggregation.rs:696-723", "columns": [[6.0, 2.0, 9.0], [1.0, 2.0, 3.0]],
+     "aggs": [{"kind": "min", "expr": _I(0), "expect": 2.0},
+              {"kind": "min", "expr": ["sub", _I(0), _I(1)], "expect": 0.0}]},
+    {"src": "ebi/tests/aggregation.rs:726-753", "columns": [[1.0, 0.0, 3.0, 4.0], [5.0, 6.0, 7.0, 8.0]],
+     "bitmask": [0, 2],
+     "aggs": [{"kind": "sum", "expr": _I(0), "expect": 4.0},
+              {"kind": "max", "expr": ["add", _I(0), _I(1)], "expect": 10.0}]},
+]
+EXPR_CHUNK = ["record_count", 3]
+
+
 def main():
     out = {
         "about": "Known-answer vectors transcribed from lemolatoon/ebi's own tests; see make_golden.py.",
@@ -160,6 +203,8 @@ def main():
         "agg_cases": AGG_CASES,
         "agg_buff_scale": AGG_BUFF_SCALE,
         "buff_precision": BUFF_PRECISION,
+        "expr_cases": EXPR_CASES,
+        "expr_chunk": EXPR_CHUNK,
     }
     path = Path(__file__).resolve().parent / "kat.json"
     path.write_text(json.dumps(out, indent=1) + "\n")

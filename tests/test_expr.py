@@ -1,0 +1,281 @@
+"""Aggregation / Expr over several columns (api/decoder.rs:755-917,
+decoder/expr.rs): the oracle against the reference's fixed cases and a plain
+Python model of the chunk loop (CPU); the engine against both (GPU)."""
+import math
+
+import numpy as np
+import pytest
+
+import ebi_gb300 as E
+from oracle import oracle as O
+from tests.kat import KAT
+from tests.parity import same_f64, same_scalar, sum_ok
+
+KIND = {"sum": O.AGGR_SUM, "min": O.AGGR_MIN, "max": O.AGGR_MAX, "none": O.AGGR_NONE}
+OPS = {"add": E.Op.Add, "sub": E.Op.Sub, "mul": E.Op.Mul, "div": E.Op.Div}
+
+
+def to_expr(j):
+    if j[0] == "index":
+        return E.Expr.Index(j[1])
+    if j[0] == "lit":
+        return E.Expr.Literal(j[1])
+    return E.Expr.Binary(OPS[j[0]], to_expr(j[1]), to_expr(j[2]))
+
+
+def oracle_decoders(columns, chunk=("record_count", 3), scheme=O.UNCOMPRESSED, scale=1):
+    kinds = {"record_count": O.CHUNK_RECORD_COUNT, "byte_size": O.CHUNK_BYTE_SIZE, "full": O.CHUNK_FULL}
+    return [O.Decoder(O.encode(np.asarray(c, float), scheme, kinds[chunk[0]], chunk[1], scale)) for c in columns]
+
+
+# ---- a plain model of Aggregation::compute (no codec: values and chunk row counts) ----
+def model(columns, chunk_rows, expr, kind, rows=None):
+    """columns[j]: values; chunk_rows[j]: rows per chunk of column j."""
+    sel = None if rows is None else set(rows)
+
+    def chunk_vals(j, c):
+        r0 = sum(chunk_rows[j][:c])
+        return [columns[j][r] for r in range(r0, r0 + chunk_rows[j][c]) if sel is None or r in sel]
+
+    def ev(e, c):
+        if e.kind == "index":
+            return chunk_vals(e.index, c)
+        if e.kind == "literal":
+            raise ValueError("precondition")
+        lit_l, lit_r = e.lhs.kind == "literal", e.rhs.kind == "literal"
+        f = {E.Op.Add: lambda a, b: a + b, E.Op.Sub: lambda a, b: a - b, E.Op.Mul: lambda a, b: a * b,
+             E.Op.Div: lambda a, b: a / b if b != 0 else (math.copysign(math.inf, a) * math.copysign(1, b)
+                                                          if a != 0 and a == a else math.nan)}[e.op]
+        if lit_l and lit_r:
+            raise ValueError("precondition")
+        if lit_r:
+            return [f(x, e.rhs.value) for x in ev(e.lhs, c)]
+        if lit_l:
+            return [f(e.lhs.value, x) for x in ev(e.rhs, c)]
+        return [f(a, b) for a, b in zip(ev(e.lhs, c), ev(e.rhs, c))]
+
+    out = [] if kind == O.AGGR_NONE else (0.0 if kind == O.AGGR_SUM else math.inf if kind == O.AGGR_MIN else -math.inf)
+    for c in range(len(chunk_rows[0])):
+        v = ev(expr, c)
+        if kind == O.AGGR_NONE:
+            out += v
+        elif kind == O.AGGR_SUM:
+            s = -0.0
+            for x in v:
+                s += x
+            out += s
+        else:
+            for x in v:
+                if x == x:
+                    out = min(out, x) if kind == O.AGGR_MIN else max(out, x)
+    return out
+
+
+def chunk_rows_of(n, k):
+    return [min(k, n - r) for r in range(0, n, k)]
+
+
+# ---- CPU: the oracle --------------------------------------------------------------------
+@pytest.mark.parametrize("idx", range(len(KAT["expr_cases"])))
+def test_oracle_expr_kats(idx):
+    case = KAT["expr_cases"][idx]
+    ds = oracle_decoders(case["columns"], tuple(KAT["expr_chunk"]))
+    n = max(len(c) for c in case["columns"])
+    mask = O.mask_from_rows(case["bitmask"], n) if "bitmask" in case else None
+    for agg in case["aggs"]:
+        got = O.aggregate(ds, KIND[agg["kind"]], to_expr(agg["expr"]).postfix(), mask)
+        assert got == agg["expect"], (case["src"], agg)
+
+
+EXPRS = [
+    E.Expr.Index(0) * E.Expr.Index(1),
+    E.Expr.Index(0) * (1.0 - E.Expr.Index(1)),
+    (E.Expr.Index(0) * (1.0 - E.Expr.Index(1))) * (1.0 + E.Expr.Index(2)),
+    (E.Expr.Index(0) + E.Expr.Index(1)) * (E.Expr.Index(1) - E.Expr.Index(2)),
+    2.0 / E.Expr.Index(2),
+    E.Expr.Index(1) - E.Expr.Index(0) / 3.0,
+]
+
+
+@pytest.mark.parametrize("ei", range(len(EXPRS)))
+@pytest.mark.parametrize("kind", [O.AGGR_SUM, O.AGGR_MIN, O.AGGR_MAX, O.AGGR_NONE])
+def test_oracle_matches_model_misaligned_chunks(ei, kind):
+    rng = np.random.default_rng(40 + ei)
+    n = 300
+    cols = [np.round(rng.normal(0, 3, n), 2).tolist() for _ in range(3)]
+    cols[2][5] = 0.0  # a division by zero
+    ks = [32, 25, 40]  # chunk sizes differ: chunk i of each column covers other rows
+    ds = [O.Decoder(O.encode(np.asarray(c), O.UNCOMPRESSED, O.CHUNK_RECORD_COUNT, k)) for c, k in zip(cols, ks)]
+    ds = [ds[2], ds[0], ds[1]]  # the first column has the fewest chunks (40 rows each)
+    cols = [cols[2], cols[0], cols[1]]
+    crs = [chunk_rows_of(n, 40), chunk_rows_of(n, 32), chunk_rows_of(n, 25)]
+    rows = sorted(rng.choice(n, 120, replace=False).tolist())
+    for mask_rows in (None, rows):
+        mask = None if mask_rows is None else O.mask_from_rows(mask_rows, n)
+        got = O.aggregate(ds, kind, EXPRS[ei].postfix(), mask)
+        want = model(cols, crs, EXPRS[ei], kind, mask_rows)
+        if kind == O.AGGR_NONE:
+            assert same_f64(np.nan_to_num(got, nan=7.5), np.nan_to_num(np.asarray(want, float), nan=7.5))
+        else:
+            assert same_scalar(got, want) or (np.isnan(got) and np.isnan(want)), (got, want)
+
+
+def test_oracle_expr_errors():
+    ds = oracle_decoders([[1.0, 2.0, 3.0, 4.0], [5.0, 6.0, 7.0, 8.0]])
+    lit = [(O.EXPR_LITERAL, 0, 1.0)]
+    with pytest.raises(O.OracleError) as e:
+        O.aggregate(ds, O.AGGR_SUM, lit)
+    assert e.value.code == 4  # PreconditionsNotMet
+    with pytest.raises(O.OracleError) as e:
+        O.aggregate(ds, O.AGGR_SUM, (E.Expr.Index(0) + (E.Expr.Literal(1) * E.Expr.Literal(2))).postfix())
+    assert e.value.code == 4
+    with pytest.raises(O.OracleError) as e:
+        O.aggregate(ds, O.AGGR_SUM, (E.Expr.Index(0) + E.Expr.Index(2)).postfix())
+    assert e.value.code == 7  # index past the decoders: the reference panics
+    with pytest.raises(O.OracleError) as e:
+        O.aggregate(ds, O.AGGR_NONE, E.Expr.Index(0).postfix())
+    assert e.value.code == 7  # todo!() in the reference
+    short = oracle_decoders([[1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0], [1.0, 2.0]])
+    with pytest.raises(O.OracleError) as e:
+        O.aggregate(short, O.AGGR_SUM, (E.Expr.Index(0) * E.Expr.Index(1)).postfix())
+    assert e.value.code == 7  # chunk_handles[i] out of range: the reference panics
+    # more chunks in a later column: only the first column's chunk count is visited
+    longer = oracle_decoders([[1.0, 2.0, 3.0], [1.0, 2.0, 3.0, 4.0, 5.0]])
+    assert O.aggregate(longer, O.AGGR_SUM, (E.Expr.Index(0) * E.Expr.Index(1)).postfix()) == 14.0
+
+
+# ---- GPU: the engine ------------------------------------------------------------------
+def engine_decoders(columns, chunk=("record_count", 3), scheme="uncompressed", scale=1):
+    return [E.Decoder(E.encode(np.asarray(c, float), scheme, chunk, scale)) for c in columns]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("idx", range(len(KAT["expr_cases"])))
+def test_engine_expr_kats(idx):
+    case = KAT["expr_cases"][idx]
+    ds = engine_decoders(case["columns"], tuple(KAT["expr_chunk"]))
+    n = max(len(c) for c in case["columns"])
+    mask = O.mask_from_rows(case["bitmask"], n) if "bitmask" in case else None
+    aggs = [E.Aggregation(KIND[a["kind"]], to_expr(a["expr"])) for a in case["aggs"]]
+    got = E.Aggregation.compute_multiple(aggs, ds, mask)
+    assert got == [a["expect"] for a in case["aggs"]], case["src"]
+    for a, g in zip(aggs, got):  # Aggregation::compute gives the same
+        assert a.compute(ds, mask) == g
+
+
+def _check_engine(ds_e, ds_o, expr, kind, mask):
+    got = E.Aggregation(kind, expr).compute(ds_e, mask)
+    want = O.aggregate(ds_o, kind, expr.postfix(), mask)
+    if kind == O.AGGR_NONE:
+        g = got.cpu().numpy()
+        assert g.shape == want.shape
+        assert same_f64(np.where(np.isnan(g), 0.5, g), np.where(np.isnan(want), 0.5, want))
+    elif kind == O.AGGR_SUM:
+        vals = O.aggregate(ds_o, O.AGGR_NONE, expr.postfix(), mask)
+        assert sum_ok(got, want, False, vals), (got, want)
+    else:
+        assert same_scalar(got, want), (got, want)
+
+
+CODEC_CASES = [("buff", 100), ("gorilla", 1), ("chimp", 1), ("chimp128", 1), ("rle", 1), ("uncompressed", 1),
+               ("elf", 1), ("elf_on_chimp", 1)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme,scale", CODEC_CASES)
+def test_engine_expr_parity(scheme, scale):
+    rng = np.random.default_rng(7)
+    n = 70_000
+    cols = [np.round(rng.uniform(900, 105000, n), 2), np.round(rng.integers(0, 11, n) / 100.0, 2),
+            np.round(rng.integers(0, 9, n) / 100.0, 2)]
+    if scheme == "rle":
+        cols = [np.repeat(c[: n // 40], 40) for c in cols]
+    ds_o = [O.Decoder(O.encode(c, O.SCHEMES[scheme], O.CHUNK_RECORD_COUNT, 8192, scale)) for c in cols]
+    ds_e = [E.Decoder(E.encode(c, scheme, ("record_count", 8192), scale)) for c in cols]
+    rows = np.sort(rng.choice(n, n // 3, replace=False))
+    for mask in (None, O.mask_from_rows(rows.tolist(), n)):
+        for expr in EXPRS:
+            for kind in (O.AGGR_SUM, O.AGGR_MIN, O.AGGR_MAX, O.AGGR_NONE):
+                _check_engine(ds_e, ds_o, expr, kind, mask)
+
+
+@pytest.mark.gpu
+def test_engine_misaligned_chunks_and_mixed_codecs():
+    rng = np.random.default_rng(9)
+    n = 50_000
+    cols = [np.round(rng.normal(10, 4, n), 2) for _ in range(3)]
+    specs = [("buff", 5000, 100), ("gorilla", 3000, 1), ("chimp128", 4096, 1)]
+    ds_o = [O.Decoder(O.encode(c, O.SCHEMES[s], O.CHUNK_RECORD_COUNT, k, sc)) for c, (s, k, sc) in zip(cols, specs)]
+    ds_e = [E.Decoder(E.encode(c, s, ("record_count", k), sc)) for c, (s, k, sc) in zip(cols, specs)]
+    rows = np.sort(rng.choice(n, 20_000, replace=False))
+    for mask in (None, O.mask_from_rows(rows.tolist(), n)):
+        for expr in EXPRS:
+            for kind in (O.AGGR_SUM, O.AGGR_MIN, O.AGGR_MAX, O.AGGR_NONE):
+                _check_engine(ds_e, ds_o, expr, kind, mask)
+    # compute_multiple: Index aggregations first, then the expressions in one pass
+    aggs = [E.Aggregation.sum(E.Expr.Index(0)), E.Aggregation.max(EXPRS[2]), E.Aggregation.sum(EXPRS[3]),
+            E.Aggregation.min(E.Expr.Index(1)), E.Aggregation.none(EXPRS[0])]
+    got = E.Aggregation.compute_multiple(aggs, ds_e)
+    for a, g in zip(aggs, got):
+        one = a.compute(ds_e)
+        if a.kind == E.AggregationKind.NONE:
+            assert same_f64(g.cpu().numpy(), one.cpu().numpy())
+        else:
+            assert same_scalar(g, one)
+
+
+@pytest.mark.gpu
+def test_engine_expr_errors():
+    ds = engine_decoders([[1.0, 2.0, 3.0, 4.0], [5.0, 6.0, 7.0, 8.0]])
+    with pytest.raises(E.PreconditionsNotMet):
+        E.Aggregation.sum(E.Expr.Literal(1.0)).compute(ds)
+    with pytest.raises(E.PreconditionsNotMet):
+        E.Aggregation.sum(E.Expr.Index(0) + (E.Expr.Literal(1) * E.Expr.Literal(2))).compute(ds)
+    with pytest.raises(E.InvalidArgument):
+        E.Aggregation.sum(E.Expr.Index(0) + E.Expr.Index(2)).compute(ds)
+    with pytest.raises(E.Unsupported):
+        E.Aggregation.none(E.Expr.Index(0)).compute(ds)
+    short = engine_decoders([[1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0], [1.0, 2.0]])
+    with pytest.raises(E.InvalidArgument):
+        E.Aggregation.sum(E.Expr.Index(0) * E.Expr.Index(1)).compute(short)
+    longer = engine_decoders([[1.0, 2.0, 3.0], [1.0, 2.0, 3.0, 4.0, 5.0]])
+    assert E.Aggregation.sum(E.Expr.Index(0) * E.Expr.Index(1)).compute(longer) == 14.0
+
+
+@pytest.mark.gpu
+def test_tpch_q6_and_q1_shapes():
+    """experimenter/src/tpch.rs:190-461: Q6 filters l_discount, then l_quantity
+    under that mask, then sums l_extendedprice * l_discount; Q1 runs five
+    aggregations with compute_multiple."""
+    rng = np.random.default_rng(6)
+    n = 300_000
+    price = np.round(rng.uniform(900, 105000, n), 2)
+    disc = np.round(rng.integers(0, 11, n) / 100.0, 2)
+    qty = rng.integers(1, 51, n).astype(float)
+    tax = np.round(rng.integers(0, 9, n) / 100.0, 2)
+    cols = [qty, price, disc, tax]
+    ds_o = [O.Decoder(O.encode(c, O.BUFF, O.CHUNK_RECORD_COUNT, 65536, 100)) for c in cols]
+    ds_e = [E.Decoder(E.encode(c, "buff", ("record_count", 65536), 100)) for c in cols]
+    # Q6
+    p0 = E.Predicate.range(E.RangeValue.inclusive(0.05), E.RangeValue.inclusive(0.07))
+    p1 = E.Predicate.range(E.RangeValue.NONE, E.RangeValue.exclusive(24.0))
+    m = ds_e[2].filter(p0)
+    m = ds_e[0].filter(p1, m)
+    o0 = ds_o[2].filter(O.rng(O.BOUND_INCLUSIVE, 0.05, O.BOUND_INCLUSIVE, 0.07))
+    o1 = ds_o[0].filter(O.rng(O.BOUND_NONE, 0.0, O.BOUND_EXCLUSIVE, 24.0), o0)
+    assert same_f64(m.cpu().numpy().view(np.uint64)[: len(o1)], o1)
+    q6 = E.Expr.Index(1) * E.Expr.Index(2)
+    got = E.Aggregation.sum(q6).compute(ds_e, m)
+    want = O.aggregate(ds_o, O.AGGR_SUM, q6.postfix(), o1)
+    assert sum_ok(got, want, False, O.aggregate(ds_o, O.AGGR_NONE, q6.postfix(), o1))
+    # Q1
+    one = E.Expr.Literal(1.0)
+    q1 = [E.Aggregation.sum(E.Expr.Index(0)), E.Aggregation.sum(E.Expr.Index(1)),
+          E.Aggregation.sum(E.Expr.Index(1) * (one - E.Expr.Index(2))),
+          E.Aggregation.sum((E.Expr.Index(1) * (one - E.Expr.Index(2))) * (one + E.Expr.Index(3))),
+          E.Aggregation.sum(E.Expr.Index(2))]
+    got = E.Aggregation.compute_multiple(q1, ds_e)
+    for a, g in zip(q1, got):
+        want = O.aggregate(ds_o, a.kind, a.expr.postfix())
+        vals = O.aggregate(ds_o, O.AGGR_NONE, a.expr.postfix()) if a.expr.kind != "index" else None
+        assert sum_ok(g, want, a.expr.kind == "index", vals), (a.expr, g, want)
