@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <atomic>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -437,14 +438,23 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
             if (first) { c->buff_frac = b.frac; first = false; }
             if (b.frac != c->buff_frac || b.frac > 1022 || b.bits == 0) c->buff_fast_ok = false;
         }
-        // bound of sum |base + delta| over every readable row
-        long double bound = 0.0L;
+        // bound of sum |base + delta| over every readable row, and of each |base + delta|
+        long double bound = 0.0L, widest = 0.0L;
+        c->buff_same_frac = true;
+        bool seen = false;
+        uint32_t frac0 = 0;
         for (const BuffChunkInfo& b : binfo) {
             if (b.status) continue;
             const long double lo = static_cast<long double>(b.base);
             const long double hi = lo + (b.bits >= 64 ? 18446744073709551615.0L : static_cast<long double>((1ull << b.bits) - 1));
-            bound += static_cast<long double>(b.n) * std::max(lo < 0 ? -lo : lo, hi < 0 ? -hi : hi);
+            const long double m = std::max(lo < 0 ? -lo : lo, hi < 0 ? -hi : hi);
+            bound += static_cast<long double>(b.n) * m;
+            widest = std::max(widest, m);
+            if (!seen) { frac0 = b.frac; seen = true; }
+            if (b.frac != frac0 || b.frac > 1022) c->buff_same_frac = false;
         }
+        c->buff_fixed_bits = 0;
+        while (c->buff_fixed_bits < 64 && std::ldexp(1.0L, static_cast<int>(c->buff_fixed_bits)) <= widest) ++c->buff_fixed_bits;
         c->buff_exact = c->buff_fast_ok && bound < 4503599627370496.0L;  // 2^52
         uint32_t per_sm = 1;
         c->layout = buff_stage_layout(np_max, tb_max, &per_sm);

@@ -35,6 +35,8 @@ struct ebi_column {
     uint32_t buff_frac = 0;
     bool buff_fast_ok = false;
     bool buff_exact = false;     // fast_ok and sum |value| over all rows < 2^52: every query's totals exact
+    bool buff_same_frac = false; // every readable chunk has frac buff_frac <= 1022 (constant chunks included)
+    uint32_t buff_fixed_bits = 64;  // |base + delta| < 2^buff_fixed_bits on every readable row
     // register-streaming scan (every readable chunk 8..32 bits wide)
     bool stream_ok = false;
     uint2* d_units = nullptr;

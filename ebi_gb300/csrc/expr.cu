@@ -20,7 +20,10 @@
 //      values themselves for an array result; expr_fold (one CTA per
 //      aggregation) combines the items in chunk order.
 #include <algorithm>
+#include <climits>
 #include <cmath>
+#include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "column.h"
@@ -42,9 +45,12 @@ constexpr int kMaxCols = 16;    // distinct columns per evaluation pass
 enum : uint8_t { I_LOAD = 0, I_PUSH = 1, I_ADD = 2, I_SUB = 3, I_MUL = 4, I_DIV = 5 };
 enum : uint8_t { S_ACC = 0, S_POP = 1, S_COL = 2, S_LIT = 3 };
 struct Instr {
-    uint8_t op, a, b, pad;
+    uint8_t op, a, b;
+    uint8_t sa, sb;     // exact BUFF programs: left shifts aligning the operands' scales
+    uint8_t pad[3];
     uint16_t ca, cb;    // column slot of an S_COL operand (a column index until a pass assigns slots)
-    double la, lb;      // literal of an S_LIT operand
+    uint16_t pad2[2];
+    double la, lb;      // literal of an S_LIT operand (exact programs: its integer numerator's bits)
 };
 
 struct ExprPass {
@@ -70,7 +76,7 @@ struct ExprScratch {
     unsigned long long* aoff;  // [n_aggs][n_chunks]: array output offset
     unsigned long long* item0; // [n_chunks + 1]: first item of each chunk
     unsigned long long* totals;  // [n_aggs + 1]: array lengths, then the item count
-    Quad* part;             // [n_aggs][items_cap]: sum hi, sum lo, min key, max key
+    Quad* part;             // [n_aggs][grid]: per CTA sum hi, sum lo, min key, max key
     Quad* res;              // [n_aggs]: sum, min, max, count
     const Instr* prog;
 };
@@ -152,6 +158,85 @@ __global__ void __launch_bounds__(kExprThreads) expr_prepare(ExprPass P, ExprScr
 }
 
 // ---- step 3: evaluation ---------------------------------------------------
+// GB300's FP64 pipe is a small fraction of its integer throughput, so FP64
+// work is kept to the expression's own operations: a thread sums its values
+// of an item plainly and adds that subtotal to a compensated running sum kept
+// across all its items (its error stays far below the 1e-12 bound), min and
+// max are ordered keys on the integer pipes, and the CTA reduces once.
+
+// Per-thread running aggregate of one aggregation (shared memory).
+struct RunAcc {
+    double hi, lo;
+    unsigned long long mn, mx;
+};
+
+__device__ __forceinline__ void run_init(RunAcc* runs, uint32_t n_aggs) {
+    for (uint32_t a = 0; a < n_aggs; ++a)
+        runs[a * blockDim.x + threadIdx.x] = RunAcc{0.0, 0.0, kKeyPosInf, kKeyNegInf};
+}
+
+// Adds the values v[i] with bit i of ok set.
+template <int N>
+__device__ __forceinline__ void run_add(RunAcc& r, const double (&v)[N], uint32_t ok, uint32_t kind) {
+    if (!ok) return;
+    if (kind == EBI_AGGR_SUM) {
+        double s = 0.0;
+        bool any = false;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            if ((ok >> i) & 1u) { s = any ? __dadd_rn(s, v[i]) : v[i]; any = true; }
+        neumaier_add(r.hi, r.lo, s);
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        const uint64_t b = static_cast<uint64_t>(__double_as_longlong(v[i]));
+        if (((ok >> i) & 1u) && !is_nan_bits(b)) {
+            const unsigned long long k = order_key(b);
+            r.mn = k < r.mn ? k : r.mn;
+            r.mx = k > r.mx ? k : r.mx;
+        }
+    }
+}
+
+// The CTA's partial of every scalar aggregation: part[a * gridDim.x + blockIdx.x].
+__device__ void cta_partials(const ExprPass& P, const ExprScratch& S, const RunAcc* runs) {
+    __shared__ double red_h[32], red_l[32];
+    __shared__ unsigned long long red_mn[32], red_mx[32];
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x / 32;
+    for (uint32_t a = 0; a < P.n_aggs; ++a) {
+        if (P.kind[a] == EBI_AGGR_NONE) continue;
+        const RunAcc r = runs[a * blockDim.x + threadIdx.x];
+        double hi = r.hi, lo = r.lo;
+        unsigned long long mn = r.mn, mx = r.mx;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
+            if ((lane & (2 * o - 1)) == 0) dd_add(hi, lo, oh, ol);
+        }
+        mn = warp_min_u64(mn);
+        mx = warp_max_u64(mx);
+        if (lane == 0) { red_h[wid] = hi; red_l[wid] = lo; red_mn[wid] = mn; red_mx[wid] = mx; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double th = 0.0, tl = 0.0;
+            unsigned long long tmn = kKeyPosInf, tmx = kKeyNegInf;
+            for (uint32_t w = 0; w < nw; ++w) {
+                dd_add(th, tl, red_h[w], red_l[w]);
+                tmn = red_mn[w] < tmn ? red_mn[w] : tmn;
+                tmx = red_mx[w] > tmx ? red_mx[w] : tmx;
+            }
+            Quad q;
+            q.x = th;
+            q.y = tl;
+            q.z = __longlong_as_double(static_cast<long long>(tmn));
+            q.w = __longlong_as_double(static_cast<long long>(tmx));
+            S.part[a * uint64_t(gridDim.x) + blockIdx.x] = q;
+        }
+        __syncthreads();
+    }
+}
+
 __device__ __forceinline__ double operand(uint8_t src, uint16_t col, double lit, double acc_e,
                                           const double (&st)[kMaxStack][kExprPerThread], int sp, int e,
                                           const double* const* base, uint64_t k, bool ok) {
@@ -164,14 +249,14 @@ __device__ __forceinline__ double operand(uint8_t src, uint16_t col, double lit,
 }
 
 __global__ void __launch_bounds__(kExprThreads) expr_eval(ExprPass P, ExprScratch S) {
+    extern __shared__ RunAcc runs[];  // [n_aggs][kExprThreads]
     __shared__ Instr prog[kPassInstr];
     __shared__ const double* base[kMaxCols];
-    __shared__ double red_h[kExprThreads / 32], red_l[kExprThreads / 32];
-    __shared__ unsigned long long red_mn[kExprThreads / 32], red_mx[kExprThreads / 32];
     __shared__ uint32_t s_c;
     const uint32_t n_instr = P.first[P.n_aggs];
     for (uint32_t i = threadIdx.x; i < n_instr; i += kExprThreads) prog[i] = S.prog[i];
-    const uint32_t C = P.n_chunks, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    run_init(runs, P.n_aggs);
+    const uint32_t C = P.n_chunks;
     const unsigned long long n_items = S.totals[P.n_aggs];
     for (unsigned long long item = blockIdx.x; item < n_items; item += gridDim.x) {
         __syncthreads();  // the previous item's shared values are consumed
@@ -216,6 +301,10 @@ __global__ void __launch_bounds__(kExprThreads) expr_eval(ExprPass P, ExprScratc
                 }
                 if (I.a == S_POP || I.b == S_POP) --sp;
             }
+            uint32_t ok = 0;
+#pragma unroll
+            for (int e = 0; e < kExprPerThread; ++e)
+                if (k0 + uint64_t(e) * kExprThreads + threadIdx.x < len) ok |= 1u << e;
             const uint32_t kind = P.kind[a];
             if (kind == EBI_AGGR_NONE) {
                 double* out = P.out[a];
@@ -223,61 +312,27 @@ __global__ void __launch_bounds__(kExprThreads) expr_eval(ExprPass P, ExprScratc
 #pragma unroll
                 for (int e = 0; e < kExprPerThread; ++e) {
                     const uint64_t k = k0 + uint64_t(e) * kExprThreads + threadIdx.x;
-                    if (k < len && o + k < cap) out[o + k] = acc[e];
+                    if (((ok >> e) & 1u) && o + k < cap) out[o + k] = acc[e];
                 }
                 continue;
             }
-            ValAgg g = val_agg_init(kind == EBI_AGGR_SUM ? AGG_SUM : (AGG_MIN | AGG_MAX));
-#pragma unroll
-            for (int e = 0; e < kExprPerThread; ++e) {
-                const uint64_t k = k0 + uint64_t(e) * kExprThreads + threadIdx.x;
-                if (k < len) val_agg_add1(g, static_cast<uint64_t>(__double_as_longlong(acc[e])));
-            }
-            // fixed-order tree: lanes, then warps
-            double hi = g.hi, lo = g.lo;
-            unsigned long long mn = g.mnk, mx = g.mxk;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const double oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
-                if ((lane & (2 * o - 1)) == 0) dd_add(hi, lo, oh, ol);
-            }
-            mn = warp_min_u64(mn);
-            mx = warp_max_u64(mx);
-            if (lane == 0) { red_h[wid] = hi; red_l[wid] = lo; red_mn[wid] = mn; red_mx[wid] = mx; }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double th = 0.0, tl = 0.0;
-                unsigned long long tmn = kKeyPosInf, tmx = kKeyNegInf;
-                for (int w = 0; w < kExprThreads / 32; ++w) {
-                    dd_add(th, tl, red_h[w], red_l[w]);
-                    tmn = red_mn[w] < tmn ? red_mn[w] : tmn;
-                    tmx = red_mx[w] > tmx ? red_mx[w] : tmx;
-                }
-                Quad p;
-                p.x = th;
-                p.y = tl;
-                p.z = __longlong_as_double(static_cast<long long>(tmn));
-                p.w = __longlong_as_double(static_cast<long long>(tmx));
-                S.part[a * n_items + item] = p;
-            }
-            __syncthreads();
+            run_add(runs[a * kExprThreads + threadIdx.x], acc, ok, kind);
         }
     }
+    __syncthreads();
+    cta_partials(P, S, runs);
 }
 
-// One CTA per aggregation: the items' partials in item (= chunk) order.
-__global__ void __launch_bounds__(kExprThreads) expr_fold(ExprPass P, ExprScratch S) {
+// One CTA per aggregation: the CTAs' partials in CTA order.
+__global__ void __launch_bounds__(kExprThreads) expr_fold(ExprPass P, ExprScratch S, uint32_t n_parts) {
     __shared__ double sh_h[kExprThreads / 32], sh_l[kExprThreads / 32];
     __shared__ unsigned long long sh_mn[kExprThreads / 32], sh_mx[kExprThreads / 32];
     const uint32_t a = blockIdx.x;
     if (a >= P.n_aggs || P.kind[a] == EBI_AGGR_NONE) return;
-    const unsigned long long n = S.totals[P.n_aggs];
-    const Quad* part = S.part + a * n;
-    const unsigned long long per = (n + kExprThreads - 1) / kExprThreads;
-    const unsigned long long i0 = min(n, threadIdx.x * per), i1 = min(n, i0 + per);
+    const Quad* part = S.part + uint64_t(a) * n_parts;
     double hi = 0.0, lo = 0.0;
     unsigned long long mn = kKeyPosInf, mx = kKeyNegInf;
-    for (unsigned long long i = i0; i < i1; ++i) {
+    for (uint32_t i = threadIdx.x; i < n_parts; i += kExprThreads) {
         const Quad p = part[i];
         dd_add(hi, lo, p.x, p.y);
         const unsigned long long pm = static_cast<unsigned long long>(__double_as_longlong(p.z));
@@ -308,6 +363,381 @@ __global__ void __launch_bounds__(kExprThreads) expr_fold(ExprPass P, ExprScratc
         r.y = __longlong_as_double(static_cast<long long>(key_bits(tmn)));
         r.z = __longlong_as_double(static_cast<long long>(key_bits(tmx)));
         r.w = 0.0;
+        S.res[a] = r;
+    }
+}
+
+// ---- fused path: BUFF columns with aligned chunks ---------------------------
+// When every column of a pass is BUFF, read at full precision, and its first
+// C chunks cover the same rows as the other columns', element k of a chunk is
+// the same row in every column: the zip is row-wise and the values need not
+// be materialized.  Each warp walks its own contiguous range of units (256
+// rows of one chunk): a lane reads its 8 consecutive rows of every column
+// straight from the planes, the values of the selected rows are packed into
+// the warp's shared-memory slots (in row order, warp shuffles for the
+// offsets), and the lanes run every aggregation's program on the packed
+// values.  Warps synchronise only with themselves, so each one's memory
+// latency overlaps the others' work.
+constexpr int kFuseThreads = 256;
+constexpr int kFuseWarps = kFuseThreads / 32;
+constexpr int kFuseRows = 8;                         // rows per lane
+constexpr uint32_t kFuseUnit = 32 * kFuseRows;       // rows per warp unit
+constexpr int kFuseStride = kFuseUnit + kFuseUnit / 8;  // doubles per column slot (one pad every 8: conflict-free)
+constexpr int kFuseCols = 4;
+constexpr int kFuseStack = 2;  // accumulators a fused program may push
+
+__device__ __forceinline__ uint32_t fuse_pad(uint32_t p) { return p + (p >> 3); }
+
+struct FusePass {
+    const uint8_t* file[kFuseCols];
+    const BuffChunkInfo* info[kFuseCols];
+    const ChunkDesc* chunks;    // row ranges (identical in every column)
+    const uint32_t* in_mask;    // u32 view of the bitmask, or null
+    uint64_t n_records;         // rows the mask covers
+    const uint32_t* unit0;      // [C + 1]: first unit of each chunk
+    uint32_t n_units;
+    unsigned int* bad;          // set when a chunk's status is not 0
+};
+
+// The 8 deltas of rows [8 g, 8 g + 8) of a chunk (BUFF planes, MSB plane first, then the tail bits).
+__device__ __forceinline__ void fuse_deltas(const uint8_t* file, const BuffChunkInfo& ci, uint32_t g,
+                                            unsigned long long (&d)[kFuseRows]) {
+    const uint32_t np = ci.bits / 8, tb = ci.bits % 8;
+#pragma unroll
+    for (int i = 0; i < kFuseRows; ++i) d[i] = 0;
+    for (uint32_t p = 0; p < np; ++p) {
+        const unsigned long long w = *reinterpret_cast<const unsigned long long*>(file + ci.planes + p * ci.stride +
+                                                                                 uint64_t(g) * 8);
+#pragma unroll
+        for (int i = 0; i < kFuseRows; ++i) d[i] = (d[i] << 8) | (((w >> (8 * i)) & 0xffull) ^ 0x80ull);
+    }
+    if (tb) {
+        // bits [64 g tb, 64 g tb + 8 tb) of the tail plane: bytes [g tb, g tb + tb)
+        const uint64_t b0 = uint64_t(g) * tb, w0 = b0 & ~3ull;
+        const uint32_t* t = reinterpret_cast<const uint32_t*>(file + ci.tail + w0);
+        const uint32_t sh = static_cast<uint32_t>(b0 & 3) * 8;
+        const uint64_t last = b0 + tb - 1;  // the words read end inside the (4-byte aligned) tail plane
+        const uint32_t x0 = t[0];
+        const uint32_t x1 = w0 + 4 <= last ? t[1] : 0u;
+        const uint32_t x2 = w0 + 8 <= last ? t[2] : 0u;
+        const unsigned long long lo = static_cast<unsigned long long>(x0) | (static_cast<unsigned long long>(x1) << 32);
+        const unsigned long long bits = sh ? (lo >> sh) | (static_cast<unsigned long long>(x2) << (64 - sh)) : lo;
+        const unsigned long long m = (1ull << tb) - 1ull;
+#pragma unroll
+        for (int i = 0; i < kFuseRows; ++i) d[i] = (d[i] << tb) | ((bits >> (i * tb)) & m);
+    }
+}
+
+// (base + delta) / 2^frac exactly as the BUFF materialize kernel computes it
+// (int64 -> f64, then * 2^-frac or / 2^frac); when the integer is below 2^53
+// and the result normal the conversion is exact and its bits are built on
+// the integer pipes.  inv_ok: frac <= 1022 (the materialize kernel's inv != 0).
+__device__ __forceinline__ double fuse_value(long long fixed, uint32_t frac, bool inv_ok, double inv, double scale) {
+    const unsigned long long u = fixed < 0 ? 0ull - static_cast<unsigned long long>(fixed)
+                                           : static_cast<unsigned long long>(fixed);
+    if (u == 0) return 0.0;
+    const int msb = 63 - __clzll(static_cast<long long>(u));
+    const int e = msb - static_cast<int>(frac) + 1023;
+    if (msb <= 52 && e >= 1 && inv_ok) {
+        const unsigned long long bits = (fixed < 0 ? 0x8000000000000000ull : 0ull) |
+                                        (static_cast<unsigned long long>(e) << 52) |
+                                        ((u << (52 - msb)) & 0x000fffffffffffffull);
+        return __longlong_as_double(static_cast<long long>(bits));
+    }
+    return inv_ok ? static_cast<double>(fixed) * inv : static_cast<double>(fixed) / scale;
+}
+
+// Exact programs' running aggregate: a 128-bit sum and the extreme values,
+// as the bits of a RunAcc.
+struct RunAccI {
+    unsigned long long lo, hi;   // two's complement 128-bit sum
+    unsigned long long mn, mx;   // signed order keys (sign bit flipped)
+};
+__device__ __forceinline__ unsigned long long skey(long long v) {
+    return static_cast<unsigned long long>(v) ^ 0x8000000000000000ull;
+}
+__device__ __forceinline__ void add128(unsigned long long& lo, unsigned long long& hi, unsigned long long blo,
+                                       unsigned long long bhi) {
+    const unsigned long long o = lo;
+    lo += blo;
+    hi += bhi + (lo < o ? 1ull : 0ull);
+}
+
+// kExact: the program runs on the fixed-point integers (each value is
+// fixed * 2^-frac; the host proved every intermediate below 2^53, where each
+// IEEE operation is exact and equals the integer one); else on the f64 values.
+template <bool kExact>
+__global__ void __launch_bounds__(kFuseThreads) expr_buff_fused(ExprPass P, ExprScratch S, FusePass F) {
+    extern __shared__ double dyn[];  // [warp][n_cols][kFuseStride] packed values, then RunAcc[n_aggs][kFuseThreads]
+    __shared__ Instr prog[kPassInstr];
+    __shared__ BuffChunkInfo s_ci[kFuseWarps][kFuseCols];
+    __shared__ const uint8_t* s_file[kFuseCols];
+    __shared__ uint32_t s_kind[kMaxAggs], s_first[kMaxAggs + 1];
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double* wslot = dyn + wid * P.n_cols * kFuseStride;
+    long long* islot = reinterpret_cast<long long*>(wslot);
+    RunAcc* runs = reinterpret_cast<RunAcc*>(dyn + kFuseWarps * P.n_cols * kFuseStride);
+    RunAccI* iruns = reinterpret_cast<RunAccI*>(runs);
+    const uint32_t n_instr = P.first[P.n_aggs];
+    for (uint32_t i = threadIdx.x; i < n_instr; i += kFuseThreads) prog[i] = S.prog[i];
+    if (threadIdx.x < kFuseCols) s_file[threadIdx.x] = F.file[threadIdx.x];
+    if (threadIdx.x < kMaxAggs) s_kind[threadIdx.x] = P.kind[threadIdx.x];
+    if (threadIdx.x <= kMaxAggs) s_first[threadIdx.x] = P.first[threadIdx.x];
+    for (uint32_t a = 0; a < P.n_aggs; ++a) {
+        if (kExact) iruns[a * kFuseThreads + threadIdx.x] = RunAccI{0, 0, skey(LLONG_MAX), skey(LLONG_MIN)};
+        else runs[a * kFuseThreads + threadIdx.x] = RunAcc{0.0, 0.0, kKeyPosInf, kKeyNegInf};
+    }
+    __syncthreads();
+    // the warp's units: a contiguous share of all units, in column order
+    const uint32_t C = P.n_chunks, n_warps = gridDim.x * kFuseWarps, gw = blockIdx.x * kFuseWarps + wid;
+    const uint32_t per = (F.n_units + n_warps - 1) / n_warps;
+    const uint32_t u_begin = min(F.n_units, gw * per), u_end = min(F.n_units, u_begin + per);
+    uint32_t c = 0xffffffffu, c_end = 0, c_first = 0, n_rows = 0;
+    uint64_t row_off = 0;
+    for (uint32_t u = u_begin; u < u_end; ++u) {
+        if (c == 0xffffffffu || u >= c_end) {
+            // the chunk of unit u (searched once, then stepped)
+            if (c == 0xffffffffu) {
+                uint32_t lo = 0, hi = C;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) / 2;
+                    if (F.unit0[mid] <= u) lo = mid; else hi = mid;
+                }
+                c = lo;
+            } else {
+                do { ++c; } while (F.unit0[c + 1] <= u);
+            }
+            c_first = F.unit0[c];
+            c_end = F.unit0[c + 1];
+            const ChunkDesc cd = F.chunks[c];
+            n_rows = cd.n_rows;
+            row_off = cd.row_off;
+            __syncwarp();
+            if (lane < P.n_cols) s_ci[wid][lane] = F.info[lane][c];
+            __syncwarp();
+        }
+        const uint32_t r = (u - c_first) * kFuseUnit + lane * kFuseRows;  // the lane's first row (in the chunk)
+        uint32_t sel = 0;
+        if (r < n_rows) {
+            const uint32_t left = n_rows - r;
+            sel = left >= kFuseRows ? 0xffu : ((1u << left) - 1u);
+            if (F.in_mask) sel &= mask_word(F.in_mask, row_off + r, F.n_records);
+        }
+        // pack position of the lane's first selected row: warp-exclusive prefix of the counts
+        const uint32_t cnt = __popc(sel);
+        uint32_t inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (static_cast<int>(lane) >= o) inc += y;
+        }
+        const uint32_t n_sel = __shfl_sync(0xffffffffu, inc, 31);
+        if (n_sel == 0) continue;
+        // decode the lane's rows of every column (no loads without selected rows)
+        if (sel) {
+            for (uint32_t j = 0; j < P.n_cols; ++j) {
+                const BuffChunkInfo ci = s_ci[wid][j];
+                if (ci.status) { atomicOr(F.bad, 1u); continue; }
+                unsigned long long d[kFuseRows];
+                fuse_deltas(s_file[j], ci, r / kFuseRows, d);
+                const bool inv_ok = ci.frac <= 1022;
+                const double scale = ci.frac <= 1023 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 + ci.frac) << 52))
+                                                     : __longlong_as_double(0x7ff0000000000000ll);
+                const double inv = inv_ok ? __longlong_as_double(static_cast<long long>(uint64_t(1023 - ci.frac) << 52)) : 0.0;
+                uint32_t p = inc - cnt;
+#pragma unroll
+                for (int i = 0; i < kFuseRows; ++i) {
+                    if (!((sel >> i) & 1u)) continue;
+                    const long long fixed = static_cast<long long>(static_cast<unsigned long long>(ci.base) + d[i]);
+                    if (kExact) islot[j * kFuseStride + fuse_pad(p++)] = fixed;
+                    else wslot[j * kFuseStride + fuse_pad(p++)] = fuse_value(fixed, ci.frac, inv_ok, inv, scale);
+                }
+            }
+        }
+        __syncwarp();
+        // the packed values p = lane + 32 k, k < 8
+        uint32_t ok = 0;
+#pragma unroll
+        for (int k = 0; k < kFuseRows; ++k)
+            if (lane + uint32_t(k) * 32 < n_sel) ok |= 1u << k;
+        for (uint32_t a = 0; a < P.n_aggs; ++a) {
+            using V = typename std::conditional<kExact, long long, double>::type;
+            // accumulator and a two-deep stack, all in registers: the operand
+            // kinds are the same for every lane, so each instruction branches
+            // once and then runs over the lane's values
+            V acc[kFuseRows], st0[kFuseRows], st1[kFuseRows];
+            int sp = 0;
+#pragma unroll
+            for (int k = 0; k < kFuseRows; ++k) acc[k] = st0[k] = st1[k] = 0;
+            for (uint32_t q = s_first[a]; q < s_first[a + 1]; ++q) {
+                const uint8_t op = prog[q].op, src_a = prog[q].a, src_b = prog[q].b;
+                if (op == I_PUSH) {
+                    if (sp == 0) {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) st0[k] = acc[k];
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) st1[k] = acc[k];
+                    }
+                    ++sp;
+                    continue;
+                }
+                V x[kFuseRows], y[kFuseRows];
+                auto fetch = [&](uint8_t src, uint16_t col, double lit_bits, uint32_t sh, V (&out)[kFuseRows]) {
+                    if (src == S_COL) {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) {
+                            const uint32_t at = col * kFuseStride + fuse_pad(lane + uint32_t(k) * 32);
+                            if constexpr (kExact) out[k] = ((ok >> k) & 1u) ? islot[at] : 0;
+                            else out[k] = ((ok >> k) & 1u) ? wslot[at] : 0.0;
+                        }
+                    } else if (src == S_LIT) {
+                        V l;
+                        if constexpr (kExact) l = __double_as_longlong(lit_bits);
+                        else l = lit_bits;
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) out[k] = l;
+                    } else if (src == S_ACC) {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) out[k] = acc[k];
+                    } else if (sp == 1) {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) out[k] = st0[k];
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) out[k] = st1[k];
+                    }
+                    if constexpr (kExact) {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k)
+                            out[k] = static_cast<long long>(static_cast<unsigned long long>(out[k]) << sh);
+                    }
+                };
+                fetch(src_a, prog[q].ca, prog[q].la, prog[q].sa, x);
+                if (op == I_LOAD) {
+#pragma unroll
+                    for (int k = 0; k < kFuseRows; ++k) acc[k] = x[k];
+                    continue;
+                }
+                fetch(src_b, prog[q].cb, prog[q].lb, prog[q].sb, y);
+                if (src_a == S_POP || src_b == S_POP) --sp;
+                if constexpr (kExact) {
+                    if (op == I_ADD) {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) acc[k] = x[k] + y[k];
+                    } else if (op == I_SUB) {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) acc[k] = x[k] - y[k];
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < kFuseRows; ++k) acc[k] = x[k] * y[k];
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < kFuseRows; ++k)
+                        if ((ok >> k) & 1u) acc[k] = op_doit(op, x[k], y[k]);
+                }
+            }
+            if constexpr (kExact) {
+                RunAccI& R = iruns[a * kFuseThreads + threadIdx.x];
+                if (s_kind[a] == EBI_AGGR_SUM) {
+                    unsigned long long lo = 0, hi = 0;
+#pragma unroll
+                    for (int k = 0; k < kFuseRows; ++k)
+                        if ((ok >> k) & 1u) add128(lo, hi, static_cast<unsigned long long>(acc[k]), acc[k] < 0 ? ~0ull : 0ull);
+                    add128(R.lo, R.hi, lo, hi);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < kFuseRows; ++k) {
+                        if (!((ok >> k) & 1u)) continue;
+                        const unsigned long long kk = skey(acc[k]);
+                        R.mn = kk < R.mn ? kk : R.mn;
+                        R.mx = kk > R.mx ? kk : R.mx;
+                    }
+                }
+            } else {
+                run_add(runs[a * kFuseThreads + threadIdx.x], acc, ok, s_kind[a]);
+            }
+        }
+        __syncwarp();  // the slots are rewritten by the next unit
+    }
+    __syncthreads();
+    if constexpr (!kExact) {
+        cta_partials(P, S, runs);
+    } else {
+        // 128-bit sums and keys: per warp, then across warps (part bits: lo, hi, min key, max key)
+        __shared__ unsigned long long r_lo[kFuseWarps], r_hi[kFuseWarps], r_mn[kFuseWarps], r_mx[kFuseWarps];
+        for (uint32_t a = 0; a < P.n_aggs; ++a) {
+            const RunAccI R = iruns[a * kFuseThreads + threadIdx.x];
+            unsigned long long lo = R.lo, hi = R.hi, mn = R.mn, mx = R.mx;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                add128(lo, hi, __shfl_xor_sync(0xffffffffu, lo, o), __shfl_xor_sync(0xffffffffu, hi, o));
+                const unsigned long long omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
+                mn = omn < mn ? omn : mn;
+                mx = omx > mx ? omx : mx;
+            }
+            if (lane == 0) { r_lo[wid] = lo; r_hi[wid] = hi; r_mn[wid] = mn; r_mx[wid] = mx; }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned long long tl = 0, th = 0, tmn = ~0ull, tmx = 0;
+                for (int w = 0; w < kFuseWarps; ++w) {
+                    add128(tl, th, r_lo[w], r_hi[w]);
+                    tmn = r_mn[w] < tmn ? r_mn[w] : tmn;
+                    tmx = r_mx[w] > tmx ? r_mx[w] : tmx;
+                }
+                Quad q;
+                q.x = __longlong_as_double(static_cast<long long>(tl));
+                q.y = __longlong_as_double(static_cast<long long>(th));
+                q.z = __longlong_as_double(static_cast<long long>(tmn));
+                q.w = __longlong_as_double(static_cast<long long>(tmx));
+                S.part[a * uint64_t(gridDim.x) + blockIdx.x] = q;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Exact programs: the CTAs' 128-bit sums and keys, added in CTA order (res
+// bits: sum lo, sum hi, min key, max key; the host scales them).
+__global__ void __launch_bounds__(kExprThreads) expr_fold_exact(ExprPass P, ExprScratch S, uint32_t n_parts) {
+    __shared__ unsigned long long r_lo[kExprThreads / 32], r_hi[kExprThreads / 32], r_mn[kExprThreads / 32],
+        r_mx[kExprThreads / 32];
+    const uint32_t a = blockIdx.x;
+    if (a >= P.n_aggs) return;
+    const Quad* part = S.part + uint64_t(a) * n_parts;
+    unsigned long long lo = 0, hi = 0, mn = ~0ull, mx = 0;
+    for (uint32_t i = threadIdx.x; i < n_parts; i += kExprThreads) {
+        const Quad p = part[i];
+        add128(lo, hi, static_cast<unsigned long long>(__double_as_longlong(p.x)),
+               static_cast<unsigned long long>(__double_as_longlong(p.y)));
+        const unsigned long long pm = static_cast<unsigned long long>(__double_as_longlong(p.z));
+        const unsigned long long px = static_cast<unsigned long long>(__double_as_longlong(p.w));
+        mn = pm < mn ? pm : mn;
+        mx = px > mx ? px : mx;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        add128(lo, hi, __shfl_xor_sync(0xffffffffu, lo, o), __shfl_xor_sync(0xffffffffu, hi, o));
+        const unsigned long long omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
+        mn = omn < mn ? omn : mn;
+        mx = omx > mx ? omx : mx;
+    }
+    if (lane == 0) { r_lo[wid] = lo; r_hi[wid] = hi; r_mn[wid] = mn; r_mx[wid] = mx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long tl = 0, th = 0, tmn = ~0ull, tmx = 0;
+        for (int w = 0; w < kExprThreads / 32; ++w) {
+            add128(tl, th, r_lo[w], r_hi[w]);
+            tmn = r_mn[w] < tmn ? r_mn[w] : tmn;
+            tmx = r_mx[w] > tmx ? r_mx[w] : tmx;
+        }
+        Quad r;
+        r.x = __longlong_as_double(static_cast<long long>(tl));
+        r.y = __longlong_as_double(static_cast<long long>(th));
+        r.z = __longlong_as_double(static_cast<long long>(tmn));
+        r.w = __longlong_as_double(static_cast<long long>(tmx));
         S.res[a] = r;
     }
 }
@@ -475,6 +905,251 @@ int materialize_column(ebi_column* col, const uint64_t* d_mask, uint32_t C, unsi
     return EBI_OK;
 }
 
+// ---- exact BUFF programs ------------------------------------------------------
+// Every value of a BUFF column is fixed * 2^-frac.  A program of +, -, * over
+// such values and dyadic literals runs on the integers when every
+// intermediate stays below 2^53 at its scale: each IEEE operation then
+// returns its exact result, which the integer operation also gives.
+struct Scale {
+    int f;     // value = n * 2^-f
+    int bits;  // |n| < 2^bits
+};
+
+int bitlen(unsigned long long v) { return v ? 64 - __builtin_clzll(v) : 0; }
+
+// x = n * 2^-f with |n| < 2^53 and the least f >= 0.
+bool dyadic(double x, long long* n, Scale* sc) {
+    if (x == 0.0) { *n = 0; *sc = Scale{0, 0}; return true; }
+    if (!std::isfinite(x)) return false;
+    int e = 0;
+    const double m = std::frexp(std::fabs(x), &e);  // |x| = m * 2^e, m in [0.5, 1)
+    unsigned long long M = static_cast<unsigned long long>(std::ldexp(m, 53));
+    int k = e - 53;
+    while (!(M & 1ull)) { M >>= 1; ++k; }
+    if (k >= 0) {
+        if (bitlen(M) + k > 53) return false;
+        M <<= k;
+        k = 0;
+    }
+    *n = x < 0 ? -static_cast<long long>(M) : static_cast<long long>(M);
+    *sc = Scale{-k, bitlen(M)};
+    return true;
+}
+
+// Rewrites the pass's program for integer evaluation (shifts, integer
+// literals) and gives each aggregation's result scale; false when a step is
+// not provably exact.
+bool exact_program(std::vector<Instr>& prog, const ExprPass& P, const std::vector<Scale>& col, std::vector<int>& f_out) {
+    f_out.assign(P.n_aggs, 0);
+    for (uint32_t a = 0; a < P.n_aggs; ++a) {
+        Scale acc{0, 0};
+        std::vector<Scale> stack;
+        for (uint32_t q = P.first[a]; q < P.first[a + 1]; ++q) {
+            Instr& I = prog[q];
+            if (I.op == I_PUSH) { stack.push_back(acc); continue; }
+            if (I.op == I_DIV) return false;
+            auto operand = [&](uint8_t src, uint16_t c, double& lit, Scale& sc) -> bool {
+                if (src == S_ACC) { sc = acc; return true; }
+                if (src == S_POP) { sc = stack.back(); return true; }
+                if (src == S_COL) { sc = col[c]; return true; }
+                long long n = 0;
+                if (!dyadic(lit, &n, &sc)) return false;
+                std::memcpy(&lit, &n, sizeof n);
+                return true;
+            };
+            Scale x{}, y{};
+            if (!operand(I.a, I.ca, I.la, x)) return false;
+            I.sa = I.sb = 0;
+            if (I.op == I_LOAD) {
+                acc = x;
+            } else {
+                if (!operand(I.b, I.cb, I.lb, y)) return false;
+                if (I.a == S_POP || I.b == S_POP) stack.pop_back();
+                if (I.op == I_MUL) {
+                    acc = Scale{x.f + y.f, x.bits + y.bits};
+                } else {
+                    const int f = std::max(x.f, y.f);
+                    I.sa = static_cast<uint8_t>(f - x.f);
+                    I.sb = static_cast<uint8_t>(f - y.f);
+                    if (x.bits + I.sa > 62 || y.bits + I.sb > 62) return false;
+                    acc = Scale{f, std::max(x.bits + I.sa, y.bits + I.sb) + 1};
+                }
+            }
+            if (acc.bits > 53 || acc.f > 1000) return false;
+        }
+        f_out[a] = acc.f;
+    }
+    return true;
+}
+
+// n * 2^-f for a two's complement 128-bit n, rounded to nearest even once.
+double scaled_i128(unsigned long long lo, unsigned long long hi, int f) {
+    const __int128 v = static_cast<__int128>((static_cast<unsigned __int128>(hi) << 64) | lo);
+    const bool neg = v < 0;
+    unsigned __int128 m = neg ? -static_cast<unsigned __int128>(v) : static_cast<unsigned __int128>(v);
+    if (m == 0) return 0.0;
+    const unsigned long long mh = static_cast<unsigned long long>(m >> 64);
+    const int p = mh ? 127 - __builtin_clzll(mh) : 63 - __builtin_clzll(static_cast<unsigned long long>(m));
+    double d;
+    if (p <= 52) {
+        d = static_cast<double>(static_cast<unsigned long long>(m));
+    } else {
+        int sh = p - 52;
+        unsigned __int128 top = m >> sh;
+        const unsigned __int128 rem = m & ((static_cast<unsigned __int128>(1) << sh) - 1);
+        const unsigned __int128 half = static_cast<unsigned __int128>(1) << (sh - 1);
+        if (rem > half || (rem == half && (top & 1))) {
+            ++top;
+            if (top >> 53) { top >>= 1; ++sh; }
+        }
+        d = std::ldexp(static_cast<double>(static_cast<unsigned long long>(top)), sh);
+    }
+    d = std::ldexp(d, -f);
+    return neg ? -d : d;
+}
+
+// The fused path applies: scalar results only, programs at most kFuseStack
+// deep, at most kFuseCols BUFF columns at full precision whose first C
+// chunks cover the same rows.
+bool fusable(ebi_column* const* cols, const std::vector<uint32_t>& slot_cols, const ebi_aggregation* aggs,
+             const std::vector<uint32_t>& idx, const std::vector<std::vector<Instr>>& progs, uint32_t C) {
+    if (slot_cols.empty() || slot_cols.size() > static_cast<size_t>(kFuseCols)) return false;
+    for (uint32_t a : idx)
+        if (aggs[a].kind == EBI_AGGR_NONE) return false;
+    for (uint32_t a : idx) {  // the fused kernels keep a two-deep stack in registers
+        int depth = 0;
+        for (const Instr& I : progs[a]) {
+            if (I.op == I_PUSH && ++depth > kFuseStack) return false;
+            if (I.a == S_POP || I.b == S_POP) --depth;
+        }
+    }
+    const ebi_column* r = cols[slot_cols[0]];
+    for (uint32_t j : slot_cols) {
+        const ebi_column* c = cols[j];
+        if (c->scheme != EBI_BUFF || c->precision >= 0 || !c->d_buff) return false;
+        for (uint32_t k = 0; k < C; ++k)
+            if (c->chunks[k].n_rows != r->chunks[k].n_rows || c->chunks[k].row_off != r->chunks[k].row_off) return false;
+    }
+    return true;
+}
+
+// Runs a fusable pass.  *fell_back: a chunk is unreadable, the caller runs
+// the general path (which reports the chunk's error in chunk order).
+int run_fused(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<uint32_t>& idx, const ExprPass& P,
+              const std::vector<Instr>& prog, const std::vector<uint32_t>& slot_cols, const uint64_t* d_mask,
+              uint32_t C, cudaStream_t s, bool* fell_back) {
+    const ebi_column* r = cols[slot_cols[0]];
+    std::vector<uint32_t> unit0(C + 1);
+    uint64_t units = 0;
+    for (uint32_t c = 0; c < C; ++c) {
+        unit0[c] = static_cast<uint32_t>(units);
+        units += (r->chunks[c].n_rows + kFuseUnit - 1) / kFuseUnit;
+    }
+    if (units > 0xffffffffull) return fail(EBI_E_INVALID, "too many rows");
+    unit0[C] = static_cast<uint32_t>(units);
+    const uint32_t n_units = static_cast<uint32_t>(units);
+    // integer evaluation when every column has one scale and the program is provably exact
+    std::vector<Instr> iprog = prog;
+    std::vector<int> f_out;
+    std::vector<Scale> col_scale;
+    bool exact = true;
+    for (uint32_t j : slot_cols) {
+        const ebi_column* c = cols[j];
+        if (!c->buff_same_frac || c->buff_fixed_bits > 53) exact = false;
+        col_scale.push_back(Scale{static_cast<int>(c->buff_frac), static_cast<int>(c->buff_fixed_bits)});
+    }
+    exact = exact && exact_program(iprog, P, col_scale, f_out);
+    auto kernel = exact ? expr_buff_fused<true> : expr_buff_fused<false>;
+    // grid: the CTAs that fit the device at once (each keeps running sums)
+    const size_t smem = size_t(kFuseWarps) * P.n_cols * kFuseStride * sizeof(double) +
+                        size_t(P.n_aggs) * kFuseThreads * sizeof(RunAcc);
+    constexpr int kSmemMax = static_cast<int>(kFuseWarps * kFuseCols * kFuseStride * sizeof(double) +
+                                              kMaxAggs * kFuseThreads * sizeof(RunAcc));
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(expr_buff_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax) != cudaSuccess
+            ? cudaGetLastError()
+            : cudaFuncSetAttribute(expr_buff_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax);
+    if (attr != cudaSuccess) return cuda_fail(attr, "expr_buff_fused shared memory");
+    int dev = 0, sms = 0, per_sm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFuseThreads, smem));
+    const uint32_t grid = std::max<uint32_t>(
+        1, std::min<uint32_t>((n_units + kFuseWarps - 1) / kFuseWarps, static_cast<uint32_t>(sms * std::max(per_sm, 1))));
+    // device: unit0, bad flag, program, partials + results
+    uint32_t* d_unit0 = nullptr;
+    unsigned long long* d_tot = nullptr;
+    Instr* d_prog = nullptr;
+    Quad* d_part = nullptr;
+    auto done = [&](int code) {
+        if (d_unit0) cudaFreeAsync(d_unit0, s);
+        if (d_tot) cudaFreeAsync(d_tot, s);
+        if (d_prog) cudaFreeAsync(d_prog, s);
+        if (d_part) cudaFreeAsync(d_part, s);
+        return code;
+    };
+    if (cudaMallocAsync(reinterpret_cast<void**>(&d_unit0), (C + 1) * sizeof(uint32_t), s) != cudaSuccess ||
+        cudaMallocAsync(reinterpret_cast<void**>(&d_tot), 8, s) != cudaSuccess ||
+        cudaMallocAsync(reinterpret_cast<void**>(&d_prog), prog.size() * sizeof(Instr), s) != cudaSuccess ||
+        cudaMallocAsync(reinterpret_cast<void**>(&d_part), (uint64_t(grid) + 1) * P.n_aggs * sizeof(Quad), s) !=
+            cudaSuccess)
+        return done(fail(EBI_E_OOM, "expression scratch"));
+    ExprScratch S{};
+    S.part = d_part;
+    S.res = d_part + uint64_t(grid) * P.n_aggs;
+    S.prog = d_prog;
+    FusePass F{};
+    for (uint32_t j = 0; j < P.n_cols; ++j) {
+        F.file[j] = cols[slot_cols[j]]->d_file;
+        F.info[j] = cols[slot_cols[j]]->d_buff;
+    }
+    F.chunks = r->d_chunks;
+    F.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
+    F.n_records = r->n_records;
+    F.unit0 = d_unit0;
+    F.n_units = n_units;
+    F.bad = reinterpret_cast<unsigned int*>(d_tot);
+    std::vector<Quad> res(P.n_aggs);
+    unsigned long long bad = 0;
+    CK(cudaMemcpyAsync(d_unit0, unit0.data(), unit0.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(d_tot, 0, 8, s));
+    CK(cudaMemcpyAsync(d_prog, (exact ? iprog : prog).data(), prog.size() * sizeof(Instr), cudaMemcpyHostToDevice, s));
+    // every CTA writes its partials (identities when it gets no tile)
+    kernel<<<grid, kFuseThreads, smem, s>>>(P, S, F);
+    if (exact) expr_fold_exact<<<P.n_aggs, kExprThreads, 0, s>>>(P, S, grid);
+    else expr_fold<<<P.n_aggs, kExprThreads, 0, s>>>(P, S, grid);
+    count_launch(2);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(res.data(), S.res, res.size() * sizeof(Quad), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_tot, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // unit0 and prog are host memory
+    if (e != cudaSuccess) return done(cuda_fail(e, "fused expression evaluation"));
+    if (bad) {
+        *fell_back = true;
+        return done(EBI_OK);
+    }
+    for (uint32_t a = 0; a < P.n_aggs; ++a) {
+        ebi_aggregation& g = aggs[idx[a]];
+        if (!exact) {
+            g.scalar = g.kind == EBI_AGGR_SUM ? res[a].x : g.kind == EBI_AGGR_MIN ? res[a].y : res[a].z;
+            continue;
+        }
+        unsigned long long w[4];
+        std::memcpy(w, &res[a], sizeof w);
+        const unsigned long long sign = 0x8000000000000000ull;
+        if (g.kind == EBI_AGGR_SUM) {
+            g.scalar = scaled_i128(w[0], w[1], f_out[a]);
+        } else if (g.kind == EBI_AGGR_MIN) {
+            g.scalar = w[2] == (static_cast<unsigned long long>(LLONG_MAX) ^ sign)
+                           ? HUGE_VAL : std::ldexp(static_cast<double>(static_cast<long long>(w[2] ^ sign)), -f_out[a]);
+        } else {
+            g.scalar = w[3] == (static_cast<unsigned long long>(LLONG_MIN) ^ sign)
+                           ? -HUGE_VAL : std::ldexp(static_cast<double>(static_cast<long long>(w[3] ^ sign)), -f_out[a]);
+        }
+    }
+    return done(EBI_OK);
+}
+
 // One evaluation pass: aggregations idx (at most kMaxAggs, kPassInstr
 // instructions and kMaxCols columns together) with their programs.
 int run_pass(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<uint32_t>& idx,
@@ -504,6 +1179,11 @@ int run_pass(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<u
     }
     P.first[P.n_aggs] = static_cast<uint32_t>(prog.size());
     P.n_cols = static_cast<uint32_t>(slot_cols.size());
+    if (fusable(cols, slot_cols, aggs, idx, progs, C)) {
+        bool fell_back = false;
+        if (int st = run_fused(cols, aggs, idx, P, prog, slot_cols, d_mask, C, s, &fell_back)) return st;
+        if (!fell_back) return EBI_OK;
+    }
 
     // scratch: chunk offsets, lengths, array offsets, items, totals; the
     // columns' values; the item partials; the program
@@ -542,24 +1222,31 @@ int run_pass(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<u
         P.vals[j] = vals[j];
         total_vals += n;
     }
-    // items: at most sum over chunks of ceil(longest run / kExprItem)
+    // items: at most sum over chunks of ceil(longest run / kExprItem); the
+    // grid: the CTAs that fit the device at once (each keeps running sums)
     const uint64_t items_cap = total_vals / kExprItem + C + 1;
-    if (cudaMallocAsync(reinterpret_cast<void**>(&d_part), (items_cap + 1) * P.n_aggs * sizeof(Quad), s) !=
+    const size_t smem = size_t(P.n_aggs) * kExprThreads * sizeof(RunAcc);
+    static const cudaError_t attr = cudaFuncSetAttribute(expr_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         static_cast<int>(kMaxAggs * kExprThreads * sizeof(RunAcc)));
+    if (attr != cudaSuccess) return done(cuda_fail(attr, "expr_eval shared memory"));
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, expr_eval, kExprThreads, smem);
+    const uint32_t grid = static_cast<uint32_t>(
+        std::max<uint64_t>(1, std::min<uint64_t>(items_cap, uint64_t(sms) * std::max(per_sm, 1))));
+    if (cudaMallocAsync(reinterpret_cast<void**>(&d_part), (uint64_t(grid) + 1) * P.n_aggs * sizeof(Quad), s) !=
         cudaSuccess)
         return done(fail(EBI_E_OOM, "expression partials"));
     S.part = d_part;
-    S.res = d_part + items_cap * P.n_aggs;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t grid = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(items_cap, uint64_t(sms) * 4)));
+    S.res = d_part + uint64_t(grid) * P.n_aggs;
     std::vector<unsigned long long> totals(P.n_aggs + 1);
     std::vector<Quad> res(P.n_aggs);
     cudaError_t e = cudaMemcpyAsync(d_prog, prog.data(), prog.size() * sizeof(Instr), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
         expr_prepare<<<1, kExprThreads, 0, s>>>(P, S);
-        expr_eval<<<grid, kExprThreads, 0, s>>>(P, S);
-        expr_fold<<<P.n_aggs, kExprThreads, 0, s>>>(P, S);
+        expr_eval<<<grid, kExprThreads, smem, s>>>(P, S);
+        expr_fold<<<P.n_aggs, kExprThreads, 0, s>>>(P, S, grid);
         count_launch(3);
         e = cudaGetLastError();
     }
