@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -467,6 +468,171 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+TPCH_ROWS = 59_986_052       # lineitem rows at scale factor 10
+TPCH_CHUNK = 16_777_216      # ChunkOption::RecordCount(128 MiB / 8), the experimenter's default chunking
+
+
+def tpch_columns(n, seed=6):
+    """lineitem-shaped columns (l_quantity, l_extendedprice, l_discount, l_tax) drawn like dbgen's:
+    quantity 1..50, price = quantity x part price (900..2000 + cents), discount 0.00..0.10, tax 0.00..0.08."""
+    rng = np.random.default_rng(seed)
+    qty = rng.integers(1, 51, n).astype(np.float64)
+    part = np.round(rng.uniform(900.0, 2000.0, n), 2)
+    price = np.round(qty * part, 2)
+    disc = rng.integers(0, 11, n) / 100.0
+    tax = rng.integers(0, 9, n) / 100.0
+    return [qty, price, disc, tax]
+
+
+def tpch_queries(E):
+    one = E.Expr.Literal(1.0)
+    q1 = [E.Aggregation.sum(E.Expr.Index(0)), E.Aggregation.sum(E.Expr.Index(1)),
+          E.Aggregation.sum(E.Expr.Index(1) * (one - E.Expr.Index(2))),
+          E.Aggregation.sum((E.Expr.Index(1) * (one - E.Expr.Index(2))) * (one + E.Expr.Index(3))),
+          E.Aggregation.sum(E.Expr.Index(2))]
+    p_disc = E.Predicate.range(E.RangeValue.inclusive(0.05), E.RangeValue.inclusive(0.07))
+    p_qty = E.Predicate.range(E.RangeValue.NONE, E.RangeValue.exclusive(24.0))
+    q6 = E.Aggregation.sum(E.Expr.Index(1) * E.Expr.Index(2))
+    return q1, p_disc, p_qty, q6
+
+
+def tpch_oracle(datas, query, O, n, exact=False):
+    """The query on the oracle (the restatement of ebi's Decoder / Aggregation loops), one thread.
+    exact: each sum's exactly rounded value instead (fsum of the values the oracle's expression yields;
+    the in-situ BUFF sums of single columns are exact integer sums already)."""
+    import math
+
+    ds = [O.Decoder(d) for d in datas]
+    if exact:
+        I = lambda i: (O.EXPR_INDEX, i, 0.0)
+        L = lambda x: (O.EXPR_LITERAL, 0, x)
+        if query == "tpch_q6":
+            m = ds[2].filter(O.rng(O.BOUND_INCLUSIVE, 0.05, O.BOUND_INCLUSIVE, 0.07))
+            m = ds[0].filter(O.rng(O.BOUND_NONE, 0.0, O.BOUND_EXCLUSIVE, 24.0), m)
+            v = O.aggregate(ds, O.AGGR_NONE, [I(1), I(2), (O.EXPR_MUL, 0, 0.0)], m)
+            return [math.fsum(v)], [float(np.abs(v).sum())]
+        pfs = [[I(1), L(1.0), I(2), (O.EXPR_SUB, 0, 0.0), (O.EXPR_MUL, 0, 0.0)],
+               [I(1), L(1.0), I(2), (O.EXPR_SUB, 0, 0.0), (O.EXPR_MUL, 0, 0.0), L(1.0), I(3), (O.EXPR_ADD, 0, 0.0),
+                (O.EXPR_MUL, 0, 0.0)]]
+        vals = [O.aggregate(ds, O.AGGR_NONE, pf) for pf in pfs]
+        ex = [ds[0].sum(), ds[1].sum(), math.fsum(vals[0]), math.fsum(vals[1]), ds[2].sum()]
+        mag = [abs(ex[0]), abs(ex[1]), float(np.abs(vals[0]).sum()), float(np.abs(vals[1]).sum()), abs(ex[4])]
+        return ex, mag
+    I = lambda i: (O.EXPR_INDEX, i, 0.0)
+    L = lambda x: (O.EXPR_LITERAL, 0, x)
+    if query == "tpch_q6":
+        m = ds[2].filter(O.rng(O.BOUND_INCLUSIVE, 0.05, O.BOUND_INCLUSIVE, 0.07))
+        m = ds[0].filter(O.rng(O.BOUND_NONE, 0.0, O.BOUND_EXCLUSIVE, 24.0), m)
+        return [O.aggregate(ds, O.AGGR_SUM, [I(1), I(2), (O.EXPR_MUL, 0, 0.0)], m)]
+    q1 = [[I(0)], [I(1)], [I(1), L(1.0), I(2), (O.EXPR_SUB, 0, 0.0), (O.EXPR_MUL, 0, 0.0)],
+          [I(1), L(1.0), I(2), (O.EXPR_SUB, 0, 0.0), (O.EXPR_MUL, 0, 0.0), L(1.0), I(3), (O.EXPR_ADD, 0, 0.0),
+           (O.EXPR_MUL, 0, 0.0)], [I(2)]]
+    return [O.aggregate(ds, O.AGGR_SUM, pf) for pf in q1]
+
+
+def run_tpch(args):
+    """TPC-H Q1 / Q6 shapes over lineitem-shaped BUFF columns (experimenter/src/tpch.rs:190-461): Q6 filters
+    l_discount, then l_quantity under that bitmask, then sums l_extendedprice * l_discount over it; Q1 runs
+    five sums (two of expressions) with Aggregation::compute_multiple."""
+    import torch
+
+    import ebi_gb300 as E
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    E.load_library()
+    n = args.rows or TPCH_ROWS
+    cols = tpch_columns(n)
+    datas = [E.encode(c, "buff", ("record_count", TPCH_CHUNK), 100) for c in cols]
+    ds = [E.Decoder(d, device=str(dev)) for d in datas]
+    q1, p_disc, p_qty, q6 = tpch_queries(E)
+    col_bytes = [sum(d.chunk_info(c)[1] for c in range(d.n_chunks)) for d in ds]
+    mask_bytes = 8 * ds[0].mask_words
+    if args.workload == "tpch_q6":
+        used = [0, 1, 2]
+        # disc + mask out; qty + mask in + mask out; price + disc + mask in
+        alg = col_bytes[2] + mask_bytes + col_bytes[0] + 2 * mask_bytes + col_bytes[1] + col_bytes[2] + mask_bytes
+
+        def step():
+            m = ds[2].filter(p_disc)
+            m = ds[0].filter(p_qty, m)
+            return [q6.compute(ds, m)]
+    else:
+        used = [0, 1, 2, 3]
+        # three in-situ sums (qty, price, disc) and one fused pass over price, disc and tax
+        alg = col_bytes[0] + col_bytes[1] + col_bytes[2] + (col_bytes[1] + col_bytes[2] + col_bytes[3])
+
+        def step():
+            return E.Aggregation.compute_multiple(q1, ds)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    clean = torch.zeros(32 << 20, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    steps = min(args.steps, 100)
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = E.kernel_launches()
+    ts = []
+    t0 = time.perf_counter()
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        clean.sum()
+        torch.cuda._sleep(1_000_000)
+        ev0.record(stream)
+        got = step()
+        ev1.record(stream)
+        ev1.synchronize()
+        ts.append(ev0.elapsed_time(ev1) / 1e3)
+    t1 = time.perf_counter()
+    sampler.stop()
+    launches = E.kernel_launches() - launches0
+    t = statistics.median(ts)
+    rows_dec = n * len(used)
+    peak, peak_kind = measured_peak()
+    line = {"metric": "decode+filter+aggregate GB/s (decoded, all columns read)", "value": round(8.0 * rows_dec / t / 1e9, 3),
+            "unit": "GB/s", "n_gpus": 1, "steps": steps, "warmup": max(args.warmup, 3), "ms_per_step": round(1e3 * t, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i64 -> f64",
+            "data": "synthetic lineitem-shaped columns (seeded numpy; dbgen's value ranges)",
+            "config": {"workload": f"{args.workload}: TPC-H {'Q6' if args.workload == 'tpch_q6' else 'Q1'} shape over "
+                                   f"{n} lineitem rows (scale factor {n / 5_998_405:.1f}), BUFF scale 100, "
+                                   f"{TPCH_CHUNK}-row chunks", "rows": n, "column_bytes": col_bytes,
+                       "l2": "flushed before every step (256 MiB write, then a 256 MiB read of another buffer)"},
+            "roofline": {"bound": "hbm", "achieved": round(alg / t / 1e9, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(alg / t / 1e9 / peak, 4), "traffic": None, "scope": "whole step (every launch)",
+                         "algorithmic_bytes_per_step": alg, "peak_source": peak_kind},
+            "gpu_launches": int(launches), "clocks": sampler.summary(t0, t1), "result": got}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        m = min(n, 5_998_405)
+        sample = [E.encode(c[:m], "buff", ("record_count", TPCH_CHUNK), 100) for c in cols]
+        c0 = time.perf_counter()
+        tpch_oracle(sample, args.workload, O, m)
+        dt = time.perf_counter() - c0
+        line["cpu_baseline"] = {"value": round(8.0 * m * len(used) / dt / 1e9, 3), "unit": "GB/s", "cores": 1,
+                                "kind": "port", "sample": f"the same query over the first {m} rows (scale factor 1), "
+                                                          "the C restatement of ebi's Decoder and Aggregation loops, one thread"}
+    if not args.no_parity_check:
+        from oracle import oracle as O
+
+        # the reference sums each chunk sequentially in f64; over 16,777,216-row chunks its own rounding
+        # error (at most (n - 1) u sum|x| per chunk) exceeds 1e-12, so the check is against both that
+        # sequential oracle, within its error bound, and the exactly rounded sum
+        want = tpch_oracle(datas, args.workload, O, n)
+        exact, mag = tpch_oracle(datas, args.workload, O, n, exact=True)
+        u = 2.0 ** -53
+        bound = [(TPCH_CHUNK - 1) * u * m + 1e-12 * m for m in mag]
+        line["parity_check"] = {
+            "sequential_oracle": want, "exact": exact,
+            "max_rel_diff_vs_sequential_oracle": max(abs(g - w) / max(abs(w), 1e-300) for g, w in zip(got, want)),
+            "max_ulps_from_exact": max(abs(g - e) / max(math.ulp(e), 5e-324) for g, e in zip(got, exact)),
+            "within_sequential_oracle_error_bound": bool(all(abs(g - w) <= b for g, w, b in zip(got, want, bound)))}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -478,11 +644,18 @@ def main():
     ap.add_argument("--no-parity-check", action="store_true")
     ap.add_argument("--rows", type=int, default=0, help="column length (profiling runs use smaller columns)")
     ap.add_argument("--workload", default="buff", choices=["buff", "gorilla", "chimp128", "rle", "elf", "elf_on_chimp",
-                                                               "batched", "serving"])
+                                                               "batched", "serving", "tpch_q6", "tpch_q1"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="batched / serving: fraction of the configuration's columns to build")
     args = ap.parse_args()
     wl = None
+    if args.workload in ("tpch_q6", "tpch_q1"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the TPC-H shapes are measured against the oracle in "
+                                                                  "their own line (cpu_baseline)"}))
+            return
+        run_tpch(args)
+        return
     if args.workload in ("batched", "serving"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "batched and serving shapes have no CPU reference path"}))

@@ -303,11 +303,13 @@ typedef struct {
  * values of its column's chunk i selected by the mask, the operands of an
  * operator are zipped to the shorter one (Expr::compute_chunk,
  * expr.rs:67-135), and the chunk results combine in chunk order
- * (AggregationResult::concat).  Sums are within 1e-12 of the reference's
- * per-chunk sequential sums relative to the sum of magnitudes (each thread
- * adds a few values plainly and their subtotals with compensation: within
- * 16 eps of the exact sum relative to it); min / max ignore NaN operands as
- * f64::min / f64::max do.
+ * (AggregationResult::concat).  Sums: on chunk-aligned BUFF columns whose
+ * intermediates provably stay below 2^53 (integer evaluation) the exactly
+ * rounded sum; otherwise within 16 eps of the exact sum relative to the sum
+ * of magnitudes.  Against the reference's per-chunk sequential f64 sums the
+ * difference stays within their own rounding-error bound, (n - 1) 2^-53 of
+ * the magnitudes per chunk of n values: below 1e-12 for chunks up to 9,007
+ * values.  Min / max ignore NaN operands as f64::min / f64::max do.
  * d_mask (device, NULL = None) covers the rows of every column read.
  * Errors: EBI_E_PRECONDITION for a Literal root or an operator over two
  * literals (when cols[0] has chunks); EBI_E_INVALID where the reference
