@@ -61,6 +61,11 @@ struct Partial {
 };
 
 
+__device__ __forceinline__ unsigned long long sat_add(unsigned long long a, unsigned long long b) {
+    const unsigned long long c = a + b;
+    return c < a ? ~0ull : c;
+}
+
 // Ends a warp's run over one chunk: per-chunk partials (for the chunk-ordered
 // fallback fold) and the warp's exact query totals.
 // `to_acc` false: the column's totals are exact whatever the query (see
@@ -80,7 +85,7 @@ __device__ __forceinline__ void flush_partial(const QueryParams& q, uint32_t chu
         const __int128 ap = piece < 0 ? -piece : piece;
         wt.sum_fixed += static_cast<unsigned long long>(piece);
         if (ap >= (static_cast<__int128>(1) << 53)) wt.nonexact = 1;
-        else wt.abs_bound += static_cast<double>(static_cast<long long>(ap));
+        else wt.abs_bound = sat_add(wt.abs_bound, static_cast<unsigned long long>(ap));
         wt.count += c;
         const long long fmax = static_cast<long long>(static_cast<unsigned long long>(base) + mx);
         const long long fmin = static_cast<long long>(static_cast<unsigned long long>(base) + mn);
@@ -95,6 +100,13 @@ __device__ __forceinline__ void chunk_error(const QueryParams& q, ScanTotals* T,
     atomicMin(&T->bad_chunk, c);
 }
 
+// A scan's totals at rest (the state every query starts from).
+__device__ __forceinline__ void scan_totals_rest(ScanTotals* T) {
+    T->sum_fixed = 0; T->abs_bound = 0; T->count = 0;
+    T->max_fixed = LLONG_MIN; T->min_fixed = LLONG_MAX;
+    T->done = 0; T->bad_chunk = 0xffffffffu; T->nonexact = 0; T->next = 0;
+}
+
 // The last CTA's fold of the query totals (chunk-ordered fallback when the
 // exact integer total does not apply).
 __device__ void scan_finalize(const QueryParams& q, const BuffChunkInfo* info, ScanTotals* T, const ScanTotals& t,
@@ -107,7 +119,7 @@ __device__ void scan_finalize(const QueryParams& q, const BuffChunkInfo* info, S
         if (t.bad_chunk != 0xffffffffu) r.status = q.acc[t.bad_chunk].status;
         r.count = t.count;
         r.sum = 0.0; r.min = inf; r.max = -inf;
-        if (fast_ok && !t.nonexact && t.abs_bound < 4503599627370496.0 /* 2^52 */) {
+        if (fast_ok && !t.nonexact && t.abs_bound < (1ull << 52)) {
             // Every chunk sum and every prefix of the chunk-ordered fold is an
             // exact multiple of 2^-frac below 2^53 of them: the reference's
             // sequential f64 fold is exact and equals the exact total.
@@ -120,7 +132,7 @@ __device__ void scan_finalize(const QueryParams& q, const BuffChunkInfo* info, S
             fold_buff_chunks(q, r);
         }
         *res = r;
-        T->done = 0; T->bad_chunk = 0xffffffffu; T->next = 0;
+        scan_totals_rest(T);
     }
     __syncthreads();
     // re-arm the accumulators the query touched (all of them but in an exact
@@ -139,7 +151,7 @@ __device__ void scan_finalize(const QueryParams& q, const BuffChunkInfo* info, S
 __device__ __forceinline__ void add_tot(WarpTot& a, const WarpTot& b) {
     a.sum_fixed += b.sum_fixed;
     a.count += b.count;
-    a.abs_bound += b.abs_bound;  // integers below 2^53: exact in any order while the total stays below 2^53
+    a.abs_bound = sat_add(a.abs_bound, b.abs_bound);
     a.max_fixed = b.max_fixed > a.max_fixed ? b.max_fixed : a.max_fixed;
     a.min_fixed = b.min_fixed < a.min_fixed ? b.min_fixed : a.min_fixed;
     a.nonexact |= b.nonexact;
@@ -151,14 +163,34 @@ __device__ __forceinline__ void add_tot(WarpTot& a, const WarpTot& b) {
 // `exact`: the column's totals are exact for any query (its chunks share one
 // frac and the sum of |value| over all rows stays below 2^52), so the
 // per-chunk accumulators are neither fed nor re-armed.
+// totals_only: the CTA adds its totals into T with fire-and-forget atomics
+// and no CTA folds (no fence, no slot reduction): the host reads T after the
+// kernel and scales the exact totals itself.  Only for exact columns queried
+// without an input bitmask, whose per-chunk accumulators are never touched.
 __device__ __forceinline__ void cta_finish(const QueryParams& q, const BuffChunkInfo* info, ScanTotals* T,
                                            QueryResult* res, uint32_t frac, bool fast_ok, const WarpTot* wtot,
-                                           int n_warps, bool exact = false) {
+                                           int n_warps, bool exact = false, bool totals_only = false) {
     WarpTot* slots = scan_slots(T);
     __syncthreads();
+    if (totals_only) {
+        if (threadIdx.x == 0) {
+            WarpTot c{0, 0, 0, LLONG_MIN, LLONG_MAX, 0};
+            for (int w = 0; w < n_warps; ++w) add_tot(c, wtot[w]);
+            if (c.count) {
+                atomicAdd(&T->sum_fixed, c.sum_fixed);
+                atomicAdd(&T->count, c.count);
+                atomicMax(&T->max_fixed, c.max_fixed);
+                atomicMin(&T->min_fixed, c.min_fixed);
+                // every CTA's bound is below 2^52 or flagged: the sum of at most kScanSlots of them cannot wrap
+                if (c.nonexact || c.abs_bound >= (1ull << 52)) atomicOr(&T->nonexact, 1u);
+                else atomicAdd(&T->abs_bound, c.abs_bound);
+            }
+        }
+        return;
+    }
     __shared__ unsigned int s_last;
     if (threadIdx.x == 0) {
-        WarpTot c{0, 0, 0.0, LLONG_MIN, LLONG_MAX, 0};
+        WarpTot c{0, 0, 0, LLONG_MIN, LLONG_MAX, 0};
         for (int w = 0; w < n_warps; ++w) add_tot(c, wtot[w]);
         slots[blockIdx.x] = c;
         // release: the slot is visible before the count; acquire: the last
@@ -170,7 +202,7 @@ __device__ __forceinline__ void cta_finish(const QueryParams& q, const BuffChunk
     if (!s_last) return;
     // reduce the CTAs' slots (published before their `done` increments,
     // read from L2): per thread, then per warp, then across warps
-    WarpTot c{0, 0, 0.0, LLONG_MIN, LLONG_MAX, 0};
+    WarpTot c{0, 0, 0, LLONG_MIN, LLONG_MAX, 0};
     static_assert(sizeof(WarpTot) == 48, "three 16-byte words per slot");
     for (uint32_t i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
         // L2 loads (the slots were written by other SMs), three per slot, all in flight together
@@ -179,7 +211,7 @@ __device__ __forceinline__ void cta_finish(const QueryParams& q, const BuffChunk
         WarpTot x;
         x.sum_fixed = a.x;
         x.count = a.y;
-        x.abs_bound = __longlong_as_double(static_cast<long long>(b.x));
+        x.abs_bound = b.x;
         x.max_fixed = static_cast<long long>(b.y);
         x.min_fixed = static_cast<long long>(d.x);
         x.nonexact = static_cast<unsigned int>(d.y);
@@ -201,7 +233,7 @@ __device__ __forceinline__ void cta_finish(const QueryParams& q, const BuffChunk
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
     __syncthreads();
     if (threadIdx.x == 0) {
-        WarpTot a{0, 0, 0.0, LLONG_MIN, LLONG_MAX, 0};
+        WarpTot a{0, 0, 0, LLONG_MIN, LLONG_MAX, 0};
         for (uint32_t w = 0; w < (blockDim.x + 31) / 32; ++w) add_tot(a, part[w]);
         t.sum_fixed = a.sum_fixed;
         t.count = a.count;

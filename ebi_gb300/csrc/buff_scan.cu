@@ -547,7 +547,7 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
     if (threadIdx.x < kScanConsumers) {
     // ---- consumer warps ----
     Partial part{0, 0, 0, ~0ull};
-    WarpTot wt{0, 0, 0.0, LLONG_MIN, LLONG_MAX, 0};
+    WarpTot wt{0, 0, 0, LLONG_MIN, LLONG_MAX, 0};
     uint32_t cur = 0xffffffffu;
     int64_t cur_base = 0;
     for (uint32_t i = 0; i < count; ++i) {

@@ -322,11 +322,18 @@ buff_stream_kernel(QueryParams q, const BuffChunkInfo* info, const uint2* __rest
                    uint32_t n_units, uint32_t upc, ScanTotals* T, QueryResult* res, uint32_t frac, uint32_t fold) {
     __shared__ WarpTot wtot[kStreamWarps];
     const bool exact = (fold & 2u) != 0;
+    const bool totals_only = (fold & 4u) != 0;
+    // totals-only queries alternate between two totals blocks (fold bit 3: the
+    // upper one); this launch sets the other block at rest for the next query
+    if (totals_only && blockIdx.x == 0 && threadIdx.x == 0)
+        scan_totals_rest(reinterpret_cast<ScanTotals*>(reinterpret_cast<uint8_t*>(T) +
+                                                      ((fold & 8u) ? -static_cast<ptrdiff_t>(kScanTotalsBytes)
+                                                                   : static_cast<ptrdiff_t>(kScanTotalsBytes))));
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const bool store = (q.op == OP_FILTER || q.op == OP_FILTER_AGG) && q.out_mask;
     const bool want_mm = (q.op == OP_FILTER_AGG || q.op == OP_AGG) && (q.agg & (AGG_MIN | AGG_MAX));
     // the warp's query totals stay in shared memory (lane 0 updates them once per chunk)
-    if (lane == 0) wtot[wid] = WarpTot{0, 0, 0.0, LLONG_MIN, LLONG_MAX, 0};
+    if (lane == 0) wtot[wid] = WarpTot{0, 0, 0, LLONG_MIN, LLONG_MAX, 0};
     StreamChunk k{};
     k.chunk = 0xffffffffu;
     Part32 part{0, 0, 0, ~0u};
@@ -374,7 +381,7 @@ buff_stream_kernel(QueryParams q, const BuffChunkInfo* info, const uint2* __rest
         Partial p64{part.sum, part.cnt, part.mx, part.cnt ? part.mn : ~0ull};
         flush_partial(q, k.chunk, k.base, p64, wtot[wid], !exact);
     }
-    cta_finish(q, info, T, res, frac, (fold & 1u) != 0, wtot, kStreamWarps, exact);
+    cta_finish(q, info, T, res, frac, (fold & 1u) != 0, wtot, kStreamWarps, exact, totals_only);
 }
 
 // Launch of the kernel for widths NP * 8 + TB (instantiated by buff_stream_np{1,2,3,4}.cu).

@@ -65,31 +65,47 @@ static void tune_pool_once() {
 // Pinned result slots: every column needs one small pinned QueryResult for
 // its scalar outputs.  cudaMallocHost / cudaFreeHost are slow, synchronizing
 // calls, so the slots come from pinned slabs allocated once and recycled.
+template <typename T>
 class PinnedSlots {
   public:
-    QueryResult* take() {
+    T* take() {
         std::lock_guard<std::mutex> lk(mu_);
         if (free_.empty()) {
             constexpr size_t kSlab = 1024;
             void* p = nullptr;
-            if (cudaMallocHost(&p, kSlab * sizeof(QueryResult)) != cudaSuccess) return nullptr;
-            QueryResult* q = static_cast<QueryResult*>(p);
+            if (cudaMallocHost(&p, kSlab * sizeof(T)) != cudaSuccess) return nullptr;
+            T* q = static_cast<T*>(p);
             for (size_t i = 0; i < kSlab; ++i) free_.push_back(q + i);
         }
-        QueryResult* r = free_.back();
+        T* r = free_.back();
         free_.pop_back();
         return r;
     }
-    void give(QueryResult* r) {
+    void give(T* r) {
         std::lock_guard<std::mutex> lk(mu_);
         free_.push_back(r);
     }
 
   private:
     std::mutex mu_;
-    std::vector<QueryResult*> free_;  // slabs are kept for the life of the process
+    std::vector<T*> free_;  // slabs are kept for the life of the process
 };
-static PinnedSlots g_pinned;
+static PinnedSlots<QueryResult> g_pinned;
+static PinnedSlots<ScanTotals> g_pinned_tot;
+
+// (double)x / 2^frac as the device's fold_scale rounds it (one conversion, one
+// exact power-of-two scaling).
+static double host_fold_scale(long long x, uint32_t frac) {
+    auto pow2 = [](int e) {  // 2^e for -1022 <= e <= 1023
+        const uint64_t b = uint64_t(1023 + e) << 52;
+        double d;
+        std::memcpy(&d, &b, sizeof d);
+        return d;
+    };
+    const double v = static_cast<double>(x);
+    if (frac <= 1022) return v * pow2(-static_cast<int>(frac));
+    return v / (frac <= 1023 ? pow2(1023) : HUGE_VAL);
+}
 
 }  // namespace ebi
 
@@ -211,6 +227,11 @@ cudaError_t launch_values(const ebi_column* c, const QueryParams& q, uint32_t ch
     }
 }
 
+// The totals block of the next scan.
+ScanTotals* scan_totals(ebi_column* c) {
+    return reinterpret_cast<ScanTotals*>(reinterpret_cast<uint8_t*>(c->d_tot) + (c->tot_flip ? kScanTotalsBytes : 0));
+}
+
 // Tile range of the query: all tiles, or those of chunk_id (none when out of range).
 void tile_range(const ebi_column* c, int64_t chunk_id, uint32_t* begin, uint32_t* count) {
     if (chunk_id < 0) { *begin = 0; *count = static_cast<uint32_t>(c->tiles.tiles.size()); return; }
@@ -243,14 +264,44 @@ int mark_scan(ebi_column* c, cudaStream_t s) {
     return EBI_OK;
 }
 
-// Enqueues finalize (unless the scan kernel already folded), copies the result back and waits.
+// Enqueues finalize (unless the scan kernel already folded, or left exact
+// totals for the host to scale), copies the result back and waits.
 int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
     if (c->timing) CK(cudaEventRecord(c->ev[1], s));
-    if (!c->fused_pending) CK(launch_finalize(q, c->d_res, s));
-    c->fused_pending = false;
-    if (c->timing) CK(cudaEventRecord(c->ev[2], s));
-    CK(cudaMemcpyAsync(c->h_res, c->d_res, sizeof(QueryResult), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    bool done = false;
+    if (c->totals_pending) {
+        c->totals_pending = false;
+        if (c->timing) CK(cudaEventRecord(c->ev[2], s));
+        CK(cudaMemcpyAsync(c->h_tot, c->pending_tot, sizeof(ScanTotals), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        const ScanTotals t = *c->h_tot;
+        if (t.bad_chunk == 0xffffffffu && !t.nonexact && t.abs_bound < (1ull << 52)) {
+            // every chunk total and prefix of the chunk-ordered fold is an exact
+            // multiple of 2^-frac below 2^53 of them: the fold equals the exact total
+            QueryResult& r = *c->h_res;
+            r.status = 0;
+            r.bad_chunk = 0xffffffffu;
+            r.count = t.count;
+            r.sum = 0.0;
+            r.min = HUGE_VAL;
+            r.max = -HUGE_VAL;
+            if (t.count) {
+                r.sum = host_fold_scale(static_cast<long long>(t.sum_fixed), c->buff_frac);
+                r.max = host_fold_scale(t.max_fixed, c->buff_frac);
+                r.min = host_fold_scale(t.min_fixed, c->buff_frac);
+            }
+            done = true;
+        } else {
+            c->fused_pending = false;  // a failing chunk: the chunk-ordered fold reports it and re-arms
+        }
+    }
+    if (!done) {
+        if (!c->fused_pending) CK(launch_finalize(q, c->d_res, s));
+        c->fused_pending = false;
+        if (c->timing) CK(cudaEventRecord(c->ev[2], s));
+        CK(cudaMemcpyAsync(c->h_res, c->d_res, sizeof(QueryResult), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
     c->last.kernels = ebi_kernel_launches() - c->launches_at_start;
     if (c->timing) {
         float a = 0.f, b = 0.f, t = 0.f;
@@ -308,12 +359,22 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
         } else if (c->stream_ok) {
             const uint32_t ub = chunk_id < 0 ? 0u : c->first_unit[chunk_id];
             const uint32_t un = chunk_id < 0 ? c->first_unit.back() : c->first_unit[chunk_id + 1] - ub;
-            const uint32_t fold = (c->buff_fast_ok ? 1u : 0u) | (c->buff_exact ? 2u : 0u);
-            CK(launch_buff_stream(q, c->d_buff, c->d_units, ub, un, c->units_per_chunk, c->stream_bits, c->sms, c->d_tot, c->d_res,
+            // exact columns without an input bitmask: totals only, scaled on the host
+            const bool totals_only = c->buff_exact && !d_mask;
+            const uint32_t fold = (c->buff_fast_ok ? 1u : 0u) | (c->buff_exact ? 2u : 0u) |
+                                  (totals_only ? 4u | (c->tot_flip ? 8u : 0u) : 0u);
+            ScanTotals* T = scan_totals(c);
+            CK(launch_buff_stream(q, c->d_buff, c->d_units, ub, un, c->units_per_chunk, c->stream_bits, c->sms, T, c->d_res,
                                   c->buff_frac, fold, s));
-            c->fused_pending = true;
+            if (totals_only) {
+                c->totals_pending = true;
+                c->pending_tot = T;
+                c->tot_flip ^= 1u;  // the launch set the other block at rest
+            } else {
+                c->fused_pending = true;
+            }
         } else {
-            CK(launch_buff_scan(q, c->d_buff, tb, tn, c->layout, c->scan_grid, c->d_tot, c->d_res, c->buff_frac,
+            CK(launch_buff_scan(q, c->d_buff, tb, tn, c->layout, c->scan_grid, scan_totals(c), c->d_res, c->buff_frac,
                                 c->buff_fast_ok, s));
             c->fused_pending = true;
         }
@@ -515,8 +576,10 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st) st = dev_alloc(&c->d_res, 1, s);
     if (!st && !binfo.empty()) st = dev_alloc(&c->d_buff, binfo.size(), s);
     // the scan totals and, behind them, one slot per CTA of a scan launch
-    if (!st) st = dev_alloc(&c->d_tot, (kScanTotalsBytes + sizeof(ScanTotals) - 1) / sizeof(ScanTotals), s);
+    // two totals blocks (totals-only queries alternate between them)
+    if (!st) st = dev_alloc(&c->d_tot, (2 * kScanTotalsBytes + sizeof(ScanTotals) - 1) / sizeof(ScanTotals), s);
     if (!st && !(c->h_res = g_pinned.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
+    if (!st && !(c->h_tot = g_pinned_tot.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st) {
         cudaError_t e = cudaSuccess;
         if (!src) {
@@ -541,8 +604,11 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
                                 cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && !binfo.empty())
             e = cudaMemcpyAsync(c->d_buff, binfo.data(), binfo.size() * sizeof(BuffChunkInfo), cudaMemcpyHostToDevice, s);
-        static const ScanTotals kRest = {0, 0.0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0, 0};
+        static const ScanTotals kRest = {0, 0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0, 0};
         if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_tot, &kRest, sizeof kRest, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(c->d_tot) + kScanTotalsBytes, &kRest, sizeof kRest,
+                                cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
         if (e == cudaSuccess && c->scheme == EBI_BUFF)
             e = launch_buff_repack(src, c->d_file, d_segs, static_cast<uint32_t>(segs.size()), s);
@@ -602,9 +668,10 @@ int ebi_column_close(ebi_column* c) {
     void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
                     c->d_scratch_mask, c->d_buff, c->d_tot, c->d_units};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
-    if (c->h_res) {
-        cudaStreamSynchronize(s);  // no copy into the slot is pending when it is recycled
-        g_pinned.give(c->h_res);
+    if (c->h_res || c->h_tot) {
+        cudaStreamSynchronize(s);  // no copy into the slots is pending when they are recycled
+        if (c->h_res) g_pinned.give(c->h_res);
+        if (c->h_tot) g_pinned_tot.give(c->h_tot);
     }
     delete c;
     return EBI_OK;

@@ -45,6 +45,10 @@ struct ebi_column {
     uint32_t stream_bits = 0;    // most common width of the readable chunks
     uint32_t sms = 0;            // SMs of the column's device
     bool fused_pending = false;  // the last query's kernel already folded into d_res
+    bool totals_pending = false; // the last query's kernel left exact totals in pending_tot for the host
+    ScanTotals* pending_tot = nullptr;
+    ScanTotals* h_tot = nullptr; // pinned copy of those totals
+    uint32_t tot_flip = 0;       // which of the two totals blocks the next scan uses
     uint32_t stage_bytes = 0;    // Gorilla: shared-memory staging per chunk
     const double* dec_tab = nullptr;  // Elf / ElfOnChimp: the device's decimal tables
     // segment timing (ebi_column_set_timing)

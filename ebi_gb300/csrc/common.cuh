@@ -83,7 +83,7 @@ struct ChunkAcc {
 // min_fixed = INT64_MAX, bad_chunk = ~0.
 struct ScanTotals {
     unsigned long long sum_fixed;  // wrapping sum of every (CTA, chunk) piece of sum_with_bitmask's integer
-    double abs_bound;              // sum of |piece|: bounds every chunk total and their prefix sums
+    unsigned long long abs_bound;  // saturating sum of |piece|: bounds every chunk total and their prefix sums
     unsigned long long count;      // rows selected
     long long max_fixed, min_fixed;
     unsigned int done;             // CTAs finished
@@ -97,7 +97,7 @@ constexpr uint32_t kScanSlots = 1024;  // CTAs of one scan launch, at most
 // Running query totals of one warp (kept by lane 0), and of one CTA in its slot.
 struct alignas(16) WarpTot {
     unsigned long long sum_fixed, count;
-    double abs_bound;
+    unsigned long long abs_bound;  // saturating (integer pipes: no FP64 on the scan's tail)
     long long max_fixed, min_fixed;
     unsigned int nonexact;
 };
