@@ -3,7 +3,9 @@
 //
 // A batch is a list of work items, each naming a query and a unit of one of
 // its columns: an 8,192-row BUFF tile, a whole Uncompressed / RLE / Chimp /
-// Chimp128 / Elf / ElfOnChimp chunk, or a group of Gorilla chunks (one per warp).  A persistent
+// Chimp128 / Elf / ElfOnChimp chunk, or a group of Gorilla chunks (one per warp).
+// A Chimp-family item may name a run of consecutive queries over one column
+// (count of them, at most 32): the chunk is decoded once for all of them.  A persistent
 // grid of 256-thread CTAs pulls items from a device counter, so columns of
 // very different lengths and codecs share the GPU without a launch per
 // column; each item runs the same per-chunk device code as the single-column
@@ -43,16 +45,16 @@ __device__ __noinline__ void item_gorilla(const QueryParams& q, const BatchItem&
     if (warp < it.count) gorilla_chunk_l1(q, it.unit + warp, it.unit + warp, VAL_SCAN, nullptr);
 }
 __device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& it) {
-    xor_chunk<CODEC_CHIMP>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+    xor_chunk<CODEC_CHIMP>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
 }
 __device__ __noinline__ void item_chimp128(const QueryParams& q, const BatchItem& it) {
-    xor_chunk<CODEC_CHIMP128>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+    xor_chunk<CODEC_CHIMP128>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
 }
 __device__ __noinline__ void item_elf_chimp(const QueryParams& q, const BatchItem& it) {
-    xor_chunk<CODEC_ELF_CHIMP>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+    xor_chunk<CODEC_ELF_CHIMP>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
 }
 __device__ __noinline__ void item_elf(const QueryParams& q, const BatchItem& it) {
-    xor_chunk<CODEC_ELF>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+    xor_chunk<CODEC_ELF>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
 }
 
 __global__ void __launch_bounds__(kBatchThreads, 2)

@@ -54,6 +54,7 @@ struct Slot {
     BatchItem* h_items = nullptr;
     QueryResult* h_res = nullptr;
     std::vector<Pending> reqs;   // requests of the batch in flight
+    std::vector<uint32_t> qindex;  // (request, column) in request order -> its query in the batch
     bool busy = false;
     uint64_t launch_ns = 0;
 };
@@ -95,26 +96,56 @@ void footprint(const ebi_server* s, const ebi_request& r, uint64_t* chunks, uint
 
 // Builds and launches slot sl's batch from its admitted requests.
 cudaError_t launch_slot(ebi_server* s, Slot& sl) {
-    uint32_t nq = 0;
+    // The batch's queries in column order, so that the queries on one column
+    // are consecutive: a Chimp-family chunk is then decoded once for all of
+    // them (items naming up to 32 consecutive queries).
+    struct Ent { uint32_t col, req, k; };
+    std::vector<Ent> ents;
+    std::vector<uint32_t> base(sl.reqs.size() + 1, 0);
+    for (uint32_t ri = 0; ri < sl.reqs.size(); ++ri) {
+        const Pending& p = sl.reqs[ri];
+        base[ri + 1] = base[ri] + p.req.n_columns;
+        for (uint32_t k = 0; k < p.req.n_columns; ++k) ents.push_back({p.req.columns[k], ri, k});
+    }
+    std::stable_sort(ents.begin(), ents.end(), [](const Ent& a, const Ent& b) { return a.col < b.col; });
+    sl.qindex.assign(ents.size(), 0);
+    const uint32_t nq = static_cast<uint32_t>(ents.size());
     uint64_t acc_used = 0;
+    for (uint32_t qi = 0; qi < nq; ++qi) {
+        const Ent& en = ents[qi];
+        const Pending& p = sl.reqs[en.req];
+        const ebi_column* c = s->cols[en.col];
+        QueryParams q = column_params(c);
+        q.op = OP_FILTER_AGG;
+        q.pred = p.req.pred;
+        q.pred_on = 1;
+        q.agg = p.req.aggregates & AGG_ALL;
+        q.out_mask = nullptr;
+        q.out_atomic = 1;
+        q.stage_bytes = 0;
+        q.acc = sl.d_acc + acc_used;
+        acc_used += c->n_chunks;
+        sl.h_qp[qi] = q;
+        sl.qindex[base[en.req] + en.k] = qi;
+    }
     std::vector<BatchItem> items;
-    for (const Pending& p : sl.reqs) {
-        for (uint32_t k = 0; k < p.req.n_columns; ++k) {
-            const ebi_column* c = s->cols[p.req.columns[k]];
-            QueryParams q = column_params(c);
-            q.op = OP_FILTER_AGG;
-            q.pred = p.req.pred;
-            q.pred_on = 1;
-            q.agg = p.req.aggregates & AGG_ALL;
-            q.out_mask = nullptr;
-            q.out_atomic = 1;
-            q.stage_bytes = 0;
-            q.acc = sl.d_acc + acc_used;
-            acc_used += c->n_chunks;
-            sl.h_qp[nq] = q;
-            column_items(c->scheme, c->n_chunks, static_cast<uint32_t>(c->tiles.tiles.size()), nq, items);
-            ++nq;
+    for (uint32_t g = 0; g < nq;) {
+        uint32_t h = g;
+        while (h < nq && ents[h].col == ents[g].col) ++h;  // queries g .. h - 1: one column
+        const ebi_column* c = s->cols[ents[g].col];
+        const uint32_t tiles = static_cast<uint32_t>(c->tiles.tiles.size());
+        const bool shared = c->scheme == EBI_CHIMP || c->scheme == EBI_CHIMP128 || c->scheme == EBI_ELF_ON_CHIMP ||
+                            c->scheme == EBI_ELF;
+        if (shared) {
+            for (uint32_t q0 = g; q0 < h; q0 += 32) {
+                const size_t first = items.size();
+                column_items(c->scheme, c->n_chunks, tiles, q0, items);
+                for (size_t i = first; i < items.size(); ++i) items[i].count = std::min<uint32_t>(32, h - q0);
+            }
+        } else {
+            for (uint32_t qi = g; qi < h; ++qi) column_items(c->scheme, c->n_chunks, tiles, qi, items);
         }
+        g = h;
     }
     std::stable_sort(items.begin(), items.end(), [](const BatchItem& x, const BatchItem& y) {
         return item_cost(x.kind, x.count) > item_cost(y.kind, y.count);
@@ -135,7 +166,7 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
 // Combines a finished slot's per-column results into one response per request.
 void finish_slot(ebi_server* s, Slot& sl, std::vector<ebi_response>& out) {
     const uint64_t t = now_ns();
-    uint32_t qi = 0;
+    uint32_t pos = 0;
     const double inf = __builtin_inf();
     for (const Pending& p : sl.reqs) {
         ebi_response r{};
@@ -146,8 +177,8 @@ void finish_slot(ebi_server* s, Slot& sl, std::vector<ebi_response>& out) {
         r.sum = 0.0;
         r.min = inf;
         r.max = -inf;
-        for (uint32_t k = 0; k < p.req.n_columns; ++k, ++qi) {
-            const QueryResult& q = sl.h_res[qi];
+        for (uint32_t k = 0; k < p.req.n_columns; ++k, ++pos) {
+            const QueryResult& q = sl.h_res[sl.qindex[pos]];
             if (q.status && !r.status) r.status = static_cast<int32_t>(q.status);
             r.sum += q.sum;
             r.min = std::fmin(r.min, q.min);

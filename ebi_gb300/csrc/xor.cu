@@ -8,7 +8,7 @@ namespace {
 template <int CODEC>
 __global__ void __launch_bounds__(kXorThreads, 2) xor_kernel(QueryParams q, uint32_t chunk_base, int mode,
                                                           const unsigned long long* chunk_offsets) {
-    xor_chunk<CODEC>(q, blockIdx.x, chunk_base + blockIdx.x, mode, chunk_offsets);
+    xor_chunk<CODEC>(&q, 1, blockIdx.x, chunk_base + blockIdx.x, mode, chunk_offsets);
 }
 
 template <int CODEC>

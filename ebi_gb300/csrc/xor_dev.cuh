@@ -193,10 +193,14 @@ __device__ __noinline__ void elf_restore(Smem sm, uint32_t end, const double* __
 
 // One Chimp / Chimp128 chunk c by a CTA of kXorThreads threads with
 // xor_smem_bytes(CODEC) bytes of dynamic shared memory; li indexes the pass's
-// per-chunk counts / offsets.
+// per-chunk counts / offsets.  qs[0, nq) (nq <= 32) are queries over the same
+// column: the chunk is decoded once and each query that selects it runs its
+// own query phase over the decoded values (a batch's requests on one column
+// share the decode).
 template <int CODEC>
-__device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uint32_t c, int mode,
+__device__ __forceinline__ void xor_chunk(const QueryParams* qs, uint32_t nq, uint32_t li, uint32_t c, int mode,
                                           const unsigned long long* chunk_offsets) {
+    const QueryParams& q = qs[0];  // the column (file, chunk table, tables) of every query
     extern __shared__ __align__(16) uint8_t smem_raw[];
     Smem sm;
     sm.vals = reinterpret_cast<uint64_t*>(smem_raw);
@@ -207,39 +211,43 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
     __shared__ uint32_t s_red[kXorThreads / 32];
     __shared__ uint64_t s_x[kXorThreads / 32];
     __shared__ ValAgg sh_agg[kXorThreads / 32];
-    __shared__ int s_ok;
+    __shared__ uint32_t s_ok;  // bit k: query k selects the chunk
     __shared__ uint32_t s_status;
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const ChunkDesc cd = q.chunks[c];
-    ChunkAcc* acc = q.acc + c;
-    const bool has_mask = q.in_mask != nullptr;
     if (tid == 0) {
-        int ok = 1;
-        if (mode == VAL_SCAN) {
-            ok = has_mask ? acc->selected != 0 : (q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
-            if (ok && !has_mask) acc->selected = 1;
-        } else if (mode == VAL_MATERIALIZE) {
-            ok = chunk_offsets[li + 1] != chunk_offsets[li];
-        } else if (has_mask) {
-            uint32_t any = 0;
-            for (uint64_t r = 0; r < cd.n_rows && !any; r += 32) {
-                uint32_t w = mask_word(q.in_mask, cd.row_off + r, q.n_records);
-                if (cd.n_rows - r < 32) w &= (1u << (cd.n_rows - r)) - 1u;
-                any = w;
+        uint32_t okm = 0;
+        for (uint32_t k = 0; k < nq; ++k) {
+            const QueryParams& qk = qs[k];
+            ChunkAcc* ak = qk.acc + c;
+            const bool hm = qk.in_mask != nullptr;
+            int ok = 1;
+            if (mode == VAL_SCAN) {
+                ok = hm ? ak->selected != 0 : (qk.chunk_id < 0 || static_cast<uint64_t>(qk.chunk_id) == c);
+                if (ok && !hm) ak->selected = 1;
+            } else if (mode == VAL_MATERIALIZE) {
+                ok = chunk_offsets[li + 1] != chunk_offsets[li];
+            } else if (hm) {
+                uint32_t any = 0;
+                for (uint64_t r = 0; r < cd.n_rows && !any; r += 32) {
+                    uint32_t w = mask_word(qk.in_mask, cd.row_off + r, qk.n_records);
+                    if (cd.n_rows - r < 32) w &= (1u << (cd.n_rows - r)) - 1u;
+                    any = w;
+                }
+                ok = any != 0;
             }
-            ok = any != 0;
+            if (ok && (cd.flags & kChunkBadGeometry)) { set_status(ak, EBI_E_IO); ok = 0; }
+            if (!ok && mode == VAL_COUNT) qk.tile_counts[li] = 0;
+            if (ok) okm |= 1u << k;
         }
-        if (ok && (cd.flags & kChunkBadGeometry)) { set_status(acc, EBI_E_IO); ok = 0; }
-        if (!ok && mode == VAL_COUNT) q.tile_counts[li] = 0;
-        s_ok = ok;
+        s_ok = okm;
         s_status = 0;
     }
     __syncthreads();
-    if (!s_ok) return;
+    const uint32_t okm = s_ok;
+    if (!okm) return;
 
-    const bool pred_on = q.pred_on != 0;
-    const bool store = mode == VAL_SCAN && pred_on && q.out_mask != nullptr;
     const uint64_t B = cd.byte_len * 8;
     const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
     const uint64_t bit0 = cd.byte_off * 8;
@@ -411,60 +419,77 @@ __device__ __forceinline__ void xor_chunk(const QueryParams& q, uint32_t li, uin
         } else if (R > kRcap) {
             serial = true;  // the end marker lies past the records held in shared memory
         } else {
-            if (tid == 0) set_status(acc, s_status ? s_status : EBI_E_UNEXPECTED_END);
-            if (mode == VAL_COUNT && tid == 0) q.tile_counts[li] = 0;
+            if (tid == 0)
+                for (uint32_t k = 0; k < nq; ++k) {
+                    if (!((okm >> k) & 1u)) continue;
+                    set_status(qs[k].acc + c, s_status ? s_status : EBI_E_UNEXPECTED_END);
+                    if (mode == VAL_COUNT) qs[k].tile_counts[li] = 0;
+                }
             return;
         }
     }
 
     if (serial) {
         __syncthreads();
-        if (tid == 0) {
-            SerialSink sink{&q, cd.row_off, mode, has_mask, pred_on, store, key_pred(q.pred),
-                            val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u),
-                            mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull, 0, 0};
-            const uint32_t e = decode_serial<CODEC>(fw, bit0, B, sm.vals, sink);
-            if (e) {
-                set_status(acc, e);
-                if (mode == VAL_COUNT) q.tile_counts[li] = 0;
-            } else if (mode == VAL_COUNT) {
-                q.tile_counts[li] = sink.agg.cnt;
-            } else if (mode == VAL_SCAN) {
-                if (store) sink.flush();
-                val_agg_store(acc, sink.agg);
+        if (tid == 0)
+            for (uint32_t k = 0; k < nq; ++k) {  // each query decodes the chunk again (chunks past kRcap records)
+                if (!((okm >> k) & 1u)) continue;
+                const QueryParams& qk = qs[k];
+                ChunkAcc* ak = qk.acc + c;
+                const bool pk = qk.pred_on != 0, sk = mode == VAL_SCAN && pk && qk.out_mask != nullptr;
+                SerialSink sink{&qk, cd.row_off, mode, qk.in_mask != nullptr, pk, sk, key_pred(qk.pred),
+                                val_agg_init(qk.op == OP_FILTER_AGG || qk.op == OP_AGG ? qk.agg : 0u),
+                                mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull, 0, 0};
+                const uint32_t e = decode_serial<CODEC>(fw, bit0, B, sm.vals, sink);
+                if (e) {
+                    set_status(ak, e);
+                    if (mode == VAL_COUNT) qk.tile_counts[li] = 0;
+                } else if (mode == VAL_COUNT) {
+                    qk.tile_counts[li] = sink.agg.cnt;
+                } else if (mode == VAL_SCAN) {
+                    if (sk) sink.flush();
+                    val_agg_store(ak, sink.agg);
+                }
             }
-        }
         return;
     }
 
-    // ---- query over vals[0, end) ------------------------------------------
-    const KeyPred kp = key_pred(q.pred);
-    ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
-    unsigned long long pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0;
-    for (uint32_t r0 = 0; r0 < end; r0 += kXorThreads) {
-        const uint32_t i = r0 + tid;
-        const uint64_t g = cd.row_off + i;
-        const bool in = i < end && (!has_mask || mask_row(q.in_mask, q.n_records, g));
-        const uint64_t vb = in ? sm.vals[i] : 0;
-        const bool pass = in && (!pred_on || kp.pass(vb));
-        if (mode == VAL_MATERIALIZE) {
-            uint32_t total;
-            const uint32_t before = block_excl_scan_u32<kXorThreads>(pass, s_red, &total);
-            if (pass && pos + before < q.out_cap) q.out_vals[pos + before] = __longlong_as_double(static_cast<long long>(vb));
-            pos += total;
-            continue;
+    // ---- each selecting query over vals[0, end) ------------------------------
+    for (uint32_t k = 0; k < nq; ++k) {
+        if (!((okm >> k) & 1u)) continue;
+        __syncthreads();  // the previous query's block reduction is read
+        const QueryParams& qk = qs[k];
+        const bool has_mask = qk.in_mask != nullptr, pred_on = qk.pred_on != 0;
+        const bool store = mode == VAL_SCAN && pred_on && qk.out_mask != nullptr;
+        const KeyPred kp = key_pred(qk.pred);
+        ValAgg agg = val_agg_init(qk.op == OP_FILTER_AGG || qk.op == OP_AGG ? qk.agg : 0u);
+        unsigned long long pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0;
+        for (uint32_t r0 = 0; r0 < end; r0 += kXorThreads) {
+            const uint32_t i = r0 + tid;
+            const uint64_t g = cd.row_off + i;
+            const bool in = i < end && (!has_mask || mask_row(qk.in_mask, qk.n_records, g));
+            const uint64_t vb = in ? sm.vals[i] : 0;
+            const bool pass = in && (!pred_on || kp.pass(vb));
+            if (mode == VAL_MATERIALIZE) {
+                uint32_t total;
+                const uint32_t before = block_excl_scan_u32<kXorThreads>(pass, s_red, &total);
+                if (pass && pos + before < qk.out_cap) qk.out_vals[pos + before] = __longlong_as_double(static_cast<long long>(vb));
+                pos += total;
+                continue;
+            }
+            if (store) {
+                const uint32_t word = __ballot_sync(0xffffffffu, pass && g < qk.n_records);
+                if (lane == 0 && word) store_mask_word(qk.out_mask, g, word, true);
+            }
+            if (pass) val_agg_add1(agg, vb);
         }
-        if (store) {
-            const uint32_t word = __ballot_sync(0xffffffffu, pass && g < q.n_records);
-            if (lane == 0 && word) store_mask_word(q.out_mask, g, word, true);
+        if (mode == VAL_MATERIALIZE) continue;
+        const ValAgg a = val_agg_block(agg, sh_agg);
+        if (tid == 0) {
+            if (mode == VAL_COUNT) qk.tile_counts[li] = a.cnt;
+            else val_agg_store(qk.acc + c, a);
         }
-        if (pass) val_agg_add1(agg, vb);
     }
-    if (mode == VAL_MATERIALIZE) return;
-    const ValAgg a = val_agg_block(agg, sh_agg);
-    if (tid != 0) return;
-    if (mode == VAL_COUNT) q.tile_counts[li] = a.cnt;
-    else val_agg_store(acc, a);
 }
 
 constexpr size_t xor_smem_bytes(int codec) {
