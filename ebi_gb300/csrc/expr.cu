@@ -585,11 +585,13 @@ __global__ void __launch_bounds__(kFuseThreads) expr_buff_fused(ExprPass P, Expr
                 V x[kFuseRows], y[kFuseRows];
                 auto fetch = [&](uint8_t src, uint16_t col, double lit_bits, uint32_t sh, V (&out)[kFuseRows]) {
                     if (src == S_COL) {
+                        // slots past the packed count hold stale values of the warp's own region:
+                        // read anyway (in bounds), their rows are dropped when aggregating
 #pragma unroll
                         for (int k = 0; k < kFuseRows; ++k) {
                             const uint32_t at = col * kFuseStride + fuse_pad(lane + uint32_t(k) * 32);
-                            if constexpr (kExact) out[k] = ((ok >> k) & 1u) ? islot[at] : 0;
-                            else out[k] = ((ok >> k) & 1u) ? wslot[at] : 0.0;
+                            if constexpr (kExact) out[k] = islot[at];
+                            else out[k] = wslot[at];
                         }
                     } else if (src == S_LIT) {
                         V l;
@@ -608,9 +610,11 @@ __global__ void __launch_bounds__(kFuseThreads) expr_buff_fused(ExprPass P, Expr
                         for (int k = 0; k < kFuseRows; ++k) out[k] = st1[k];
                     }
                     if constexpr (kExact) {
+                        if (sh) {  // the same for every lane
 #pragma unroll
-                        for (int k = 0; k < kFuseRows; ++k)
-                            out[k] = static_cast<long long>(static_cast<unsigned long long>(out[k]) << sh);
+                            for (int k = 0; k < kFuseRows; ++k)
+                                out[k] = static_cast<long long>(static_cast<unsigned long long>(out[k]) << sh);
+                        }
                     }
                 };
                 fetch(src_a, prog[q].ca, prog[q].la, prog[q].sa, x);
@@ -622,15 +626,18 @@ __global__ void __launch_bounds__(kFuseThreads) expr_buff_fused(ExprPass P, Expr
                 fetch(src_b, prog[q].cb, prog[q].lb, prog[q].sb, y);
                 if (src_a == S_POP || src_b == S_POP) --sp;
                 if constexpr (kExact) {
+                    // wrapping (unsigned) arithmetic: exact for the rows aggregated, whose
+                    // intermediates stay below 2^53; defined for the stale ones dropped later
+                    using U = unsigned long long;
                     if (op == I_ADD) {
 #pragma unroll
-                        for (int k = 0; k < kFuseRows; ++k) acc[k] = x[k] + y[k];
+                        for (int k = 0; k < kFuseRows; ++k) acc[k] = static_cast<long long>(U(x[k]) + U(y[k]));
                     } else if (op == I_SUB) {
 #pragma unroll
-                        for (int k = 0; k < kFuseRows; ++k) acc[k] = x[k] - y[k];
+                        for (int k = 0; k < kFuseRows; ++k) acc[k] = static_cast<long long>(U(x[k]) - U(y[k]));
                     } else {
 #pragma unroll
-                        for (int k = 0; k < kFuseRows; ++k) acc[k] = x[k] * y[k];
+                        for (int k = 0; k < kFuseRows; ++k) acc[k] = static_cast<long long>(U(x[k]) * U(y[k]));
                     }
                 } else {
 #pragma unroll
@@ -641,11 +648,11 @@ __global__ void __launch_bounds__(kFuseThreads) expr_buff_fused(ExprPass P, Expr
             if constexpr (kExact) {
                 RunAccI& R = iruns[a * kFuseThreads + threadIdx.x];
                 if (s_kind[a] == EBI_AGGR_SUM) {
-                    unsigned long long lo = 0, hi = 0;
+                    long long sum = 0;  // at most 8 values below 2^53: no overflow
 #pragma unroll
                     for (int k = 0; k < kFuseRows; ++k)
-                        if ((ok >> k) & 1u) add128(lo, hi, static_cast<unsigned long long>(acc[k]), acc[k] < 0 ? ~0ull : 0ull);
-                    add128(R.lo, R.hi, lo, hi);
+                        if ((ok >> k) & 1u) sum += acc[k];
+                    add128(R.lo, R.hi, static_cast<unsigned long long>(sum), sum < 0 ? ~0ull : 0ull);
                 } else {
 #pragma unroll
                     for (int k = 0; k < kFuseRows; ++k) {
