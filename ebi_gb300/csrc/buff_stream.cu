@@ -1,11 +1,14 @@
 // buff_stream.cu -- host side of the register-streaming BUFF scan
 // (buff_stream.cuh): the unit list of a column and the launch, which picks the
-// kernel built for the column's most common chunk width (buff_stream_np1..4.cu;
-// one or two byte planes: three CTAs per SM, else two).
+// kernel built for the column's most common chunk width (buff_stream_np0..4.cu;
+// up to two byte planes: three CTAs per SM, else two).
 #include "internal.h"
 
 namespace ebi {
 
+cudaError_t launch_buff_stream_np0(uint32_t tb, const QueryParams& q, const BuffChunkInfo* info, const uint2* units,
+                                   uint32_t unit_base, uint32_t n_units, uint32_t upc, uint32_t grid, ScanTotals* T,
+                                   QueryResult* res, uint32_t frac, uint32_t fold, cudaStream_t s);
 cudaError_t launch_buff_stream_np1(uint32_t tb, const QueryParams& q, const BuffChunkInfo* info, const uint2* units,
                                    uint32_t unit_base, uint32_t n_units, uint32_t upc, uint32_t grid, ScanTotals* T,
                                    QueryResult* res, uint32_t frac, uint32_t fold, cudaStream_t s);
@@ -50,6 +53,8 @@ cudaError_t launch_buff_stream(const QueryParams& q, const BuffChunkInfo* info, 
     const uint32_t g = grid < max_grid ? grid : (max_grid ? max_grid : 1);
     if (g > kScanSlots) return cudaErrorInvalidConfiguration;
     switch (np) {
+    case 0: return tb ? launch_buff_stream_np0(tb, q, info, units, unit_base, n_units, upc, g, T, res, frac, fold, s)
+                      : cudaErrorInvalidValue;
     case 1: return launch_buff_stream_np1(tb, q, info, units, unit_base, n_units, upc, g, T, res, frac, fold, s);
     case 2: return launch_buff_stream_np2(tb, q, info, units, unit_base, n_units, upc, g, T, res, frac, fold, s);
     case 3: return launch_buff_stream_np3(tb, q, info, units, unit_base, n_units, upc, g, T, res, frac, fold, s);

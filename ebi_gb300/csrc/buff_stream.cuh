@@ -1,5 +1,5 @@
 // buff_stream.cuh -- the register-streaming BUFF scan: filter / filter+aggregate
-// / aggregate over a column whose chunks are 8 to 32 bits wide, in one launch.
+// / aggregate over a column whose chunks are 1 to 32 bits wide, in one launch.
 //
 // The column's planes sit in HBM in the aligned plane layout (buff_layout.cu),
 // so a group of 64 consecutive rows owns 64 bytes of every byte plane and
@@ -85,14 +85,21 @@ __device__ StreamChunk stream_chunk(const QueryParams& q, ScanTotals* T, uint32_
     return k;
 }
 
+// Byte-plane words of a lane's group: NP planes (one row of storage for
+// tail-only chunks, NP = 0, which read none).
+template <int NP>
+using PlaneWords = uint32_t[NP > 0 ? NP : 1][16];
+
 // The four deltas of rows 4j .. 4j + 3 of a lane's group.
 template <int NP, int TB>
-__device__ __forceinline__ void quad_deltas(const uint32_t (&pw)[NP][16], const uint32_t* tw, int j, uint32_t (&d)[4]) {
-    uint32_t x[NP];
+__device__ __forceinline__ void quad_deltas(const PlaneWords<NP>& pw, const uint32_t* tw, int j, uint32_t (&d)[4]) {
+    uint32_t x[NP > 0 ? NP : 1];
 #pragma unroll
     for (int p = 0; p < NP; ++p) x[p] = pw[p][j] ^ 0x80808080u;
-    uint32_t v[4];
-    if constexpr (NP == 1) {
+    uint32_t v[4] = {0u, 0u, 0u, 0u};
+    if constexpr (NP == 0) {
+        // tail-only chunk (1..7 bits): the deltas are the tail bits
+    } else if constexpr (NP == 1) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) v[k] = __byte_perm(x[0], 0u, 0x4440u | k);
     } else if constexpr (NP == 2) {
@@ -139,7 +146,7 @@ __device__ __forceinline__ GroupOut group_body(const uint8_t* planes, const uint
                                                uint32_t lo, uint32_t span, uint32_t m0, uint32_t m1, bool neg) {
     constexpr bool kSum32 = NP * 8 + TB <= 26;  // 64 deltas fit a u32 sum
     const uint8_t* pp = planes + g0;
-    uint32_t pw[NP][16];
+    PlaneWords<NP> pw;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
 #pragma unroll
@@ -251,7 +258,7 @@ __device__ __forceinline__ uint32_t run_chunk(const QueryParams& q, const Stream
     return u;
 }
 
-// Any width (1..4 byte planes, 0..7 tail bits) decided at run time: chunks
+// Any width (0..4 byte planes, 0..7 tail bits) decided at run time: chunks
 // whose width differs from the one the kernel is built for.
 __device__ __noinline__ GroupOut group_any(const uint8_t* planes, const uint8_t* tail, uint64_t stride, uint32_t np,
                                            uint32_t tb, uint32_t g0, uint32_t lo, uint32_t span, uint32_t m0,
@@ -313,7 +320,8 @@ __device__ __forceinline__ uint32_t run_chunk_any(const QueryParams& q, const St
     return u;
 }
 
-// The kernel built for chunks of NP byte planes and TB tail bits (the
+// The kernel built for chunks of NP byte planes and TB tail bits (NP = 0:
+// tail-only chunks of 1..7 bits; the
 // column's most common width); chunks of other widths take run_chunk_any.
 // Narrow widths keep fewer registers and fit three CTAs per SM.
 template <int NP, int TB>
@@ -384,7 +392,7 @@ buff_stream_kernel(QueryParams q, const BuffChunkInfo* info, const uint2* __rest
     cta_finish(q, info, T, res, frac, (fold & 1u) != 0, wtot, kStreamWarps, exact, totals_only);
 }
 
-// Launch of the kernel for widths NP * 8 + TB (instantiated by buff_stream_np{1,2,3,4}.cu).
+// Launch of the kernel for widths NP * 8 + TB (instantiated by buff_stream_np{0,1,2,3,4}.cu).
 template <int NP, int TB>
 cudaError_t launch_stream_kernel(const QueryParams& q, const BuffChunkInfo* info, const uint2* units, uint32_t unit_base,
                                  uint32_t n_units, uint32_t upc, uint32_t grid, ScanTotals* T, QueryResult* res,

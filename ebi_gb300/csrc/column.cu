@@ -493,7 +493,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         c->stream_ok = true;
         for (const BuffChunkInfo& b : binfo) {
             if (b.status) continue;
-            if (b.bits < 8 || b.bits > 32) c->stream_ok = false;
+            if (b.bits < 1 || b.bits > 32) c->stream_ok = false;  // constant and > 32-bit chunks: the pipelined scan
             np_max = std::max(np_max, b.bits / 8);
             tb_max = std::max(tb_max, b.bits % 8);
             if (first) { c->buff_frac = b.frac; first = false; }
@@ -527,7 +527,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         uint64_t rows_of[65] = {};
         for (const BuffChunkInfo& b : binfo)
             if (!b.status) rows_of[b.bits] += b.n;
-        c->stream_bits = static_cast<uint32_t>(std::max_element(rows_of + 8, rows_of + 33) - rows_of);
+        c->stream_bits = static_cast<uint32_t>(std::max_element(rows_of + 1, rows_of + 33) - rows_of);
     } else {
         if (c->scheme == EBI_GORILLA) c->stage_bytes = gorilla_stage_bytes(c->chunks.data(), c->n_chunks);
         if (c->scheme == EBI_ELF || c->scheme == EBI_ELF_ON_CHIMP) {
