@@ -165,3 +165,31 @@ def test_errors_match_oracle():
 def test_empty_column():
     data = enc(np.zeros(0), ("record_count", 100), 1000)
     check_query_suite(data, [E.Predicate.eq(1.0)], masks=(None,))
+
+
+def test_alternating_query_kinds_on_one_column():
+    """On a column whose totals are exact for any query, queries without an
+    input bitmask leave their totals for the host (two alternating totals
+    blocks) and the others fold on the device: any sequence of them gives the
+    oracle's results."""
+    rng = np.random.default_rng(21)
+    v = np.round(rng.uniform(-1000, 1000, 300_000), 3)
+    data = enc(v, ("record_count", 65536), 1000)
+    d, o = E.Decoder(data), O.Decoder(data)
+    n = d.n_records
+    mask = random_mask(n, 0.3, rng)
+    p = E.Predicate.range(E.RangeValue.inclusive(-100.0), E.RangeValue.exclusive(250.0))
+    op = O.rng(O.BOUND_INCLUSIVE, -100.0, O.BOUND_EXCLUSIVE, 250.0)
+    for rep in range(3):
+        assert d.sum() == o.sum()
+        assert d.max(mask) == o.max(mask)
+        assert d.min() == o.min()
+        assert d.sum(chunk_id=2) == o.sum(chunk_id=2)
+        assert same_f64(mask_np(d.filter(p))[: (n + 63) // 64], o.filter(op))
+        _, s_, mn_, mx_, cnt_ = d.filter_agg(p, mask, want_mask=True)
+        ms, ss, smn, smx = o.filter_agg(op, mask)
+        assert (s_, mn_, mx_) == (ss, smn, smx)
+        _, s2, mn2, mx2, cnt2 = d.filter_agg(p, want_mask=False)
+        _, s3, mn3, mx3 = o.filter_agg(op)
+        assert (s2, mn2, mx2) == (s3, mn3, mx3)
+        assert d.sum(mask) == o.sum(mask)
