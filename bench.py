@@ -86,28 +86,28 @@ class Workload:
         self.rows = rows
         if name == "buff":
             self.codec, self.chunk, self.scale = "buff", CHUNK, SCALE
-            self.values = lambda: W.buff_uniform(rows)
+            self.values = lambda: W.buff_uniform(self.rows)
             self.ranges = [(k, -a, a) for k, a in W.BUFF_RANGES.items()]
             self.aggregates = ("sum",)
             self.describe = ("BUFF 67,108,864 f64 U[-1000,1000] rounded to 3 dp, 65,536-row chunks, scale 1000; "
                              "fused filter (bitmask out) + sum at 1%/10%/50% selectivity")
         elif name == "gorilla":
             self.codec, self.chunk, self.scale = "gorilla", 8192, 1
-            self.values = lambda: W.gorilla_walk(rows)
+            self.values = lambda: W.gorilla_walk(self.rows)
             self.ranges = [("10<=x<=50", 10.0, 50.0)]
             self.aggregates = ("sum", "min", "max")
             self.describe = ("Gorilla 1,048,576 f64 random walk x0=30, N(0,0.5) steps, 2 dp, 8,192-row chunks; "
                              "fused filter 10<=x<=50 (bitmask out) + sum/min/max")
         elif name == "chimp128":
             self.codec, self.chunk, self.scale = "chimp128", 8192, 1
-            self.values = lambda: W.sensor(rows)
+            self.values = lambda: W.sensor(self.rows)
             self.ranges = [("15<=x<=25", 15.0, 25.0)]
             self.aggregates = ("max",)
             self.describe = ("Chimp128 16,777,216 f64 sensor series 20+10sin(2pi i/1440)+N(0,0.1), 4 dp, "
                              "8,192-row chunks; fused decode + filter 15<=x<=25 (bitmask out) + max")
         elif name in ("elf", "elf_on_chimp"):
             self.codec, self.chunk, self.scale = name, 8192, 1
-            self.values = lambda: W.sensor(rows)
+            self.values = lambda: W.sensor(self.rows)
             self.ranges = [("15<=x<=25", 15.0, 25.0)]
             self.aggregates = ("max",)
             label = "Elf" if name == "elf" else "ElfOnChimp"
@@ -115,7 +115,7 @@ class Workload:
                              "8,192-row chunks; fused decode + decimal restore + filter 15<=x<=25 (bitmask out) + max")
         elif name == "rle":
             self.codec, self.chunk, self.scale = "rle", 8192, 1
-            self.values = lambda: W.steps(rows)
+            self.values = lambda: W.steps(self.rows)
             self.ranges = None  # the middle 30 % of the values, fixed once the column exists
             self.aggregates = ("max",)
             self.describe = ("RLE 16,777,216 f64 step series, Geometric(1/64) runs, 8,192-row chunks; "
