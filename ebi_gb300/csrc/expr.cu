@@ -467,9 +467,9 @@ __device__ __forceinline__ void add128(unsigned long long& lo, unsigned long lon
 // fixed * 2^-frac; the host proved every intermediate below 2^53, where each
 // IEEE operation is exact and equals the integer one); else on the f64 values.
 template <bool kExact>
-__global__ void __launch_bounds__(kFuseThreads) expr_buff_fused(ExprPass P, ExprScratch S, FusePass F) {
+__global__ void __launch_bounds__(kFuseThreads, 3) expr_buff_fused(ExprPass P, ExprScratch S, FusePass F) {
     extern __shared__ double dyn[];  // [warp][n_cols][kFuseStride] packed values, then RunAcc[n_aggs][kFuseThreads]
-    __shared__ Instr prog[kPassInstr];
+    const Instr* __restrict__ prog = S.prog;  // every lane reads the same instruction: one L1 line
     __shared__ BuffChunkInfo s_ci[kFuseWarps][kFuseCols];
     __shared__ const uint8_t* s_file[kFuseCols];
     __shared__ uint32_t s_kind[kMaxAggs], s_first[kMaxAggs + 1];
@@ -478,8 +478,6 @@ __global__ void __launch_bounds__(kFuseThreads) expr_buff_fused(ExprPass P, Expr
     long long* islot = reinterpret_cast<long long*>(wslot);
     RunAcc* runs = reinterpret_cast<RunAcc*>(dyn + kFuseWarps * P.n_cols * kFuseStride);
     RunAccI* iruns = reinterpret_cast<RunAccI*>(runs);
-    const uint32_t n_instr = P.first[P.n_aggs];
-    for (uint32_t i = threadIdx.x; i < n_instr; i += kFuseThreads) prog[i] = S.prog[i];
     if (threadIdx.x < kFuseCols) s_file[threadIdx.x] = F.file[threadIdx.x];
     if (threadIdx.x < kMaxAggs) s_kind[threadIdx.x] = P.kind[threadIdx.x];
     if (threadIdx.x <= kMaxAggs) s_first[threadIdx.x] = P.first[threadIdx.x];

@@ -332,3 +332,39 @@ def test_buff_wide_values_take_the_f64_kernel():
                      (E.Expr.Index(0) - E.Expr.Index(1)) * (E.Expr.Index(1) + E.Expr.Index(2))):
             for kind in (O.AGGR_SUM, O.AGGR_MIN, O.AGGR_MAX):
                 _check_engine(ds_e, ds_o, expr, kind, mask)
+
+
+@pytest.mark.gpu
+def test_errors_in_a_column_reach_the_aggregation():
+    """A chunk whose header claims more bits than its bytes hold: the fused pass
+    sees its status and the general pass reports the reference's error."""
+    rng = np.random.default_rng(31)
+    v = np.round(rng.uniform(-1, 1, 5000), 3)
+    data = bytearray(E.encode(v, "buff", ("record_count", 1000), 1000))
+    d = O.Decoder(bytes(data))
+    phys, _, _, _ = d.chunk_info(1)
+    data[phys + 12] = 40
+    other = E.encode(np.round(rng.uniform(0, 1, 5000), 2), "buff", ("record_count", 1000), 100)
+    ds_e = [E.Decoder(bytes(data)), E.Decoder(other)]
+    ds_o = [O.Decoder(bytes(data)), O.Decoder(other)]
+    expr = E.Expr.Index(0) * E.Expr.Index(1)
+    with pytest.raises(O.OracleError) as eo:
+        O.aggregate(ds_o, O.AGGR_SUM, expr.postfix())
+    with pytest.raises(E.DecoderError) as ee:
+        E.Aggregation.sum(expr).compute(ds_e)
+    assert ee.value.code == eo.value.code == E.UnexpectedEndOfChunk.code
+    # a mask that misses the bad chunk's rows: neither side reads it
+    mask = O.mask_from_rows(list(range(0, 900)), 5000)
+    assert E.Aggregation.max(expr).compute(ds_e, mask) == O.aggregate(ds_o, O.AGGR_MAX, expr.postfix(), mask)
+
+
+@pytest.mark.gpu
+def test_empty_columns():
+    ds_e = [E.Decoder(E.encode(np.zeros(0), "buff", ("record_count", 100), 1000)) for _ in range(2)]
+    ds_o = [O.Decoder(E.encode(np.zeros(0), "buff", ("record_count", 100), 1000)) for _ in range(2)]
+    expr = E.Expr.Index(0) + E.Expr.Index(1)
+    for kind in (O.AGGR_SUM, O.AGGR_MIN, O.AGGR_MAX):
+        assert same_scalar(E.Aggregation(kind, expr).compute(ds_e), O.aggregate(ds_o, kind, expr.postfix()))
+    assert E.Aggregation.sum(E.Expr.Index(0)).compute(ds_e) == O.aggregate(ds_o, O.AGGR_SUM, E.Expr.Index(0).postfix())
+    # AggregationResult::zero: a Literal is not even looked at without chunks
+    assert E.Aggregation.sum(E.Expr.Literal(2.0)).compute(ds_e) == 0.0
