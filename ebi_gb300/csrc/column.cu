@@ -249,18 +249,22 @@ int ensure_scratch(ebi_column* c, cudaStream_t s) {
     return st;
 }
 
-// Query timing: events at the query's start, around the codec kernels and
-// after the finalize fold.  mark_scan re-records the scan start right before
-// the first codec kernel (after the query's memsets and chunk selection).
+// Query timing: events at the query's start (ev[0]), right before the first
+// codec kernel (ev[3], after the query's memsets and chunk selection; the
+// scan is timed from ev[0] when a query marks none), after the codec kernels
+// (ev[1]) and after the finalize fold (ev[2]; a query whose totals the host
+// scales has no fold and ends at ev[1]).  Only events that delimit work are
+// recorded: each one is a timestamp write on the device's timeline.
 int begin_query(ebi_column* c, cudaStream_t s) {
     c->launches_at_start = ebi_kernel_launches();
+    c->scan_marked = false;
     if (c->timing) CK(cudaEventRecord(c->ev[0], s));
-    if (c->timing) CK(cudaEventRecord(c->ev[3], s));
     return EBI_OK;
 }
 
 int mark_scan(ebi_column* c, cudaStream_t s) {
     if (c->timing) CK(cudaEventRecord(c->ev[3], s));
+    c->scan_marked = true;
     return EBI_OK;
 }
 
@@ -268,10 +272,9 @@ int mark_scan(ebi_column* c, cudaStream_t s) {
 // totals for the host to scale), copies the result back and waits.
 int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
     if (c->timing) CK(cudaEventRecord(c->ev[1], s));
-    bool done = false;
+    bool done = false, folded = false;
     if (c->totals_pending) {
         c->totals_pending = false;
-        if (c->timing) CK(cudaEventRecord(c->ev[2], s));
         CK(cudaMemcpyAsync(c->h_tot, c->pending_tot, sizeof(ScanTotals), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         const ScanTotals t = *c->h_tot;
@@ -299,15 +302,17 @@ int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
         if (!c->fused_pending) CK(launch_finalize(q, c->d_res, s));
         c->fused_pending = false;
         if (c->timing) CK(cudaEventRecord(c->ev[2], s));
+        folded = true;
         CK(cudaMemcpyAsync(c->h_res, c->d_res, sizeof(QueryResult), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
     }
     c->last.kernels = ebi_kernel_launches() - c->launches_at_start;
     if (c->timing) {
         float a = 0.f, b = 0.f, t = 0.f;
-        CK(cudaEventElapsedTime(&a, c->ev[3], c->ev[1]));
-        CK(cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
-        CK(cudaEventElapsedTime(&t, c->ev[0], c->ev[2]));
+        cudaEvent_t end = folded ? c->ev[2] : c->ev[1];
+        CK(cudaEventElapsedTime(&a, c->scan_marked ? c->ev[3] : c->ev[0], c->ev[1]));
+        if (folded) CK(cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
+        CK(cudaEventElapsedTime(&t, c->ev[0], end));
         c->last.scan_ms = a;
         c->last.finalize_ms = b;
         c->last.total_ms = t;

@@ -55,6 +55,7 @@ struct ebi_column {
     bool timing = false;
     // query start, scan end, finalize end, scan start
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool scan_marked = false;    // the query recorded ev[3]
     ebi_segment_times last{};
     uint64_t launches_at_start = 0;
 };
