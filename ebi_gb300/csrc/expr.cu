@@ -22,11 +22,15 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
+#include <string>
 #include <type_traits>
 #include <vector>
 
 #include "column.h"
+#include "expr_fused.cuh"
+#include "expr_prog.h"
 #include "values.cuh"
 
 namespace ebi {
@@ -40,18 +44,6 @@ constexpr int kPassInstr = 2 * kMaxInstr;          // one pass (shared memory)
 constexpr int kMaxStack = 8;    // pushed accumulators
 constexpr int kMaxAggs = 8;     // aggregations per evaluation pass
 constexpr int kMaxCols = 16;    // distinct columns per evaluation pass
-
-// One instruction: acc = a OP b (LOAD: acc = a; PUSH: push acc).
-enum : uint8_t { I_LOAD = 0, I_PUSH = 1, I_ADD = 2, I_SUB = 3, I_MUL = 4, I_DIV = 5 };
-enum : uint8_t { S_ACC = 0, S_POP = 1, S_COL = 2, S_LIT = 3 };
-struct Instr {
-    uint8_t op, a, b;
-    uint8_t sa, sb;     // exact BUFF programs: left shifts aligning the operands' scales
-    uint8_t pad[3];
-    uint16_t ca, cb;    // column slot of an S_COL operand (a column index until a pass assigns slots)
-    uint16_t pad2[2];
-    double la, lb;      // literal of an S_LIT operand (exact programs: its integer numerator's bits)
-};
 
 struct ExprPass {
     uint32_t n_aggs, n_cols, n_chunks;
@@ -371,62 +363,35 @@ __global__ void __launch_bounds__(kExprThreads) expr_fold(ExprPass P, ExprScratc
 // When every column of a pass is BUFF, read at full precision, and its first
 // C chunks cover the same rows as the other columns', element k of a chunk is
 // the same row in every column: the zip is row-wise and the values need not
-// be materialized.  Each warp walks its own contiguous range of units (256
-// rows of one chunk): a lane reads its 8 consecutive rows of every column
-// straight from the planes, the values of the selected rows are packed into
-// the warp's shared-memory slots (in row order, warp shuffles for the
-// offsets), and the lanes run every aggregation's program on the packed
-// values.  Warps synchronise only with themselves, so each one's memory
-// latency overlaps the others' work.
-constexpr int kFuseThreads = 256;
-constexpr int kFuseWarps = kFuseThreads / 32;
-constexpr int kFuseRows = 8;                         // rows per lane
-constexpr uint32_t kFuseUnit = 32 * kFuseRows;       // rows per warp unit
-constexpr int kFuseStride = kFuseUnit + kFuseUnit / 8;  // doubles per column slot (one pad every 8: conflict-free)
-constexpr int kFuseCols = 4;
+// be materialized.  The walk over the planes is expr_fused.cuh's; the
+// program objects below interpret the pass's programs, on the fixed-point
+// integers (exact programs) or on the f64 values.  Exact passes may instead
+// run the same walk compiled at run time with the programs written out
+// (expr_jit.cu).
+constexpr int kFuseThreads = ebi_fx::kThreads;
+constexpr int kFuseWarps = ebi_fx::kWarps;
+constexpr int kFuseRows = ebi_fx::kRows;
+constexpr uint32_t kFuseUnit = ebi_fx::kUnit;
+constexpr int kFuseStride = ebi_fx::kStride;
+constexpr int kFuseCols = ebi_fx::kCols;
 constexpr int kFuseStack = 2;  // accumulators a fused program may push
 
-__device__ __forceinline__ uint32_t fuse_pad(uint32_t p) { return p + (p >> 3); }
-
-struct FusePass {
-    const uint8_t* file[kFuseCols];
-    const BuffChunkInfo* info[kFuseCols];
-    const ChunkDesc* chunks;    // row ranges (identical in every column)
-    const uint32_t* in_mask;    // u32 view of the bitmask, or null
-    uint64_t n_records;         // rows the mask covers
-    const uint32_t* unit0;      // [C + 1]: first unit of each chunk
-    uint32_t n_units;
-    unsigned int* bad;          // set when a chunk's status is not 0
-};
-
-// The 8 deltas of rows [8 g, 8 g + 8) of a chunk (BUFF planes, MSB plane first, then the tail bits).
-__device__ __forceinline__ void fuse_deltas(const uint8_t* file, const BuffChunkInfo& ci, uint32_t g,
-                                            unsigned long long (&d)[kFuseRows]) {
-    const uint32_t np = ci.bits / 8, tb = ci.bits % 8;
-#pragma unroll
-    for (int i = 0; i < kFuseRows; ++i) d[i] = 0;
-    for (uint32_t p = 0; p < np; ++p) {
-        const unsigned long long w = *reinterpret_cast<const unsigned long long*>(file + ci.planes + p * ci.stride +
-                                                                                 uint64_t(g) * 8);
-#pragma unroll
-        for (int i = 0; i < kFuseRows; ++i) d[i] = (d[i] << 8) | (((w >> (8 * i)) & 0xffull) ^ 0x80ull);
-    }
-    if (tb) {
-        // bits [64 g tb, 64 g tb + 8 tb) of the tail plane: bytes [g tb, g tb + tb)
-        const uint64_t b0 = uint64_t(g) * tb, w0 = b0 & ~3ull;
-        const uint32_t* t = reinterpret_cast<const uint32_t*>(file + ci.tail + w0);
-        const uint32_t sh = static_cast<uint32_t>(b0 & 3) * 8;
-        const uint64_t last = b0 + tb - 1;  // the words read end inside the (4-byte aligned) tail plane
-        const uint32_t x0 = t[0];
-        const uint32_t x1 = w0 + 4 <= last ? t[1] : 0u;
-        const uint32_t x2 = w0 + 8 <= last ? t[2] : 0u;
-        const unsigned long long lo = static_cast<unsigned long long>(x0) | (static_cast<unsigned long long>(x1) << 32);
-        const unsigned long long bits = sh ? (lo >> sh) | (static_cast<unsigned long long>(x2) << (64 - sh)) : lo;
-        const unsigned long long m = (1ull << tb) - 1ull;
-#pragma unroll
-        for (int i = 0; i < kFuseRows; ++i) d[i] = (d[i] << tb) | ((bits >> (i * tb)) & m);
-    }
-}
+static_assert(sizeof(ebi_fx::ChunkInfo) == sizeof(BuffChunkInfo) &&
+                  offsetof(ebi_fx::ChunkInfo, planes) == offsetof(BuffChunkInfo, planes) &&
+                  offsetof(ebi_fx::ChunkInfo, tail) == offsetof(BuffChunkInfo, tail) &&
+                  offsetof(ebi_fx::ChunkInfo, base) == offsetof(BuffChunkInfo, base) &&
+                  offsetof(ebi_fx::ChunkInfo, bits) == offsetof(BuffChunkInfo, bits) &&
+                  offsetof(ebi_fx::ChunkInfo, frac) == offsetof(BuffChunkInfo, frac) &&
+                  offsetof(ebi_fx::ChunkInfo, status) == offsetof(BuffChunkInfo, status) &&
+                  offsetof(ebi_fx::ChunkInfo, stride) == offsetof(BuffChunkInfo, stride),
+              "ebi_fx::ChunkInfo is BuffChunkInfo's layout twin");
+static_assert(sizeof(ebi_fx::Chunk) == sizeof(ChunkDesc) &&
+                  offsetof(ebi_fx::Chunk, row_off) == offsetof(ChunkDesc, row_off) &&
+                  offsetof(ebi_fx::Chunk, n_rows) == offsetof(ChunkDesc, n_rows),
+              "ebi_fx::Chunk is ChunkDesc's layout twin");
+static_assert(ebi_fx::kSum == EBI_AGGR_SUM && ebi_fx::kMin == EBI_AGGR_MIN && ebi_fx::kMax == EBI_AGGR_MAX,
+              "aggregation kinds");
+static_assert(sizeof(ebi_fx::Acc) == sizeof(Quad) && sizeof(RunAcc) == sizeof(ebi_fx::Acc), "partials");
 
 // (base + delta) / 2^frac exactly as the BUFF materialize kernel computes it
 // (int64 -> f64, then * 2^-frac or / 2^frac); when the integer is below 2^53
@@ -447,118 +412,39 @@ __device__ __forceinline__ double fuse_value(long long fixed, uint32_t frac, boo
     return inv_ok ? static_cast<double>(fixed) * inv : static_cast<double>(fixed) / scale;
 }
 
-// Exact programs' running aggregate: a 128-bit sum and the extreme values,
-// as the bits of a RunAcc.
-struct RunAccI {
-    unsigned long long lo, hi;   // two's complement 128-bit sum
-    unsigned long long mn, mx;   // signed order keys (sign bit flipped)
-};
-__device__ __forceinline__ unsigned long long skey(long long v) {
-    return static_cast<unsigned long long>(v) ^ 0x8000000000000000ull;
-}
-__device__ __forceinline__ void add128(unsigned long long& lo, unsigned long long& hi, unsigned long long blo,
-                                       unsigned long long bhi) {
-    const unsigned long long o = lo;
-    lo += blo;
-    hi += bhi + (lo < o ? 1ull : 0ull);
-}
-
-// kExact: the program runs on the fixed-point integers (each value is
-// fixed * 2^-frac; the host proved every intermediate below 2^53, where each
-// IEEE operation is exact and equals the integer one); else on the f64 values.
+// The program interpreter of a fused pass.  kExact: the program runs on the
+// fixed-point integers (each value is fixed * 2^-frac; the host proved every
+// intermediate below 2^53, where each IEEE operation is exact and equals the
+// integer one); else on the f64 values.  Running aggregates live in shared
+// memory: ebi_fx::Acc (exact) or RunAcc (f64) per thread and aggregation.
 template <bool kExact>
-__global__ void __launch_bounds__(kFuseThreads, 3) expr_buff_fused(ExprPass P, ExprScratch S, FusePass F) {
-    extern __shared__ double dyn[];  // [warp][n_cols][kFuseStride] packed values, then RunAcc[n_aggs][kFuseThreads]
-    const Instr* __restrict__ prog = S.prog;  // every lane reads the same instruction: one L1 line
-    __shared__ BuffChunkInfo s_ci[kFuseWarps][kFuseCols];
-    __shared__ const uint8_t* s_file[kFuseCols];
-    __shared__ uint32_t s_kind[kMaxAggs], s_first[kMaxAggs + 1];
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double* wslot = dyn + wid * P.n_cols * kFuseStride;
-    long long* islot = reinterpret_cast<long long*>(wslot);
-    RunAcc* runs = reinterpret_cast<RunAcc*>(dyn + kFuseWarps * P.n_cols * kFuseStride);
-    RunAccI* iruns = reinterpret_cast<RunAccI*>(runs);
-    if (threadIdx.x < kFuseCols) s_file[threadIdx.x] = F.file[threadIdx.x];
-    if (threadIdx.x < kMaxAggs) s_kind[threadIdx.x] = P.kind[threadIdx.x];
-    if (threadIdx.x <= kMaxAggs) s_first[threadIdx.x] = P.first[threadIdx.x];
-    for (uint32_t a = 0; a < P.n_aggs; ++a) {
-        if (kExact) iruns[a * kFuseThreads + threadIdx.x] = RunAccI{0, 0, skey(LLONG_MAX), skey(LLONG_MIN)};
-        else runs[a * kFuseThreads + threadIdx.x] = RunAcc{0.0, 0.0, kKeyPosInf, kKeyNegInf};
+struct FuseInterp {
+    const Instr* __restrict__ prog;  // every lane reads the same instruction: one L1 line
+    const uint32_t* first;           // shared: [n_aggs + 1]
+    const uint32_t* kind;            // shared: [n_aggs]
+    void* runs;                      // shared: [n_aggs][kFuseThreads]
+    uint32_t n;
+
+    __device__ uint32_t n_aggs() const { return n; }
+    __device__ void begin() {
+        for (uint32_t a = 0; a < n; ++a) {
+            if (kExact) static_cast<ebi_fx::Acc*>(runs)[a * kFuseThreads + threadIdx.x] = ebi_fx::acc_rest();
+            else static_cast<RunAcc*>(runs)[a * kFuseThreads + threadIdx.x] = RunAcc{0.0, 0.0, kKeyPosInf, kKeyNegInf};
+        }
     }
-    __syncthreads();
-    // the warp's units: a contiguous share of all units, in column order
-    const uint32_t C = P.n_chunks, n_warps = gridDim.x * kFuseWarps, gw = blockIdx.x * kFuseWarps + wid;
-    const uint32_t per = (F.n_units + n_warps - 1) / n_warps;
-    const uint32_t u_begin = min(F.n_units, gw * per), u_end = min(F.n_units, u_begin + per);
-    uint32_t c = 0xffffffffu, c_end = 0, c_first = 0, n_rows = 0;
-    uint64_t row_off = 0;
-    for (uint32_t u = u_begin; u < u_end; ++u) {
-        if (c == 0xffffffffu || u >= c_end) {
-            // the chunk of unit u (searched once, then stepped)
-            if (c == 0xffffffffu) {
-                uint32_t lo = 0, hi = C;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) / 2;
-                    if (F.unit0[mid] <= u) lo = mid; else hi = mid;
-                }
-                c = lo;
-            } else {
-                do { ++c; } while (F.unit0[c + 1] <= u);
-            }
-            c_first = F.unit0[c];
-            c_end = F.unit0[c + 1];
-            const ChunkDesc cd = F.chunks[c];
-            n_rows = cd.n_rows;
-            row_off = cd.row_off;
-            __syncwarp();
-            if (lane < P.n_cols) s_ci[wid][lane] = F.info[lane][c];
-            __syncwarp();
-        }
-        const uint32_t r = (u - c_first) * kFuseUnit + lane * kFuseRows;  // the lane's first row (in the chunk)
-        uint32_t sel = 0;
-        if (r < n_rows) {
-            const uint32_t left = n_rows - r;
-            sel = left >= kFuseRows ? 0xffu : ((1u << left) - 1u);
-            if (F.in_mask) sel &= mask_word(F.in_mask, row_off + r, F.n_records);
-        }
-        // pack position of the lane's first selected row: warp-exclusive prefix of the counts
-        const uint32_t cnt = __popc(sel);
-        uint32_t inc = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (static_cast<int>(lane) >= o) inc += y;
-        }
-        const uint32_t n_sel = __shfl_sync(0xffffffffu, inc, 31);
-        if (n_sel == 0) continue;
-        // decode the lane's rows of every column (no loads without selected rows)
-        if (sel) {
-            for (uint32_t j = 0; j < P.n_cols; ++j) {
-                const BuffChunkInfo ci = s_ci[wid][j];
-                if (ci.status) { atomicOr(F.bad, 1u); continue; }
-                unsigned long long d[kFuseRows];
-                fuse_deltas(s_file[j], ci, r / kFuseRows, d);
-                const bool inv_ok = ci.frac <= 1022;
-                const double scale = ci.frac <= 1023 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 + ci.frac) << 52))
-                                                     : __longlong_as_double(0x7ff0000000000000ll);
-                const double inv = inv_ok ? __longlong_as_double(static_cast<long long>(uint64_t(1023 - ci.frac) << 52)) : 0.0;
-                uint32_t p = inc - cnt;
-#pragma unroll
-                for (int i = 0; i < kFuseRows; ++i) {
-                    if (!((sel >> i) & 1u)) continue;
-                    const long long fixed = static_cast<long long>(static_cast<unsigned long long>(ci.base) + d[i]);
-                    if (kExact) islot[j * kFuseStride + fuse_pad(p++)] = fixed;
-                    else wslot[j * kFuseStride + fuse_pad(p++)] = fuse_value(fixed, ci.frac, inv_ok, inv, scale);
-                }
-            }
-        }
-        __syncwarp();
-        // the packed values p = lane + 32 k, k < 8
-        uint32_t ok = 0;
-#pragma unroll
-        for (int k = 0; k < kFuseRows; ++k)
-            if (lane + uint32_t(k) * 32 < n_sel) ok |= 1u << k;
-        for (uint32_t a = 0; a < P.n_aggs; ++a) {
+    __device__ long long pack(const ebi_fx::ChunkInfo& ci, long long fixed) const {
+        if (kExact) return fixed;
+        const bool inv_ok = ci.frac <= 1022;
+        const double scale = ci.frac <= 1023 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 + ci.frac) << 52))
+                                             : __longlong_as_double(0x7ff0000000000000ll);
+        const double inv = inv_ok ? __longlong_as_double(static_cast<long long>(uint64_t(1023 - ci.frac) << 52)) : 0.0;
+        return __double_as_longlong(fuse_value(fixed, ci.frac, inv_ok, inv, scale));
+    }
+    __device__ ebi_fx::Acc result(uint32_t a) const { return static_cast<ebi_fx::Acc*>(runs)[a * kFuseThreads + threadIdx.x]; }
+
+    __device__ void unit(const long long* islot, uint32_t lane, uint32_t ok) {
+        const double* wslot = reinterpret_cast<const double*>(islot);
+        for (uint32_t a = 0; a < n; ++a) {
             using V = typename std::conditional<kExact, long long, double>::type;
             // accumulator and a two-deep stack, all in registers: the operand
             // kinds are the same for every lane, so each instruction branches
@@ -567,7 +453,7 @@ __global__ void __launch_bounds__(kFuseThreads, 3) expr_buff_fused(ExprPass P, E
             int sp = 0;
 #pragma unroll
             for (int k = 0; k < kFuseRows; ++k) acc[k] = st0[k] = st1[k] = 0;
-            for (uint32_t q = s_first[a]; q < s_first[a + 1]; ++q) {
+            for (uint32_t q = first[a]; q < first[a + 1]; ++q) {
                 const uint8_t op = prog[q].op, src_a = prog[q].a, src_b = prog[q].b;
                 if (op == I_PUSH) {
                     if (sp == 0) {
@@ -587,7 +473,7 @@ __global__ void __launch_bounds__(kFuseThreads, 3) expr_buff_fused(ExprPass P, E
                         // read anyway (in bounds), their rows are dropped when aggregating
 #pragma unroll
                         for (int k = 0; k < kFuseRows; ++k) {
-                            const uint32_t at = col * kFuseStride + fuse_pad(lane + uint32_t(k) * 32);
+                            const uint32_t at = col * kFuseStride + ebi_fx::pad(lane + uint32_t(k) * 32);
                             if constexpr (kExact) out[k] = islot[at];
                             else out[k] = wslot[at];
                         }
@@ -644,63 +530,30 @@ __global__ void __launch_bounds__(kFuseThreads, 3) expr_buff_fused(ExprPass P, E
                 }
             }
             if constexpr (kExact) {
-                RunAccI& R = iruns[a * kFuseThreads + threadIdx.x];
-                if (s_kind[a] == EBI_AGGR_SUM) {
-                    long long sum = 0;  // at most 8 values below 2^53: no overflow
-#pragma unroll
-                    for (int k = 0; k < kFuseRows; ++k)
-                        if ((ok >> k) & 1u) sum += acc[k];
-                    add128(R.lo, R.hi, static_cast<unsigned long long>(sum), sum < 0 ? ~0ull : 0ull);
-                } else {
-#pragma unroll
-                    for (int k = 0; k < kFuseRows; ++k) {
-                        if (!((ok >> k) & 1u)) continue;
-                        const unsigned long long kk = skey(acc[k]);
-                        R.mn = kk < R.mn ? kk : R.mn;
-                        R.mx = kk > R.mx ? kk : R.mx;
-                    }
-                }
+                ebi_fx::acc_add(static_cast<ebi_fx::Acc*>(runs)[a * kFuseThreads + threadIdx.x], kind[a], acc, ok);
             } else {
-                run_add(runs[a * kFuseThreads + threadIdx.x], acc, ok, s_kind[a]);
+                run_add(static_cast<RunAcc*>(runs)[a * kFuseThreads + threadIdx.x], acc, ok, kind[a]);
             }
         }
-        __syncwarp();  // the slots are rewritten by the next unit
     }
-    __syncthreads();
-    if constexpr (!kExact) {
-        cta_partials(P, S, runs);
-    } else {
-        // 128-bit sums and keys: per warp, then across warps (part bits: lo, hi, min key, max key)
-        __shared__ unsigned long long r_lo[kFuseWarps], r_hi[kFuseWarps], r_mn[kFuseWarps], r_mx[kFuseWarps];
-        for (uint32_t a = 0; a < P.n_aggs; ++a) {
-            const RunAccI R = iruns[a * kFuseThreads + threadIdx.x];
-            unsigned long long lo = R.lo, hi = R.hi, mn = R.mn, mx = R.mx;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                add128(lo, hi, __shfl_xor_sync(0xffffffffu, lo, o), __shfl_xor_sync(0xffffffffu, hi, o));
-                const unsigned long long omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
-                mn = omn < mn ? omn : mn;
-                mx = omx > mx ? omx : mx;
-            }
-            if (lane == 0) { r_lo[wid] = lo; r_hi[wid] = hi; r_mn[wid] = mn; r_mx[wid] = mx; }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                unsigned long long tl = 0, th = 0, tmn = ~0ull, tmx = 0;
-                for (int w = 0; w < kFuseWarps; ++w) {
-                    add128(tl, th, r_lo[w], r_hi[w]);
-                    tmn = r_mn[w] < tmn ? r_mn[w] : tmn;
-                    tmx = r_mx[w] > tmx ? r_mx[w] : tmx;
-                }
-                Quad q;
-                q.x = __longlong_as_double(static_cast<long long>(tl));
-                q.y = __longlong_as_double(static_cast<long long>(th));
-                q.z = __longlong_as_double(static_cast<long long>(tmn));
-                q.w = __longlong_as_double(static_cast<long long>(tmx));
-                S.part[a * uint64_t(gridDim.x) + blockIdx.x] = q;
-            }
-            __syncthreads();
-        }
-    }
+};
+
+// Dynamic shared memory of an interpreted fused pass: the packed values, then
+// the running aggregates.
+__host__ __device__ constexpr size_t fuse_smem(uint32_t n_cols, uint32_t n_aggs) {
+    return size_t(kFuseWarps) * n_cols * kFuseStride * sizeof(double) + size_t(n_aggs) * kFuseThreads * sizeof(RunAcc);
+}
+
+template <bool kExact>
+__global__ void __launch_bounds__(kFuseThreads, 3) expr_buff_fused(ExprPass P, ExprScratch S, ebi_fx::Params F) {
+    extern __shared__ double dyn[];  // [warp][n_cols][kFuseStride] packed values, then the running aggregates
+    __shared__ uint32_t s_kind[kMaxAggs], s_first[kMaxAggs + 1];
+    if (threadIdx.x < kMaxAggs) s_kind[threadIdx.x] = P.kind[threadIdx.x];
+    if (threadIdx.x <= kMaxAggs) s_first[threadIdx.x] = P.first[threadIdx.x];
+    FuseInterp<kExact> I{S.prog, s_first, s_kind, dyn + kFuseWarps * P.n_cols * kFuseStride, P.n_aggs};
+    ebi_fx::fused_walk(F, I, reinterpret_cast<long long*>(dyn));  // synchronises after s_kind, s_first
+    if constexpr (kExact) ebi_fx::fused_finish_exact(F, I);
+    else cta_partials(P, S, static_cast<RunAcc*>(I.runs));
 }
 
 // Exact programs: the CTAs' 128-bit sums and keys, added in CTA order (res
@@ -714,7 +567,7 @@ __global__ void __launch_bounds__(kExprThreads) expr_fold_exact(ExprPass P, Expr
     unsigned long long lo = 0, hi = 0, mn = ~0ull, mx = 0;
     for (uint32_t i = threadIdx.x; i < n_parts; i += kExprThreads) {
         const Quad p = part[i];
-        add128(lo, hi, static_cast<unsigned long long>(__double_as_longlong(p.x)),
+        ebi_fx::add128(lo, hi, static_cast<unsigned long long>(__double_as_longlong(p.x)),
                static_cast<unsigned long long>(__double_as_longlong(p.y)));
         const unsigned long long pm = static_cast<unsigned long long>(__double_as_longlong(p.z));
         const unsigned long long px = static_cast<unsigned long long>(__double_as_longlong(p.w));
@@ -724,7 +577,7 @@ __global__ void __launch_bounds__(kExprThreads) expr_fold_exact(ExprPass P, Expr
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        add128(lo, hi, __shfl_xor_sync(0xffffffffu, lo, o), __shfl_xor_sync(0xffffffffu, hi, o));
+        ebi_fx::add128(lo, hi, __shfl_xor_sync(0xffffffffu, lo, o), __shfl_xor_sync(0xffffffffu, hi, o));
         const unsigned long long omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
         mn = omn < mn ? omn : mn;
         mx = omx > mx ? omx : mx;
@@ -734,7 +587,7 @@ __global__ void __launch_bounds__(kExprThreads) expr_fold_exact(ExprPass P, Expr
     if (threadIdx.x == 0) {
         unsigned long long tl = 0, th = 0, tmn = ~0ull, tmx = 0;
         for (int w = 0; w < kExprThreads / 32; ++w) {
-            add128(tl, th, r_lo[w], r_hi[w]);
+            ebi_fx::add128(tl, th, r_lo[w], r_hi[w]);
             tmn = r_mn[w] < tmn ? r_mn[w] : tmn;
             tmx = r_mx[w] > tmx ? r_mx[w] : tmx;
         }
@@ -1064,16 +917,27 @@ int run_fused(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<
         col_scale.push_back(Scale{static_cast<int>(c->buff_frac), static_cast<int>(c->buff_fixed_bits)});
     }
     exact = exact && exact_program(iprog, P, col_scale, f_out);
-    auto kernel = exact ? expr_buff_fused<true> : expr_buff_fused<false>;
-    // grid: the CTAs that fit the device at once (each keeps running sums)
-    const size_t smem = size_t(kFuseWarps) * P.n_cols * kFuseStride * sizeof(double) +
-                        size_t(P.n_aggs) * kFuseThreads * sizeof(RunAcc);
-    constexpr int kSmemMax = static_cast<int>(kFuseWarps * kFuseCols * kFuseStride * sizeof(double) +
-                                              kMaxAggs * kFuseThreads * sizeof(RunAcc));
+    // exact passes: the walk compiled with these programs written out, when
+    // the run-time compiler is there; else (and for f64 programs) interpreted
+    cudaKernel_t jit = nullptr;
+    if (exact) {
+        std::string why;
+        bool required = false;
+        jit = fused_jit_kernel(iprog, P.first, P.kind, P.n_aggs, P.n_cols, &why, &required);
+        if (!jit && required) return fail(EBI_E_CUDA, "run-time compiled expression pass: " + why);
+    }
+    const void* kernel = jit ? reinterpret_cast<const void*>(jit)
+                             : exact ? reinterpret_cast<const void*>(expr_buff_fused<true>)
+                                     : reinterpret_cast<const void*>(expr_buff_fused<false>);
+    // grid: the CTAs that fit the device at once (each keeps running sums);
+    // the compiled walk keeps its running aggregates in registers
+    const size_t smem = jit ? fuse_smem(P.n_cols, 0) : fuse_smem(P.n_cols, P.n_aggs);
     static const cudaError_t attr =
-        cudaFuncSetAttribute(expr_buff_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax) != cudaSuccess
+        cudaFuncSetAttribute(expr_buff_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(fuse_smem(kFuseCols, kMaxAggs))) != cudaSuccess
             ? cudaGetLastError()
-            : cudaFuncSetAttribute(expr_buff_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax);
+            : cudaFuncSetAttribute(expr_buff_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(fuse_smem(kFuseCols, kMaxAggs)));
     if (attr != cudaSuccess) return cuda_fail(attr, "expr_buff_fused shared memory");
     int dev = 0, sms = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
@@ -1103,24 +967,35 @@ int run_fused(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<
     S.part = d_part;
     S.res = d_part + uint64_t(grid) * P.n_aggs;
     S.prog = d_prog;
-    FusePass F{};
+    ebi_fx::Params F{};
     for (uint32_t j = 0; j < P.n_cols; ++j) {
         F.file[j] = cols[slot_cols[j]]->d_file;
-        F.info[j] = cols[slot_cols[j]]->d_buff;
+        F.info[j] = reinterpret_cast<const ebi_fx::ChunkInfo*>(cols[slot_cols[j]]->d_buff);
     }
-    F.chunks = r->d_chunks;
+    F.chunks = reinterpret_cast<const ebi_fx::Chunk*>(r->d_chunks);
     F.in_mask = reinterpret_cast<const uint32_t*>(d_mask);
     F.n_records = r->n_records;
     F.unit0 = d_unit0;
     F.n_units = n_units;
+    F.n_chunks = C;
+    F.n_cols = P.n_cols;
+    F.n_aggs = P.n_aggs;
     F.bad = reinterpret_cast<unsigned int*>(d_tot);
+    F.part = reinterpret_cast<ebi_fx::Acc*>(d_part);
     std::vector<Quad> res(P.n_aggs);
     unsigned long long bad = 0;
     CK(cudaMemcpyAsync(d_unit0, unit0.data(), unit0.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(d_tot, 0, 8, s));
     CK(cudaMemcpyAsync(d_prog, (exact ? iprog : prog).data(), prog.size() * sizeof(Instr), cudaMemcpyHostToDevice, s));
     // every CTA writes its partials (identities when it gets no tile)
-    kernel<<<grid, kFuseThreads, smem, s>>>(P, S, F);
+    if (jit) {
+        void* args[] = {&F};
+        CK(cudaLaunchKernel(kernel, dim3(grid), dim3(kFuseThreads), args, smem, s));
+    } else if (exact) {
+        expr_buff_fused<true><<<grid, kFuseThreads, smem, s>>>(P, S, F);
+    } else {
+        expr_buff_fused<false><<<grid, kFuseThreads, smem, s>>>(P, S, F);
+    }
     if (exact) expr_fold_exact<<<P.n_aggs, kExprThreads, 0, s>>>(P, S, grid);
     else expr_fold<<<P.n_aggs, kExprThreads, 0, s>>>(P, S, grid);
     count_launch(2);

@@ -1,0 +1,242 @@
+// expr_jit.cu -- the fused exact Expr pass compiled at run time for the
+// programs of a pass.  The interpreter (expr.cu) decodes every instruction
+// of every program for every unit of 256 rows and runs 64-bit shifts by
+// amounts it learns at run time; written out, a program is a few integer
+// operations per row with constant shifts and literals, and expressions
+// that several aggregations share (TPC-H Q1's price * (1 - discount)) are
+// computed once.  The walk itself is expr_fused.cuh's text, compiled as is.
+//
+// NVRTC is opened at first use (dlopen): the library itself does not
+// depend on it, and without it the interpreter runs.
+#include <dlfcn.h>
+
+#include <cinttypes>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <sstream>
+
+#include <nvrtc.h>
+
+#include "expr_fused.cuh"
+#include "expr_prog.h"
+
+namespace ebi {
+namespace {
+
+// expr_fused.cuh as text (generated beside the objects at build time).
+const char kFusedSource[] =
+#include "expr_fused_src.inc"
+    ;
+
+constexpr const char* kKernelName = "ebi_expr_fused_jit";
+
+// The C++ of a pass's program object: aggregation a's value of row k is
+// v<a>[k], built from the columns' slot values c<j> with wrapping 64-bit
+// arithmetic, exactly as the interpreter computes it.
+std::string program_source(const std::vector<Instr>& prog, const uint32_t* first, const uint32_t* kind,
+                           uint32_t n_aggs, uint32_t n_cols) {
+    std::ostringstream body;
+    std::vector<bool> used(n_cols, false);
+    int tmp = 0;
+    for (uint32_t a = 0; a < n_aggs; ++a) {
+        std::string acc;
+        std::vector<std::string> stack;
+        auto operand = [&](uint8_t src, uint16_t col, double lit, uint8_t sh) {
+            std::string e;
+            if (src == S_COL) {
+                e = "c" + std::to_string(col);
+                if (col < n_cols) used[col] = true;
+            } else if (src == S_LIT) {
+                long long n = 0;
+                std::memcpy(&n, &lit, sizeof n);
+                char buf[32];
+                std::snprintf(buf, sizeof buf, "0x%016llxull", static_cast<unsigned long long>(n));
+                e = buf;
+            } else if (src == S_ACC) {
+                e = acc;
+            } else {
+                e = stack.back();
+            }
+            if (sh) e = "(" + e + " << " + std::to_string(sh) + ")";
+            return e;
+        };
+        for (uint32_t q = first[a]; q < first[a + 1]; ++q) {
+            const Instr& I = prog[q];
+            if (I.op == I_PUSH) {
+                stack.push_back(acc);
+                continue;
+            }
+            const std::string x = operand(I.a, I.ca, I.la, I.sa);
+            if (I.op == I_LOAD) {
+                acc = x;
+                continue;
+            }
+            const std::string y = operand(I.b, I.cb, I.lb, I.sb);
+            if (I.a == S_POP || I.b == S_POP) stack.pop_back();
+            const char* op = I.op == I_ADD ? " + " : I.op == I_SUB ? " - " : " * ";
+            const std::string t = "t" + std::to_string(tmp++);
+            body << "      const u64 " << t << " = " << x << op << y << ";\n";
+            acc = t;
+        }
+        body << "      v" << a << "[k] = static_cast<i64>(" << acc << ");\n";
+    }
+    std::ostringstream o;
+    o << "namespace ebi_fx {\nstruct Gen {\n";
+    for (uint32_t a = 0; a < n_aggs; ++a) o << "  Acc A" << a << ";\n";
+    o << "  __device__ u32 n_aggs() const { return " << n_aggs << "u; }\n";
+    o << "  __device__ void begin() {";
+    for (uint32_t a = 0; a < n_aggs; ++a) o << " A" << a << " = acc_rest();";
+    o << " }\n";
+    o << "  __device__ i64 pack(const ChunkInfo&, i64 fixed) const { return fixed; }\n";
+    o << "  __device__ Acc result(u32 a) const {";
+    for (uint32_t a = 0; a + 1 < n_aggs; ++a) o << " if (a == " << a << "u) return A" << a << ";";
+    o << " return A" << n_aggs - 1 << "; }\n";
+    o << "  __device__ void unit(const i64* s, u32 lane, u32 ok) {\n";
+    for (uint32_t a = 0; a < n_aggs; ++a) o << "    i64 v" << a << "[kRows];\n";
+    o << "#pragma unroll\n    for (int k = 0; k < kRows; ++k) {\n";
+    o << "      const u32 at = pad(lane + 32u * static_cast<u32>(k));\n";
+    for (uint32_t j = 0; j < n_cols; ++j)
+        if (used[j]) o << "      const u64 c" << j << " = static_cast<u64>(s[" << j << " * kStride + at]);\n";
+    o << body.str() << "    }\n";
+    for (uint32_t a = 0; a < n_aggs; ++a) {
+        const char* fn = kind[a] == ebi_fx::kSum ? "acc_sum" : kind[a] == ebi_fx::kMin ? "acc_min" : "acc_max";
+        o << "    " << fn << "(A" << a << ", v" << a << ", ok);\n";
+    }
+    o << "  }\n};\n}  // namespace ebi_fx\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(" << ebi_fx::kThreads << ", 3) " << kKernelName
+      << "(ebi_fx::Params F) {\n"
+         "  extern __shared__ long long fx_slots[];\n"
+         "  ebi_fx::Gen g;\n"
+         "  ebi_fx::fused_walk(F, g, fx_slots);\n"
+         "  ebi_fx::fused_finish_exact(F, g);\n"
+         "}\n";
+    return o.str();
+}
+
+// NVRTC entry points, resolved once.
+struct Nvrtc {
+    bool ok = false;
+    std::string why;
+    nvrtcResult (*create)(nvrtcProgram*, const char*, const char*, int, const char* const*, const char* const*);
+    nvrtcResult (*compile)(nvrtcProgram, int, const char* const*);
+    nvrtcResult (*log_size)(nvrtcProgram, size_t*);
+    nvrtcResult (*log)(nvrtcProgram, char*);
+    nvrtcResult (*cubin_size)(nvrtcProgram, size_t*);
+    nvrtcResult (*cubin)(nvrtcProgram, char*);
+    nvrtcResult (*destroy)(nvrtcProgram*);
+};
+
+const Nvrtc& nvrtc() {
+    static const Nvrtc N = [] {
+        Nvrtc n{};
+        void* h = nullptr;
+        for (const char* name : {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13"})
+            if ((h = dlopen(name, RTLD_NOW | RTLD_LOCAL))) break;
+        if (!h) {
+            n.why = "NVRTC not found (libnvrtc.so.13)";
+            return n;
+        }
+        auto sym = [&](const char* s) { return dlsym(h, s); };
+        n.create = reinterpret_cast<decltype(n.create)>(sym("nvrtcCreateProgram"));
+        n.compile = reinterpret_cast<decltype(n.compile)>(sym("nvrtcCompileProgram"));
+        n.log_size = reinterpret_cast<decltype(n.log_size)>(sym("nvrtcGetProgramLogSize"));
+        n.log = reinterpret_cast<decltype(n.log)>(sym("nvrtcGetProgramLog"));
+        n.cubin_size = reinterpret_cast<decltype(n.cubin_size)>(sym("nvrtcGetCUBINSize"));
+        n.cubin = reinterpret_cast<decltype(n.cubin)>(sym("nvrtcGetCUBIN"));
+        n.destroy = reinterpret_cast<decltype(n.destroy)>(sym("nvrtcDestroyProgram"));
+        n.ok = n.create && n.compile && n.log_size && n.log && n.cubin_size && n.cubin && n.destroy;
+        if (!n.ok) n.why = "NVRTC lacks an entry point";
+        return n;
+    }();
+    return N;
+}
+
+struct Compiled {
+    cudaKernel_t kernel = nullptr;
+    std::string why;  // the failure, when kernel is null
+};
+
+// Compiles the walk with a program object for this device's architecture.
+Compiled compile(const std::string& program) {
+    Compiled out;
+    const Nvrtc& N = nvrtc();
+    if (!N.ok) {
+        out.why = N.why;
+        return out;
+    }
+    int dev = 0, major = 0, minor = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess) {
+        out.why = "no device";
+        return out;
+    }
+    const std::string src = std::string(kFusedSource) + "\n" + program;
+    const std::string arch = "-arch=sm_" + std::to_string(major * 10 + minor) + "a";
+    const char* opts[] = {arch.c_str(), "-std=c++17"};
+    nvrtcProgram p = nullptr;
+    if (N.create(&p, src.c_str(), "ebi_expr_fused_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+        out.why = "nvrtcCreateProgram failed";
+        return out;
+    }
+    std::vector<char> cubin;
+    if (N.compile(p, 2, opts) != NVRTC_SUCCESS) {
+        size_t n = 0;
+        N.log_size(p, &n);
+        std::string log(n, '\0');
+        if (n) N.log(p, &log[0]);
+        out.why = "NVRTC compile failed: " + log.substr(0, 2000);
+    } else {
+        size_t n = 0;
+        if (N.cubin_size(p, &n) == NVRTC_SUCCESS && n) {
+            cubin.resize(n);
+            if (N.cubin(p, cubin.data()) != NVRTC_SUCCESS) cubin.clear();
+        }
+        if (cubin.empty()) out.why = "NVRTC produced no cubin";
+    }
+    N.destroy(&p);
+    if (cubin.empty()) return out;
+    cudaLibrary_t lib = nullptr;
+    cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&out.kernel, lib, kKernelName);
+    // the packed values of four columns exceed the default 48 KB
+    constexpr int kSmem = ebi_fx::kWarps * ebi_fx::kCols * ebi_fx::kStride * 8;
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(out.kernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kSmem);
+    if (e != cudaSuccess) {
+        out.kernel = nullptr;
+        out.why = std::string("loading the compiled pass: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+    }
+    return out;  // the library stays loaded for the process: its kernel is cached
+}
+
+}  // namespace
+
+cudaKernel_t fused_jit_kernel(const std::vector<Instr>& prog, const uint32_t* first, const uint32_t* kind,
+                              uint32_t n_aggs, uint32_t n_cols, std::string* why, bool* required) {
+    const char* env = std::getenv("EBI_EXPR_JIT");
+    *required = env && std::strcmp(env, "require") == 0;
+    if (env && std::strcmp(env, "0") == 0) {
+        *why = "off (EBI_EXPR_JIT=0)";
+        return nullptr;
+    }
+    if (n_aggs == 0) {
+        *why = "no aggregation";
+        return nullptr;
+    }
+    const std::string program = program_source(prog, first, kind, n_aggs, n_cols);
+    static std::mutex mu;
+    static std::map<std::string, Compiled> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(program);
+    if (it == cache.end()) it = cache.emplace(program, compile(program)).first;
+    if (!it->second.kernel) *why = it->second.why;
+    return it->second.kernel;
+}
+
+}  // namespace ebi

@@ -317,6 +317,45 @@ def test_buff_fused_and_general_paths_agree():
 
 
 @pytest.mark.gpu
+def test_fused_pass_compiled_at_run_time_matches_interpreter(monkeypatch):
+    """Exact fused passes run the walk compiled at run time with the programs
+    written out (EBI_EXPR_JIT=require: a compile failure is an error); the
+    same passes through the interpreter (EBI_EXPR_JIT=0) give bit-identical
+    results, and both follow the oracle.  Rows not a multiple of the 256-row
+    unit, masks, stacks, shifted literals, several aggregations per pass."""
+    rng = np.random.default_rng(14)
+    n = 70_001
+    price = np.round(rng.uniform(900, 105000, n), 2)
+    disc = np.round(rng.integers(0, 11, n) / 100.0, 2)
+    tax = np.round(rng.integers(0, 9, n) / 100.0, 2)
+    neg = np.round(rng.uniform(-50, 50, n), 2)
+    cols = [price, disc, tax, neg]
+    ds_o = [O.Decoder(O.encode(c, O.BUFF, O.CHUNK_RECORD_COUNT, 16_384, 100)) for c in cols]
+    ds_e = [E.Decoder(E.encode(c, "buff", ("record_count", 16_384), 100)) for c in cols]
+    one = E.Expr.Literal(1.0)
+    i0, i1, i2, i3 = (E.Expr.Index(k) for k in range(4))
+    aggs = [E.Aggregation.sum(i0 * (one - i1)), E.Aggregation.sum((i0 * (one - i1)) * (one + i2)),
+            E.Aggregation.min(i3 * i1 - 0.25), E.Aggregation.max((i3 + i2) * (i1 - i3)),
+            E.Aggregation.sum(i3 - i0), E.Aggregation.max(i0 * i1)]
+    rows = np.sort(rng.choice(n, 20_000, replace=False))
+    for mask in (None, O.mask_from_rows(rows.tolist(), n)):
+        results = {}
+        for mode in ("0", "require"):
+            monkeypatch.setenv("EBI_EXPR_JIT", mode)
+            results[mode] = E.Aggregation.compute_multiple(aggs, ds_e, mask)
+            for a in aggs[:3]:
+                _check_engine(ds_e, ds_o, a.expr, a.kind, mask)
+        got, ref = results["require"], results["0"]
+        assert np.array_equal(np.array(got, float).view(np.uint64), np.array(ref, float).view(np.uint64)), (got, ref)
+        for a, g in zip(aggs, got):
+            want = O.aggregate(ds_o, a.kind, a.expr.postfix(), mask)
+            if a.kind == O.AGGR_SUM:
+                assert expr_sum_ok(g, want, O.aggregate(ds_o, O.AGGR_NONE, a.expr.postfix(), mask)), (a.expr, g, want)
+            else:
+                assert same_scalar(g, want), (a.expr, g, want)
+
+
+@pytest.mark.gpu
 def test_buff_wide_values_take_the_f64_kernel():
     """Scale 10^6 on values near 10^6: 41-bit fixed-point integers, whose
     products pass 2^53, so the fused path evaluates in f64 (sums of single
