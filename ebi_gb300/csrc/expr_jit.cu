@@ -106,7 +106,9 @@ std::string program_source(const std::vector<Instr>& prog, const uint32_t* first
         o << "    " << fn << "(A" << a << ", v" << a << ", ok);\n";
     }
     o << "  }\n};\n}  // namespace ebi_fx\n";
-    o << "extern \"C\" __global__ void __launch_bounds__(" << ebi_fx::kThreads << ", 3) " << kKernelName
+    // up to three columns the packed values (55 KB) leave room for four CTAs per SM
+    const int min_blocks = n_cols <= 3 ? 4 : 3;
+    o << "extern \"C\" __global__ void __launch_bounds__(" << ebi_fx::kThreads << ", " << min_blocks << ") " << kKernelName
       << "(ebi_fx::Params F) {\n"
          "  extern __shared__ long long fx_slots[];\n"
          "  ebi_fx::Gen g;\n"
