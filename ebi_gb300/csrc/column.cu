@@ -531,7 +531,10 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         c->sms = static_cast<uint32_t>(std::max(sms, 1));
         uint64_t rows_of[65] = {};
         for (const BuffChunkInfo& b : binfo)
-            if (!b.status) rows_of[b.bits] += b.n;
+            if (!b.status) {
+                rows_of[b.bits] += b.n;
+                c->buff_max_bits = std::max(c->buff_max_bits, b.bits);
+            }
         c->stream_bits = static_cast<uint32_t>(std::max_element(rows_of + 1, rows_of + 33) - rows_of);
     } else {
         if (c->scheme == EBI_GORILLA) c->stage_bytes = gorilla_stage_bytes(c->chunks.data(), c->n_chunks);

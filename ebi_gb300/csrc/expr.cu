@@ -419,6 +419,7 @@ __device__ __forceinline__ double fuse_value(long long fixed, uint32_t frac, boo
 // memory: ebi_fx::Acc (exact) or RunAcc (f64) per thread and aggregation.
 template <bool kExact>
 struct FuseInterp {
+    static constexpr bool kPacked = true;
     const Instr* __restrict__ prog;  // every lane reads the same instruction: one L1 line
     const uint32_t* first;           // shared: [n_aggs + 1]
     const uint32_t* kind;            // shared: [n_aggs]
@@ -920,18 +921,22 @@ int run_fused(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<
     // exact passes: the walk compiled with these programs written out, when
     // the run-time compiler is there; else (and for f64 programs) interpreted
     cudaKernel_t jit = nullptr;
-    if (exact) {
+    bool narrow = true;  // the compiled walk decodes in 32-bit arithmetic
+    for (uint32_t j : slot_cols) narrow = narrow && cols[j]->buff_max_bits <= 32;
+    if (exact && narrow) {
         std::string why;
         bool required = false;
-        jit = fused_jit_kernel(iprog, P.first, P.kind, P.n_aggs, P.n_cols, &why, &required);
+        uint32_t widths[kFuseCols] = {};
+        for (uint32_t j = 0; j < P.n_cols; ++j) widths[j] = cols[slot_cols[j]]->stream_bits;
+        jit = fused_jit_kernel(iprog, P.first, P.kind, P.n_aggs, P.n_cols, widths, &why, &required);
         if (!jit && required) return fail(EBI_E_CUDA, "run-time compiled expression pass: " + why);
     }
     const void* kernel = jit ? reinterpret_cast<const void*>(jit)
                              : exact ? reinterpret_cast<const void*>(expr_buff_fused<true>)
                                      : reinterpret_cast<const void*>(expr_buff_fused<false>);
     // grid: the CTAs that fit the device at once (each keeps running sums);
-    // the compiled walk keeps its running aggregates in registers
-    const size_t smem = jit ? fuse_smem(P.n_cols, 0) : fuse_smem(P.n_cols, P.n_aggs);
+    // the compiled walk decodes and aggregates in registers
+    const size_t smem = jit ? 0 : fuse_smem(P.n_cols, P.n_aggs);
     static const cudaError_t attr =
         cudaFuncSetAttribute(expr_buff_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(fuse_smem(kFuseCols, kMaxAggs))) != cudaSuccess

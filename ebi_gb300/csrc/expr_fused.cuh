@@ -16,14 +16,21 @@
 // reduction, so each one's memory latency overlaps the others' work.
 //
 // A program object provides
+//   kPacked                       true: the walk packs the selected rows
 //   n_aggs()                      aggregations of the pass
 //   begin()                       sets the thread's running aggregates at rest
+//   result(a)                     the thread's running aggregate of aggregation
+//                                 a (exact passes: fused_finish_exact)
+// and, when kPacked,
 //   pack(ci, fixed)               the slot bits of a row's fixed-point integer
 //                                 (the integer itself, or its f64 value's bits)
 //   unit(slots, lane, ok)         evaluates packed values lane + 32 k (k with
 //                                 bit k of ok) and adds them
-//   result(a)                     the thread's running aggregate of aggregation
-//                                 a (exact passes: fused_finish_exact)
+// else
+//   rows(ci, file, g, sel, bad)   decodes rows 8 g .. 8 g + 7 of the warp's
+//                                 chunk (headers ci, planes file) itself and
+//                                 adds those with bit k of sel set; sets *bad
+//                                 when a header carries an error
 #pragma once
 
 namespace ebi_fx {
@@ -151,16 +158,46 @@ __device__ __forceinline__ void deltas(const unsigned char* file, const ChunkInf
     }
 }
 
-// The walk over the units.  slots: the dynamic shared memory, kWarps *
-// n_cols * kStride values first (more after them is the program object's).
-// Ends with the CTA synchronised.
+// deltas for a chunk NP * 8 + TB <= 32 bits wide, in 32-bit arithmetic
+// (the same values).
+template <int NP, int TB>
+__device__ __forceinline__ void deltas32(const unsigned char* file, const ChunkInfo& ci, u32 g, u32 (&d)[kRows]) {
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) d[i] = 0;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const u64 w = *reinterpret_cast<const u64*>(file + ci.planes + u64(p) * ci.stride + u64(g) * 8) ^
+                      0x8080808080808080ull;
+        const u32 lo = static_cast<u32>(w), hi = static_cast<u32>(w >> 32);
+#pragma unroll
+        for (int i = 0; i < kRows; ++i) d[i] = (d[i] << 8) | (((i < 4 ? lo : hi) >> (8 * (i & 3))) & 0xffu);
+    }
+    if (TB) {
+        const u64 b0 = u64(g) * TB, w0 = b0 & ~3ull;
+        const u32* t = reinterpret_cast<const u32*>(file + ci.tail + w0);
+        const u32 sh = static_cast<u32>(b0 & 3) * 8;
+        const u64 last = b0 + TB - 1;
+        const u32 x0 = t[0];
+        const u32 x1 = w0 + 4 <= last ? t[1] : 0u;
+        const u32 x2 = w0 + 8 <= last ? t[2] : 0u;
+        const u64 lo = static_cast<u64>(x0) | (static_cast<u64>(x1) << 32);
+        const u64 bits = sh ? (lo >> sh) | (static_cast<u64>(x2) << (64 - sh)) : lo;
+#pragma unroll
+        for (int i = 0; i < kRows; ++i)
+            d[i] = (d[i] << (TB & 7)) | static_cast<u32>((bits >> (i * TB)) & ((1ull << TB) - 1ull));
+    }
+}
+
+// The walk over the units.  slots (packing program objects): the dynamic
+// shared memory, kWarps * n_cols * kStride values first (more after them is
+// the program object's).  Ends with the CTA synchronised.
 template <class Prog>
 __device__ __forceinline__ void fused_walk(const Params& F, Prog& prog, i64* slots) {
     __shared__ ChunkInfo s_ci[kWarps][kCols];
     __shared__ const unsigned char* s_file[kCols];
     __shared__ const ChunkInfo* s_info[kCols];
     const u32 lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    i64* islot = slots + wid * F.n_cols * kStride;
+    i64* islot = Prog::kPacked ? slots + wid * F.n_cols * kStride : nullptr;
 #pragma unroll
     for (int j = 0; j < kCols; ++j)  // constant indices: the parameter arrays stay in the parameter bank
         if (threadIdx.x == j) {
@@ -203,40 +240,44 @@ __device__ __forceinline__ void fused_walk(const Params& F, Prog& prog, i64* slo
             sel = left >= kRows ? 0xffu : ((1u << left) - 1u);
             if (F.in_mask) sel &= mask_bits(F.in_mask, row_off + r, F.n_records);
         }
-        // pack position of the lane's first selected row: warp-exclusive prefix of the counts
-        const u32 cnt = __popc(sel);
-        u32 inc = cnt;
+        if constexpr (!Prog::kPacked) {
+            if (sel) prog.rows(s_ci[wid], s_file, r / kRows, sel, F.bad);
+        } else {
+            // pack position of the lane's first selected row: warp-exclusive prefix of the counts
+            const u32 cnt = __popc(sel);
+            u32 inc = cnt;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const u32 y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (static_cast<int>(lane) >= o) inc += y;
-        }
-        const u32 n_sel = __shfl_sync(0xffffffffu, inc, 31);
-        if (n_sel == 0) continue;
-        // the lane's rows of every column (no loads without selected rows)
-        if (sel) {
-            for (u32 j = 0; j < F.n_cols; ++j) {
-                const ChunkInfo ci = s_ci[wid][j];
-                if (ci.status) { atomicOr(F.bad, 1u); continue; }
-                u64 d[kRows];
-                deltas(s_file[j], ci, r / kRows, d);
-                u32 p = inc - cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const u32 y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (static_cast<int>(lane) >= o) inc += y;
+            }
+            const u32 n_sel = __shfl_sync(0xffffffffu, inc, 31);
+            if (n_sel == 0) continue;
+            // the lane's rows of every column (no loads without selected rows)
+            if (sel) {
+                for (u32 j = 0; j < F.n_cols; ++j) {
+                    const ChunkInfo ci = s_ci[wid][j];
+                    if (ci.status) { atomicOr(F.bad, 1u); continue; }
+                    u64 d[kRows];
+                    deltas(s_file[j], ci, r / kRows, d);
+                    u32 p = inc - cnt;
 #pragma unroll
-                for (int i = 0; i < kRows; ++i) {
-                    if (!((sel >> i) & 1u)) continue;
-                    islot[j * kStride + pad(p++)] = prog.pack(ci, static_cast<i64>(static_cast<u64>(ci.base) + d[i]));
+                    for (int i = 0; i < kRows; ++i) {
+                        if (!((sel >> i) & 1u)) continue;
+                        islot[j * kStride + pad(p++)] = prog.pack(ci, static_cast<i64>(static_cast<u64>(ci.base) + d[i]));
+                    }
                 }
             }
-        }
-        __syncwarp();
-        // the packed values p = lane + 32 k, k < 8; slots past n_sel hold
-        // stale values of the warp's own region, read but not aggregated
-        u32 ok = 0;
+            __syncwarp();
+            // the packed values p = lane + 32 k, k < 8; slots past n_sel hold
+            // stale values of the warp's own region, read but not aggregated
+            u32 ok = 0;
 #pragma unroll
-        for (int k = 0; k < kRows; ++k)
-            if (lane + u32(k) * 32 < n_sel) ok |= 1u << k;
-        prog.unit(islot, lane, ok);
-        __syncwarp();  // the slots are rewritten by the next unit
+            for (int k = 0; k < kRows; ++k)
+                if (lane + u32(k) * 32 < n_sel) ok |= 1u << k;
+            prog.unit(islot, lane, ok);
+            __syncwarp();  // the slots are rewritten by the next unit
+        }
     }
     __syncthreads();
 }

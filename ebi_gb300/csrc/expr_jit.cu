@@ -1,10 +1,12 @@
 // expr_jit.cu -- the fused exact Expr pass compiled at run time for the
 // programs of a pass.  The interpreter (expr.cu) decodes every instruction
-// of every program for every unit of 256 rows and runs 64-bit shifts by
-// amounts it learns at run time; written out, a program is a few integer
-// operations per row with constant shifts and literals, and expressions
-// that several aggregations share (TPC-H Q1's price * (1 - discount)) are
-// computed once.  The walk itself is expr_fused.cuh's text, compiled as is.
+// of every program for every unit of 256 rows, runs 64-bit shifts by
+// amounts it learns at run time and reads its values back from shared
+// memory; written out, a program is a few integer operations per row on
+// registers with constant shifts and literals, expressions that several
+// aggregations share (TPC-H Q1's price * (1 - discount)) are computed once,
+// and the columns decode at their common widths in 32-bit arithmetic.  The
+// walk itself is expr_fused.cuh's text, compiled as is.
 //
 // NVRTC is opened at first use (dlopen): the library itself does not
 // depend on it, and without it the interpreter runs.
@@ -33,11 +35,15 @@ const char kFusedSource[] =
 
 constexpr const char* kKernelName = "ebi_expr_fused_jit";
 
-// The C++ of a pass's program object: aggregation a's value of row k is
-// v<a>[k], built from the columns' slot values c<j> with wrapping 64-bit
-// arithmetic, exactly as the interpreter computes it.
+// The C++ of a pass's program object.  It decodes the rows of the columns it
+// reads itself, in registers (no packing), in 32-bit arithmetic (every chunk
+// of the columns is at most 32 bits wide): at the columns' common chunk
+// widths with the plane count and tail width constant, other chunks through
+// the general decode.  Aggregation a's value of
+// row k is v<a>[k], built from the columns' fixed-point integers c<j> with
+// wrapping 64-bit arithmetic, exactly as the interpreter computes it.
 std::string program_source(const std::vector<Instr>& prog, const uint32_t* first, const uint32_t* kind,
-                           uint32_t n_aggs, uint32_t n_cols) {
+                           uint32_t n_aggs, uint32_t n_cols, const uint32_t* widths) {
     std::ostringstream body;
     std::vector<bool> used(n_cols, false);
     int tmp = 0;
@@ -83,36 +89,84 @@ std::string program_source(const std::vector<Instr>& prog, const uint32_t* first
         }
         body << "      v" << a << "[k] = static_cast<i64>(" << acc << ");\n";
     }
+    std::vector<uint32_t> U;  // the columns read
+    for (uint32_t j = 0; j < n_cols; ++j)
+        if (used[j]) U.push_back(j);
+    bool fast = !U.empty();
+    for (uint32_t j : U) fast = fast && widths[j] >= 1 && widths[j] <= 32;  // else every chunk decodes generally
+    auto list = [&](const char* pre, const char* post) {
+        std::string l;
+        for (size_t i = 0; i < U.size(); ++i) l += (i ? ", " : "") + std::string(pre) + std::to_string(U[i]) + post;
+        return l;
+    };
+
     std::ostringstream o;
-    o << "namespace ebi_fx {\nstruct Gen {\n";
+    o << "namespace ebi_fx {\nstruct Gen {\n  static constexpr bool kPacked = false;\n";
     for (uint32_t a = 0; a < n_aggs; ++a) o << "  Acc A" << a << ";\n";
     o << "  __device__ u32 n_aggs() const { return " << n_aggs << "u; }\n";
     o << "  __device__ void begin() {";
     for (uint32_t a = 0; a < n_aggs; ++a) o << " A" << a << " = acc_rest();";
     o << " }\n";
-    o << "  __device__ i64 pack(const ChunkInfo&, i64 fixed) const { return fixed; }\n";
     o << "  __device__ Acc result(u32 a) const {";
     for (uint32_t a = 0; a + 1 < n_aggs; ++a) o << " if (a == " << a << "u) return A" << a << ";";
     o << " return A" << n_aggs - 1 << "; }\n";
-    o << "  __device__ void unit(const i64* s, u32 lane, u32 ok) {\n";
+    // eval over the decoded deltas (u32 or u64) and the chunks' bases
+    o << "  template <" << list("class D", "") << ">\n";
+    o << "  __device__ __forceinline__ void eval(";
+    for (uint32_t j : U) o << "const D" << j << " (&d" << j << ")[kRows], i64 b" << j << ", ";
+    o << "u32 sel) {\n";
     for (uint32_t a = 0; a < n_aggs; ++a) o << "    i64 v" << a << "[kRows];\n";
     o << "#pragma unroll\n    for (int k = 0; k < kRows; ++k) {\n";
-    o << "      const u32 at = pad(lane + 32u * static_cast<u32>(k));\n";
-    for (uint32_t j = 0; j < n_cols; ++j)
-        if (used[j]) o << "      const u64 c" << j << " = static_cast<u64>(s[" << j << " * kStride + at]);\n";
+    for (uint32_t j : U)
+        o << "      const u64 c" << j << " = static_cast<u64>(b" << j << ") + static_cast<u64>(d" << j << "[k]);\n";
     o << body.str() << "    }\n";
     for (uint32_t a = 0; a < n_aggs; ++a) {
         const char* fn = kind[a] == ebi_fx::kSum ? "acc_sum" : kind[a] == ebi_fx::kMin ? "acc_min" : "acc_max";
-        o << "    " << fn << "(A" << a << ", v" << a << ", ok);\n";
+        o << "    " << fn << "(A" << a << ", v" << a << ", sel);\n";
+    }
+    o << "  }\n";
+    o << "  __device__ void rows(const ChunkInfo* ci, const unsigned char* const* file, u32 g, u32 sel, u32* bad) {\n";
+    o << "    if (";
+    for (size_t i = 0; i < U.size(); ++i) o << (i ? " | " : "") << "ci[" << U[i] << "].status";
+    o << ") { atomicOr(bad, 1u); return; }\n";
+    // every chunk is at most 32 bits wide (the host checks): the deltas fit u32
+    auto decode = [&](bool common) {
+        o << "      u32 " << list("d", "[kRows]") << ";\n";
+        for (uint32_t j : U) {
+            if (common)
+                o << "      deltas32<" << widths[j] / 8 << ", " << widths[j] % 8 << ">(file[" << j << "], ci[" << j
+                  << "], g, d" << j << ");\n";
+            else
+                o << "      { u64 w[kRows]; deltas(file[" << j << "], ci[" << j << "], g, w);"
+                  << " for (int i = 0; i < kRows; ++i) d" << j << "[i] = static_cast<u32>(w[i]); }\n";
+        }
+        o << "      eval(";
+        for (uint32_t j : U) o << "d" << j << ", ci[" << j << "].base, ";
+        o << "sel);\n";
+    };
+    if (fast) {
+        o << "    if (";
+        for (size_t i = 0; i < U.size(); ++i)
+            o << (i ? " && " : "") << "ci[" << U[i] << "].bits == " << widths[U[i]] << "u";
+        o << ") {\n";
+        decode(true);
+        o << "    } else {\n";
+        decode(false);
+        o << "    }\n";
+    } else {
+        o << "    {\n";
+        decode(false);
+        o << "    }\n";
     }
     o << "  }\n};\n}  // namespace ebi_fx\n";
-    // up to three columns the packed values (55 KB) leave room for four CTAs per SM
-    const int min_blocks = n_cols <= 3 ? 4 : 3;
-    o << "extern \"C\" __global__ void __launch_bounds__(" << ebi_fx::kThreads << ", " << min_blocks << ") " << kKernelName
+    // 4 CTAs per SM (64 registers) hold up to three columns' deltas and three
+    // aggregations without spilling; larger passes take 80 registers
+    const int min_blocks = U.size() <= 3 && n_aggs <= 3 ? 4 : 3;
+    o << "extern \"C\" __global__ void __launch_bounds__(" << ebi_fx::kThreads << ", " << min_blocks << ") "
+      << kKernelName
       << "(ebi_fx::Params F) {\n"
-         "  extern __shared__ long long fx_slots[];\n"
          "  ebi_fx::Gen g;\n"
-         "  ebi_fx::fused_walk(F, g, fx_slots);\n"
+         "  ebi_fx::fused_walk(F, g, nullptr);\n"
          "  ebi_fx::fused_finish_exact(F, g);\n"
          "}\n";
     return o.str();
@@ -204,11 +258,6 @@ Compiled compile(const std::string& program) {
     cudaLibrary_t lib = nullptr;
     cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (e == cudaSuccess) e = cudaLibraryGetKernel(&out.kernel, lib, kKernelName);
-    // the packed values of four columns exceed the default 48 KB
-    constexpr int kSmem = ebi_fx::kWarps * ebi_fx::kCols * ebi_fx::kStride * 8;
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(out.kernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 kSmem);
     if (e != cudaSuccess) {
         out.kernel = nullptr;
         out.why = std::string("loading the compiled pass: ") + cudaGetErrorString(e);
@@ -220,7 +269,8 @@ Compiled compile(const std::string& program) {
 }  // namespace
 
 cudaKernel_t fused_jit_kernel(const std::vector<Instr>& prog, const uint32_t* first, const uint32_t* kind,
-                              uint32_t n_aggs, uint32_t n_cols, std::string* why, bool* required) {
+                              uint32_t n_aggs, uint32_t n_cols, const uint32_t* widths, std::string* why,
+                              bool* required) {
     const char* env = std::getenv("EBI_EXPR_JIT");
     *required = env && std::strcmp(env, "require") == 0;
     if (env && std::strcmp(env, "0") == 0) {
@@ -231,7 +281,7 @@ cudaKernel_t fused_jit_kernel(const std::vector<Instr>& prog, const uint32_t* fi
         *why = "no aggregation";
         return nullptr;
     }
-    const std::string program = program_source(prog, first, kind, n_aggs, n_cols);
+    const std::string program = program_source(prog, first, kind, n_aggs, n_cols, widths);
     static std::mutex mu;
     static std::map<std::string, Compiled> cache;
     std::lock_guard<std::mutex> lock(mu);

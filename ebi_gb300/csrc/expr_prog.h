@@ -25,11 +25,15 @@ struct Instr {
 // The fused exact pass (expr_fused.cuh) with the programs of a pass written
 // out as straight-line code and compiled for this device at run time:
 // aggregation a runs prog[first[a], first[a + 1]) (integer form: shifts,
-// literal numerators) and has kind kind[a].  Kernels are cached by their
-// source.  Returns null, with the reason in *why, when run-time compilation
-// is off (EBI_EXPR_JIT=0) or unavailable; *required is set when
-// EBI_EXPR_JIT=require asks that a failure be an error.
+// literal numerators) and has kind kind[a]; every chunk of the columns is at
+// most 32 bits wide, and widths[j] is the common chunk width of column slot j
+// (1..32: its chunks decode with constant plane counts).
+// The kernel takes ebi_fx::Params and no dynamic shared memory.  Kernels are
+// cached by their source.  Returns null, with the reason in *why, when
+// run-time compilation is off (EBI_EXPR_JIT=0) or unavailable; *required is
+// set when EBI_EXPR_JIT=require asks that a failure be an error.
 cudaKernel_t fused_jit_kernel(const std::vector<Instr>& prog, const uint32_t* first, const uint32_t* kind,
-                              uint32_t n_aggs, uint32_t n_cols, std::string* why, bool* required);
+                              uint32_t n_aggs, uint32_t n_cols, const uint32_t* widths, std::string* why,
+                              bool* required);
 
 }  // namespace ebi

@@ -322,13 +322,16 @@ def test_fused_pass_compiled_at_run_time_matches_interpreter(monkeypatch):
     written out (EBI_EXPR_JIT=require: a compile failure is an error); the
     same passes through the interpreter (EBI_EXPR_JIT=0) give bit-identical
     results, and both follow the oracle.  Rows not a multiple of the 256-row
-    unit, masks, stacks, shifted literals, several aggregations per pass."""
+    unit, masks, stacks, shifted literals, several aggregations per pass,
+    chunks at and off a column's common width."""
     rng = np.random.default_rng(14)
     n = 70_001
     price = np.round(rng.uniform(900, 105000, n), 2)
     disc = np.round(rng.integers(0, 11, n) / 100.0, 2)
     tax = np.round(rng.integers(0, 9, n) / 100.0, 2)
-    neg = np.round(rng.uniform(-50, 50, n), 2)
+    # chunk-dependent magnitudes: the chunks of this column differ in width, so
+    # the compiled pass decodes some at the common width and some generally
+    neg = np.round(rng.uniform(-50, 50, n) * (1 + (np.arange(n) // 16_384) * 40), 2)
     cols = [price, disc, tax, neg]
     ds_o = [O.Decoder(O.encode(c, O.BUFF, O.CHUNK_RECORD_COUNT, 16_384, 100)) for c in cols]
     ds_e = [E.Decoder(E.encode(c, "buff", ("record_count", 16_384), 100)) for c in cols]
