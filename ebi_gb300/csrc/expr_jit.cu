@@ -263,7 +263,7 @@ Compiled compile(const std::string& program) {
         out.why = std::string("loading the compiled pass: ") + cudaGetErrorString(e);
         cudaGetLastError();
     }
-    return out;  // the library stays loaded for the process: its kernel is cached
+    return out;
 }
 
 }  // namespace
@@ -282,11 +282,21 @@ cudaKernel_t fused_jit_kernel(const std::vector<Instr>& prog, const uint32_t* fi
         return nullptr;
     }
     const std::string program = program_source(prog, first, kind, n_aggs, n_cols, widths);
+    // Compiled passes stay loaded for the process (a launch of one may still be
+    // in flight on some stream), so the cache is bounded: past kMaxCompiled
+    // distinct programs, new ones run on the interpreter.
+    constexpr size_t kMaxCompiled = 256;
     static std::mutex mu;
     static std::map<std::string, Compiled> cache;
     std::lock_guard<std::mutex> lock(mu);
     auto it = cache.find(program);
-    if (it == cache.end()) it = cache.emplace(program, compile(program)).first;
+    if (it == cache.end()) {
+        if (cache.size() >= kMaxCompiled) {
+            *why = "compiled-pass cache full";
+            return nullptr;
+        }
+        it = cache.emplace(program, compile(program)).first;
+    }
     if (!it->second.kernel) *why = it->second.why;
     return it->second.kernel;
 }
