@@ -530,10 +530,13 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         c->scan_grid = static_cast<uint32_t>(std::max(sms, 1)) * per_sm;
         c->sms = static_cast<uint32_t>(std::max(sms, 1));
         uint64_t rows_of[65] = {};
+        c->buff_all_readable = true;
         for (const BuffChunkInfo& b : binfo)
             if (!b.status) {
                 rows_of[b.bits] += b.n;
                 c->buff_max_bits = std::max(c->buff_max_bits, b.bits);
+            } else {
+                c->buff_all_readable = false;
             }
         c->stream_bits = static_cast<uint32_t>(std::max_element(rows_of + 1, rows_of + 33) - rows_of);
     } else {

@@ -44,6 +44,7 @@ struct ebi_column {
     uint32_t units_per_chunk = 0;      // when uniform (buff_uniform_units), else 0
     uint32_t stream_bits = 0;    // most common width of the readable chunks
     uint32_t buff_max_bits = 0;  // widest readable chunk
+    bool buff_all_readable = false;  // no chunk header carries an error
     uint32_t sms = 0;            // SMs of the column's device
     bool fused_pending = false;  // the last query's kernel already folded into d_res
     bool totals_pending = false; // the last query's kernel left exact totals in pending_tot for the host

@@ -1152,6 +1152,49 @@ int run_pass(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<u
     return done(st);
 }
 
+// Bare Index aggregations that may join the fused pass of the others.  The
+// column's own query (exact integer partials for an exact BUFF column) and the
+// fused exact pass agree bit for bit when every partial sum in either is
+// exactly representable: the column's sum of |value| bounds every partial sum
+// of a subset, and buff_exact holds it below 2^52; min and max are exact in
+// both.  Folded only when the whole set then fits one fused pass compiled at
+// run time (at most kFuseCols BUFF columns, every one readable, exact, at
+// most 32 bits wide and chunked like the first column, at most kMaxAggs
+// aggregations), so the fold never trades a scan for a slower pass.
+std::vector<bool> fold_index_aggregations(ebi_column* const* cols, const ebi_aggregation* aggs, uint32_t n_aggs,
+                                          const std::vector<std::vector<Node>>& trees, const std::vector<int>& roots) {
+    std::vector<bool> fold(n_aggs, false);
+    const ebi_column* r = cols[0];
+    auto eligible = [&](const ebi_column* c) {
+        if (c->scheme != EBI_BUFF || c->precision >= 0 || !c->d_buff || !c->buff_exact || !c->buff_all_readable ||
+            c->buff_max_bits > 32 || c->n_chunks != r->n_chunks || c->n_records != r->n_records || c->n_chunks == 0)
+            return false;
+        for (uint64_t k = 0; k < c->n_chunks; ++k)
+            if (c->chunks[k].n_rows != r->chunks[k].n_rows || c->chunks[k].row_off != r->chunks[k].row_off) return false;
+        return true;
+    };
+    std::vector<uint32_t> used;  // columns of the pass
+    uint32_t n_pass = 0, n_index = 0;
+    for (uint32_t a = 0; a < n_aggs; ++a) {
+        const bool index = trees[a][roots[a]].kind == EBI_EXPR_INDEX;
+        if (index && aggs[a].kind == EBI_AGGR_NONE) continue;  // stays an error of its own
+        if (!index && aggs[a].kind == EBI_AGGR_NONE) return fold;  // an array result: no fused pass
+        for (const Node& n : trees[a])
+            if (n.kind == EBI_EXPR_INDEX && std::find(used.begin(), used.end(), n.index) == used.end())
+                used.push_back(n.index);
+        ++n_pass;
+        n_index += index ? 1 : 0;
+    }
+    if (n_index == 0 || n_index == n_pass || n_pass > static_cast<uint32_t>(kMaxAggs) ||
+        used.size() > static_cast<size_t>(kFuseCols) || !fused_jit_enabled())
+        return fold;
+    for (uint32_t j : used)
+        if (!eligible(cols[j])) return fold;
+    for (uint32_t a = 0; a < n_aggs; ++a)
+        fold[a] = trees[a][roots[a]].kind == EBI_EXPR_INDEX && aggs[a].kind != EBI_AGGR_NONE;
+    return fold;
+}
+
 }  // namespace
 }  // namespace ebi
 
@@ -1171,10 +1214,14 @@ extern "C" int ebi_aggregate(ebi_column* const* cols, uint32_t n_cols, ebi_aggre
         if (roots[a] < 0) return fail(EBI_E_INVALID, "malformed expression (or an index past the columns)");
         aggs[a].n_array = 0;
     }
-    // bare Index expressions first, in order (Aggregation::compute_multiple)
+    // bare Index expressions first, in order (Aggregation::compute_multiple),
+    // each through its column's own query -- unless fold_index_aggregations
+    // shows that the pass compiled for the other aggregations gives the same
+    // results while reading those columns anyway
+    const std::vector<bool> folded = fold_index_aggregations(cols, aggs, n_aggs, trees, roots);
     std::vector<uint32_t> rest;
     for (uint32_t a = 0; a < n_aggs; ++a) {
-        if (trees[a][roots[a]].kind != EBI_EXPR_INDEX) { rest.push_back(a); continue; }
+        if (trees[a][roots[a]].kind != EBI_EXPR_INDEX || folded[a]) { rest.push_back(a); continue; }
         if (int st = aggregate_index(cols[trees[a][roots[a]].index], aggs[a], d_mask, stream)) return st;
     }
     if (rest.empty()) return EBI_OK;

@@ -268,6 +268,11 @@ Compiled compile(const std::string& program) {
 
 }  // namespace
 
+bool fused_jit_enabled() {
+    const char* env = std::getenv("EBI_EXPR_JIT");
+    return !(env && std::strcmp(env, "0") == 0) && nvrtc().ok;
+}
+
 cudaKernel_t fused_jit_kernel(const std::vector<Instr>& prog, const uint32_t* first, const uint32_t* kind,
                               uint32_t n_aggs, uint32_t n_cols, const uint32_t* widths, std::string* why,
                               bool* required) {

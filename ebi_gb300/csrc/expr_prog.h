@@ -32,6 +32,10 @@ struct Instr {
 // cached by their source.  Returns null, with the reason in *why, when
 // run-time compilation is off (EBI_EXPR_JIT=0) or unavailable; *required is
 // set when EBI_EXPR_JIT=require asks that a failure be an error.
+// Whether exact passes may be compiled at run time here (NVRTC found, not
+// switched off); a later compile can still fail.
+bool fused_jit_enabled();
+
 cudaKernel_t fused_jit_kernel(const std::vector<Instr>& prog, const uint32_t* first, const uint32_t* kind,
                               uint32_t n_aggs, uint32_t n_cols, const uint32_t* widths, std::string* why,
                               bool* required);
