@@ -41,8 +41,9 @@ __device__ __noinline__ void item_rle(const QueryParams& q, const BatchItem& it)
     rle_chunk(q, it.unit, it.unit, VAL_SCAN, nullptr);
 }
 __device__ __noinline__ void item_gorilla(const QueryParams& q, const BatchItem& it) {
-    const uint32_t warp = threadIdx.x >> 5;
-    if (warp < it.count) gorilla_chunk_l1(q, it.unit + warp, it.unit + warp, VAL_SCAN, nullptr);
+    const uint32_t warp = threadIdx.x >> 5, chunks = it.count & 0xffu;
+    const uint32_t nq = it.count >> 8 ? it.count >> 8 : 1u;  // queries it.query .. + nq: one column
+    if (warp < chunks) gorilla_chunk_l1<kGorillaShare>(&q, nq, it.unit + warp, it.unit + warp, VAL_SCAN, nullptr);
 }
 __device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& it) {
     xor_chunk<CODEC_CHIMP>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
@@ -121,7 +122,7 @@ void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t quer
 
 double item_cost(uint32_t kind, uint32_t count) {
     switch (kind) {
-    case ITEM_GORILLA: return 40.0 * count;
+    case ITEM_GORILLA: return 40.0 * (count & 0xffu);  // the chunks; queries sharing them cost little more
     case ITEM_ELF: return 35.0;
     case ITEM_ELF_CHIMP: return 35.0;
     case ITEM_CHIMP128: return 30.0;

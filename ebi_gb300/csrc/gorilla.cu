@@ -43,11 +43,12 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) gorilla_kernel(QueryParams 
             return;
         }
         const uint64_t bit0 = (cd.byte_off & 15) * 8;
-        walk(q, cd, acc, li, mode, chunk_offsets, [stage, bit0](uint64_t p) { return peek64_le_smem(stage, bit0 + p); });
+        walk<1>(&q, 1, 1u, cd, c, li, mode, chunk_offsets,
+                [stage, bit0](uint64_t p) { return peek64_le_smem(stage, bit0 + p); });
     } else {
         const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
         const uint64_t bit0 = cd.byte_off * 8;
-        walk(q, cd, acc, li, mode, chunk_offsets, [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); });
+        walk<1>(&q, 1, 1u, cd, c, li, mode, chunk_offsets, [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); });
     }
 }
 

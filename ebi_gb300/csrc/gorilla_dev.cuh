@@ -51,21 +51,28 @@ __host__ __device__ __forceinline__ uint64_t stage_span(uint64_t byte_off, uint6
 }
 
 // Decodes chunk cd and runs the query over its values (one warp).
-template <typename Peek>
-__device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, ChunkAcc* acc, uint32_t li, int mode,
-                                     const unsigned long long* chunk_offsets, Peek peek) {
+// The walk of one chunk for up to MaxQ queries over the same column at once
+// (qs[0 .. nq), those with bit j of okm set): the stream is parsed once and
+// each emitted run of values goes through every query's bitmask, predicate
+// and aggregates.  Materialize and count passes take one query.
+template <int MaxQ, typename Peek>
+__device__ __forceinline__ void walk(const QueryParams* qs, uint32_t nq, uint32_t okm, const ChunkDesc& cd, uint32_t c,
+                                     uint32_t li, int mode, const unsigned long long* chunk_offsets, Peek peek) {
     const int lane = threadIdx.x & 31;
-    const bool has_mask = q.in_mask != nullptr;
     const uint64_t B = cd.byte_len * 8;
-    const bool pred_on = q.pred_on != 0;
-    const bool store = mode == VAL_SCAN && pred_on && q.out_mask != nullptr;
-    const KeyPred kp = key_pred(q.pred);
-    ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
+    KeyPred kp[MaxQ];
+    ValAgg agg[MaxQ];
+#pragma unroll
+    for (int j = 0; j < MaxQ; ++j) {
+        const QueryParams& q = qs[j < static_cast<int>(nq) ? j : 0];
+        kp[j] = key_pred(q.pred);
+        agg[j] = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
+    }
     unsigned long long out_pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull;
     uint64_t idx = 0;  // chunk row of the next value
 
     // Lanes [0, k) hold the values (bits) of rows idx + lane.  Applies the end
-    // marker and the query; returns true when the stream ended here.
+    // marker and the queries; returns true when the stream ended here.
     auto emit = [&](uint32_t k, uint64_t vbits) -> bool {
         const uint32_t nanm = __ballot_sync(kFull, static_cast<uint32_t>(lane) < k && vbits == kNanBits);
         bool ended = false;
@@ -74,23 +81,29 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
             ended = true;
         }
         const uint64_t g = cd.row_off + idx + lane;
-        const bool in = static_cast<uint32_t>(lane) < k && (!has_mask || mask_row(q.in_mask, q.n_records, g));
-        const bool pass = in && (!pred_on || kp.pass(vbits));
-        if (mode == VAL_MATERIALIZE) {
-            const uint32_t bal = __ballot_sync(kFull, pass);
-            if (pass) {
-                const unsigned long long pos = out_pos + __popc(bal & ((1u << lane) - 1u));
-                if (pos < q.out_cap) q.out_vals[pos] = __longlong_as_double(static_cast<long long>(vbits));
-            }
-            out_pos += __popc(bal);
-        } else {
-            if (store) {
-                const uint32_t word = __ballot_sync(kFull, pass && g < q.n_records);
-                if (lane == 0 && word) store_mask_word(q.out_mask, cd.row_off + idx, word, true);
-            }
-            if (pass) {
-                if (mode == VAL_COUNT) ++agg.cnt;
-                else val_agg_add1(agg, vbits);
+#pragma unroll
+        for (int j = 0; j < MaxQ; ++j) {
+            if (j >= static_cast<int>(nq) || !((okm >> j) & 1u)) continue;  // the same for every lane
+            const QueryParams& q = qs[j];
+            const bool pred_on = q.pred_on != 0;
+            const bool in = static_cast<uint32_t>(lane) < k && (!q.in_mask || mask_row(q.in_mask, q.n_records, g));
+            const bool pass = in && (!pred_on || kp[j].pass(vbits));
+            if (mode == VAL_MATERIALIZE) {
+                const uint32_t bal = __ballot_sync(kFull, pass);
+                if (pass) {
+                    const unsigned long long pos = out_pos + __popc(bal & ((1u << lane) - 1u));
+                    if (pos < q.out_cap) q.out_vals[pos] = __longlong_as_double(static_cast<long long>(vbits));
+                }
+                out_pos += __popc(bal);
+            } else {
+                if (mode == VAL_SCAN && pred_on && q.out_mask != nullptr) {
+                    const uint32_t word = __ballot_sync(kFull, pass && g < q.n_records);
+                    if (lane == 0 && word) store_mask_word(q.out_mask, cd.row_off + idx, word, true);
+                }
+                if (pass) {
+                    if (mode == VAL_COUNT) ++agg[j].cnt;
+                    else val_agg_add1(agg[j], vbits);
+                }
             }
         }
         idx += k;
@@ -163,16 +176,21 @@ __device__ __forceinline__ void walk(const QueryParams& q, const ChunkDesc& cd, 
     }
     if (status) {
         if (lane == 0) {
-            set_status(acc, status);
-            if (mode == VAL_COUNT) q.tile_counts[li] = 0;
+            for (uint32_t j = 0; j < nq; ++j)
+                if ((okm >> j) & 1u) set_status(qs[j].acc + c, status);
+            if (mode == VAL_COUNT) qs[0].tile_counts[li] = 0;
         }
         return;
     }
     if (mode == VAL_MATERIALIZE) return;
-    const ValAgg a = val_agg_warp(agg);
-    if (lane != 0) return;
-    if (mode == VAL_COUNT) q.tile_counts[li] = a.cnt;
-    else val_agg_store(acc, a);
+#pragma unroll
+    for (int j = 0; j < MaxQ; ++j) {
+        if (j >= static_cast<int>(nq) || !((okm >> j) & 1u)) continue;  // the same for every lane
+        const ValAgg a = val_agg_warp(agg[j]);
+        if (lane != 0) continue;
+        if (mode == VAL_COUNT) qs[j].tile_counts[li] = a.cnt;
+        else val_agg_store(qs[j].acc + c, a);
+    }
 }
 
 // Chunk selection and geometry checks of one Gorilla chunk (warp-uniform
@@ -211,14 +229,20 @@ __device__ __forceinline__ bool gorilla_begin(const QueryParams& q, uint32_t li,
 
 }
 
-// One Gorilla chunk by one warp, reading the stream through L1 (no staging).
-__device__ __forceinline__ void gorilla_chunk_l1(const QueryParams& q, uint32_t li, uint32_t c, int mode,
+// One Gorilla chunk by one warp for nq <= MaxQ queries over the same column
+// (qs[0 .. nq)), reading the stream through L1 (no staging).
+template <int MaxQ>
+__device__ __forceinline__ void gorilla_chunk_l1(const QueryParams* qs, uint32_t nq, uint32_t li, uint32_t c, int mode,
                                                  const unsigned long long* chunk_offsets) {
-    if (!gorilla_begin(q, li, c, mode, chunk_offsets)) return;
-    const ChunkDesc cd = q.chunks[c];
-    const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
+    uint32_t okm = 0;
+    for (uint32_t j = 0; j < nq; ++j)  // the same for every lane
+        if (gorilla_begin(qs[j], li, c, mode, chunk_offsets)) okm |= 1u << j;
+    if (!okm) return;
+    const ChunkDesc cd = qs[0].chunks[c];
+    const uint32_t* fw = reinterpret_cast<const uint32_t*>(qs[0].file);
     const uint64_t bit0 = cd.byte_off * 8;
-    walk(q, cd, q.acc + c, li, mode, chunk_offsets, [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); });
+    walk<MaxQ>(qs, nq, okm, cd, c, li, mode, chunk_offsets,
+               [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); });
 }
 
 }  // namespace

@@ -123,8 +123,10 @@ struct BatchItem {
     uint32_t query;  // index into the batch's QueryParams
     uint32_t kind;   // BatchItemKind
     uint32_t unit;
-    uint32_t count;
+    uint32_t count;  // Chimp family: queries sharing the chunk; Gorilla: chunks | (queries sharing them) << 8
 };
+// Queries over one Gorilla column that one batch item serves at once.
+constexpr uint32_t kGorillaShare = 3;
 // Appends the items of one query over a column (scheme, chunks, BUFF tiles).
 void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t query, std::vector<BatchItem>& out);
 // Relative cost of one item of each kind (device time of an 8,192-row unit

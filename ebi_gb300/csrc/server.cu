@@ -98,7 +98,8 @@ void footprint(const ebi_server* s, const ebi_request& r, uint64_t* chunks, uint
 cudaError_t launch_slot(ebi_server* s, Slot& sl) {
     // The batch's queries in column order, so that the queries on one column
     // are consecutive: a Chimp-family chunk is then decoded once for all of
-    // them (items naming up to 32 consecutive queries).
+    // them (items naming up to 32 consecutive queries), a group of Gorilla
+    // chunks once for up to kGorillaShare.
     struct Ent { uint32_t col, req, k; };
     std::vector<Ent> ents;
     std::vector<uint32_t> base(sl.reqs.size() + 1, 0);
@@ -141,6 +142,14 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
                 const size_t first = items.size();
                 column_items(c->scheme, c->n_chunks, tiles, q0, items);
                 for (size_t i = first; i < items.size(); ++i) items[i].count = std::min<uint32_t>(32, h - q0);
+            }
+        } else if (c->scheme == EBI_GORILLA) {
+            // a group of chunks is parsed once for up to kGorillaShare queries
+            for (uint32_t q0 = g; q0 < h; q0 += kGorillaShare) {
+                const size_t first = items.size();
+                column_items(c->scheme, c->n_chunks, tiles, q0, items);
+                const uint32_t share = std::min<uint32_t>(kGorillaShare, h - q0);
+                for (size_t i = first; i < items.size(); ++i) items[i].count |= share << 8;
             }
         } else {
             for (uint32_t qi = g; qi < h; ++qi) column_items(c->scheme, c->n_chunks, tiles, qi, items);
