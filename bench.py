@@ -76,11 +76,27 @@ def replica_throughput(local_s: float, local_rows: int, dist=None, device=None):
     return t, 8.0 * rows / t / 1e9
 
 
+def workload_generators():
+    """The seeded value generators (ebi_gb300/workloads.py), loaded from their file alone.
+
+    Loading the file by path keeps the package (and so libebi_gpu.so) out of the
+    reference arm's process: that arm runs only ebi's CPU path."""
+    import importlib.util
+
+    mod = sys.modules.get("_ebi_workloads")
+    if mod is None:
+        spec = importlib.util.spec_from_file_location("_ebi_workloads", ROOT / "ebi_gb300" / "workloads.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        sys.modules["_ebi_workloads"] = mod
+    return mod
+
+
 class Workload:
     """One measured shape: its column (EBI1 bytes) and the range queries a step cycles through."""
 
     def __init__(self, name, rows):
-        from ebi_gb300 import workloads as W
+        W = workload_generators()
 
         self.name = name
         self.rows = rows
@@ -123,15 +139,22 @@ class Workload:
         else:
             raise SystemExit(f"unknown workload {name}")
 
-    def build(self):
-        import ebi_gb300 as E
-
+    def build(self, encoder="engine"):
+        """The column's EBI1 bytes, written by the engine's host encoder or (encoder="oracle") by the
+        oracle's; the two write identical bytes (tests/test_cpu_abi.py)."""
         t = time.perf_counter()
         v = self.values()
         if self.ranges is None:
             lo, hi = np.quantile(v, [0.35, 0.65])
             self.ranges = [(f"{lo:.1f}<=x<={hi:.1f}", float(lo), float(hi))]
-        data = E.encode(v, self.codec, ("record_count", self.chunk), self.scale)
+        if encoder == "oracle":
+            from oracle import oracle as O
+
+            data = O.encode(v, self.codec, O.CHUNK_RECORD_COUNT, self.chunk, self.scale)
+        else:
+            import ebi_gb300 as E
+
+            data = E.encode(v, self.codec, ("record_count", self.chunk), self.scale)
         log(f"workload {self.name}: {self.rows} rows, {len(data)} B EBI1 ({time.perf_counter() - t:.1f} s to generate)")
         return data
 
@@ -228,33 +251,62 @@ def ncu_traffic(workload="buff"):
     return None
 
 
-def cpu_baseline(data: bytes, threads: int, wl, budget_s: float = 15.0):
-    """The oracle port timed on the host cores over a bounded sample of the same queries."""
+def time_cpu_queries(d, preds, n, two_call=False, aggregates=("sum",)):
+    """Seconds per query of n queries on the oracle Decoder d, cycling preds.
+
+    two_call: the reference's own shape of a filtered aggregate, Decoder::filter followed by
+    Decoder::sum / min / max(Some(&bitmask)), each call reading every chunk again
+    (api/decoder.rs:242-281, 323-439); otherwise one fused pass per query."""
+    ts = []
+    for i in range(n):
+        p = preds[i % len(preds)]
+        t = time.perf_counter()
+        if two_call:
+            m = d.filter(p)
+            for a in aggregates:
+                getattr(d, a)(m)
+        else:
+            d.filter_agg(p)
+        ts.append(time.perf_counter() - t)
+    return ts
+
+
+def cpu_figures(data: bytes, wl, threads: int, n_all: int = 9, n_one: int = 3):
+    """The oracle port on the host cores, over the full column and the workload's own queries.
+
+    Three figures, as decoded GB/s (8 B x rows / median seconds per query):
+      value      fused filter+aggregate, chunk-parallel on `threads` host threads;
+      threads_1  the same on one thread, the reference's execution model (single-threaded Decoder);
+      two_call   filter, then the aggregates over its bitmask, each a separate chunk loop, on `threads`."""
     from oracle import oracle as O
 
-    d = O.Decoder(data, threads=threads)
     preds = wl.oracle_preds()
-    rows = 0
-    t0 = time.perf_counter()
-    i = 0
-    while True:
-        d.filter_agg(preds[i % len(preds)])
-        rows += d.n_records
-        i += 1
-        if time.perf_counter() - t0 > budget_s or i >= 9:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": round(8.0 * rows / dt / 1e9, 3), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{i} fused filter+aggregate queries ({', '.join(k for k, _, _ in wl.ranges)} cycled) over the "
-                      f"full {d.n_records}-row column, chunk-parallel C restatement of ebi's Decoder, {threads} threads"}
+    dall = O.Decoder(data, threads=threads)
+    n = dall.n_records
+    dall.filter_agg(preds[0])  # first touch of the file's pages
+    fused = time_cpu_queries(dall, preds, n_all)
+    two = time_cpu_queries(dall, preds, max(n_one, len(preds)), two_call=True, aggregates=wl.aggregates)
+    one = time_cpu_queries(O.Decoder(data, threads=1), preds, n_one)
+    gbs = lambda ts: round(8.0 * n / statistics.median(ts) / 1e9, 3)
+    qs = ", ".join(k for k, _, _ in wl.ranges)
+    return {"value": gbs(fused), "unit": UNIT, "cores": threads, "kind": "port",
+            "mean_value": round(8.0 * n * len(fused) / sum(fused) / 1e9, 3),
+            "threads_1": {"value": gbs(one), "cores": 1, "queries": len(one)},
+            "two_call": {"value": gbs(two), "cores": threads, "queries": len(two),
+                         "calls": f"filter, then {'/'.join(wl.aggregates)}(Some(&bitmask))"},
+            "sample": f"median of {len(fused)} fused filter+aggregate queries ({qs} cycled) over the full {n}-row "
+                      f"column, chunk-parallel C restatement of ebi's Decoder on {threads} host threads; threads_1: "
+                      f"{len(one)} queries on one thread; two_call: {len(two)} queries as the reference's two calls"}
 
 
 def run_reference(args):
     """Reference arm: ebi's CPU path (the C restatement; the Rust crate has no toolchain here).
 
-    Each step is one fused filter+sum query, run chunk-parallel on every host
-    core, over the first 8,388,608 rows (128 chunks) of the same column: a
-    bounded sample so that the whole run ends within minutes."""
+    The column is the configuration's full column, written by the oracle's encoder (the same
+    bytes the engine's encoder writes), and nothing of the engine is loaded in this process.
+    Each step is one fused filter+aggregate query run chunk-parallel on every host thread;
+    value uses the median step time.  The line also carries the one-thread figure (the
+    reference's own execution model) and the reference's two-call filter-then-aggregate time."""
     rank, _, world = dist_env()
     if rank != 0:
         return
@@ -262,30 +314,32 @@ def run_reference(args):
     from oracle import oracle as O
 
     wl = Workload(args.workload, args.rows or DEFAULT_ROWS[args.workload])
-    full_rows = wl.rows
-    wl.rows = max(wl.chunk, min(wl.rows, N_ROWS // 8))  # bounded sample: the leading rows of the same series
-    data = wl.build()
-    sample_rows = wl.rows
+    data = wl.build(encoder="oracle")
     d = O.Decoder(data, threads=threads)
     preds = wl.oracle_preds()
     for i in range(args.warmup):
         d.filter_agg(preds[i % len(preds)])
-    t0 = time.perf_counter()
-    for i in range(args.steps):
-        d.filter_agg(preds[i % len(preds)])
-    dt = time.perf_counter() - t0
-    value = 8.0 * sample_rows * args.steps / dt / 1e9
-    sample = (f"per step one fused filter+aggregate ({', '.join(k for k, _, _ in wl.ranges)}) over the first "
-              f"{sample_rows} of the workload's {full_rows} rows ({d.n_chunks} chunks), chunk-parallel C "
-              f"restatement of ebi's CPU path on {threads} host threads (ebi is Rust; no Rust toolchain exists "
-              f"on this image)")
+    ts = time_cpu_queries(d, preds, args.steps)
+    med = statistics.median(ts)
+    value = 8.0 * wl.rows / med / 1e9
+    one = time_cpu_queries(O.Decoder(data, threads=1), preds, 3)
+    two = time_cpu_queries(d, preds, max(3, len(preds)), two_call=True, aggregates=wl.aggregates)
+    gbs = lambda t: round(8.0 * wl.rows / statistics.median(t) / 1e9, 3)
+    sample = (f"per step one fused filter+aggregate ({', '.join(k for k, _, _ in wl.ranges)} cycled) over the "
+              f"full {wl.rows}-row column ({d.n_chunks} chunks), chunk-parallel C restatement of ebi's CPU path "
+              f"on {threads} host threads (ebi is Rust; no Rust toolchain exists on this image); median step")
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 4),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * med, 4),
+            "mean_ms_per_step": round(1e3 * sum(ts) / len(ts), 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 -> f64",
             "data": "synthetic (seeded numpy, the configuration's shape)",
-            "config": {"workload": wl.describe, "rows": full_rows, "chunk_rows": wl.chunk},
+            "config": {"workload": wl.describe, "rows": wl.rows, "chunk_rows": wl.chunk,
+                       "column_bytes": len(data), "encoder": "oracle (byte-identical to the engine's)"},
             "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample,
+                             "threads_1": {"value": gbs(one), "cores": 1, "queries": len(one)},
+                             "two_call": {"value": gbs(two), "cores": threads, "queries": len(two),
+                                          "calls": f"filter, then {'/'.join(wl.aggregates)}(Some(&bitmask))"}},
             "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -736,11 +790,15 @@ def main():
     sampler.stop()
     clocks = sampler.summary(t0, t1)
 
-    dev_s, value = replica_throughput(sum(total) / 1e3, n * args.steps, dist, dev)
+    # value: the median step (BASELINE's "median of >= 20 reps"); the mean is reported beside it
+    med_step_s = statistics.median(total) / 1e3
+    dev_s, value = replica_throughput(med_step_s * args.steps, n * args.steps, dist, dev)
+    _, mean_value = replica_throughput(sum(total) / 1e3, n * args.steps, dist, dev)
 
     # roofline of the dominant kernel (the fused BUFF filter+sum kernel)
     peak, peak_kind = measured_peak()
     scan_avg_s = statistics.mean(scan) / 1e3
+    scan_med_s = statistics.median(scan) / 1e3
     achieved = alg_bytes / scan_avg_s / 1e9
     traffic = ncu_traffic(wl.name)
 
@@ -778,12 +836,13 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(data, os.cpu_count() or 1, wl)
+        cpu = cpu_figures(data, wl, os.cpu_count() or 1)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1e3 * dev_s / args.steps, 5),
+            "mean_value": round(mean_value, 3), "value_statistic": "median step (mean_value: mean step)",
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64 -> f64",
             "data": "synthetic (seeded numpy, the configuration's shape)",
             "config": {"workload": wl.describe, "queries": [k for k, _, _ in wl.ranges],
@@ -794,6 +853,8 @@ def main():
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "kernel": KERNELS[wl.name],
                          "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": round(1e3 * scan_avg_s, 5),
+                         "median_launch_ms": round(1e3 * scan_med_s, 5),
+                         "frac_at_median_launch": round(alg_bytes / scan_med_s / 1e9 / peak, 4),
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s"},
             "e2e": {"value": round(e2e_val, 3) if e2e_val else None, "unit": UNIT, "h2d_bytes_per_step": len(data),

@@ -2,7 +2,7 @@
 // with FileWriter / ChunkWriter framing (encoder.rs:190-529) and the chunk
 // encoders of the codecs this engine decodes:
 //   Uncompressed (compressor/uncompressed.rs), RLE (compressor/run_length.rs:49-117),
-//   Gorilla (compressor/gorilla.rs:248-380), Chimp (compressor/chimp.rs:51-146),
+//   Gorilla (compressor/gorilla.rs:118-190), Chimp (compressor/chimp.rs:51-146),
 //   Chimp128 (compressor/chimp_n.rs:126-258), BUFF (compressor/buff.rs:127-307),
 //   Elf and ElfOnChimp (compressor/elf.rs: ElfEncoderWrapper over ElfXorEncoder
 //   or ChimpEncoder).

@@ -43,7 +43,7 @@ __device__ inline BuffVal buff_value(const QueryParams& q, uint32_t c, const Chu
         v.sum_fixed = static_cast<long long>(a.isum + static_cast<unsigned long long>(ci.base) * a.count);
         v.sum_exact = v.sum_fixed < kExact && v.sum_fixed > -kExact && ci.frac <= 1022;
         v.max_fixed = static_cast<long long>(static_cast<unsigned long long>(ci.base) + a.dmax);
-        // min_without_bitmask returns base / scale (buff/min_max.rs:435-460)
+        // min_without_bitmask returns base / scale (buff/min_max.rs:316-341)
         v.min_fixed = has_mask ? static_cast<long long>(static_cast<unsigned long long>(ci.base) + a.dmin) : ci.base;
     }
     return v;

@@ -1,6 +1,6 @@
 // gorilla_dev.cuh -- Gorilla chunks decoded and queried by one warp per chunk.
 //
-// Format (decoder/chunk_reader/gorilla.rs:215-296; encoder compressor/gorilla.rs:118-190):
+// Format (decoder/chunk_reader/gorilla.rs:90-157; encoder compressor/gorilla.rs:118-190):
 // 64 raw bits, then per value '0' (repeat), '10' + payload in the inherited
 // window (significant bits = 64 - lead - trail), or '11' + 5-bit leading +
 // 6-bit (significant - 1) + payload.  The stream ends at the first value

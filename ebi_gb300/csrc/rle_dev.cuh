@@ -1,6 +1,6 @@
 // rle_dev.cuh -- RLE chunks (compressor/run_length.rs:49-117): a u64 field count,
 // then packed 9-byte fields (u8 run length, f64 little-endian value).  The
-// reader expands every run in order (decoder/chunk_reader/run_length.rs:314-337);
+// reader expands every run in order (decoder/chunk_reader/run_length.rs:68-91);
 // row i of the chunk is global row logical_offset + i, and the default
 // operators (decoder/query.rs:14-154) run over the expanded rows.
 //

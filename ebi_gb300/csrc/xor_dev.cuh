@@ -3,12 +3,12 @@
 // per chunk).
 //
 // Formats (big-endian bit order, MSB of the first byte first):
-//   Gorilla   decoder/chunk_reader/gorilla.rs:215-296: 64 raw bits, then per
+//   Gorilla   decoder/chunk_reader/gorilla.rs:90-157: 64 raw bits, then per
 //             value '0' (repeat), '10' + payload in the inherited window, or
 //             '11' + 5-bit leading + 6-bit (significant - 1) + payload.
-//   Chimp     decoder/chunk_reader/chimp.rs:288-354: 2-bit flags; '01' carries
+//   Chimp     decoder/chunk_reader/chimp.rs:58-124: 2-bit flags; '01' carries
 //             a 3-bit leading code (LEADING_REPR) and 6 significant bits.
-//   Chimp128  decoder/chunk_reader/chimp_n.rs:544-646: as Chimp, but '00' and
+//   Chimp128  decoder/chunk_reader/chimp_n.rs:160-285: as Chimp, but '00' and
 //             '01' name one of the last 128 values by a 7-bit ring index.
 //   Elf       decoder/chunk_reader/elf.rs: per value a wrapper prefix ('0'
 //             restore, '10' as is, '11' + 4-bit beta* and restore) and an

@@ -89,10 +89,10 @@ int ebi_column_open_file(const char* path, void* stream, ebi_column** out);
 /* Drops the device copy (Decoder going out of scope). */
 int ebi_column_close(ebi_column* col);
 
-/* NativeFileFooter::{number_of_records, number_of_chunks} (format/native.rs:482-488) */
+/* NativeFileFooter::{number_of_records, number_of_chunks} (format/native.rs:117-124) */
 uint64_t ebi_column_num_records(const ebi_column* col);
 uint64_t ebi_column_num_chunks(const ebi_column* col);
-/* NativeFileConfig::compression_scheme (format/native.rs:410-414) */
+/* NativeFileConfig::compression_scheme (format/native.rs:45-49) */
 int ebi_column_scheme(const ebi_column* col);
 /* GeneralChunkHandle::{physical_offset, chunk_size, logical_offset,
  * number_of_records} (decoder.rs:283-328) */

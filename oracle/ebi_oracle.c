@@ -116,7 +116,7 @@ int ora_read_bits(const uint8_t* buf, uint64_t len, uint64_t* bitpos, int n, uin
 
 /* ------------------------------------------------------------------------ */
 /* Gorilla encoder: modified_tsz::GorillaFloatEncoder                        */
-/* (compressor/gorilla.rs:248-380, close = encode(NaN) + one 0 bit :202-205) */
+/* (compressor/gorilla.rs:118-190, close = encode(NaN) + one 0 bit :27-30) */
 /* ------------------------------------------------------------------------ */
 static void gorilla_encode(bitw* w, const double* v, uint64_t n) {
     uint64_t value = 0;
@@ -161,7 +161,7 @@ static const uint8_t LEAD_REPR[64] = {
 static const uint8_t LEAD_ROUND[64] = {
     0,0,0,0,0,0,0,0,8,8,8,8,12,12,12,12,16,16,18,18,20,20,22,22,24,24,24,24,24,24,24,24,
     24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24,24};
-static const uint32_t LEAD_DECODE[8] = {0, 8, 12, 16, 18, 20, 22, 24}; /* decoder/chunk_reader/chimp.rs:268 */
+static const uint32_t LEAD_DECODE[8] = {0, 8, 12, 16, 18, 20, 22, 24}; /* decoder/chunk_reader/chimp.rs:38 */
 
 static void chimp_encode(bitw* w, const double* v, uint64_t n) {
     uint32_t stored_lead = 0xffffffffu;
@@ -767,7 +767,7 @@ static int dv_push(dvec* d, double x) {
 #define PUSH(x) do { if (!dv_push(out, (x))) return ORA_E_OOM; } while (0)
 #define RB(n, dst) do { if (!br_bits(&r, (n), (dst))) return ORA_E_UNEXPECTED_END; } while (0)
 
-/* GorillaDecoder::next (decoder/chunk_reader/gorilla.rs:215-296) */
+/* GorillaDecoder::next (decoder/chunk_reader/gorilla.rs:90-157) */
 static int gorilla_decode(const uint8_t* c, uint64_t len, dvec* out) {
     bitr r = {c, len, 0};
     uint64_t value = 0, t;
@@ -791,7 +791,7 @@ static int gorilla_decode(const uint8_t* c, uint64_t len, dvec* out) {
     }
 }
 
-/* ChimpDecoder::read_value / next_value (decoder/chunk_reader/chimp.rs:288-354) */
+/* ChimpDecoder::read_value / next_value (decoder/chunk_reader/chimp.rs:58-124) */
 static int chimp_decode(const uint8_t* c, uint64_t len, dvec* out) {
     bitr r = {c, len, 0};
     uint32_t stored_lead = 0xffffffffu, stored_trail = 0;
@@ -825,7 +825,7 @@ static int chimp_decode(const uint8_t* c, uint64_t len, dvec* out) {
     }
 }
 
-/* ChimpNDecoder<128>::next / next_value (decoder/chunk_reader/chimp_n.rs:544-646) */
+/* ChimpNDecoder<128>::next / next_value (decoder/chunk_reader/chimp_n.rs:160-285) */
 static int chimp128_decode(const uint8_t* c, uint64_t len, dvec* out) {
     bitr r = {c, len, 0};
     uint64_t ring[CN];
@@ -992,7 +992,7 @@ static int elf_decode(const uint8_t* c, uint64_t len, int on_chimp, dvec* out) {
     }
 }
 
-/* RunLengthReaderImpl::decompress (decoder/chunk_reader/run_length.rs:314-337) */
+/* RunLengthReaderImpl::decompress (decoder/chunk_reader/run_length.rs:68-91) */
 static int rle_decode(const uint8_t* c, uint64_t len, dvec* out) {
     if (len < 8) return ORA_E_IO;
     uint64_t nf = rd_u64le(c);
@@ -1007,7 +1007,7 @@ static int rle_decode(const uint8_t* c, uint64_t len, dvec* out) {
     return ORA_OK;
 }
 
-/* UncompressedReaderImpl::decompress (decoder/chunk_reader/uncompressed.rs:587-602) */
+/* UncompressedReaderImpl::decompress (decoder/chunk_reader/uncompressed.rs:56-71) */
 static int raw_decode(const uint8_t* c, uint64_t len, uint64_t n_rows, dvec* out) {
     if (n_rows > len / 8) return ORA_E_IO;
     for (uint64_t i = 0; i < n_rows; ++i) PUSH(u2f(rd_u64le(c + 8 * i)));
@@ -1315,7 +1315,7 @@ static int buff_max_masked(const uint8_t* c, uint64_t len, int is_min, const uin
     return ORA_OK;
 }
 
-/* max_without_bitmask (buff/min_max.rs:279-432) */
+/* max_without_bitmask (buff/min_max.rs:160-313) */
 static int buff_max_all(const uint8_t* c, uint64_t len, double* out) {
     buffh h;
     int st = buff_header(c, len, &h);

@@ -5,7 +5,7 @@ project is built, so its tests cannot be run to dump fixtures.  Instead the
 fixed (non-random) cases of its test suite are transcribed here, each with the
 reference file:line it comes from.  Its randomised tests draw from an unseeded
 RNG (`StdRng::from_entropy()`, ebi/tests/common/mod.rs:34) and hold no
-vectors; tests/test_parity_*.py restate their pattern with a seeded RNG.
+vectors; tests/test_gpu_values.py and tests/test_gpu_buff.py restate their pattern with a seeded RNG.
 
 Run:  python tests/golden/make_golden.py      (rewrites kat.json next to this file)
 """
@@ -34,12 +34,12 @@ BIT_READS = [
      "expect": [0b1011, None, 0b0000], "check": [True, True, True]},
 ]
 
-# --- Gorilla [12.0, 24.0] (decoder/chunk_reader/gorilla.rs:309-344) --------------------
+# --- Gorilla [12.0, 24.0] (decoder/chunk_reader/gorilla.rs:161-207) --------------------
 # The test lists `_encoded` but never asserts it; its first 80 bits are ebi's
 # stream (12.0 raw, '11', leading 01011, sig-1 000000, payload '1', and the
 # '11' that opens the end marker); the bytes after that follow upstream tsz's
-# end marker, not ebi's NaN marker (compressor/gorilla.rs:202-205).
-GORILLA_PREFIX = {"src": "ebi/src/decoder/chunk_reader/gorilla.rs:311-330",
+# end marker, not ebi's NaN marker (compressor/gorilla.rs:27-30).
+GORILLA_PREFIX = {"src": "ebi/src/decoder/chunk_reader/gorilla.rs:173-192",
                   "values": [12.0, 24.0],
                   "prefix_bytes": [0x40, 0x28, 0, 0, 0, 0, 0, 0, 0b11010110, 0b00000111]}
 

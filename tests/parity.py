@@ -128,6 +128,37 @@ def check_query_suite(data: bytes, preds, masks=(None,), chunk_ids=(None,), exac
         o.close()
 
 
+def oracle_filter_agg(o: "O.Decoder", p):
+    """One filter + aggregate query on the oracle: (bitmask, sum, min, max, count, selected values),
+    sum / min / max over the filter's bitmask as the reference's second call computes them."""
+    op = to_oracle_pred(p) if isinstance(p, E.Predicate) else p
+    m, s, mn, mx = o.filter_agg(op)
+    sel = o.filter_materialize(op)
+    return m, s, mn, mx, len(sel), sel
+
+
+def oracle_request(odecs, ids, p):
+    """A serving request (one predicate over the columns `ids`) answered by the oracle and combined
+    as a request is: per-column sums added in column order, fmin / fmax, counts added.
+    Returns (sum, min, max, count, sum of |selected value|)."""
+    s, mn, mx, cnt, mag = 0.0, math.inf, -math.inf, 0, 0.0
+    for i in ids:
+        _, si, mni, mxi, ni, sel = oracle_filter_agg(odecs[i], p)
+        s += si
+        mn = float(np.fmin(mn, mni))
+        mx = float(np.fmax(mx, mxi))
+        cnt += ni
+        mag += float(np.abs(sel).sum()) if len(sel) else 0.0
+    return s, mn, mx, cnt, mag
+
+
+def combined_sum_ok(g: float, o: float, mag: float) -> bool:
+    """A sum combined from several columns' sums: within 1e-12 of the summed magnitudes of the oracle's."""
+    if np.isnan(o) or np.isinf(o):
+        return same_scalar(g, o)
+    return abs(g - o) <= SUM_RTOL * max(mag, 1e-300)
+
+
 def random_mask(n, density, rng):
     rows = np.nonzero(rng.random(n) < density)[0]
     return O.mask_from_rows(rows.tolist(), n)

@@ -1,11 +1,14 @@
 """ebi_batch (one persistent mixed-codec launch for many queries) against the
-single-column ebi_filter_agg: every query's bitmask, sum, min, max and count
-are bit-identical to the same query run alone."""
+oracle and against the single-column ebi_filter_agg: every query's bitmask,
+min, max and count equal the oracle's Decoder on the same bytes bit for bit,
+its sum is exact (BUFF) or within the compensated-sum bound of the oracle's
+sequential sum, and all of them are bit-identical to the same query run alone."""
 import numpy as np
 import pytest
 
 import ebi_gb300 as E
-from tests.parity import mask_np, random_preds
+from oracle import oracle as O
+from tests.parity import mask_np, oracle_filter_agg, random_preds, same_scalar, sum_ok
 
 pytestmark = pytest.mark.gpu
 
@@ -26,7 +29,7 @@ def make_columns(rng, n_cols):
         else:
             v = walk
             data = E.encode(v, codec, ("record_count", [8192, 4096, 20000][i % 3]))
-        cols.append((E.Decoder(data), v))
+        cols.append((E.Decoder(data), v, O.Decoder(data), codec))
     return cols
 
 
@@ -45,7 +48,7 @@ def test_batch_matches_single_queries(seed):
     cols = make_columns(rng, 30)
     queries, expect = [], []
     for k in range(45):  # some columns appear in several queries
-        d, v = cols[k % len(cols)]
+        d, v = cols[k % len(cols)][:2]
         p = random_preds(v, rng, k=1)[int(rng.integers(4))]
         aggs = [("sum", "min", "max"), ("sum",), ("max",)][k % 3]
         queries.append((d, p, aggs))
@@ -62,6 +65,16 @@ def test_batch_matches_single_queries(seed):
         for k, (d, p, aggs) in enumerate(queries):
             m, s, mn, mx, n = alone(d, p, aggs)
             gs, gmn, gmx, gn = got[k]
+            _, _, o, codec = cols[k % len(cols)]
+            om, os_, omn, omx, on, sel = oracle_filter_agg(o, p)
+            assert gn == on, (k, gn, on)
+            assert np.array_equal(mask_np(b.masks[k])[: len(om)], om), k
+            if "sum" in aggs:
+                assert sum_ok(gs, os_, codec == "buff", sel), (k, codec, gs, os_)
+            if "min" in aggs:
+                assert same_scalar(gmn, omn), (k, gmn, omn)
+            if "max" in aggs:
+                assert same_scalar(gmx, omx), (k, gmx, omx)
             assert gn == n, (k, gn, n)
             assert same(gs, s) and same(gmn, mn) and same(gmx, mx), (k, gs, s, gmn, mn, gmx, mx)
             assert np.array_equal(mask_np(b.masks[k]), mask_np(m)), k

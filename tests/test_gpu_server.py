@@ -1,30 +1,35 @@
 """The continuous-batching server: every request's result, answered in the
 mix (batched with whatever arrived around it, batches overlapping on the
 device), equals the same request answered alone with plain per-column
-filter_agg calls, bit for bit."""
+filter_agg calls, bit for bit, and equals the oracle's answer on the same
+columns (count, min and max bit for bit; the sum within the compensated-sum
+bound of the oracle's sequential sums, added in column order)."""
 import numpy as np
 import pytest
 
 import ebi_gb300 as E
+from oracle import oracle as O
+from tests.parity import combined_sum_ok, oracle_request
 
 pytestmark = pytest.mark.gpu
 
 
-def columns(rng, n_cols):
+def columns(rng, n_cols, codecs=("buff", "gorilla", "chimp128", "rle", "elf"), lo=2_000, hi=200_000):
+    """(device Decoder, values, oracle Decoder) per column."""
     out = []
-    codecs = ["buff", "gorilla", "chimp128", "rle", "elf"]
     for i in range(n_cols):
         codec = codecs[i % len(codecs)]
-        n = int(np.exp(rng.uniform(np.log(2_000), np.log(200_000))))
+        n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
         if codec == "buff":
             v = np.round(rng.uniform(-1000, 1000, n), 3) + 0.0
-            out.append((E.Decoder(E.encode(v, "buff", ("record_count", 65536), 1000)), v))
+            data = E.encode(v, "buff", ("record_count", 65536), 1000)
         elif codec == "rle":
             v = np.repeat(np.round(50 + np.cumsum(rng.integers(-5, 6, n // 40 + 1) * 0.1), 1), 40)[:n] + 0.0
-            out.append((E.Decoder(E.encode(v, "rle", ("record_count", 8192))), v))
+            data = E.encode(v, "rle", ("record_count", 8192))
         else:
             v = np.round(30 + np.cumsum(rng.normal(0, 0.5, n)), 2) + 0.0
-            out.append((E.Decoder(E.encode(v, codec, ("record_count", 8192))), v))
+            data = E.encode(v, codec, ("record_count", 8192))
+        out.append((E.Decoder(data), v, O.Decoder(data)))
     return out
 
 
@@ -45,11 +50,24 @@ def same(x, y):
     return x == y or (np.isnan(x) and np.isnan(y))
 
 
+def check_oracle(cols, reqs, got):
+    odecs = [o for _, _, o in cols]
+    for i, ((ids, p, aggs), m) in enumerate(zip(reqs, got)):
+        s, mn, mx, cnt, mag = oracle_request(odecs, ids, p)
+        assert m["count"] == cnt, (i, m, cnt)
+        if "sum" in aggs:
+            assert combined_sum_ok(m["sum"], s, mag), (i, m["sum"], s)
+        if "min" in aggs:
+            assert same(m["min"], mn), (i, m["min"], mn)
+        if "max" in aggs:
+            assert same(m["max"], mx), (i, m["max"], mx)
+
+
 @pytest.mark.parametrize("rate", [5_000, 50_000, None])
 def test_results_equal_alone_and_in_the_mix(rate):
     rng = np.random.default_rng(7)
     cols = columns(rng, 24)
-    decs = [d for d, _ in cols]
+    decs = [d for d, _, _ in cols]
     reqs = requests(rng, cols, 400)
     alone = E.run_plain(decs, reqs)
     srv = E.Server(decs, slots=4, max_queries=512, max_chunks=1 << 16, max_items=1 << 17)
@@ -65,14 +83,43 @@ def test_results_equal_alone_and_in_the_mix(rate):
         assert a["count"] == m["count"], (i, a, m)
         assert same(a["sum"], m["sum"]) and same(a["min"], m["min"]) and same(a["max"], m["max"]), (i, a, m)
         assert m["done_ns"] >= m["launch_ns"] >= m["submit_ns"]
+    check_oracle(cols, reqs, mixed)
     if rate is None:  # everything queued at once: requests share batches
         assert st["batches"] < len(reqs)
+
+
+@pytest.mark.parametrize("codecs", [("chimp128", "gorilla", "chimp"), ("elf", "elf_on_chimp", "gorilla")])
+def test_shared_decodes_match_oracle(codecs):
+    # Three columns and 300 requests queued at once: every batch holds many queries per
+    # column, so a Chimp-family chunk is decoded once for up to 32 of them and a Gorilla
+    # chunk group is walked once for up to 3.  Each answer is checked against the oracle.
+    rng = np.random.default_rng(17)
+    cols = columns(rng, 3, codecs=codecs, lo=30_000, hi=120_000)
+    decs = [d for d, _, _ in cols]
+    reqs = []
+    for k in range(300):
+        ids = [k % 3] if k % 4 else [0, 1, 2]
+        vals = np.concatenate([cols[i][1] for i in ids])
+        a, b = np.sort(rng.choice(vals, 2))
+        p = E.Predicate.range(E.RangeValue.inclusive(float(a)), E.RangeValue.inclusive(float(b)))
+        reqs.append((ids, p, [("sum", "min", "max"), ("sum",), ("min",), ("max",)][k % 4]))
+    srv = E.Server(decs, slots=2, max_queries=512, max_chunks=1 << 16, max_items=1 << 17)
+    mixed = srv.replay(reqs)
+    st = srv.stats()
+    srv.close()
+    assert st["batches"] * 10 <= len(reqs)  # batches of tens of requests: queries share chunks
+    for m in mixed:
+        assert m["status"] == 0
+    check_oracle(cols, reqs, mixed)
+    alone = E.run_plain(decs, reqs)
+    for a, m in zip(alone, mixed):
+        assert a["count"] == m["count"] and same(a["sum"], m["sum"]) and same(a["min"], m["min"]) and same(a["max"], m["max"])
 
 
 def test_poll_interface():
     rng = np.random.default_rng(3)
     cols = columns(rng, 6)
-    decs = [d for d, _ in cols]
+    decs = [d for d, _, _ in cols]
     srv = E.Server(decs, slots=2, max_queries=64, max_chunks=1 << 14, max_items=1 << 15)
     reqs = requests(rng, cols, 20)
     tickets = [srv.submit(*r) for r in reqs]
@@ -85,6 +132,7 @@ def test_poll_interface():
     srv.close()
     alone = E.run_plain(decs, reqs)
     assert sorted(got) == sorted(tickets)
+    check_oracle(cols, reqs, [got[t] for t in tickets])
     for t, a in zip(tickets, alone):
         m = got[t]
         assert a["count"] == m["count"] and same(a["sum"], m["sum"]) and same(a["min"], m["min"]) and same(a["max"], m["max"])
