@@ -2,30 +2,28 @@
 // persistent launch.
 //
 // A batch is a list of work items, each naming a query and a unit of one of
-// its columns: an 8,192-row BUFF tile, a whole Uncompressed / RLE chunk, or
-// a group of XOR chunks (Gorilla, Chimp, Chimp128, Elf, ElfOnChimp), one per
-// warp.  An XOR item may name a run of consecutive queries over one column
-// (up to kGorillaShare for Gorilla, kXorShare for the Chimp family): the
-// chunk is parsed once for all of them.  A persistent grid of 256-thread
-// CTAs pulls items from a device counter, so columns of very different
-// lengths and codecs share the GPU without a launch per column; each item
-// runs the same per-chunk device code as the single-column kernels and
-// leaves its result in the query's own per-chunk accumulators.  A second
-// launch folds every query (one CTA per query, chunk order).
+// its columns: an 8,192-row BUFF tile, a whole Uncompressed / RLE / Chimp /
+// Chimp128 / Elf / ElfOnChimp chunk, or a group of Gorilla chunks (one per warp).
+// A Chimp-family item may name a run of consecutive queries over one column
+// (count of them, at most 32): the chunk is decoded once for all of them.  A persistent
+// grid of 256-thread CTAs pulls items from a device counter, so columns of
+// very different lengths and codecs share the GPU without a launch per
+// column; each item runs the same per-chunk device code as the single-column
+// kernels and leaves its result in the query's own per-chunk accumulators.
+// A second launch folds every query (one CTA per query, chunk order).
 #include "internal.h"
 #include "buff_tile.cuh"
 #include "finalize.cuh"
 #include "gorilla_dev.cuh"
 #include "raw_dev.cuh"
 #include "rle_dev.cuh"
-#include "xor_warp.cuh"
+#include "xor_dev.cuh"
 
 namespace ebi {
 namespace {
 
 constexpr int kBatchThreads = 256;
-static_assert(kBatchThreads == kRleThreads, "codec CTA shapes");
-static_assert(kBatchXorChunks == kBatchThreads / 32 && kBatchRingSets <= kBatchXorChunks, "one XOR chunk per warp");
+static_assert(kBatchThreads == kXorThreads && kBatchThreads == kRleThreads, "codec CTA shapes");
 
 // One function per item kind, kept out of line so that each gets its own
 // register allocation (the kernel's is the largest, not the sum of all paths).
@@ -47,30 +45,18 @@ __device__ __noinline__ void item_gorilla(const QueryParams& q, const BatchItem&
     const uint32_t nq = it.count >> 8 ? it.count >> 8 : 1u;  // queries it.query .. + nq: one column
     if (warp < chunks) gorilla_chunk_l1<kGorillaShare>(&q, nq, it.unit + warp, it.unit + warp, VAL_SCAN, nullptr);
 }
-// Chimp-family items: chunk unit + warp for the warps below the item's chunk count.
-template <int CODEC>
-__device__ __forceinline__ void item_xor(const QueryParams& q, const BatchItem& it) {
-    extern __shared__ __align__(16) uint8_t smem_batch[];
-    const uint32_t warp = threadIdx.x >> 5, chunks = it.count & 0xffu;
-    const uint32_t nq = it.count >> 8 ? it.count >> 8 : 1u;  // queries it.query .. + nq: one column
-    if (warp >= chunks) return;
-    // shared memory: the 8 warps' stream windows, their waiting bitmask words, then kBatchRingSets ring sets
-    uint32_t* win = reinterpret_cast<uint32_t*>(smem_batch + size_t(warp) * kWinBytes);
-    uint32_t* bits = reinterpret_cast<uint32_t*>(smem_batch + size_t(kBatchXorChunks) * kWinBytes +
-                                                 size_t(warp) * kXorPassQueries * kBitBytes);
-    uint64_t* rx = nullptr;
-    uint8_t* re = nullptr;
-    if (CODEC == CODEC_CHIMP128) {
-        rx = reinterpret_cast<uint64_t*>(smem_batch + size_t(kBatchXorChunks) * (kWinBytes + kXorPassQueries * kBitBytes) +
-                                         size_t(warp) * kRingBytes);
-        re = reinterpret_cast<uint8_t*>(rx + kLanes * kRingSlots);
-    }
-    xor_chunk_warp<CODEC, kXorPassQueries>(&q, nq, it.unit + warp, it.unit + warp, VAL_SCAN, nullptr, win, bits, rx, re);
+__device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_CHIMP>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
 }
-__device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& it) { item_xor<CODEC_CHIMP>(q, it); }
-__device__ __noinline__ void item_chimp128(const QueryParams& q, const BatchItem& it) { item_xor<CODEC_CHIMP128>(q, it); }
-__device__ __noinline__ void item_elf_chimp(const QueryParams& q, const BatchItem& it) { item_xor<CODEC_ELF_CHIMP>(q, it); }
-__device__ __noinline__ void item_elf(const QueryParams& q, const BatchItem& it) { item_xor<CODEC_ELF>(q, it); }
+__device__ __noinline__ void item_chimp128(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_CHIMP128>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
+}
+__device__ __noinline__ void item_elf_chimp(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_ELF_CHIMP>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
+}
+__device__ __noinline__ void item_elf(const QueryParams& q, const BatchItem& it) {
+    xor_chunk<CODEC_ELF>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
+}
 
 __global__ void __launch_bounds__(kBatchThreads, 2)
 batch_kernel(const QueryParams* __restrict__ qp, const BatchItem* __restrict__ items, uint32_t n_items,
@@ -108,7 +94,8 @@ __global__ void __launch_bounds__(kFinThreads) batch_finalize_kernel(const Query
 }  // namespace
 
 size_t batch_smem_bytes() {
-    return size_t(kBatchXorChunks) * (kWinBytes + kXorPassQueries * kBitBytes) + size_t(kBatchRingSets) * kRingBytes;
+    static_assert(xor_smem_bytes(CODEC_CHIMP128) >= xor_smem_bytes(CODEC_ELF), "largest codec body");
+    return xor_smem_bytes(CODEC_CHIMP128);
 }
 
 void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t query, std::vector<BatchItem>& out) {
@@ -116,37 +103,30 @@ void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t quer
     case EBI_BUFF:
         for (uint32_t t = 0; t < n_tiles; ++t) out.push_back({query, ITEM_BUFF_TILE, t, 1});
         return;
-    case EBI_UNCOMPRESSED:
-    case EBI_RLE:
-        for (uint64_t k = 0; k < n_chunks; ++k)
-            out.push_back({query, scheme == EBI_RLE ? ITEM_RLE : ITEM_RAW, static_cast<uint32_t>(k), 1});
+    case EBI_GORILLA:
+        for (uint64_t k = 0; k < n_chunks; k += 8)
+            out.push_back({query, ITEM_GORILLA, static_cast<uint32_t>(k),
+                           static_cast<uint32_t>(n_chunks - k < 8 ? n_chunks - k : 8)});
         return;
     default: {
-        const uint32_t kind = scheme == EBI_GORILLA      ? ITEM_GORILLA
+        const uint32_t kind = scheme == EBI_UNCOMPRESSED ? ITEM_RAW
+                            : scheme == EBI_RLE          ? ITEM_RLE
                             : scheme == EBI_CHIMP        ? ITEM_CHIMP
                             : scheme == EBI_CHIMP128     ? ITEM_CHIMP128
                             : scheme == EBI_ELF_ON_CHIMP ? ITEM_ELF_CHIMP
                                                          : ITEM_ELF;
-        const uint64_t per = xor_item_chunks(scheme);
-        for (uint64_t k = 0; k < n_chunks; k += per)
-            out.push_back({query, kind, static_cast<uint32_t>(k),
-                           static_cast<uint32_t>(n_chunks - k < per ? n_chunks - k : per)});
+        for (uint64_t k = 0; k < n_chunks; ++k) out.push_back({query, kind, static_cast<uint32_t>(k), 1});
     }
     }
-}
-
-uint32_t xor_item_chunks(int scheme) {
-    return scheme == EBI_GORILLA ? 8u : scheme == EBI_CHIMP128 ? kBatchRingSets : kBatchXorChunks;
 }
 
 double item_cost(uint32_t kind, uint32_t count) {
-    const double chunks = count & 0xffu;  // XOR items: queries sharing the chunks cost little more
     switch (kind) {
-    case ITEM_GORILLA: return 40.0 * chunks;
-    case ITEM_ELF: return 12.0 * chunks;
-    case ITEM_ELF_CHIMP: return 12.0 * chunks;
-    case ITEM_CHIMP128: return 10.0 * chunks;
-    case ITEM_CHIMP: return 8.0 * chunks;
+    case ITEM_GORILLA: return 40.0 * (count & 0xffu);  // the chunks; queries sharing them cost little more
+    case ITEM_ELF: return 35.0;
+    case ITEM_ELF_CHIMP: return 35.0;
+    case ITEM_CHIMP128: return 30.0;
+    case ITEM_CHIMP: return 25.0;
     case ITEM_BUFF_TILE: return 1.0;
     case ITEM_RLE: return 0.5;
     default: return 2.0;

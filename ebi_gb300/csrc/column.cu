@@ -196,7 +196,6 @@ int dev_alloc(T** p, size_t count, cudaStream_t s) {
 QueryParams base_params(const ebi_column* c) {
     QueryParams q{};
     q.file = c->d_file;
-    q.file_bytes = c->d_file_bytes;
     q.chunks = c->d_chunks;
     q.acc = c->d_acc;
     q.tiles = c->d_tiles;
@@ -560,7 +559,6 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     c->mask_words = (c->n_records + 63) / 64;
     if (c->mask_words == 0) c->mask_words = 1;
     st = dev_alloc(&c->d_file, dev_len + kFilePad, s);
-    c->d_file_bytes = dev_len + kFilePad;
     // BUFF: the planes are repacked into d_file straight from the caller's
     // buffer when the device can read it (pinned host memory: one pass over
     // the host link), else from a device copy of the file

@@ -18,7 +18,6 @@ struct ebi_column {
     bool rows_aligned32 = true;
     int32_t precision = -1;
     uint8_t* d_file = nullptr;
-    uint64_t d_file_bytes = 0;  // allocation of d_file (the resident bytes and their zero padding)
     ChunkDesc* d_chunks = nullptr;
     Tile* d_tiles = nullptr;
     ChunkAcc* d_acc = nullptr;

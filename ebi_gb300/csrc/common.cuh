@@ -129,7 +129,6 @@ enum Op : int {
 // Arguments of the per-chunk query kernels (passed by value).
 struct QueryParams {
     const uint8_t* file;
-    uint64_t file_bytes;       // allocation of file (no read reaches past it)
     const ChunkDesc* chunks;
     ChunkAcc* acc;
     const Tile* tiles;

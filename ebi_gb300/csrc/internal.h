@@ -113,33 +113,22 @@ enum BatchItemKind : uint32_t {
     ITEM_BUFF_TILE = 0,  // unit = tile index of the query's column
     ITEM_RAW = 1,        // unit = chunk
     ITEM_RLE = 2,
-    ITEM_GORILLA = 3,    // XOR codecs: chunks [unit, unit + (count & 0xff)), one warp each
+    ITEM_GORILLA = 3,    // chunks [unit, unit + count), one warp each
     ITEM_CHIMP = 4,
     ITEM_CHIMP128 = 5,
-    ITEM_ELF_CHIMP = 6,
+    ITEM_ELF_CHIMP = 6,  // unit = chunk
     ITEM_ELF = 7,
 };
 struct BatchItem {
     uint32_t query;  // index into the batch's QueryParams
     uint32_t kind;   // BatchItemKind
     uint32_t unit;
-    uint32_t count;  // XOR codecs: chunks | (consecutive queries over the column sharing them) << 8 (0: one)
+    uint32_t count;  // Chimp family: queries sharing the chunk; Gorilla: chunks | (queries sharing them) << 8
 };
 // Queries over one Gorilla column that one batch item serves at once.
 constexpr uint32_t kGorillaShare = 3;
-// Queries over one Chimp-family column that one batch item serves: the
-// chunk's parse and value-chain starts are shared by all of them, each value
-// pass over the chunk runs kXorPassQueries of them.
-constexpr uint32_t kXorShare = 32;
-constexpr int kXorPassQueries = 1;
-// Chimp128 chunks per batch item: each needs a warp's 36 KB of rings in the CTA.
-constexpr uint32_t kBatchRingSets = 1;
-// Chunks per batch item of the other XOR codecs: one per warp of the CTA.
-constexpr uint32_t kBatchXorChunks = 8;
 // Appends the items of one query over a column (scheme, chunks, BUFF tiles).
 void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t query, std::vector<BatchItem>& out);
-// Chunks per batch item of an XOR scheme.
-uint32_t xor_item_chunks(int scheme);
 // Relative cost of one item of each kind (device time of an 8,192-row unit
 // measured on the single-column kernels), for the cost-descending order.
 double item_cost(uint32_t kind, uint32_t count);

@@ -87,10 +87,8 @@ void footprint(const ebi_server* s, const ebi_request& r, uint64_t* chunks, uint
     for (uint32_t k = 0; k < r.n_columns; ++k) {
         const ebi_column* col = s->cols[r.columns[k]];
         c += col->n_chunks;
-        const bool xorc = col->scheme == EBI_GORILLA || col->scheme == EBI_CHIMP || col->scheme == EBI_CHIMP128 ||
-                          col->scheme == EBI_ELF_ON_CHIMP || col->scheme == EBI_ELF;
         it += col->scheme == EBI_BUFF ? col->tiles.tiles.size()
-            : xorc ? (col->n_chunks + xor_item_chunks(col->scheme) - 1) / xor_item_chunks(col->scheme) : col->n_chunks;
+            : col->scheme == EBI_GORILLA ? (col->n_chunks + 7) / 8 : col->n_chunks;
     }
     *chunks = c;
     *items = it;
@@ -99,9 +97,9 @@ void footprint(const ebi_server* s, const ebi_request& r, uint64_t* chunks, uint
 // Builds and launches slot sl's batch from its admitted requests.
 cudaError_t launch_slot(ebi_server* s, Slot& sl) {
     // The batch's queries in column order, so that the queries on one column
-    // are consecutive: a group of Chimp-family chunks is then parsed once for
-    // up to kXorShare of them, a group of Gorilla chunks once for up to
-    // kGorillaShare.
+    // are consecutive: a Chimp-family chunk is then decoded once for all of
+    // them (items naming up to 32 consecutive queries), a group of Gorilla
+    // chunks once for up to kGorillaShare.
     struct Ent { uint32_t col, req, k; };
     std::vector<Ent> ents;
     std::vector<uint32_t> base(sl.reqs.size() + 1, 0);
@@ -140,11 +138,10 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
         const bool shared = c->scheme == EBI_CHIMP || c->scheme == EBI_CHIMP128 || c->scheme == EBI_ELF_ON_CHIMP ||
                             c->scheme == EBI_ELF;
         if (shared) {
-            for (uint32_t q0 = g; q0 < h; q0 += kXorShare) {
+            for (uint32_t q0 = g; q0 < h; q0 += 32) {
                 const size_t first = items.size();
                 column_items(c->scheme, c->n_chunks, tiles, q0, items);
-                const uint32_t share = std::min<uint32_t>(kXorShare, h - q0);
-                for (size_t i = first; i < items.size(); ++i) items[i].count |= share << 8;
+                for (size_t i = first; i < items.size(); ++i) items[i].count = std::min<uint32_t>(32, h - q0);
             }
         } else if (c->scheme == EBI_GORILLA) {
             // a group of chunks is parsed once for up to kGorillaShare queries

@@ -43,13 +43,10 @@ XOR_HD uint32_t lead_decode(uint32_t t) {
 // Parser state: bit position in the chunk and the inherited window
 // (Gorilla: lead | trail << 8; Chimp/Chimp128/ElfOnChimp: stored leading zeros
 // or kNoLead; Elf: lead | trail << 8, kNoWin before any).
-// P: the position type (uint32_t for chunks under 2^31 bits, uint64_t above).
-template <typename P>
-struct PStateT {
-    P pos;
+struct PState {
+    uint64_t pos;
     uint32_t win;
 };
-using PState = PStateT<uint64_t>;
 XOR_HD uint64_t pack_state(PState s) { return s.pos | (uint64_t(s.win) << 48); }
 XOR_HD PState unpack_state(uint64_t v) { return PState{v & ((1ull << 48) - 1), static_cast<uint32_t>(v >> 48)}; }
 
@@ -64,8 +61,8 @@ struct Rec {
 };
 
 // payload of n <= 64 bits at q (0 for n == 0)
-template <typename Peek, typename P>
-XOR_HD uint64_t take_bits(Peek peek, P q, uint32_t n) {
+template <typename Peek>
+XOR_HD uint64_t take_bits(Peek peek, uint64_t q, uint32_t n) {
     return n ? peek(q) >> (64 - n) : 0;
 }
 
@@ -75,15 +72,15 @@ XOR_HD uint64_t take_bits(Peek peek, P q, uint32_t n) {
 // stream's first value (ElfXor read_first :121-141: 7-bit trailing zeros
 // and the bits above the lowest set one; Chimp: 64 raw bits), else an
 // ElfXor record (decompress_float_inner :143-221) or a Chimp record.
-template <int CODEC, typename Peek, typename P>
-XOR_HD uint32_t parse_elf(Peek peek, P B, PStateT<P>& s, Rec& r);
+template <int CODEC, typename Peek>
+XOR_HD uint32_t parse_elf(Peek peek, uint64_t B, PState& s, Rec& r);
 
 // Parses one record at s.pos; returns 0 or the error the reader raises there
 // (EBI_E_UNEXPECTED_END for a read past the chunk, EBI_E_CORRUPT for a
 // window the reader's u8/u32 arithmetic cannot represent).  B = chunk bits.
-template <int CODEC, typename Peek, typename P>
-XOR_HD uint32_t parse_rec(Peek peek, P B, PStateT<P>& s, Rec& r) {
-    const P p = s.pos;
+template <int CODEC, typename Peek>
+XOR_HD uint32_t parse_rec(Peek peek, uint64_t B, PState& s, Rec& r) {
+    const uint64_t p = s.pos;
     r.ring = kRefPrev;
     r.nan_ok = true;
     r.meta = 0;
@@ -95,7 +92,7 @@ XOR_HD uint32_t parse_rec(Peek peek, P B, PStateT<P>& s, Rec& r) {
         if (!(x >> 63)) { s.pos = p + 1; r.delta = 0; return 0; }
         if (p + 2 > B) return EBI_E_UNEXPECTED_END;
         uint32_t lead = s.win & 0xffu, trail = s.win >> 8, n;
-        P q;
+        uint64_t q;
         if (!((x >> 62) & 1)) {
             n = 64 - lead - trail;
             q = p + 2;
@@ -131,7 +128,7 @@ XOR_HD uint32_t parse_rec(Peek peek, P B, PStateT<P>& s, Rec& r) {
         }
         if (flag == 3 || flag == 2) {
             uint32_t lead = s.win;
-            P q = p + 2;
+            uint64_t q = p + 2;
             if (flag == 3) {
                 if (p + 5 > B) return EBI_E_UNEXPECTED_END;
                 lead = lead_decode(static_cast<uint32_t>(x >> 59) & 7u);
@@ -156,7 +153,7 @@ XOR_HD uint32_t parse_rec(Peek peek, P B, PStateT<P>& s, Rec& r) {
         if (sig == 0) sig = 64;
         if (sig + lead > 64) return EBI_E_CORRUPT;
         const uint32_t trail = 64 - sig - lead;
-        const P q = p + 2 + hdr;
+        const uint64_t q = p + 2 + hdr;
         if (q + sig > B) return EBI_E_UNEXPECTED_END;
         r.delta = (sig == 64 ? peek(q) : peek(q) >> (64 - sig)) << trail;
         s.win = lead;
@@ -165,12 +162,12 @@ XOR_HD uint32_t parse_rec(Peek peek, P B, PStateT<P>& s, Rec& r) {
     }
 }
 
-template <int CODEC, typename Peek, typename P>
-XOR_HD uint32_t parse_elf(Peek peek, P B, PStateT<P>& s, Rec& r) {
-    const P p0 = s.pos;
+template <int CODEC, typename Peek>
+XOR_HD uint32_t parse_elf(Peek peek, uint64_t B, PState& s, Rec& r) {
+    const uint64_t p0 = s.pos;
     if (p0 + 1 > B) return EBI_E_UNEXPECTED_END;
     const uint64_t x = peek(p0);
-    P p;
+    uint64_t p;
     if (!(x >> 63)) {
         r.meta = kElfRestore;
         p = p0 + 1;
@@ -240,7 +237,7 @@ XOR_HD uint32_t parse_elf(Peek peek, P B, PStateT<P>& s, Rec& r) {
     if (center == 0) center = 1u << cb;
     if (lead + center > 64) return EBI_E_CORRUPT;
     const uint32_t trail = 64 - lead - center;
-    const P q = p + 2 + hb;
+    const uint64_t q = p + 2 + hb;
     if (flag == 2 && center == 1) {
         r.delta = 1ull << trail;
         s.pos = q;
@@ -256,9 +253,9 @@ XOR_HD uint32_t parse_elf(Peek peek, P B, PStateT<P>& s, Rec& r) {
 // Length-only step of one Chimp / Chimp128 record (the convergence rounds of
 // the segment parse need positions and windows, not payloads): selects
 // instead of branches, one 64-bit read.  Same errors as parse_rec.
-template <int CODEC, typename Peek, typename P>
-XOR_HD uint32_t step_len(Peek peek, P B, PStateT<P>& s) {
-    const P p = s.pos;
+template <int CODEC, typename Peek>
+XOR_HD uint32_t step_len(Peek peek, uint64_t B, PState& s) {
+    const uint64_t p = s.pos;
     if (p + 2 > B) return EBI_E_UNEXPECTED_END;
     const uint64_t x = peek(p);
     const uint32_t flag = static_cast<uint32_t>(x >> 62);
