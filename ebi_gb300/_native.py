@@ -13,6 +13,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libebi_gpu.so"
 # Every symbol include/ebi_gpu.h declares.
 EXPORTS = [
     "ebi_column_open", "ebi_column_open_file", "ebi_column_close", "ebi_column_num_records", "ebi_column_num_chunks",
+    "ebi_column_device_bytes", "ebi_column_set_copy_wait",
     "ebi_column_scheme", "ebi_column_chunk_info", "ebi_column_set_precision", "ebi_materialize",
     "ebi_filter", "ebi_filter_materialize", "ebi_sum", "ebi_min", "ebi_max", "ebi_filter_agg",
     "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches", "ebi_column_set_timing",
@@ -106,7 +107,8 @@ def lib() -> C.CDLL:
     L.ebi_column_open_file.argtypes = [C.c_char_p, vp, C.POINTER(vp)]
     L.ebi_aggregate.argtypes = [C.POINTER(vp), C.c_uint32, C.POINTER(Aggregation), C.c_uint32, vp, vp]
     L.ebi_column_close.argtypes = [vp]
-    for fn in (L.ebi_column_num_records, L.ebi_column_num_chunks):
+    L.ebi_column_set_copy_wait.argtypes = [vp, C.c_int64]
+    for fn in (L.ebi_column_num_records, L.ebi_column_num_chunks, L.ebi_column_device_bytes):
         fn.argtypes = [vp]
         fn.restype = u64
     L.ebi_column_scheme.argtypes = [vp]

@@ -208,6 +208,16 @@ class Decoder:
     def n_chunks(self) -> int: return _native.lib().ebi_column_num_chunks(self._h)
     @property
     def scheme(self) -> int: return _native.lib().ebi_column_scheme(self._h)
+    def set_copy_wait(self, cycles=None):
+        """Limit (SM clocks) of the column's kernels' waits for their bulk copies; None: the default.
+        A query whose copy has not landed by then raises CudaError; the column stays usable."""
+        _check(_native.lib().ebi_column_set_copy_wait(self._h, -1 if cycles is None else int(cycles)),
+               "Decoder::set_copy_wait")
+
+    @property
+    def device_bytes(self) -> int:
+        """Device memory the column holds (resident file, tables, query scratch once allocated)."""
+        return _native.lib().ebi_column_device_bytes(self._h)
     @property
     def mask_words(self) -> int: return max((self.n_records + 63) // 64, 1)
 

@@ -501,6 +501,7 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
         const uint32_t lane = threadIdx.x - kScanConsumers;
         __shared__ PreTile pre[32];
         bool stop = false;
+        uint32_t issued = 0;  // tiles whose copies lane 0 issued
         for (uint32_t i0 = 0; i0 < count && !stop; i0 += 32) {
             const uint32_t nb = count - i0 < 32 ? count - i0 : 32u;
             if (lane < nb) prepare_tile(q, info, T, tile_base + t_first + i0 + lane, has_mask, pre[lane]);
@@ -508,7 +509,7 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
             if (lane == 0) {
                 for (uint32_t j = 0; j < nb; ++j) {
                     const uint32_t i = i0 + j, s = i % L.stages, k = i / L.stages;
-                    if (k > 0 && !mbar_wait(&empty[s], (k - 1) & 1)) {
+                    if (k > 0 && !mbar_wait(&empty[s], (k - 1) & 1, q.copy_wait)) {
                         chunk_error(q, T, 0, EBI_E_CUDA);
                         stop = true;  // consumers stopped; nothing of this stage is in flight
                         break;
@@ -533,14 +534,16 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
                             bulk_g2s(st + L.np_max * L.plane_stride, reinterpret_cast<const void*>(a), len, &full[s]);
                         }
                     }
+                    issued = i + 1;
                 }
             }
             stop = __shfl_sync(0xffffffffu, stop, 0);
             __syncwarp();  // pre[] is rewritten only after lane 0 consumed it
         }
-        // drain: the last stages' copies complete before this warp leaves
+        // drain (full limit whatever q.copy_wait): the copies of the last stages
+        // issued complete before this warp leaves
         if (lane == 0)
-            for (uint32_t i = count > L.stages ? count - L.stages : 0; i < count; ++i)
+            for (uint32_t i = issued > L.stages ? issued - L.stages : 0; i < issued; ++i)
                 if (!mbar_wait(&full[i % L.stages], (i / L.stages) & 1)) { chunk_error(q, T, 0, EBI_E_CUDA); break; }
     }
     __shared__ WarpTot wtot[kScanConsumers / 32];
@@ -552,7 +555,7 @@ buff_scan_kernel(QueryParams q, const BuffChunkInfo* info, uint32_t tile_base, u
     int64_t cur_base = 0;
     for (uint32_t i = 0; i < count; ++i) {
         const uint32_t s = i % L.stages, k = i / L.stages;
-        if (!mbar_wait(&full[s], k & 1)) {
+        if (!mbar_wait(&full[s], k & 1, q.copy_wait)) {
             chunk_error(q, T, 0, EBI_E_CUDA);
             break;
         }

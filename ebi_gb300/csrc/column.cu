@@ -192,10 +192,18 @@ int dev_alloc(T** p, size_t count, cudaStream_t s) {
     *p = static_cast<T*>(v);
     return EBI_OK;
 }
+// A buffer the column keeps until close (counted in c->device_bytes).
+template <typename T>
+int col_alloc(ebi_column* c, T** p, size_t count, cudaStream_t s) {
+    const int st = dev_alloc(p, count, s);
+    if (!st) c->device_bytes += count ? count * sizeof(T) : 16;
+    return st;
+}
 
 QueryParams base_params(const ebi_column* c) {
     QueryParams q{};
     q.file = c->d_file;
+    q.copy_wait = c->copy_wait;
     q.chunks = c->d_chunks;
     q.acc = c->d_acc;
     q.tiles = c->d_tiles;
@@ -243,9 +251,9 @@ void tile_range(const ebi_column* c, int64_t chunk_id, uint32_t* begin, uint32_t
 int ensure_scratch(ebi_column* c, cudaStream_t s) {
     if (c->d_tile_counts) return EBI_OK;
     const size_t nt = c->tiles.tiles.size();
-    int st = dev_alloc(&c->d_tile_counts, nt, s);
-    if (!st) st = dev_alloc(&c->d_tile_offsets, nt + 1, s);
-    if (!st) st = dev_alloc(&c->d_scratch_mask, c->mask_words, s);
+    int st = col_alloc(c, &c->d_tile_counts, nt, s);
+    if (!st) st = col_alloc(c, &c->d_tile_offsets, nt + 1, s);
+    if (!st) st = col_alloc(c, &c->d_scratch_mask, c->mask_words, s);
     return st;
 }
 
@@ -482,6 +490,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     ebi_column* c = new (std::nothrow) ebi_column();
     if (!c) return fail(EBI_E_OOM, "host allocation failed");
     c->stream = static_cast<cudaStream_t>(stream);
+    cudaGetDevice(&c->device);
     int st = parse_file(file, len, c);
     if (st) { delete c; return st; }
     cudaStream_t s = c->stream;
@@ -558,7 +567,7 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     }
     c->mask_words = (c->n_records + 63) / 64;
     if (c->mask_words == 0) c->mask_words = 1;
-    st = dev_alloc(&c->d_file, dev_len + kFilePad, s);
+    st = col_alloc(c, &c->d_file, dev_len + kFilePad, s);
     // BUFF: the planes are repacked into d_file straight from the caller's
     // buffer when the device can read it (pinned host memory: one pass over
     // the host link), else from a device copy of the file
@@ -580,15 +589,15 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         units = buff_units(c->chunks, c->first_unit);
         c->units_per_chunk = buff_uniform_units(c->first_unit);
     }
-    if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&c->d_units, units.size(), s);
-    if (!st) st = dev_alloc(&c->d_chunks, c->n_chunks, s);
-    if (!st) st = dev_alloc(&c->d_tiles, c->tiles.tiles.size(), s);
-    if (!st) st = dev_alloc(&c->d_acc, c->n_chunks, s);
-    if (!st) st = dev_alloc(&c->d_res, 1, s);
-    if (!st && !binfo.empty()) st = dev_alloc(&c->d_buff, binfo.size(), s);
+    if (!st && c->scheme == EBI_BUFF) st = col_alloc(c, &c->d_units, units.size(), s);
+    if (!st) st = col_alloc(c, &c->d_chunks, c->n_chunks, s);
+    if (!st) st = col_alloc(c, &c->d_tiles, c->tiles.tiles.size(), s);
+    if (!st) st = col_alloc(c, &c->d_acc, c->n_chunks, s);
+    if (!st) st = col_alloc(c, &c->d_res, 1, s);
+    if (!st && !binfo.empty()) st = col_alloc(c, &c->d_buff, binfo.size(), s);
     // the scan totals and, behind them, one slot per CTA of a scan launch
     // two totals blocks (totals-only queries alternate between them)
-    if (!st) st = dev_alloc(&c->d_tot, (2 * kScanTotalsBytes + sizeof(ScanTotals) - 1) / sizeof(ScanTotals), s);
+    if (!st) st = col_alloc(c, &c->d_tot, (2 * kScanTotalsBytes + sizeof(ScanTotals) - 1) / sizeof(ScanTotals), s);
     if (!st && !(c->h_res = g_pinned.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st && !(c->h_tot = g_pinned_tot.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st) {
@@ -690,6 +699,12 @@ int ebi_column_close(ebi_column* c) {
 
 uint64_t ebi_column_num_records(const ebi_column* c) { return c ? c->n_records : 0; }
 uint64_t ebi_column_num_chunks(const ebi_column* c) { return c ? c->n_chunks : 0; }
+uint64_t ebi_column_device_bytes(const ebi_column* c) { return c ? c->device_bytes : 0; }
+int ebi_column_set_copy_wait(ebi_column* c, int64_t cycles) {
+    if (!c) return fail(EBI_E_INVALID, "column is null");
+    c->copy_wait = cycles < 0 ? kWaitCycles : cycles;
+    return EBI_OK;
+}
 int ebi_column_scheme(const ebi_column* c) { return c ? c->scheme : -1; }
 
 int ebi_column_chunk_info(const ebi_column* c, uint64_t i, uint64_t* phys, uint64_t* size, uint64_t* row,
@@ -824,6 +839,14 @@ int ebi_materialize_static(ebi_column* c, const uint64_t* d_mask, int64_t chunk_
         std::snprintf(buf, sizeof buf,
                       "ebi_materialize_static: the query covers %u tiles, the fixed scratch holds at most %u "
                       "(use ebi_materialize)", tn, kStaticTiles);
+        return fail(EBI_E_INVALID, buf);
+    }
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev != c->device) {
+        char buf[128];
+        std::snprintf(buf, sizeof buf, "ebi_materialize_static: the column lives on device %d, device %d is current",
+                      c->device, dev);
         return fail(EBI_E_INVALID, buf);
     }
     unsigned long long* counts = nullptr;

@@ -11,6 +11,9 @@ using namespace ebi;
 
 struct ebi_column {
     cudaStream_t stream = nullptr;  // stream of open/close (allocation order)
+    int device = -1;                // the device current at open: every buffer of the column lives there
+    uint64_t device_bytes = 0;      // device memory the column holds (resident file, tables, query scratch)
+    long long copy_wait = kWaitCycles;  // limit of its kernels' waits for bulk copies (ebi_column_set_copy_wait)
     int scheme = 0;
     uint64_t n_records = 0, n_chunks = 0, file_len = 0, footer_off = 0;
     std::vector<ChunkDesc> chunks;

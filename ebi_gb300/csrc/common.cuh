@@ -20,6 +20,7 @@ namespace ebi {
 
 constexpr uint64_t kNanBits = 0x7ff8000000000000ull;  // f64::NAN.to_bits()
 constexpr int kFilePad = 64;                           // zero bytes after the file in HBM
+constexpr long long kWaitCycles = 4000000000ll;        // default limit of a bounded wait: about 2 s at 2 GHz
 
 // Chunk geometry (GeneralChunkHandle, decoder.rs:283-352).
 struct ChunkDesc {
@@ -152,6 +153,7 @@ struct QueryParams {
     int pred_on;               // value codecs: the predicate selects rows (filter, filter+agg, filter_materialize)
     uint32_t stage_bytes;      // Gorilla: shared-memory staging size per chunk (0: read through L1)
     const double* dec_tab;     // Elf / ElfOnChimp: decimal tables of elf_dev.cuh (device memory)
+    long long copy_wait;       // limit (SM clocks) of a kernel's waits for its bulk copies to land; <= 0: one look
 };
 
 // Passes of the value-codec kernels (one CTA per chunk).

@@ -215,23 +215,30 @@ struct Compiled {
     std::string why;  // the failure, when kernel is null
 };
 
-// Compiles the walk with a program object for this device's architecture.
-Compiled compile(const std::string& program) {
+// The current device's architecture as an NVRTC option ("-arch=sm_103a"),
+// or an empty string when no device answers.
+std::string current_arch() {
+    int dev = 0, major = 0, minor = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
+        return std::string();
+    return "-arch=sm_" + std::to_string(major * 10 + minor) + "a";
+}
+
+// Compiles the walk with a program object for the architecture `arch`.
+Compiled compile(const std::string& program, const std::string& arch) {
     Compiled out;
     const Nvrtc& N = nvrtc();
     if (!N.ok) {
         out.why = N.why;
         return out;
     }
-    int dev = 0, major = 0, minor = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess) {
+    if (arch.empty()) {
         out.why = "no device";
         return out;
     }
     const std::string src = std::string(kFusedSource) + "\n" + program;
-    const std::string arch = "-arch=sm_" + std::to_string(major * 10 + minor) + "a";
     const char* opts[] = {arch.c_str(), "-std=c++17"};
     nvrtcProgram p = nullptr;
     if (N.create(&p, src.c_str(), "ebi_expr_fused_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
@@ -292,15 +299,18 @@ cudaKernel_t fused_jit_kernel(const std::vector<Instr>& prog, const uint32_t* fi
     // distinct programs, new ones run on the interpreter.
     constexpr size_t kMaxCompiled = 256;
     static std::mutex mu;
+    // keyed by the device architecture too: a cubin runs on the architecture it was built for
     static std::map<std::string, Compiled> cache;
+    const std::string arch = current_arch();
+    const std::string key = arch + "\n" + program;
     std::lock_guard<std::mutex> lock(mu);
-    auto it = cache.find(program);
+    auto it = cache.find(key);
     if (it == cache.end()) {
         if (cache.size() >= kMaxCompiled) {
             *why = "compiled-pass cache full";
             return nullptr;
         }
-        it = cache.emplace(program, compile(program)).first;
+        it = cache.emplace(key, compile(program, arch)).first;
     }
     if (!it->second.kernel) *why = it->second.why;
     return it->second.kernel;

@@ -32,9 +32,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) gorilla_kernel(QueryParams 
             bulk_g2s(smem + 16, src, static_cast<uint32_t>(span), bar);
         }
         __syncwarp();
-        bool arrived = mbar_wait(bar, 0);
+        bool arrived = mbar_wait(bar, 0, q.copy_wait);
         if (!__all_sync(kFull, arrived)) {
-            // give the copy a second bounded wait before the CTA leaves, then report it
+            // give the copy a second wait (full limit) before the CTA leaves, then report it
             mbar_wait(bar, 0);
             if (lane == 0) {
                 set_status(acc, EBI_E_CUDA);

@@ -92,6 +92,21 @@ int ebi_column_close(ebi_column* col);
 /* NativeFileFooter::{number_of_records, number_of_chunks} (format/native.rs:117-124) */
 uint64_t ebi_column_num_records(const ebi_column* col);
 uint64_t ebi_column_num_chunks(const ebi_column* col);
+/* Device memory the column holds, in bytes: the resident file, its tables and
+ * the query scratch it allocated on first use.  No counterpart in the
+ * reference (its Decoder reads from host memory). */
+uint64_t ebi_column_device_bytes(const ebi_column* col);
+/* Limit, in SM clock cycles, of the bounded waits with which the column's
+ * kernels wait for their bulk copies (shared-memory staging of BUFF tiles
+ * whose chunks are wider than 32 bits or constant, and of Gorilla chunks):
+ * a query whose copy has not landed by then fails with EBI_E_CUDA instead of
+ * waiting on, and the column stays usable.  Negative restores the default
+ * (about two seconds); 0 makes each such wait a single look.  A kernel still
+ * waits out its copies in flight (full limit) before it exits.  No
+ * counterpart in the reference (its reader has no device copies to wait
+ * for); for failure-path tests and for callers that want a query to give up
+ * early. */
+int ebi_column_set_copy_wait(ebi_column* col, int64_t cycles);
 /* NativeFileConfig::compression_scheme (format/native.rs:45-49) */
 int ebi_column_scheme(const ebi_column* col);
 /* GeneralChunkHandle::{physical_offset, chunk_size, logical_offset,
@@ -125,7 +140,8 @@ int ebi_materialize(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, d
  * each device looks up the array's address (cudaGetSymbolAddress, with that
  * device current); make that first call before any stream capture.  The array
  * is shared by every column on a device: calls that overlap in time (other
- * streams or host threads) race on it and must be serialised by the caller. */
+ * streams or host threads) race on it and must be serialised by the caller.
+ * The column's device must be current (else EBI_E_INVALID). */
 int ebi_materialize_static(ebi_column* col, const uint64_t* d_mask, int64_t chunk_id, double* d_out,
                            uint64_t out_cap, uint64_t* n_out, void* stream);
 

@@ -1,6 +1,8 @@
 """ebi_materialize_static (the materialize that allocates nothing) against
-ebi_materialize, through the C ABI, two calls in a row.  Collected last; it
-also passes alone in a fresh process."""
+ebi_materialize and against the oracle's Decoder::materialize on the same
+bytes, through the C ABI, two calls in a row; on a freshly opened column
+its calls leave the column's device memory unchanged (no query scratch is
+allocated).  Collected last; it also passes alone in a fresh process."""
 import ctypes as C
 
 import numpy as np
@@ -49,16 +51,38 @@ def columns():
 
 @pytest.mark.parametrize("codec,values,chunk,scale", columns(), ids=lambda x: x if isinstance(x, str) else None)
 def test_static_matches_materialize_twice(codec, values, chunk, scale):
-    d = E.Decoder(E.encode(values, codec, chunk, scale))
+    data = E.encode(values, codec, chunk, scale)
+    d = E.Decoder(data)
+    o = O.Decoder(data)
     rng = np.random.default_rng(5)
     n = d.n_records
-    for mask in (None, random_mask(n, 0.2, rng), O.mask_from_rows([], n)):
+    masks = (None, random_mask(n, 0.2, rng), O.mask_from_rows([], n))
+    # a fresh column: the static calls come first and allocate nothing on the device
+    held = d.device_bytes
+    for mask in masks:
         for cid in (None, 1):
-            want = d.materialize(mask, cid).cpu().numpy()
+            want = o.materialize(mask, cid)
             for _ in range(2):  # two calls in a row reuse the same fixed scratch
                 rc, got = static_materialize(d, mask, cid, n)
                 assert rc == 0, _native.lib().ebi_last_error()
                 assert same_f64(got, want), (codec, cid)
+    assert d.device_bytes == held
+    # the allocating entry point agrees (and its first use does allocate the column's scratch)
+    for mask in masks:
+        for cid in (None, 1):
+            rc, got = static_materialize(d, mask, cid, n)
+            assert rc == 0 and same_f64(got, d.materialize(mask, cid).cpu().numpy()), (codec, cid)
+    if codec != "buff":
+        assert d.device_bytes > held
+    d.close()
+
+
+@pytest.mark.skipif(torch.cuda.device_count() < 2, reason="needs a second GPU")
+def test_static_rejects_another_current_device():
+    d = E.Decoder(E.encode(np.arange(100.0), "gorilla", ("record_count", 32)), device="cuda:0")
+    with torch.cuda.device(1):
+        rc, _ = static_materialize(d, None, None, 100)
+    assert rc == E.InvalidArgument.code and b"device" in _native.lib().ebi_last_error()
     d.close()
 
 
