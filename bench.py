@@ -286,8 +286,8 @@ def cpu_figures(data: bytes, wl, threads: int, n_all: int = 9, n_one: int = 3):
     dall.filter_agg(preds[0])  # first touch of the file's pages
     fused = time_cpu_queries(dall, preds, n_all)
     two = time_cpu_queries(dall, preds, max(n_one, len(preds)), two_call=True, aggregates=wl.aggregates)
-    one = time_cpu_queries(O.Decoder(data, threads=1), preds, n_one)
-    gbs = lambda ts: round(8.0 * n / statistics.median(ts) / 1e9, 3)
+    one = time_cpu_queries(O.Decoder(data, threads=1), preds, n_one) if n_one else []
+    gbs = lambda ts: round(8.0 * n / statistics.median(ts) / 1e9, 3) if ts else None
     qs = ", ".join(k for k, _, _ in wl.ranges)
     return {"value": gbs(fused), "unit": UNIT, "cores": threads, "kind": "port",
             "mean_value": round(8.0 * n * len(fused) / sum(fused) / 1e9, 3),
@@ -297,6 +297,112 @@ def cpu_figures(data: bytes, wl, threads: int, n_all: int = 9, n_one: int = 3):
             "sample": f"median of {len(fused)} fused filter+aggregate queries ({qs} cycled) over the full {n}-row "
                       f"column, chunk-parallel C restatement of ebi's Decoder on {threads} host threads; threads_1: "
                       f"{len(one)} queries on one thread; two_call: {len(two)} queries as the reference's two calls"}
+
+
+def value_config(name, dev, steps, warmup, flush, clean):
+    """One of the other single-column configurations, measured as the headline is: each step one
+    fused filter + aggregate query with L2 flushed before it; the median device time of the query
+    and of its codec kernel (roofline over the compressed chunk bytes plus the bitmask), the last
+    query against the oracle, and the oracle port on all host cores over the same queries."""
+    import torch
+
+    import ebi_gb300 as E
+    from oracle import oracle as O
+
+    wl = Workload(name, DEFAULT_ROWS[name])
+    data = wl.build()
+    dec = E.Decoder(data, device=str(dev))
+    dec.set_timing(True)
+    mask = dec.new_mask()
+    qs = wl.queries()
+    alg = sum(dec.chunk_info(c)[1] for c in range(dec.n_chunks)) + 8 * dec.mask_words
+    scan, total = [], []
+    for i in range(warmup + steps):
+        flush.fill_(i & 0xFF)
+        clean.sum()
+        torch.cuda._sleep(1_000_000)
+        dec.filter_agg(qs[i % len(qs)][1], out=mask, aggregates=wl.aggregates)
+        t = dec.segmented_execution_times()
+        if i >= warmup:
+            scan.append(t["scan_ms"])
+            total.append(t["total_ms"])
+    _, p = qs[-1]
+    _, s, mn, mx, cnt = dec.filter_agg(p, out=mask)
+    o = O.Decoder(data, threads=os.cpu_count() or 1)
+    om, os_, omn, omx = o.filter_agg(O.rng(1, p.rng.start.value, 1, p.rng.end.value))
+    exact = wl.codec == "buff"
+    same = (np.array_equal(mask.cpu().numpy().view(np.uint64)[: len(om)], om) and (mn, mx) == (omn, omx)
+            and (s == os_ if exact else abs(s - os_) <= 1e-12 * max(abs(os_), 1e-300)))
+    peak, _ = measured_peak()
+    ks, ts = statistics.median(scan) / 1e3, statistics.median(total) / 1e3
+    cpu = cpu_figures(data, wl, os.cpu_count() or 1, n_all=5, n_one=0)
+    dec.close()
+    return {"workload": wl.describe, "rows": wl.rows, "chunk_rows": wl.chunk, "column_bytes": len(data),
+            "queries": [k for k, _, _ in wl.ranges], "value": round(8.0 * wl.rows / ts / 1e9, 3), "unit": UNIT,
+            "ms_per_step": round(1e3 * ts, 4), "kernel": KERNELS[name], "kernel_ms": round(1e3 * ks, 4),
+            "roofline": {"bound": "hbm", "algorithmic_bytes_per_launch": alg,
+                         "achieved": round(alg / ks / 1e9, 1), "peak": peak, "frac": round(alg / ks / 1e9 / peak, 4)},
+            "parity_check": {"bitmask_min_max_bit_exact_sum_within_tolerance": bool(same),
+                             "sum_rel_diff": abs(s - os_) / max(abs(os_), 1e-300), "rows_selected": int(cnt)},
+            "cpu_baseline": {k: cpu[k] for k in ("value", "cores", "kind")}}
+
+
+def materialize_config(dec, data, dev, steps, warmup, flush, clean):
+    """C2's full materialize: every value of the headline column written out (8 B a row, the
+    write-bound BUFF decode), median device time over L2-flushed steps, checked against the oracle."""
+    import torch
+
+    from oracle import oracle as O
+
+    n = dec.n_records
+    out = torch.empty(n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ts = []
+    for i in range(warmup + steps):
+        flush.fill_(i & 0xFF)
+        clean.sum()
+        torch.cuda._sleep(1_000_000)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dec.materialize(out=out)
+        e1.record(stream)
+        e1.synchronize()
+        if i >= warmup:
+            ts.append(e0.elapsed_time(e1) / 1e3)
+    t = statistics.median(ts)
+    want = O.Decoder(data, threads=os.cpu_count() or 1).materialize()
+    same = bool(np.array_equal(out.cpu().numpy().view(np.uint64), want.view(np.uint64)))
+    col = sum(dec.chunk_info(c)[1] for c in range(dec.n_chunks))
+    alg = col + 8 * n
+    peak, _ = measured_peak()
+    return {"workload": "C2 full materialize: every value of the headline column written to a device array",
+            "rows": n, "value": round(8.0 * n / t / 1e9, 3), "unit": UNIT, "ms_per_step": round(1e3 * t, 4),
+            "roofline": {"bound": "hbm", "algorithmic_bytes_per_launch": alg, "read_bytes": col, "write_bytes": 8 * n,
+                         "achieved": round(alg / t / 1e9, 1), "peak": peak, "frac": round(alg / t / 1e9 / peak, 4),
+                         "scope": "whole call (decode + write)"},
+            "parity_check": {"values_bit_exact": same}}
+
+
+def config_results(args, dec, data, dev, flush, clean):
+    """The other configurations in one object of the headline line: C1, C3a, C3b (and the Elf
+    codecs on C3a's series), C2's full materialize, C4 batched and C5 serving at full size."""
+    import copy
+
+    res = {"C2_materialize": materialize_config(dec, data, dev, 10, 3, flush, clean)}
+    for key, name in (("C1_gorilla", "gorilla"), ("C3a_chimp128", "chimp128"), ("C3b_rle", "rle"),
+                      ("C3a_series_elf", "elf"), ("C3a_series_elf_on_chimp", "elf_on_chimp")):
+        res[key] = value_config(name, dev, 20, 3, flush, clean)
+        log(f"config {key}: {res[key]['kernel_ms']} ms kernel")
+    a = copy.copy(args)
+    a.scale, a.steps, a.warmup = 1.0, 10, 3
+    b = batched_line(a)
+    res["C4_batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "queries_per_s", "config", "roofline",
+                                           "autotune", "parity_check")}
+    a.steps = 40
+    v = serving_line(a)
+    res["C5_serving"] = {k: v[k] for k in ("value", "unit", "plain_queries_per_s", "speedup_vs_plain",
+                                           "results_equal_alone_and_in_mix", "poisson", "config", "server_stats")}
+    return res
 
 
 def run_reference(args):
@@ -365,19 +471,28 @@ def mixed_column(rng, codec, n, seed):
 
 
 def build_mixed(n_cols, lo, hi, seed, dev):
-    """n_cols columns of log-uniform length in [lo, hi], codec drawn uniformly (seeded)."""
+    """n_cols columns of log-uniform length in [lo, hi], codec drawn uniformly (seeded).
+    Columns are generated and encoded on host threads (each from its own seeded generator),
+    then opened on the device in order."""
+    from concurrent.futures import ThreadPoolExecutor
+
     import ebi_gb300 as E
 
     rng = np.random.default_rng(seed)
     lens = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), n_cols))).astype(np.int64)
     codecs = rng.integers(0, len(MIXED_CODECS), n_cols)
-    decs, meta = [], []
     t = time.perf_counter()
-    for i in range(n_cols):
+
+    def make(i):
         codec = MIXED_CODECS[codecs[i]]
-        data = mixed_column(rng, codec, int(lens[i]), seed * 100003 + i)
+        return mixed_column(np.random.default_rng((seed, i)), codec, int(lens[i]), seed * 100003 + i)
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        datas = list(ex.map(make, range(n_cols)))
+    decs, meta = [], []
+    for i, data in enumerate(datas):
         decs.append(E.Decoder(data, device=str(dev)))
-        meta.append((codec, int(lens[i]), len(data)))
+        meta.append((MIXED_CODECS[codecs[i]], int(lens[i]), len(data)))
     log(f"built {n_cols} columns, {int(lens.sum())} rows, {sum(m[2] for m in meta)} B in {time.perf_counter() - t:.1f} s")
     return decs, meta
 
@@ -398,6 +513,10 @@ def column_range(codec, rng):
 
 
 def run_batched(args):
+    print(json.dumps(batched_line(args)), flush=True)
+
+
+def batched_line(args):
     """4,096 columns of log-uniform length 1K..4M, codec uniform over {Gorilla, Chimp128, BUFF, RLE};
     one step = filter+sum on every column as one batch (persistent mixed-codec launch, graph replay)."""
     import torch
@@ -453,11 +572,17 @@ def run_batched(args):
                          "kernel": "batch_kernel + batch_finalize_kernel (graph replay)", "peak_source": peak_kind},
             "autotune": info, "gpu_launches": int(launches),
             "parity_check": {"sum_and_count_equal_single_column_queries": bool(ok)}}
-    print(json.dumps(line), flush=True)
     batch.close()
+    for d in decs:
+        d.close()
+    return line
 
 
 def run_serving(args):
+    print(json.dumps(serving_line(args)), flush=True)
+
+
+def serving_line(args):
     """512 resident columns of log-uniform length 256K..16M, mixed codecs; Poisson arrivals; each request a
     random range plus one of sum/min/max over 1..8 columns.  Continuous batching vs plain per-query launches."""
     import torch
@@ -523,7 +648,9 @@ def run_serving(args):
             "saturated_requests": len(sat_reqs), "plain_requests": len(plain_reqs),
             "plain_queries_per_s": round(plain_qps, 1), "speedup_vs_plain": round(sat_qps / plain_qps, 2),
             "results_equal_alone_and_in_mix": bool(equal), "poisson": rates, "server_stats": st}
-    print(json.dumps(line), flush=True)
+    for d in decs:
+        d.close()
+    return line
 
 
 TPCH_ROWS = 59_986_052       # lineitem rows at scale factor 10
@@ -705,6 +832,8 @@ def main():
                                                                "batched", "serving", "tpch_q6", "tpch_q1"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="batched / serving: fraction of the configuration's columns to build")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="headline only: skip the other configurations (C1, C2 materialize, C3a, C3b, C4, C5)")
     args = ap.parse_args()
     wl = None
     if args.workload in ("tpch_q6", "tpch_q1"):
@@ -837,6 +966,9 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_figures(data, wl, os.cpu_count() or 1)
+    configs = None
+    if world == 1 and wl.name == "buff" and not args.no_configs:
+        configs = config_results(args, dec, data, dev, flush, clean)
 
     if rank == 0:
         line = {
@@ -866,6 +998,7 @@ def main():
             "cpu_baseline": cpu,
             "parity_check": check,
             "wall_ms_per_step": round(1e3 * (t1 - t0) / args.steps, 4),
+            "configs": configs,
         }
         print(json.dumps(line), flush=True)
     if dist:
