@@ -388,20 +388,38 @@ def config_results(args, dec, data, dev, flush, clean):
     codecs on C3a's series), C2's full materialize, C4 batched and C5 serving at full size."""
     import copy
 
-    res = {"C2_materialize": materialize_config(dec, data, dev, 10, 3, flush, clean)}
+    import torch
+
+    props = torch.cuda.get_device_properties(dev)
+    sampler = ClockSampler(f"GPU-{props.uuid}" if getattr(props, "uuid", None) else str(dev.index or 0))
+    sampler.start()
+    time.sleep(0.3)
+    spans = {}
+
+    def timed(key, fn):
+        t0 = time.perf_counter()
+        r = fn()
+        spans[key] = (t0, time.perf_counter())
+        return r
+
+    res = {"C2_materialize": timed("C2_materialize", lambda: materialize_config(dec, data, dev, 10, 3, flush, clean))}
     for key, name in (("C1_gorilla", "gorilla"), ("C3a_chimp128", "chimp128"), ("C3b_rle", "rle"),
                       ("C3a_series_elf", "elf"), ("C3a_series_elf_on_chimp", "elf_on_chimp")):
-        res[key] = value_config(name, dev, 20, 3, flush, clean)
+        res[key] = timed(key, lambda: value_config(name, dev, 20, 3, flush, clean))
         log(f"config {key}: {res[key]['kernel_ms']} ms kernel")
     a = copy.copy(args)
     a.scale, a.steps, a.warmup = 1.0, 10, 3
-    b = batched_line(a)
+    b = timed("C4_batched", lambda: batched_line(a))
     res["C4_batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "queries_per_s", "config", "roofline",
                                            "autotune", "parity_check")}
     a.steps = 40
-    v = serving_line(a)
+    v = timed("C5_serving", lambda: serving_line(a))
     res["C5_serving"] = {k: v[k] for k in ("value", "unit", "plain_queries_per_s", "speedup_vs_plain",
                                            "results_equal_alone_and_in_mix", "poisson", "config", "server_stats")}
+    time.sleep(0.2)
+    sampler.stop()
+    for key, (t0, t1) in spans.items():
+        res[key]["clocks"] = dict(sampler.summary(t0, t1), window="the whole configuration: column build and timed steps")
     return res
 
 

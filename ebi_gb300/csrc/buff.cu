@@ -61,10 +61,20 @@ __global__ void __launch_bounds__(kTileThreads) buff_count_kernel(QueryParams q,
 }
 
 // Materialization: the decoded values of the selected rows, in row order.
+// Each warp owns 1,024 consecutive rows of the tile and a contiguous run of
+// the output.  Its lanes form the deltas of their 32 rows each and put the
+// selected ones, compacted, into a padded shared-memory stage (one pad entry
+// per 32, so both the per-lane writes and the per-row reads are free of bank
+// conflicts); the warp then reads the stage back in output order, turns each
+// delta into its double and writes the run as consecutive doubles, 256 bytes
+// per store instruction.
+constexpr int kMatStage = 32 * 33;  // entries per warp
+constexpr size_t kMatSmem = size_t(kTileWarps) * kMatStage * sizeof(unsigned long long);
+
 template <int TB, typename D>
-__device__ void buff_mat_tile(const QueryParams& q, const BuffCtx& k, uint32_t tile, uint32_t begin,
+__device__ void buff_mat_tile(const QueryParams& q, const BuffCtx& k, uint32_t begin,
                               const unsigned long long* tile_offsets, unsigned long long base_row,
-                              unsigned int* warp_tot) {
+                              unsigned int* warp_tot, unsigned long long* stage) {
     const uint32_t r0 = begin + threadIdx.x * 32;
     const bool has_mask = q.in_mask != nullptr;
     uint32_t sel = 0;
@@ -86,39 +96,61 @@ __device__ void buff_mat_tile(const QueryParams& q, const BuffCtx& k, uint32_t t
     }
     if (lane == 31) warp_tot[wid] = inc;
     __syncthreads();
-    unsigned int before = 0;
-    for (int w = 0; w < wid; ++w) before += warp_tot[w];
-    unsigned long long pos;
-    if (has_mask) pos = tile_offsets[blockIdx.x] + before + (inc - cnt);
-    else pos = k.row_off + r0 - base_row;
-    if (!sel) return;
+    const unsigned int wcount = __shfl_sync(0xffffffffu, inc, 31);
+    if (wcount == 0) return;  // warp-uniform
+    unsigned long long wbase;
+    if (has_mask) {
+        unsigned int before = 0;
+        for (int w = 0; w < wid; ++w) before += warp_tot[w];
+        wbase = tile_offsets[blockIdx.x] + before;
+    } else {
+        // lane 0 holds rows, so every lane before the last holding any is full
+        wbase = k.row_off + begin + uint32_t(wid) * 1024u - base_row;
+    }
+    D* st = reinterpret_cast<D*>(stage) + wid * kMatStage;
+    unsigned int off = inc - cnt;
+#pragma unroll
     for (int i = 0; i < 32; ++i) {
-        if (!((sel >> i) & 1u)) continue;
-        const long long fixed = static_cast<long long>(static_cast<unsigned long long>(k.base) + static_cast<unsigned long long>(d[i]));
-        const double v = k.inv_scale != 0.0 ? static_cast<double>(fixed) * k.inv_scale : static_cast<double>(fixed) / k.scale;
-        if (pos < q.out_cap) q.out_vals[pos] = v;
-        ++pos;
+        if ((sel >> i) & 1u) {
+            st[off + (off >> 5)] = d[i];
+            ++off;
+        }
+    }
+    __syncwarp();
+    const unsigned long long base = static_cast<unsigned long long>(k.base);
+#pragma unroll 4
+    for (unsigned int j = lane; j < wcount; j += 32) {
+        const unsigned long long pos = wbase + j;
+        const long long fixed = static_cast<long long>(base + static_cast<unsigned long long>(st[j + (j >> 5)]));
+        if (pos < q.out_cap) q.out_vals[pos] = fixed_to_f64(fixed, k.frac, k.scale);
     }
 }
 
 template <typename D>
-__device__ void buff_mat_dispatch(const QueryParams& q, const BuffCtx& k, uint32_t tile, uint32_t begin,
-                                  const unsigned long long* offs, unsigned long long base_row, unsigned int* wt) {
+__device__ void buff_mat_dispatch(const QueryParams& q, const BuffCtx& k, uint32_t begin,
+                                  const unsigned long long* offs, unsigned long long base_row, unsigned int* wt,
+                                  unsigned long long* st) {
     switch (k.ok ? k.tb : 0) {
-        case 0: buff_mat_tile<0, D>(q, k, tile, begin, offs, base_row, wt); break;
-        case 1: buff_mat_tile<1, D>(q, k, tile, begin, offs, base_row, wt); break;
-        case 2: buff_mat_tile<2, D>(q, k, tile, begin, offs, base_row, wt); break;
-        case 3: buff_mat_tile<3, D>(q, k, tile, begin, offs, base_row, wt); break;
-        case 4: buff_mat_tile<4, D>(q, k, tile, begin, offs, base_row, wt); break;
-        case 5: buff_mat_tile<5, D>(q, k, tile, begin, offs, base_row, wt); break;
-        case 6: buff_mat_tile<6, D>(q, k, tile, begin, offs, base_row, wt); break;
-        default: buff_mat_tile<7, D>(q, k, tile, begin, offs, base_row, wt); break;
+        case 0: buff_mat_tile<0, D>(q, k, begin, offs, base_row, wt, st); break;
+        case 1: buff_mat_tile<1, D>(q, k, begin, offs, base_row, wt, st); break;
+        case 2: buff_mat_tile<2, D>(q, k, begin, offs, base_row, wt, st); break;
+        case 3: buff_mat_tile<3, D>(q, k, begin, offs, base_row, wt, st); break;
+        case 4: buff_mat_tile<4, D>(q, k, begin, offs, base_row, wt, st); break;
+        case 5: buff_mat_tile<5, D>(q, k, begin, offs, base_row, wt, st); break;
+        case 6: buff_mat_tile<6, D>(q, k, begin, offs, base_row, wt, st); break;
+        default: buff_mat_tile<7, D>(q, k, begin, offs, base_row, wt, st); break;
     }
 }
 
-__global__ void __launch_bounds__(kTileThreads) buff_materialize_kernel(QueryParams q, uint32_t tile_base,
-                                                                    const unsigned long long* tile_offsets,
-                                                                    unsigned long long base_row) {
+// WIDE: some readable chunk of the column is more than 32 bits wide (64-bit
+// deltas); the narrow build keeps 32-bit deltas and fits three CTAs per SM.
+// quiet: no chunk the pass reads can raise, so the chunks' accumulators are
+// left untouched and no fold follows.
+template <bool WIDE>
+__global__ void __launch_bounds__(kTileThreads, WIDE ? 2 : 3) buff_materialize_kernel(
+    QueryParams q, uint32_t tile_base, const unsigned long long* tile_offsets, unsigned long long base_row,
+    bool quiet) {
+    extern __shared__ unsigned long long mat_stage[];
     __shared__ BuffCtx k;
     __shared__ unsigned int warp_tot[kTileWarps];
     const uint32_t tile = tile_base + blockIdx.x;
@@ -126,12 +158,17 @@ __global__ void __launch_bounds__(kTileThreads) buff_materialize_kernel(QueryPar
     if (threadIdx.x == 0) {
         // with a bitmask, tiles without selected rows were counted as 0 and
         // their chunk may be unselected: only tiles that select rows read
-        buff_setup(q, t.chunk, false, k);
+        buff_setup(q, t.chunk, false, k, !quiet);
         if (q.in_mask && tile_offsets[blockIdx.x + 1] == tile_offsets[blockIdx.x]) k.ok = 0;
     }
     __syncthreads();
-    if (k.ok && k.bits > 32) buff_mat_dispatch<unsigned long long>(q, k, tile, t.begin, tile_offsets, base_row, warp_tot);
-    else buff_mat_dispatch<uint32_t>(q, k, tile, t.begin, tile_offsets, base_row, warp_tot);
+    if constexpr (WIDE) {
+        if (k.ok && k.bits > 32) {
+            buff_mat_dispatch<unsigned long long>(q, k, t.begin, tile_offsets, base_row, warp_tot, mat_stage);
+            return;
+        }
+    }
+    buff_mat_dispatch<uint32_t>(q, k, t.begin, tile_offsets, base_row, warp_tot, mat_stage);
 }
 
 
@@ -165,9 +202,15 @@ cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_
 }
 
 cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles,
-                                    const unsigned long long* tile_offsets, uint64_t base_row, cudaStream_t s) {
+                                    const unsigned long long* tile_offsets, uint64_t base_row, bool wide,
+                                    bool quiet, cudaStream_t s) {
     if (n_tiles == 0) return cudaSuccess;
-    buff_materialize_kernel<<<n_tiles, kTileThreads, 0, s>>>(q, tile_begin, tile_offsets, base_row);
+    const void* fn = wide ? reinterpret_cast<const void*>(buff_materialize_kernel<true>)
+                          : reinterpret_cast<const void*>(buff_materialize_kernel<false>);
+    const cudaError_t e = allow_dynamic_smem(fn, kMatSmem);
+    if (e != cudaSuccess) return e;
+    if (wide) buff_materialize_kernel<true><<<n_tiles, kTileThreads, kMatSmem, s>>>(q, tile_begin, tile_offsets, base_row, quiet);
+    else buff_materialize_kernel<false><<<n_tiles, kTileThreads, kMatSmem, s>>>(q, tile_begin, tile_offsets, base_row, quiet);
     count_launch();
     return cudaGetLastError();
 }

@@ -25,6 +25,35 @@ __device__ inline int64_t buff_fixed(double value, int32_t frac) {
 
 __device__ __forceinline__ uint32_t bit_length(uint64_t x) { return x ? 64u - __clzll(static_cast<long long>(x)) : 0u; }
 
+// A row's value, (fixed as f64) / 2^frac (buff/decode.rs:5-17 divides by
+// 2.0f64.powi(frac)), assembled on the integer pipes: the f64 conversion
+// rounds |fixed| to 53 significant bits, ties to even (IEEE 754
+// roundTiesToEven), and dividing by a power of two only lowers the exponent,
+// exactly, while the result stays a normal double.  The remaining cases
+// (frac > 1022, a subnormal result) take the f64 arithmetic itself.
+__device__ __forceinline__ double fixed_to_f64(long long fixed, uint32_t frac, double scale) {
+    const unsigned long long u = static_cast<unsigned long long>(fixed);
+    const unsigned long long sign = u & 0x8000000000000000ull;
+    const unsigned long long m = sign ? 0ull - u : u;
+    if (m == 0) return 0.0;
+    int e = 63 - __clzll(static_cast<long long>(m));  // m in [2^e, 2^(e+1))
+    unsigned long long mant;
+    if (e <= 52) {
+        mant = m << (52 - e);
+    } else {
+        const int sh = e - 52;
+        mant = m >> sh;
+        const unsigned long long rem = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1ull))) {
+            ++mant;
+            if (mant >> 53) { mant >>= 1; ++e; }
+        }
+    }
+    if (frac > 1022u || e + 1023 <= static_cast<int>(frac)) return static_cast<double>(fixed) / scale;
+    const unsigned long long ex = static_cast<unsigned long long>(e + 1023 - static_cast<int>(frac));
+    return __longlong_as_double(static_cast<long long>(sign | (ex << 52) | (mant & 0xfffffffffffffull)));
+}
+
 enum : uint32_t { SIDE_ABSENT = 0, SIDE_ALL = 1, SIDE_NONE = 2, SIDE_CMP = 3 };
 
 // Predicate compiled into the delta domain of one chunk, exactly as the

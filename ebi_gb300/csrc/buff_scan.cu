@@ -605,13 +605,8 @@ cudaError_t launch_buff_scan(const QueryParams& q, const BuffChunkInfo* info, ui
                             bool fast_ok, cudaStream_t s) {
     if (n_tiles == 0) return cudaSuccess;
     const size_t smem = L.data_offset + size_t(L.stages) * L.stage_bytes;
-    static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(buff_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    const cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(buff_scan_kernel), smem);
+    if (e != cudaSuccess) return e;
     if ((grid < n_tiles ? grid : n_tiles) > kScanSlots) return cudaErrorInvalidConfiguration;
     buff_scan_kernel<<<grid < n_tiles ? grid : n_tiles, kScanThreads, smem, s>>>(q, info, tile_begin, n_tiles, L, T,
                                                                                res, frac, fast_ok ? 1u : 0u);

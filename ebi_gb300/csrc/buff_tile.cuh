@@ -33,7 +33,9 @@ struct BuffCtx {
     uint64_t lthr, rthr, etgt;
 };
 
-__device__ void buff_setup(const QueryParams& q, uint32_t c, bool has_mask, BuffCtx& k) {
+// mark = false: the chunk's accumulator is left untouched (a pass whose
+// chunks cannot raise and that folds nothing).
+__device__ void buff_setup(const QueryParams& q, uint32_t c, bool has_mask, BuffCtx& k, bool mark = true) {
     const ChunkDesc cd = q.chunks[c];
     ChunkAcc* acc = q.acc + c;
     k.ok = 0;
@@ -41,10 +43,13 @@ __device__ void buff_setup(const QueryParams& q, uint32_t c, bool has_mask, Buff
     k.row_off = cd.row_off;
     k.selected = has_mask ? acc->selected : static_cast<uint32_t>(q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
     if (!k.selected) return;
-    if (!has_mask && acc->selected == 0) acc->selected = 1;  // finalize folds selected chunks
+    if (mark && !has_mask && acc->selected == 0) acc->selected = 1;  // finalize folds selected chunks
     // the header facts were read and checked at open (the chunk's status)
     const BuffChunkInfo ci = q.binfo[c];
-    if (ci.status) { set_status(acc, ci.status); return; }
+    if (ci.status) {
+        if (mark) set_status(acc, ci.status);
+        return;
+    }
     k.base = ci.base;
     k.bits = ci.bits;
     k.frac = ci.frac;

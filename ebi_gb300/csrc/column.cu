@@ -29,6 +29,30 @@ static thread_local std::string g_last_error;
 void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 
+cudaError_t allow_dynamic_smem(const void* fn, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    struct Grant {
+        const void* fn;
+        int dev;
+        size_t bytes;
+    };
+    static std::mutex mu;
+    static std::vector<Grant> grants;
+    std::lock_guard<std::mutex> lk(mu);
+    Grant* g = nullptr;
+    for (Grant& x : grants)
+        if (x.fn == fn && x.dev == dev) g = &x;
+    if (g && g->bytes >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    if (e != cudaSuccess) return e;
+    if (g) g->bytes = bytes;
+    else grants.push_back(Grant{fn, dev, bytes});
+    return cudaSuccess;
+}
+
 static int fail(int code, const std::string& msg) {
     set_last_error(msg);
     return code;
@@ -276,6 +300,23 @@ int mark_scan(ebi_column* c, cudaStream_t s) {
     return EBI_OK;
 }
 
+// Ends a pass that cannot raise and folds nothing (a quiet BUFF materialize):
+// one synchronisation, no finalize launch.
+int finish_quiet(ebi_column* c, cudaStream_t s) {
+    if (c->timing) CK(cudaEventRecord(c->ev[1], s));
+    CK(cudaStreamSynchronize(s));
+    c->last.kernels = ebi_kernel_launches() - c->launches_at_start;
+    if (c->timing) {
+        float a = 0.f, t = 0.f;
+        CK(cudaEventElapsedTime(&a, c->scan_marked ? c->ev[3] : c->ev[0], c->ev[1]));
+        CK(cudaEventElapsedTime(&t, c->ev[0], c->ev[1]));
+        c->last.scan_ms = a;
+        c->last.finalize_ms = 0.f;
+        c->last.total_ms = t;
+    }
+    return EBI_OK;
+}
+
 // Enqueues finalize (unless the scan kernel already folded, or left exact
 // totals for the host to scale), copies the result back and waits.
 int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
@@ -465,7 +506,14 @@ int run_materialize(ebi_column* c, const uint64_t* d_mask, int64_t chunk_id, dou
         CK(launch_tile_scan(c->d_tile_counts, c->d_tile_offsets, tn, s));
     }
     const uint64_t base_row = chunk_id >= 0 && static_cast<uint64_t>(chunk_id) < c->n_chunks ? c->chunks[chunk_id].row_off : 0;
-    CK(launch_buff_materialize(q, tb, tn, c->d_tile_offsets, base_row, s));
+    // without a bitmask over readable chunks nothing can raise: no fold
+    const bool quiet = !d_mask && c->buff_all_readable;
+    CK(launch_buff_materialize(q, tb, tn, c->d_tile_offsets, base_row, c->buff_max_bits > 32, quiet, s));
+    if (quiet) {
+        if (int st = finish_quiet(c, s)) return st;
+        if (n_out) *n_out = total;
+        return EBI_OK;
+    }
     if (d_mask) CK(cudaMemcpyAsync(&c->h_res->count, c->d_tile_offsets + tn, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (d_mask) total = c->h_res->count;
@@ -873,14 +921,20 @@ int ebi_materialize_static(ebi_column* c, const uint64_t* d_mask, int64_t chunk_
             return fail(EBI_E_INVALID, "output buffer smaller than the values to write");
         }
         const uint64_t base_row = chunk_id >= 0 && static_cast<uint64_t>(chunk_id) < c->n_chunks ? c->chunks[chunk_id].row_off : 0;
-        CK(launch_buff_materialize(q, tb, tn, offsets, base_row, s));
+        const bool quiet = c->buff_all_readable;  // nothing can raise: no fold
+        CK(launch_buff_materialize(q, tb, tn, offsets, base_row, c->buff_max_bits > 32, quiet, s));
+        if (quiet) {
+            if (int st3 = finish_quiet(c, s)) return st3;
+            if (n_out) *n_out = total;
+            return EBI_OK;
+        }
     } else {
         q.tile_counts = counts;
         if (c->scheme == EBI_BUFF) {
             CK(launch_buff_count(q, tb, tn, s));
             CK(launch_tile_scan(counts, offsets, tn, s));
             const uint64_t base_row = chunk_id >= 0 && static_cast<uint64_t>(chunk_id) < c->n_chunks ? c->chunks[chunk_id].row_off : 0;
-            CK(launch_buff_materialize(q, tb, tn, offsets, base_row, s));
+            CK(launch_buff_materialize(q, tb, tn, offsets, base_row, c->buff_max_bits > 32, false, s));
         } else {
             CK(launch_values(c, q, tb, tn, VAL_COUNT, nullptr, s));
             CK(launch_tile_scan(counts, offsets, tn, s));

@@ -937,13 +937,10 @@ int run_fused(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<
     // grid: the CTAs that fit the device at once (each keeps running sums);
     // the compiled walk decodes and aggregates in registers
     const size_t smem = jit ? 0 : fuse_smem(P.n_cols, P.n_aggs);
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(expr_buff_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(fuse_smem(kFuseCols, kMaxAggs))) != cudaSuccess
-            ? cudaGetLastError()
-            : cudaFuncSetAttribute(expr_buff_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(fuse_smem(kFuseCols, kMaxAggs)));
-    if (attr != cudaSuccess) return cuda_fail(attr, "expr_buff_fused shared memory");
+    if (!jit) {
+        const cudaError_t attr = allow_dynamic_smem(kernel, smem);
+        if (attr != cudaSuccess) return cuda_fail(attr, "expr_buff_fused shared memory");
+    }
     int dev = 0, sms = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1111,8 +1108,7 @@ int run_pass(ebi_column* const* cols, ebi_aggregation* aggs, const std::vector<u
     // grid: the CTAs that fit the device at once (each keeps running sums)
     const uint64_t items_cap = total_vals / kExprItem + C + 1;
     const size_t smem = size_t(P.n_aggs) * kExprThreads * sizeof(RunAcc);
-    static const cudaError_t attr = cudaFuncSetAttribute(expr_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         static_cast<int>(kMaxAggs * kExprThreads * sizeof(RunAcc)));
+    const cudaError_t attr = allow_dynamic_smem(reinterpret_cast<const void*>(expr_eval), smem);
     if (attr != cudaSuccess) return done(cuda_fail(attr, "expr_eval shared memory"));
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);

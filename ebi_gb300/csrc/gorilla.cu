@@ -69,11 +69,8 @@ cudaError_t launch_gorilla(const QueryParams& q, uint32_t chunk_begin, uint32_t 
     if (n_chunks == 0) return cudaSuccess;
     const uint32_t grid = (n_chunks + kWarpsPerCta - 1) / kWarpsPerCta;
     const size_t smem = q.stage_bytes ? 16 + size_t(q.stage_bytes) : 16;
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(gorilla_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
-    }
+    const cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(gorilla_kernel), smem);
+    if (e != cudaSuccess) return e;
     gorilla_kernel<<<grid, kWarpsPerCta * 32, smem, s>>>(q, chunk_begin, n_chunks, mode, chunk_offsets);
     count_launch();
     return cudaGetLastError();

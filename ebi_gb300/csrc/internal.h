@@ -14,6 +14,10 @@ namespace ebi {
 // Counts kernel launches (ebi_kernel_launches()).
 void count_launch(uint64_t n = 1);
 void set_last_error(const std::string& msg);
+// Raises fn's dynamic shared-memory limit to at least `bytes` on the current
+// device (the limit belongs to the function in each device's context); a
+// no-op below the 48 KB default and once a device already allows as much.
+cudaError_t allow_dynamic_smem(const void* fn, size_t bytes);
 
 // Tiles of a column: chunk c owns tiles [first_tile[c], first_tile[c + 1]).
 struct TileMap {
@@ -41,8 +45,13 @@ cudaError_t launch_buff_scan(const QueryParams& q, const BuffChunkInfo* info, ui
 cudaError_t launch_buff_count(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles, cudaStream_t s);
 // Writes the decoded values of the selected rows at tile_offsets[tile - tile_begin] + rank
 // (with a bitmask) or at their row - first row of the query (without).
+// wide: some readable chunk is more than 32 bits wide (else the kernel built
+// for 32-bit deltas runs).  quiet: every chunk the pass reads is readable and
+// no bitmask is given, so the chunks' accumulators are left untouched and the
+// caller folds nothing.
 cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, uint32_t n_tiles,
-                                    const unsigned long long* tile_offsets, uint64_t base_row, cudaStream_t s);
+                                    const unsigned long long* tile_offsets, uint64_t base_row, bool wide, bool quiet,
+                                    cudaStream_t s);
 
 // ---- register-streaming BUFF scan (buff_stream.cu) -------------------------
 // Columns whose readable chunks are all 8..32 bits wide.  A unit is 2,048

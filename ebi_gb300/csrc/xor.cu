@@ -14,14 +14,9 @@ __global__ void __launch_bounds__(kXorThreads, 2) xor_kernel(QueryParams q, uint
 template <int CODEC>
 cudaError_t launch_codec(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                          const unsigned long long* chunk_offsets, cudaStream_t s) {
-    static bool configured = false;  // per process; the attribute is per function
     constexpr size_t bytes = xor_smem_bytes(CODEC);
-    if (!configured) {
-        const cudaError_t e = cudaFuncSetAttribute(xor_kernel<CODEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   static_cast<int>(bytes));
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    const cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(xor_kernel<CODEC>), bytes);
+    if (e != cudaSuccess) return e;
     xor_kernel<CODEC><<<n_chunks, kXorThreads, bytes, s>>>(q, chunk_begin, mode, chunk_offsets);
     count_launch();
     return cudaGetLastError();
