@@ -18,7 +18,7 @@ EXPORTS = [
     "ebi_filter", "ebi_filter_materialize", "ebi_sum", "ebi_min", "ebi_max", "ebi_filter_agg",
     "ebi_encode", "ebi_free", "ebi_last_error", "ebi_kernel_launches", "ebi_column_set_timing",
     "ebi_column_last_times", "ebi_materialize_static", "ebi_batch_create", "ebi_batch_run",
-    "ebi_batch_get_info", "ebi_batch_destroy", "ebi_server_create", "ebi_server_submit", "ebi_server_poll",
+    "ebi_batch_get_info", "ebi_batch_get_trials", "ebi_batch_set_tuning_cache", "ebi_batch_destroy", "ebi_server_create", "ebi_server_submit", "ebi_server_poll",
     "ebi_server_replay", "ebi_server_get_stats", "ebi_server_destroy", "ebi_run_plain", "ebi_mask_from_rows",
     "ebi_rows_from_mask", "ebi_aggregate",
 ]
@@ -46,7 +46,15 @@ class BatchResult(C.Structure):
 class BatchInfo(C.Structure):
     """ebi_batch_info"""
     _fields_ = [("queries", C.c_uint64), ("items", C.c_uint64), ("chunks", C.c_uint64), ("shape", C.c_int32),
-                ("ctas_per_sm", C.c_uint32), ("order", C.c_uint32), ("shape_ms", C.c_double * 4)]
+                ("ctas_per_sm", C.c_uint32), ("order", C.c_uint32), ("shape_ms", C.c_double * 4),
+                ("buff_tiles", C.c_uint32 * 3), ("value_chunks", C.c_uint32 * 3), ("gorilla_chunks", C.c_uint32 * 3),
+                ("trials", C.c_uint32), ("from_cache", C.c_uint32), ("best_ms", C.c_double)]
+
+
+class BatchTrial(C.Structure):
+    """ebi_batch_trial"""
+    _fields_ = [("knob", C.c_uint32), ("bucket", C.c_uint32), ("value", C.c_uint32), ("kept", C.c_uint32),
+                ("ms", C.c_double)]
 
 
 class Request(C.Structure):
@@ -65,13 +73,15 @@ class Response(C.Structure):
 class ServerConfig(C.Structure):
     """ebi_server_config"""
     _fields_ = [("device", C.c_int32), ("slots", C.c_uint32), ("max_queries_per_batch", C.c_uint64),
-                ("max_chunks_per_batch", C.c_uint64), ("max_items_per_batch", C.c_uint64)]
+                ("max_chunks_per_batch", C.c_uint64), ("max_items_per_batch", C.c_uint64),
+                ("buff_tiles_per_item", C.c_uint32), ("value_chunks_per_item", C.c_uint32),
+                ("gorilla_chunks_per_item", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class ServerStats(C.Structure):
     """ebi_server_stats"""
     _fields_ = [("batches", C.c_uint64), ("requests", C.c_uint64), ("max_in_flight", C.c_uint64),
-                ("pending", C.c_uint64)]
+                ("pending", C.c_uint64), ("items", C.c_uint64), ("build_ns", C.c_uint64)]
 
 
 class SegmentTimes(C.Structure):
@@ -130,6 +140,8 @@ def lib() -> C.CDLL:
     L.ebi_batch_create.argtypes = [C.POINTER(BatchQuery), u64, vp, C.POINTER(vp)]
     L.ebi_batch_run.argtypes = [vp, PP, C.POINTER(BatchResult), vp]
     L.ebi_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+    L.ebi_batch_get_trials.argtypes = [vp, C.POINTER(BatchTrial), C.c_uint32, C.POINTER(C.c_uint32)]
+    L.ebi_batch_set_tuning_cache.argtypes = [C.c_char_p]
     L.ebi_batch_destroy.argtypes = [vp]
     RQ, RS = C.POINTER(Request), C.POINTER(Response)
     L.ebi_server_create.argtypes = [C.POINTER(vp), C.c_uint32, C.POINTER(ServerConfig), C.POINTER(vp)]

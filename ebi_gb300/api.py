@@ -528,11 +528,38 @@ class Batch:
         return [self._res[i].status for i in range(self._n)]
 
     def info(self) -> dict:
+        """The launch chosen by the first run: shape, tiling per column-size bucket
+        (< 262,144 rows, < 4,194,304, larger) and the timed candidates."""
         inf = _native.BatchInfo()
         _check(_native.lib().ebi_batch_get_info(self._h, C.byref(inf)), "Batch::info")
         return {"queries": inf.queries, "items": inf.items, "chunks": inf.chunks, "shape": inf.shape,
                 "ctas_per_sm": inf.ctas_per_sm, "order": ["cost", "query"][inf.order] if inf.shape >= 0 else None,
-                "shape_ms": list(inf.shape_ms)}
+                "shape_ms": list(inf.shape_ms), "buff_tiles": list(inf.buff_tiles),
+                "value_chunks": list(inf.value_chunks), "gorilla_chunks": list(inf.gorilla_chunks),
+                "trials": self.trials(), "from_cache": bool(inf.from_cache), "best_ms": inf.best_ms}
+
+    _KNOBS = ("shape", "buff_tiles", "value_chunks", "gorilla_chunks")
+
+    def trials(self) -> list:
+        """The first run's timed candidates, in the order timed."""
+        buf = (_native.BatchTrial * 256)()
+        n = C.c_uint32()
+        _check(_native.lib().ebi_batch_get_trials(self._h, buf, 256, C.byref(n)), "Batch::trials")
+        out = []
+        for t in buf[: n.value]:
+            if t.knob == 0:
+                what = {"ctas_per_sm": t.value // 2, "order": ["cost", "query"][t.value % 2]}
+            else:
+                what = {"bucket": t.bucket, "value": t.value}
+            out.append(dict(knob=self._KNOBS[t.knob], ms=round(t.ms, 4), kept=bool(t.kept), **what))
+        return out
+
+    @staticmethod
+    def set_tuning_cache(path):
+        """Process-wide JSON tuning cache (None turns it off): batches of a column
+        shape found there skip the first run's timing."""
+        _check(_native.lib().ebi_batch_set_tuning_cache(None if path is None else str(path).encode()),
+               "Batch::set_tuning_cache")
 
     def close(self):
         if getattr(self, "_h", None):
@@ -570,10 +597,14 @@ class Server:
     the C ABI; no counterpart in the reference).  Requests are
     (column ids, predicate, aggregates) over 1..8 of the server's decoders."""
 
-    def __init__(self, decoders, slots=4, max_queries=1024, max_chunks=1 << 20, max_items=1 << 21, device=None):
+    def __init__(self, decoders, slots=4, max_queries=1024, max_chunks=1 << 20, max_items=1 << 21, device=None,
+                 buff_tiles=0, value_chunks=0, gorilla_chunks=0):
+        """buff_tiles / value_chunks / gorilla_chunks: work-item tiling (BUFF tiles, RLE / Uncompressed
+        chunks, Gorilla chunks per item; 0 keeps the default: 8, 8, 16)."""
         self.decoders = list(decoders)
         dev = self.decoders[0].device if device is None else _torch().device(device)
-        cfg = _native.ServerConfig(dev.index or 0, slots, max_queries, max_chunks, max_items)
+        cfg = _native.ServerConfig(dev.index or 0, slots, max_queries, max_chunks, max_items, buff_tiles,
+                                   value_chunks, gorilla_chunks, 0)
         cols = (C.c_void_p * len(self.decoders))(*[d._h.value for d in self.decoders])
         h = C.c_void_p()
         _check(_native.lib().ebi_server_create(cols, len(self.decoders), C.byref(cfg), C.byref(h)), "Server::new")
@@ -605,7 +636,7 @@ class Server:
         st = _native.ServerStats()
         _check(_native.lib().ebi_server_get_stats(self._h, C.byref(st)), "Server::stats")
         return {"batches": st.batches, "requests": st.requests, "max_in_flight": st.max_in_flight,
-                "pending": st.pending}
+                "pending": st.pending, "items": st.items, "build_ms": round(st.build_ns / 1e6, 3)}
 
     def close(self):
         if getattr(self, "_h", None):

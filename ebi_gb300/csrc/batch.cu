@@ -2,8 +2,11 @@
 // persistent launch.
 //
 // A batch is a list of work items, each naming a query and a unit of one of
-// its columns: an 8,192-row BUFF tile, a whole Uncompressed / RLE / Chimp /
-// Chimp128 / Elf / ElfOnChimp chunk, or a group of Gorilla chunks (one per warp).
+// its columns: a run of 8,192-row BUFF tiles, a run of Uncompressed / RLE
+// chunks, a whole Chimp / Chimp128 / Elf / ElfOnChimp chunk, or a group of
+// Gorilla chunks (one warp walks each; eight warps per item).  How many tiles
+// or chunks one item covers is the batch's tiling (BatchTiling, per codec
+// family and column-size bucket), which the batch's first run tunes.
 // A Chimp-family item may name a run of consecutive queries over one column
 // (count of them, at most 32): the chunk is decoded once for all of them.  A persistent
 // grid of 256-thread CTAs pulls items from a device counter, so columns of
@@ -11,6 +14,9 @@
 // column; each item runs the same per-chunk device code as the single-column
 // kernels and leaves its result in the query's own per-chunk accumulators.
 // A second launch folds every query (one CTA per query, chunk order).
+#include <algorithm>
+#include <vector>
+
 #include "internal.h"
 #include "buff_tile.cuh"
 #include "finalize.cuh"
@@ -27,23 +33,41 @@ static_assert(kBatchThreads == kXorThreads && kBatchThreads == kRleThreads, "cod
 
 // One function per item kind, kept out of line so that each gets its own
 // register allocation (the kernel's is the largest, not the sum of all paths).
+// Tiles [unit, unit + count) of one query's column; the chunk context is set
+// up again only when the chunk changes.
 __device__ __noinline__ void item_buff_tile(const QueryParams& q, const BatchItem& it, BuffCtx& k, BlockRed& red) {
-    const Tile t = q.tiles[it.unit];
-    if (threadIdx.x == 0) buff_setup(q, t.chunk, q.in_mask != nullptr, k);
-    __syncthreads();
-    if (k.ok && k.bits > 32) buff_query_dispatch<unsigned long long>(q, k, t.chunk, it.unit, t.begin, red);
-    else buff_query_dispatch<uint32_t>(q, k, t.chunk, it.unit, t.begin, red);
+    uint32_t chunk = 0xffffffffu;
+    for (uint32_t j = 0; j < it.count; ++j) {
+        const uint32_t tile = it.unit + j;
+        const Tile t = q.tiles[tile];
+        if (t.chunk != chunk) {
+            __syncthreads();  // the previous tile is done with k
+            if (threadIdx.x == 0) buff_setup(q, t.chunk, q.in_mask != nullptr, k);
+            __syncthreads();
+            chunk = t.chunk;
+        }
+        if (k.ok && k.bits > 32) buff_query_dispatch<unsigned long long>(q, k, t.chunk, tile, t.begin, red);
+        else buff_query_dispatch<uint32_t>(q, k, t.chunk, tile, t.begin, red);
+    }
 }
 __device__ __noinline__ void item_raw(const QueryParams& q, const BatchItem& it) {
-    raw_chunk<kBatchThreads>(q, it.unit, it.unit, VAL_SCAN, nullptr);
+    for (uint32_t j = 0; j < it.count; ++j) {
+        if (j) __syncthreads();  // the previous chunk is done with shared memory
+        raw_chunk<kBatchThreads>(q, it.unit + j, it.unit + j, VAL_SCAN, nullptr);
+    }
 }
 __device__ __noinline__ void item_rle(const QueryParams& q, const BatchItem& it) {
-    rle_chunk(q, it.unit, it.unit, VAL_SCAN, nullptr);
+    for (uint32_t j = 0; j < it.count; ++j) {
+        if (j) __syncthreads();  // the previous chunk is done with shared memory
+        rle_chunk(q, it.unit + j, it.unit + j, VAL_SCAN, nullptr);
+    }
 }
+// Chunks [unit, unit + chunks): warp w walks chunks w, w + 8, ...
 __device__ __noinline__ void item_gorilla(const QueryParams& q, const BatchItem& it) {
     const uint32_t warp = threadIdx.x >> 5, chunks = it.count & 0xffu;
     const uint32_t nq = it.count >> 8 ? it.count >> 8 : 1u;  // queries it.query .. + nq: one column
-    if (warp < chunks) gorilla_chunk_l1<kGorillaShare>(&q, nq, it.unit + warp, it.unit + warp, VAL_SCAN, nullptr);
+    for (uint32_t w = warp; w < chunks; w += kBatchThreads / 32)
+        gorilla_chunk_l1<kGorillaShare>(&q, nq, it.unit + w, it.unit + w, VAL_SCAN, nullptr);
 }
 __device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& it) {
     xor_chunk<CODEC_CHIMP>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column
@@ -98,25 +122,64 @@ size_t batch_smem_bytes() {
     return xor_smem_bytes(CODEC_CHIMP128);
 }
 
-void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t query, std::vector<BatchItem>& out) {
+int size_bucket(uint64_t n_records) { return n_records < (1ull << 18) ? 0 : n_records < (1ull << 22) ? 1 : 2; }
+
+BatchTiling default_tiling() {
+    BatchTiling t{};
+    for (int b = 0; b < kSizeBuckets; ++b) {
+        t.buff_tiles[b] = 8;
+        t.value_chunks[b] = 8;
+        t.gorilla_chunks[b] = 16;
+    }
+    return t;
+}
+
+void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& tl,
+                  uint32_t query, std::vector<BatchItem>& out) {
+    const int b = size_bucket(n_records);
+    auto clamp = [](uint32_t v, uint32_t hi) { return v < 1 ? 1u : v > hi ? hi : v; };
     switch (scheme) {
-    case EBI_BUFF:
-        for (uint32_t t = 0; t < n_tiles; ++t) out.push_back({query, ITEM_BUFF_TILE, t, 1});
+    case EBI_BUFF: {
+        const uint32_t per = clamp(tl.buff_tiles[b], kMaxItemTiles);
+        for (uint32_t t = 0; t < n_tiles; t += per)
+            out.push_back({query, ITEM_BUFF_TILE, t, n_tiles - t < per ? n_tiles - t : per});
         return;
-    case EBI_GORILLA:
-        for (uint64_t k = 0; k < n_chunks; k += 8)
+    }
+    case EBI_GORILLA: {
+        const uint64_t per = clamp(tl.gorilla_chunks[b], kMaxGorillaChunks);
+        for (uint64_t k = 0; k < n_chunks; k += per)
             out.push_back({query, ITEM_GORILLA, static_cast<uint32_t>(k),
-                           static_cast<uint32_t>(n_chunks - k < 8 ? n_chunks - k : 8)});
+                           static_cast<uint32_t>(n_chunks - k < per ? n_chunks - k : per)});
         return;
+    }
+    case EBI_UNCOMPRESSED:
+    case EBI_RLE: {
+        const uint64_t per = clamp(tl.value_chunks[b], kMaxItemTiles);
+        const uint32_t kind = scheme == EBI_RLE ? ITEM_RLE : ITEM_RAW;
+        for (uint64_t k = 0; k < n_chunks; k += per)
+            out.push_back({query, kind, static_cast<uint32_t>(k), static_cast<uint32_t>(n_chunks - k < per ? n_chunks - k : per)});
+        return;
+    }
     default: {
-        const uint32_t kind = scheme == EBI_UNCOMPRESSED ? ITEM_RAW
-                            : scheme == EBI_RLE          ? ITEM_RLE
-                            : scheme == EBI_CHIMP        ? ITEM_CHIMP
+        const uint32_t kind = scheme == EBI_CHIMP        ? ITEM_CHIMP
                             : scheme == EBI_CHIMP128     ? ITEM_CHIMP128
                             : scheme == EBI_ELF_ON_CHIMP ? ITEM_ELF_CHIMP
                                                          : ITEM_ELF;
         for (uint64_t k = 0; k < n_chunks; ++k) out.push_back({query, kind, static_cast<uint32_t>(k), 1});
     }
+    }
+}
+
+uint64_t column_item_count(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& tl) {
+    const int b = size_bucket(n_records);
+    auto per = [](uint32_t v, uint32_t hi) -> uint64_t { return v < 1 ? 1u : v > hi ? hi : v; };
+    switch (scheme) {
+    case EBI_BUFF: return (n_tiles + per(tl.buff_tiles[b], kMaxItemTiles) - 1) / per(tl.buff_tiles[b], kMaxItemTiles);
+    case EBI_GORILLA:
+        return (n_chunks + per(tl.gorilla_chunks[b], kMaxGorillaChunks) - 1) / per(tl.gorilla_chunks[b], kMaxGorillaChunks);
+    case EBI_UNCOMPRESSED:
+    case EBI_RLE: return (n_chunks + per(tl.value_chunks[b], kMaxItemTiles) - 1) / per(tl.value_chunks[b], kMaxItemTiles);
+    default: return n_chunks;
     }
 }
 
@@ -127,15 +190,45 @@ double item_cost(uint32_t kind, uint32_t count) {
     case ITEM_ELF_CHIMP: return 35.0;
     case ITEM_CHIMP128: return 30.0;
     case ITEM_CHIMP: return 25.0;
-    case ITEM_BUFF_TILE: return 1.0;
-    case ITEM_RLE: return 0.5;
-    default: return 2.0;
+    case ITEM_BUFF_TILE: return 1.0 * count;
+    case ITEM_RLE: return 0.5 * count;
+    default: return 2.0 * count;
     }
 }
 
+void order_by_cost(std::vector<BatchItem>& items) {
+    // distinct costs, descending; then a stable counting sort on their rank
+    std::vector<double> costs;
+    std::vector<uint32_t> rank(items.size());
+    for (size_t i = 0; i < items.size(); ++i) {
+        const double c = item_cost(items[i].kind, items[i].count);
+        size_t r = 0;
+        while (r < costs.size() && costs[r] != c) ++r;
+        if (r == costs.size()) {
+            if (costs.size() == 256) {  // not a handful after all
+                std::stable_sort(items.begin(), items.end(), [](const BatchItem& x, const BatchItem& y) {
+                    return item_cost(x.kind, x.count) > item_cost(y.kind, y.count);
+                });
+                return;
+            }
+            costs.push_back(c);
+        }
+        rank[i] = static_cast<uint32_t>(r);
+    }
+    std::vector<uint32_t> order(costs.size());
+    for (uint32_t r = 0; r < order.size(); ++r) order[r] = r;
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return costs[a] > costs[b]; });
+    std::vector<size_t> pos_of(costs.size()), cnt(costs.size(), 0);
+    for (uint32_t r : rank) ++cnt[r];
+    size_t at = 0;
+    for (uint32_t r : order) { pos_of[r] = at; at += cnt[r]; }
+    std::vector<BatchItem> out(items.size());
+    for (size_t i = 0; i < items.size(); ++i) out[pos_of[rank[i]]++] = items[i];
+    items.swap(out);
+}
+
 cudaError_t prepare_batch_kernel() {
-    return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(batch_smem_bytes()));
+    return allow_dynamic_smem(reinterpret_cast<const void*>(batch_kernel), batch_smem_bytes());
 }
 
 cudaError_t launch_batch(const QueryParams* d_qp, const BatchItem* d_items, uint32_t n_items, unsigned int* d_counter,

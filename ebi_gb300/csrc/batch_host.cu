@@ -3,12 +3,19 @@
 // fold launch, captured once into a CUDA graph and replayed.
 //
 // Every query owns its per-chunk accumulators (the same column may appear in
-// several queries).  On the first run the batch times a few launch shapes
-// (persistent CTAs per SM, order of the work items) by replaying each shape's
-// graph, keeps the fastest and reuses it for every later run.
+// several queries).  The first run tunes the launch (graph replays timed with
+// events): the persistent CTAs per SM and the order of the work items, then,
+// per codec family and column-size bucket present in the batch, how many BUFF
+// tiles, RLE / Uncompressed chunks or Gorilla chunks one work item covers
+// (coordinate descent; a candidate is kept when it is at least 2 % faster).
+// The winner is reused for every later run and, when a tuning cache file is
+// set (ebi_batch_set_tuning_cache), stored under the batch's column shape and
+// reused by later batches of the same shape without timing.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -34,16 +41,108 @@ struct Shape {
 constexpr Shape kShapes[] = {{2, 0}, {1, 0}, {2, 1}, {1, 1}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
+// One launch configuration: a shape and a tiling.
+struct Config {
+    int shape;
+    BatchTiling tiling;
+};
+
+enum Knob : uint32_t { KNOB_SHAPE = 0, KNOB_BUFF = 1, KNOB_VALUE = 2, KNOB_GORILLA = 3 };
+constexpr uint32_t kBuffCand[] = {1, 2, 4, 8, 16};
+constexpr uint32_t kValueCand[] = {1, 2, 4, 8, 16};
+constexpr uint32_t kGorillaCand[] = {8, 16, 32};
+
+// The process-wide tuning cache: column shape -> configuration (and its time).
+struct CacheEntry {
+    Config cfg;
+    double ms;
+};
+std::mutex g_cache_mu;
+std::string g_cache_path;
+std::map<std::string, CacheEntry> g_cache;
+bool g_cache_loaded = false;
+
+uint32_t* knob_slot(BatchTiling& t, uint32_t knob, int bucket) {
+    return knob == KNOB_BUFF ? &t.buff_tiles[bucket] : knob == KNOB_VALUE ? &t.value_chunks[bucket]
+                                                                          : &t.gorilla_chunks[bucket];
+}
+
+// Reads the cache file written by save_cache (one entry per line); a line
+// that does not parse is skipped.
+void load_cache_locked() {
+    g_cache_loaded = true;
+    if (g_cache_path.empty()) return;
+    FILE* f = std::fopen(g_cache_path.c_str(), "r");
+    if (!f) return;
+    char line[4096];
+    while (std::fgets(line, sizeof line, f)) {
+        const char* q0 = std::strchr(line, '"');
+        const char* q1 = q0 ? std::strchr(q0 + 1, '"') : nullptr;
+        if (!q0 || !q1) continue;
+        const std::string key(q0 + 1, q1);
+        const char* p = q1 + 1;
+        CacheEntry e{};
+        unsigned c = 0, o = 0, b[3], v[3], g[3];
+        double ms = 0;
+        const char* fmt =
+            ": {\"ctas_per_sm\": %u, \"order\": %u, \"buff_tiles\": [%u, %u, %u], \"value_chunks\": [%u, %u, %u], "
+            "\"gorilla_chunks\": [%u, %u, %u], \"ms\": %lf";
+        if (std::sscanf(p, fmt, &c, &o, &b[0], &b[1], &b[2], &v[0], &v[1], &v[2], &g[0], &g[1], &g[2], &ms) != 12) continue;
+        e.cfg.shape = -1;
+        for (int i = 0; i < kNumShapes; ++i)
+            if (kShapes[i].ctas_per_sm == c && kShapes[i].order == o) e.cfg.shape = i;
+        if (e.cfg.shape < 0) continue;
+        bool ok = true;
+        for (int k = 0; k < kSizeBuckets; ++k) {
+            ok = ok && b[k] >= 1 && b[k] <= kMaxItemTiles && v[k] >= 1 && v[k] <= kMaxItemTiles && g[k] >= 1 &&
+                 g[k] <= kMaxGorillaChunks;
+            e.cfg.tiling.buff_tiles[k] = b[k];
+            e.cfg.tiling.value_chunks[k] = v[k];
+            e.cfg.tiling.gorilla_chunks[k] = g[k];
+        }
+        if (!ok) continue;
+        e.ms = ms;
+        g_cache[key] = e;
+    }
+    std::fclose(f);
+}
+
+void save_cache_locked() {
+    if (g_cache_path.empty()) return;
+    const std::string tmp = g_cache_path + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "w");
+    if (!f) return;
+    std::fprintf(f, "{\n");
+    size_t i = 0;
+    for (const auto& kv : g_cache) {
+        const Config& c = kv.second.cfg;
+        const BatchTiling& t = c.tiling;
+        std::fprintf(f,
+                     "\"%s\": {\"ctas_per_sm\": %u, \"order\": %u, \"buff_tiles\": [%u, %u, %u], \"value_chunks\": "
+                     "[%u, %u, %u], \"gorilla_chunks\": [%u, %u, %u], \"ms\": %.4f}%s\n",
+                     kv.first.c_str(), kShapes[c.shape].ctas_per_sm, kShapes[c.shape].order, t.buff_tiles[0],
+                     t.buff_tiles[1], t.buff_tiles[2], t.value_chunks[0], t.value_chunks[1], t.value_chunks[2],
+                     t.gorilla_chunks[0], t.gorilla_chunks[1], t.gorilla_chunks[2], kv.second.ms,
+                     ++i < g_cache.size() ? "," : "");
+    }
+    std::fprintf(f, "}\n");
+    const bool ok = std::fclose(f) == 0;
+    if (ok) std::rename(tmp.c_str(), g_cache_path.c_str());
+    else std::remove(tmp.c_str());
+}
+
 }  // namespace
 
 struct ebi_batch {
     std::vector<ebi_batch_query> queries;
-    std::vector<BatchItem> items_cost, items_query;
     uint64_t n_chunks = 0;
+    uint64_t max_items = 0;  // the most items any candidate tiling makes
     int sms = 1;
+    std::string shape_key;   // column shape (codec family x size bucket counts) + SM count
+    bool present[4][kSizeBuckets] = {};  // knob family x bucket: the batch has such columns
     // device
     QueryParams* d_qp = nullptr;
-    BatchItem* d_items[2] = {nullptr, nullptr};
+    BatchItem* d_items = nullptr;
     ChunkAcc* d_acc = nullptr;
     QueryResult* d_res = nullptr;
     unsigned int* d_counter = nullptr;
@@ -52,32 +151,53 @@ struct ebi_batch {
     QueryResult* h_res = nullptr;
     // capture and tuning stream (capture is not allowed on the legacy default stream)
     cudaStream_t cap = nullptr;
-    // the chosen graph
+    // the chosen configuration and its graph
     cudaGraphExec_t exec = nullptr;
-    int shape = -1;
+    Config cfg{-1, {}};
+    uint64_t n_items = 0;
+    double best_ms = 0;
+    bool from_cache = false;
     double shape_ms[kNumShapes] = {0, 0, 0, 0};
+    std::vector<ebi_batch_trial> trials;
 };
 
 namespace {
 
-// Records one run of the batch with launch shape `sh` on stream s (captured).
-int record(ebi_batch* b, int sh, cudaStream_t s) {
+// The work items of configuration c (query order, then cost order if asked).
+void build_items(const ebi_batch* b, const Config& c, std::vector<BatchItem>& items) {
+    items.clear();
+    for (size_t i = 0; i < b->queries.size(); ++i) {
+        const ebi_column* col = b->queries[i].col;
+        column_items(col->scheme, col->n_chunks, static_cast<uint32_t>(col->tiles.tiles.size()), col->n_records,
+                     c.tiling, static_cast<uint32_t>(i), items);
+    }
+    if (kShapes[c.shape].order == 0) order_by_cost(items);
+}
+
+// Records one run of the batch (configuration c, items already in d_items) on stream s (captured).
+int record(ebi_batch* b, const Config& c, uint64_t n_items, cudaStream_t s) {
     const uint32_t n = static_cast<uint32_t>(b->queries.size());
-    const size_t n_items = b->items_cost.size();
     BCK(cudaMemcpyAsync(b->d_qp, b->h_qp, n * sizeof(QueryParams), cudaMemcpyHostToDevice, s));
     for (const ebi_batch_query& q : b->queries)
         if (q.d_out_mask) BCK(cudaMemsetAsync(q.d_out_mask, 0, ((ebi_column_num_records(q.col) + 63) / 64) * 8, s));
-    const uint32_t grid = static_cast<uint32_t>(b->sms) * kShapes[sh].ctas_per_sm;
-    BCK(launch_batch(b->d_qp, b->d_items[kShapes[sh].order], static_cast<uint32_t>(n_items), b->d_counter, grid, s));
+    const uint32_t grid = static_cast<uint32_t>(b->sms) * kShapes[c.shape].ctas_per_sm;
+    BCK(launch_batch(b->d_qp, b->d_items, static_cast<uint32_t>(n_items), b->d_counter, grid, s));
     BCK(launch_batch_finalize(b->d_qp, b->d_res, n, s));
     BCK(cudaMemcpyAsync(b->h_res, b->d_res, n * sizeof(QueryResult), cudaMemcpyDeviceToHost, s));
     return EBI_OK;
 }
 
-int capture(ebi_batch* b, int sh, cudaStream_t s, cudaGraphExec_t* out) {
+// Uploads configuration c's items and captures its graph.
+int prepare(ebi_batch* b, const Config& c, cudaStream_t s, cudaGraphExec_t* out, uint64_t* n_items) {
+    std::vector<BatchItem> items;
+    build_items(b, c, items);
+    if (items.size() > b->max_items) return bfail(EBI_E_INVALID, "batch tiling makes more items than allocated");
+    BCK(cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, s));
+    BCK(cudaStreamSynchronize(s));  // items is pageable host memory about to go out of scope
+    *n_items = items.size();
     cudaGraph_t g = nullptr;
     BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    const int st = record(b, sh, s);
+    const int st = record(b, c, items.size(), s);
     const cudaError_t e = cudaStreamEndCapture(s, &g);
     if (st) {
         if (g) cudaGraphDestroy(g);
@@ -90,44 +210,106 @@ int capture(ebi_batch* b, int sh, cudaStream_t s, cudaGraphExec_t* out) {
     return EBI_OK;
 }
 
-// Times every launch shape (one warm-up and two timed replays each) and keeps the fastest.
+// Device time of one run of configuration c (one warm-up replay, then the mean of two).
+int time_config(ebi_batch* b, const Config& c, cudaEvent_t e0, cudaEvent_t e1, double* ms_out) {
+    cudaStream_t s = b->cap;
+    cudaGraphExec_t ex = nullptr;
+    uint64_t n_items = 0;
+    if (int st = prepare(b, c, s, &ex, &n_items)) return st;
+    cudaError_t e = cudaGraphLaunch(ex, s);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+    for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = cudaGraphLaunch(ex, s);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaGraphExecDestroy(ex);
+    if (e != cudaSuccess) return bfail(EBI_E_CUDA, std::string("batch tuning: ") + cudaGetErrorString(e));
+    *ms_out = ms / 2.0;
+    return EBI_OK;
+}
+
+// Chooses the configuration (from the cache or by timing) and captures its graph.
 int tune(ebi_batch* b, cudaStream_t user) {
     BCK(prepare_batch_kernel());
     BCK(cudaStreamSynchronize(user));  // the batch's inputs were written on the caller's stream
-    cudaStream_t s = b->cap;
-    cudaEvent_t e0, e1;
-    BCK(cudaEventCreate(&e0));
-    BCK(cudaEventCreate(&e1));
-    double best = 1e30;
-    int st = EBI_OK;
-    for (int sh = 0; sh < kNumShapes && !st; ++sh) {
-        cudaGraphExec_t ex = nullptr;
-        if ((st = capture(b, sh, s, &ex))) break;
-        cudaError_t e = cudaGraphLaunch(ex, s);
-        if (e == cudaSuccess) e = cudaEventRecord(e0, s);
-        for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = cudaGraphLaunch(ex, s);
-        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
-        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-        float ms = 0.f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-        if (e != cudaSuccess) {
-            cudaGraphExecDestroy(ex);
-            st = bfail(EBI_E_CUDA, std::string("batch tuning: ") + cudaGetErrorString(e));
-            break;
-        }
-        b->shape_ms[sh] = ms / 2.0;
-        if (b->shape_ms[sh] < best) {
-            best = b->shape_ms[sh];
-            if (b->exec) cudaGraphExecDestroy(b->exec);
-            b->exec = ex;
-            b->shape = sh;
-        } else {
-            cudaGraphExecDestroy(ex);
+    bool cached = false;
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        if (!g_cache_path.empty()) {
+            if (!g_cache_loaded) load_cache_locked();
+            auto it = g_cache.find(b->shape_key);
+            if (it != g_cache.end()) {
+                b->cfg = it->second.cfg;
+                b->best_ms = it->second.ms;
+                cached = true;
+            }
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return st;
+    if (!cached) {
+        cudaEvent_t e0, e1;
+        BCK(cudaEventCreate(&e0));
+        BCK(cudaEventCreate(&e1));
+        int st = EBI_OK;
+        Config cur{0, default_tiling()};
+        double best = 0;
+        auto trial = [&](const Config& c, uint32_t knob, uint32_t bucket, uint32_t value, double* ms) {
+            const int r = time_config(b, c, e0, e1, ms);
+            if (!r) b->trials.push_back(ebi_batch_trial{knob, bucket, value, 0, *ms});
+            return r;
+        };
+        // launch shapes on the default tiling
+        for (int sh = 0; sh < kNumShapes && !st; ++sh) {
+            Config c = cur;
+            c.shape = sh;
+            double ms = 0;
+            st = trial(c, KNOB_SHAPE, 0, kShapes[sh].ctas_per_sm * 2 + kShapes[sh].order, &ms);
+            if (st) break;
+            b->shape_ms[sh] = ms;
+            if (sh == 0 || ms < best) {
+                best = ms;
+                cur.shape = sh;
+            }
+        }
+        if (!st) {
+            for (ebi_batch_trial& t : b->trials)
+                t.kept = t.knob == KNOB_SHAPE && t.value == kShapes[cur.shape].ctas_per_sm * 2 + kShapes[cur.shape].order;
+        }
+        // tiles per item, one (family, bucket) at a time
+        for (uint32_t knob = KNOB_BUFF; knob <= KNOB_GORILLA && !st; ++knob) {
+            const uint32_t* cand = knob == KNOB_BUFF ? kBuffCand : knob == KNOB_VALUE ? kValueCand : kGorillaCand;
+            const int nc = knob == KNOB_GORILLA ? 3 : 5;
+            for (int bk = 0; bk < kSizeBuckets && !st; ++bk) {
+                if (!b->present[knob][bk]) continue;
+                for (int i = 0; i < nc && !st; ++i) {
+                    if (cand[i] == *knob_slot(cur.tiling, knob, bk)) continue;
+                    Config c = cur;
+                    *knob_slot(c.tiling, knob, bk) = cand[i];
+                    double ms = 0;
+                    st = trial(c, knob, static_cast<uint32_t>(bk), cand[i], &ms);
+                    if (!st && ms < 0.98 * best) {
+                        best = ms;
+                        cur = c;
+                        b->trials.back().kept = 1;
+                    }
+                }
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (st) return st;
+        b->cfg = cur;
+        b->best_ms = best;
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        if (!g_cache_path.empty()) {
+            g_cache[b->shape_key] = CacheEntry{cur, best};
+            save_cache_locked();
+        }
+    }
+    b->from_cache = cached;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    return prepare(b, b->cfg, b->cap, &b->exec, &b->n_items);
 }
 
 template <typename T>
@@ -153,6 +335,7 @@ int ebi_batch_create(const ebi_batch_query* queries, uint64_t n, void* stream, e
     b->queries.assign(queries, queries + n);
     std::vector<QueryParams> qp(n);
     std::vector<uint64_t> acc_off(n);
+    std::map<int, uint64_t> shape_count;  // scheme * buckets + bucket -> queries
     for (uint64_t i = 0; i < n; ++i) {
         const ebi_batch_query& bq = queries[i];
         if (!bq.col) { delete b; return bfail(EBI_E_INVALID, "query without a column"); }
@@ -173,21 +356,36 @@ int ebi_batch_create(const ebi_batch_query* queries, uint64_t n, void* stream, e
         q.out_atomic = 1;
         q.stage_bytes = 0;
         qp[i] = q;
-        // work items of this query's column
+        // the batch's column shape and the most items any candidate tiling makes
         const ebi_column* c = bq.col;
-        column_items(c->scheme, c->n_chunks, static_cast<uint32_t>(c->tiles.tiles.size()), static_cast<uint32_t>(i),
-                     b->items_query);
+        const int bk = size_bucket(c->n_records);
+        const uint32_t knob = c->scheme == EBI_BUFF ? KNOB_BUFF
+                            : c->scheme == EBI_GORILLA ? KNOB_GORILLA
+                            : (c->scheme == EBI_RLE || c->scheme == EBI_UNCOMPRESSED) ? KNOB_VALUE : KNOB_SHAPE;
+        if (knob != KNOB_SHAPE) b->present[knob][bk] = true;
+        BatchTiling finest = default_tiling();
+        for (int k = 0; k < kSizeBuckets; ++k) {
+            finest.buff_tiles[k] = 1;
+            finest.value_chunks[k] = 1;
+            finest.gorilla_chunks[k] = kGorillaCand[0];
+        }
+        b->max_items += column_item_count(c->scheme, c->n_chunks, static_cast<uint32_t>(c->tiles.tiles.size()),
+                                          c->n_records, finest);
+        shape_count[c->scheme * kSizeBuckets + bk] += 1;
     }
-    b->items_cost = b->items_query;
-    std::stable_sort(b->items_cost.begin(), b->items_cost.end(), [](const BatchItem& x, const BatchItem& y) {
-        return item_cost(x.kind, x.count) > item_cost(y.kind, y.count);
-    });
+    if (b->max_items > 0xffffffffull) {
+        delete b;
+        return bfail(EBI_E_INVALID, "a batch holds at most 2^32 - 1 work items");
+    }
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    b->shape_key = "sms=" + std::to_string(b->sms);
+    for (const auto& kv : shape_count)
+        b->shape_key += ";" + std::to_string(kv.first / kSizeBuckets) + "/" + std::to_string(kv.first % kSizeBuckets) +
+                        "x" + std::to_string(kv.second);
     int st = balloc(&b->d_qp, n);
-    if (!st) st = balloc(&b->d_items[0], b->items_cost.size());
-    if (!st) st = balloc(&b->d_items[1], b->items_query.size());
+    if (!st) st = balloc(&b->d_items, b->max_items);
     if (!st) st = balloc(&b->d_acc, b->n_chunks);
     if (!st) st = balloc(&b->d_res, n);
     if (!st) st = balloc(&b->d_counter, 1);
@@ -200,12 +398,7 @@ int ebi_batch_create(const ebi_batch_query* queries, uint64_t n, void* stream, e
             qp[i].acc = b->d_acc + acc_off[i];
             b->h_qp[i] = qp[i];
         }
-        cudaError_t e = cudaMemcpyAsync(b->d_items[0], b->items_cost.data(), b->items_cost.size() * sizeof(BatchItem),
-                                        cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(b->d_items[1], b->items_query.data(), b->items_query.size() * sizeof(BatchItem),
-                                cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = launch_acc_init(b->d_acc, static_cast<uint32_t>(b->n_chunks), s);
+        cudaError_t e = launch_acc_init(b->d_acc, static_cast<uint32_t>(b->n_chunks), s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) st = bfail(EBI_E_CUDA, std::string("batch upload: ") + cudaGetErrorString(e));
     }
@@ -262,14 +455,38 @@ int ebi_batch_get_info(const ebi_batch* b, ebi_batch_info* out) {
     if (!b || !out) return bfail(EBI_E_INVALID, "batch or out is null");
     std::memset(out, 0, sizeof *out);
     out->queries = b->queries.size();
-    out->items = b->items_cost.size();
+    out->items = b->exec ? b->n_items : 0;
     out->chunks = b->n_chunks;
-    out->shape = b->shape;
-    if (b->shape >= 0) {
-        out->ctas_per_sm = kShapes[b->shape].ctas_per_sm;
-        out->order = kShapes[b->shape].order;
+    out->shape = b->exec ? b->cfg.shape : -1;
+    if (b->exec) {
+        out->ctas_per_sm = kShapes[b->cfg.shape].ctas_per_sm;
+        out->order = kShapes[b->cfg.shape].order;
+        for (int k = 0; k < kSizeBuckets; ++k) {
+            out->buff_tiles[k] = b->cfg.tiling.buff_tiles[k];
+            out->value_chunks[k] = b->cfg.tiling.value_chunks[k];
+            out->gorilla_chunks[k] = b->cfg.tiling.gorilla_chunks[k];
+        }
     }
     for (int i = 0; i < kNumShapes && i < 4; ++i) out->shape_ms[i] = b->shape_ms[i];
+    out->trials = static_cast<uint32_t>(b->trials.size());
+    out->from_cache = b->from_cache ? 1u : 0u;
+    out->best_ms = b->best_ms;
+    return EBI_OK;
+}
+
+int ebi_batch_get_trials(const ebi_batch* b, ebi_batch_trial* out, uint32_t max, uint32_t* n_out) {
+    if (!b || (!out && max) || !n_out) return bfail(EBI_E_INVALID, "batch, output or count is null");
+    const uint32_t n = static_cast<uint32_t>(std::min<size_t>(max, b->trials.size()));
+    for (uint32_t i = 0; i < n; ++i) out[i] = b->trials[i];
+    *n_out = n;
+    return EBI_OK;
+}
+
+int ebi_batch_set_tuning_cache(const char* path) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_cache.clear();
+    g_cache_loaded = false;
+    g_cache_path = path ? path : "";
     return EBI_OK;
 }
 
@@ -277,7 +494,7 @@ int ebi_batch_destroy(ebi_batch* b) {
     if (!b) return EBI_OK;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->cap) cudaStreamDestroy(b->cap);
-    void* d[] = {b->d_qp, b->d_items[0], b->d_items[1], b->d_acc, b->d_res, b->d_counter};
+    void* d[] = {b->d_qp, b->d_items, b->d_acc, b->d_res, b->d_counter};
     for (void* p : d) if (p) cudaFree(p);
     if (b->h_qp) cudaFreeHost(b->h_qp);
     if (b->h_res) cudaFreeHost(b->h_res);

@@ -131,18 +131,42 @@ enum BatchItemKind : uint32_t {
 struct BatchItem {
     uint32_t query;  // index into the batch's QueryParams
     uint32_t kind;   // BatchItemKind
-    uint32_t unit;
-    uint32_t count;  // Chimp family: queries sharing the chunk; Gorilla: chunks | (queries sharing them) << 8
+    uint32_t unit;   // first tile (BUFF) or chunk
+    // BUFF / Uncompressed / RLE: tiles or chunks [unit, unit + count);
+    // Chimp family: queries sharing the chunk; Gorilla: chunks | (queries sharing them) << 8
+    uint32_t count;
 };
 // Queries over one Gorilla column that one batch item serves at once.
 constexpr uint32_t kGorillaShare = 3;
-// Appends the items of one query over a column (scheme, chunks, BUFF tiles).
-void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint32_t query, std::vector<BatchItem>& out);
-// Relative cost of one item of each kind (device time of an 8,192-row unit
+
+// Work-item tiling of a batch, per codec family and column-size bucket
+// (size_bucket): how many 8,192-row BUFF tiles, Uncompressed / RLE chunks and
+// Gorilla chunks (one warp each, eight warps per item) one item covers.
+constexpr int kSizeBuckets = 3;
+constexpr uint32_t kMaxItemTiles = 16;     // BUFF tiles or value chunks per item
+constexpr uint32_t kMaxGorillaChunks = 64;  // Gorilla chunks per item
+struct BatchTiling {
+    uint32_t buff_tiles[kSizeBuckets];
+    uint32_t value_chunks[kSizeBuckets];
+    uint32_t gorilla_chunks[kSizeBuckets];
+};
+// Bucket of a column of n_records rows: < 262,144, < 4,194,304, larger.
+int size_bucket(uint64_t n_records);
+BatchTiling default_tiling();
+// Appends the items of one query over a column.  Gorilla items carry their
+// chunk count in the low byte of count (callers add a sharing count above it).
+void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& t,
+                  uint32_t query, std::vector<BatchItem>& out);
+// How many items column_items appends for such a column.
+uint64_t column_item_count(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& t);
+// Relative cost of one item (device time of the 8,192-row units it covers,
 // measured on the single-column kernels), for the cost-descending order.
 double item_cost(uint32_t kind, uint32_t count);
+// Stable reorder of items by descending item_cost, in linear time (the costs
+// take a handful of values).
+void order_by_cost(std::vector<BatchItem>& items);
 // Dynamic shared memory of the batch kernel; prepare_batch_kernel raises the
-// kernel's shared-memory limit to it (once per process, outside any capture).
+// kernel's shared-memory limit to it on the current device (outside any capture).
 size_t batch_smem_bytes();
 cudaError_t prepare_batch_kernel();
 // Runs every item (persistent grid of `grid` CTAs pulling from *d_counter,

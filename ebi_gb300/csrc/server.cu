@@ -11,6 +11,7 @@
 // combined per request in column order (sum in order, min, max), stamped and
 // handed back; every result equals the request run alone.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -75,8 +76,10 @@ struct ebi_server {
     bool stop = false;
     int error = 0;
     std::thread worker;
+    BatchTiling tiling{};
     // statistics
     uint64_t batches = 0, batched_requests = 0, max_in_flight = 0;
+    std::atomic<uint64_t> items{0}, build_ns{0};  // written by the dispatcher outside the lock
 };
 
 namespace {
@@ -87,8 +90,8 @@ void footprint(const ebi_server* s, const ebi_request& r, uint64_t* chunks, uint
     for (uint32_t k = 0; k < r.n_columns; ++k) {
         const ebi_column* col = s->cols[r.columns[k]];
         c += col->n_chunks;
-        it += col->scheme == EBI_BUFF ? col->tiles.tiles.size()
-            : col->scheme == EBI_GORILLA ? (col->n_chunks + 7) / 8 : col->n_chunks;
+        it += column_item_count(col->scheme, col->n_chunks, static_cast<uint32_t>(col->tiles.tiles.size()),
+                                col->n_records, s->tiling);
     }
     *chunks = c;
     *items = it;
@@ -96,6 +99,7 @@ void footprint(const ebi_server* s, const ebi_request& r, uint64_t* chunks, uint
 
 // Builds and launches slot sl's batch from its admitted requests.
 cudaError_t launch_slot(ebi_server* s, Slot& sl) {
+    const uint64_t t_build = now_ns();
     // The batch's queries in column order, so that the queries on one column
     // are consecutive: a Chimp-family chunk is then decoded once for all of
     // them (items naming up to 32 consecutive queries), a group of Gorilla
@@ -140,26 +144,26 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
         if (shared) {
             for (uint32_t q0 = g; q0 < h; q0 += 32) {
                 const size_t first = items.size();
-                column_items(c->scheme, c->n_chunks, tiles, q0, items);
+                column_items(c->scheme, c->n_chunks, tiles, c->n_records, s->tiling, q0, items);
                 for (size_t i = first; i < items.size(); ++i) items[i].count = std::min<uint32_t>(32, h - q0);
             }
         } else if (c->scheme == EBI_GORILLA) {
             // a group of chunks is parsed once for up to kGorillaShare queries
             for (uint32_t q0 = g; q0 < h; q0 += kGorillaShare) {
                 const size_t first = items.size();
-                column_items(c->scheme, c->n_chunks, tiles, q0, items);
+                column_items(c->scheme, c->n_chunks, tiles, c->n_records, s->tiling, q0, items);
                 const uint32_t share = std::min<uint32_t>(kGorillaShare, h - q0);
                 for (size_t i = first; i < items.size(); ++i) items[i].count |= share << 8;
             }
         } else {
-            for (uint32_t qi = g; qi < h; ++qi) column_items(c->scheme, c->n_chunks, tiles, qi, items);
+            for (uint32_t qi = g; qi < h; ++qi) column_items(c->scheme, c->n_chunks, tiles, c->n_records, s->tiling, qi, items);
         }
         g = h;
     }
-    std::stable_sort(items.begin(), items.end(), [](const BatchItem& x, const BatchItem& y) {
-        return item_cost(x.kind, x.count) > item_cost(y.kind, y.count);
-    });
+    order_by_cost(items);
     std::memcpy(sl.h_items, items.data(), items.size() * sizeof(BatchItem));
+    s->items.fetch_add(items.size(), std::memory_order_relaxed);
+    s->build_ns.fetch_add(now_ns() - t_build, std::memory_order_relaxed);
     cudaError_t e = cudaMemcpyAsync(sl.d_qp, sl.h_qp, nq * sizeof(QueryParams), cudaMemcpyHostToDevice, sl.stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(sl.d_items, sl.h_items, items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, sl.stream);
@@ -292,9 +296,17 @@ int ebi_server_create(ebi_column* const* columns, uint32_t n_columns, const ebi_
     if (!s) return sfail(EBI_E_OOM, "host allocation failed");
     s->cols.assign(columns, columns + n_columns);
     s->cfg = cf;
+    s->tiling = default_tiling();
+    for (int b = 0; b < kSizeBuckets; ++b) {
+        if (cf.buff_tiles_per_item) s->tiling.buff_tiles[b] = std::min(cf.buff_tiles_per_item, kMaxItemTiles);
+        if (cf.value_chunks_per_item) s->tiling.value_chunks[b] = std::min(cf.value_chunks_per_item, kMaxItemTiles);
+        if (cf.gorilla_chunks_per_item)
+            s->tiling.gorilla_chunks[b] = std::min(cf.gorilla_chunks_per_item, kMaxGorillaChunks);
+    }
     for (ebi_column* c : s->cols) {
         if (!c) { delete s; return sfail(EBI_E_INVALID, "null column"); }
-        uint64_t its = c->scheme == EBI_BUFF ? c->tiles.tiles.size() : c->n_chunks;
+        const uint64_t its = column_item_count(c->scheme, c->n_chunks, static_cast<uint32_t>(c->tiles.tiles.size()),
+                                               c->n_records, s->tiling);
         if (c->n_chunks > cf.max_chunks_per_batch || its > cf.max_items_per_batch) {
             delete s;
             return sfail(EBI_E_INVALID, "a column is larger than one batch's capacity");
@@ -370,6 +382,8 @@ int ebi_server_get_stats(ebi_server* s, ebi_server_stats* out) {
     out->requests = s->batched_requests;
     out->max_in_flight = s->max_in_flight;
     out->pending = s->pending.size();
+    out->items = s->items.load(std::memory_order_relaxed);
+    out->build_ns = s->build_ns.load(std::memory_order_relaxed);
     return EBI_OK;
 }
 

@@ -185,14 +185,20 @@ int ebi_rows_from_mask(const uint64_t* d_mask, uint64_t n_records, uint32_t* d_r
                        void* stream);
 
 /* ---- batched queries ------------------------------------------------------ */
-/* No reference counterpart: the reference answers one Decoder call at a time.
+/* No reference counterpart: the reference answers one Decoder call at a time
+ * (its chunk loop, api/decoder.rs:243-281, is what a batch replaces).
  * A batch is a fixed list of filter + aggregate queries, each over one open
  * column (columns may repeat and mix codecs).  Running it executes every
  * query's chunks in one persistent mixed-codec launch followed by one fold
- * launch, captured once into a CUDA graph and replayed; the first run also
- * times a few launch shapes and keeps the fastest.  Results equal the
- * single-column calls (ebi_filter_agg) bit for bit.  The columns must stay
- * open while the batch exists; runs of one batch must not overlap. */
+ * launch, captured once into a CUDA graph and replayed.  The first run tunes
+ * the launch by timing graph replays: the persistent CTAs per SM and the work
+ * items' order, then, for each codec family and column-size bucket in the
+ * batch, how many 8,192-row BUFF tiles, RLE / Uncompressed chunks or Gorilla
+ * chunks one work item covers; the fastest is kept (and, with a tuning cache
+ * set, stored under the batch's column shape for later batches).  Results
+ * equal the single-column calls (ebi_filter_agg) bit for bit whatever the
+ * tiling.  The columns must stay open while the batch exists; runs of one
+ * batch must not overlap. */
 enum { EBI_AGG_SUM = 1, EBI_AGG_MIN = 2, EBI_AGG_MAX = 4 };
 typedef struct {
     ebi_column* col;
@@ -207,18 +213,41 @@ typedef struct {
     int32_t status;        /* ebi_status of this query (first failing chunk) */
     uint32_t bad_chunk;
 } ebi_batch_result;
+/* Column-size buckets of the tiling: 0: < 262,144 rows, 1: < 4,194,304, 2: larger. */
 typedef struct {
-    uint64_t queries, items, chunks;
-    int32_t shape;         /* launch shape chosen by the first run (-1 before) */
+    uint64_t queries, items, chunks;   /* items: work items of the chosen tiling (0 before the first run) */
+    int32_t shape;         /* launch shape chosen by the first run (-1 before):
+                              0: 2 CTAs/SM cost order, 1: 1 CTA/SM cost order, 2: 2 CTAs/SM query order, 3: 1 CTA/SM query order */
     uint32_t ctas_per_sm, order;
-    double shape_ms[4];    /* device time of each candidate shape */
+    double shape_ms[4];    /* device time of each candidate shape on the default tiling */
+    uint32_t buff_tiles[3];      /* chosen BUFF tiles per item, per size bucket */
+    uint32_t value_chunks[3];    /* chosen RLE / Uncompressed chunks per item */
+    uint32_t gorilla_chunks[3];  /* chosen Gorilla chunks per item (one warp walks each) */
+    uint32_t trials;       /* candidates timed by the first run (0: taken from the tuning cache) */
+    uint32_t from_cache;   /* 1: the configuration came from the tuning cache */
+    double best_ms;        /* device time of one run with the chosen configuration */
 } ebi_batch_info;
+/* One timed candidate of the first run.  knob 0: launch shape (value =
+ * ctas_per_sm * 2 + order, bucket 0); 1: BUFF tiles per item; 2: RLE /
+ * Uncompressed chunks per item; 3: Gorilla chunks per item (value = the count,
+ * for the bucket).  kept: the candidate was the fastest so far and stayed. */
+typedef struct {
+    uint32_t knob, bucket, value, kept;
+    double ms;
+} ebi_batch_trial;
 typedef struct ebi_batch ebi_batch;
 int ebi_batch_create(const ebi_batch_query* queries, uint64_t n, void* stream, ebi_batch** out);
 /* preds (n entries, may be NULL) replace the queries' predicates for this and
  * later runs; results (n entries, may be NULL) receive each query's result. */
 int ebi_batch_run(ebi_batch* batch, const ebi_predicate* preds, ebi_batch_result* results, void* stream);
 int ebi_batch_get_info(const ebi_batch* batch, ebi_batch_info* out);
+/* Copies up to max of the first run's timed candidates, in the order timed. */
+int ebi_batch_get_trials(const ebi_batch* batch, ebi_batch_trial* out, uint32_t max, uint32_t* n_out);
+/* Process-wide tuning cache: a JSON file mapping a batch's column shape (the
+ * SM count and the number of queries per codec and size bucket) to the chosen
+ * configuration.  Batches whose first run finds their shape there skip the
+ * timing; new choices are written back.  NULL (the default) turns it off. */
+int ebi_batch_set_tuning_cache(const char* path);
 int ebi_batch_destroy(ebi_batch* batch);
 
 /* ---- serving loop ----------------------------------------------------------- */
@@ -258,9 +287,16 @@ typedef struct {
     uint64_t max_queries_per_batch;  /* column queries per batch */
     uint64_t max_chunks_per_batch;   /* per-chunk accumulators per batch */
     uint64_t max_items_per_batch;    /* work items per batch */
+    /* work-item tiling (0: the default) */
+    uint32_t buff_tiles_per_item;     /* 8,192-row BUFF tiles per item (default 8, at most 16) */
+    uint32_t value_chunks_per_item;   /* RLE / Uncompressed chunks per item (default 8, at most 16) */
+    uint32_t gorilla_chunks_per_item; /* Gorilla chunks per item, one warp walks each (default 16, at most 64) */
+    uint32_t reserved;
 } ebi_server_config;
 typedef struct {
     uint64_t batches, requests, max_in_flight, pending;
+    uint64_t items;     /* work items launched */
+    uint64_t build_ns;  /* dispatcher time spent building batches (host) */
 } ebi_server_stats;
 typedef struct ebi_server ebi_server;
 int ebi_server_create(ebi_column* const* columns, uint32_t n_columns, const ebi_server_config* config,

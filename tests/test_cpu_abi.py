@@ -105,3 +105,41 @@ def test_file_header_layout(codec, chunk):
         # the chunks fill the bytes between the 30-byte header and the footer
         first_chunk, first_row = struct.unpack_from("<QQ", data, footer + 16)
         assert first_chunk == 30 and first_row == 0
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ctypes mirror in ebi_gb300/_native.py has the size and field offsets
+    of its C struct in include/ebi_gpu.h (compiled here with the host C compiler)."""
+    import ctypes
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    from ebi_gb300 import _native as N
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    pairs = {"ebi_predicate": N.Predicate, "ebi_batch_query": N.BatchQuery, "ebi_batch_result": N.BatchResult,
+             "ebi_batch_info": N.BatchInfo, "ebi_batch_trial": N.BatchTrial, "ebi_request": N.Request,
+             "ebi_response": N.Response, "ebi_server_config": N.ServerConfig, "ebi_server_stats": N.ServerStats,
+             "ebi_segment_times": N.SegmentTimes, "ebi_expr_node": N.ExprNode, "ebi_aggregation": N.Aggregation}
+    lines = ['#include <stdio.h>', '#include "ebi_gpu.h"', "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = Path(__file__).resolve().parent.parent / "include"
+    subprocess.run([cc, "-std=c11", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        name, field, val = ln.split()
+        got[(name, field)] = int(val)
+    for cname, py in pairs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])

@@ -3,6 +3,8 @@ oracle and against the single-column ebi_filter_agg: every query's bitmask,
 min, max and count equal the oracle's Decoder on the same bytes bit for bit,
 its sum is exact (BUFF) or within the compensated-sum bound of the oracle's
 sequential sum, and all of them are bit-identical to the same query run alone."""
+import json
+
 import numpy as np
 import pytest
 
@@ -97,3 +99,56 @@ def test_batch_reports_a_failing_query():
     st = b.statuses()
     assert st[0] == 0 and st[1] == E.UnexpectedEndOfChunk.code
     b.close()
+
+
+def test_tiling_is_tuned_cached_and_exact(tmp_path):
+    # Columns of every codec family in the two smaller size buckets: the first run
+    # times the launch shapes and then the tiles per item of each (family, bucket)
+    # present; whatever it picks, every query equals the oracle and the query run
+    # alone.  A second batch of the same column shape takes the choice from the
+    # tuning cache (no timing) and gives the same bits.
+    rng = np.random.default_rng(9)
+    cols = make_columns(rng, 24)
+    queries = []
+    for k, (d, v, _, _) in enumerate(cols):
+        aggs = [("sum", "min", "max"), ("sum",), ("min",), ("max",)][k % 4]
+        queries.append((d, random_preds(v, rng, k=1)[0], aggs))
+    path = tmp_path / "tuning.json"
+    E.Batch.set_tuning_cache(path)
+    try:
+        b = E.Batch(queries, want_masks=True)
+        got = b.run()
+        info = b.info()
+        knobs = {t["knob"] for t in info["trials"]}
+        assert {"shape", "buff_tiles", "value_chunks", "gorilla_chunks"} <= knobs, knobs
+        assert not info["from_cache"] and info["items"] > 0 and info["best_ms"] > 0
+        assert sum(t["kept"] for t in info["trials"] if t["knob"] == "shape") == 1
+        for k, (d, p, aggs) in enumerate(queries):
+            m, s, mn, mx, n = alone(d, p, aggs)
+            gs, gmn, gmx, gn = got[k]
+            om, os_, omn, omx, on, sel = oracle_filter_agg(cols[k][2], p)
+            assert gn == on == n, k
+            assert np.array_equal(mask_np(b.masks[k])[: len(om)], om), k
+            assert same(gs, s) and same(gmn, mn) and same(gmx, mx), k
+            if "sum" in aggs:
+                assert sum_ok(gs, os_, cols[k][3] == "buff", sel), k
+            if "min" in aggs:
+                assert same_scalar(gmn, omn), k
+            if "max" in aggs:
+                assert same_scalar(gmx, omx), k
+        cache = json.loads(path.read_text())
+        assert len(cache) == 1
+        entry = next(iter(cache.values()))
+        assert entry["buff_tiles"] == info["buff_tiles"] and entry["gorilla_chunks"] == info["gorilla_chunks"]
+        assert entry["value_chunks"] == info["value_chunks"] and entry["ctas_per_sm"] == info["ctas_per_sm"]
+        b2 = E.Batch(queries)
+        got2 = b2.run()
+        info2 = b2.info()
+        assert info2["from_cache"] and not info2["trials"]
+        assert info2["buff_tiles"] == info["buff_tiles"] and info2["value_chunks"] == info["value_chunks"]
+        for a, c in zip(got, got2):
+            assert all(same(x, y) for x, y in zip(a, c))
+        b.close()
+        b2.close()
+    finally:
+        E.Batch.set_tuning_cache(None)

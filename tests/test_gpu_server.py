@@ -136,3 +136,26 @@ def test_poll_interface():
     for t, a in zip(tickets, alone):
         m = got[t]
         assert a["count"] == m["count"] and same(a["sum"], m["sum"]) and same(a["min"], m["min"]) and same(a["max"], m["max"])
+
+
+@pytest.mark.parametrize("tiling", [(1, 1, 8), (16, 16, 64), (3, 5, 24)])
+def test_every_tiling_gives_the_same_answers(tiling):
+    # BUFF tiles, RLE / Uncompressed chunks and Gorilla chunks per work item change
+    # only how the work is cut, never a result: each setting answers as the plain
+    # per-column calls do, bit for bit, and as the oracle does.
+    rng = np.random.default_rng(23)
+    cols = columns(rng, 12, codecs=("buff", "gorilla", "rle", "chimp128"), lo=20_000, hi=400_000)
+    decs = [d for d, _, _ in cols]
+    reqs = requests(rng, cols, 120)
+    bt, vc, gc = tiling
+    srv = E.Server(decs, slots=2, max_queries=512, max_chunks=1 << 16, max_items=1 << 17, buff_tiles=bt,
+                   value_chunks=vc, gorilla_chunks=gc)
+    mixed = srv.replay(reqs)
+    st = srv.stats()
+    srv.close()
+    assert st["items"] > 0
+    alone = E.run_plain(decs, reqs)
+    for a, m in zip(alone, mixed):
+        assert m["status"] == 0
+        assert a["count"] == m["count"] and same(a["sum"], m["sum"]) and same(a["min"], m["min"]) and same(a["max"], m["max"])
+    check_oracle(cols, reqs, mixed)
