@@ -415,7 +415,8 @@ def config_results(args, dec, data, dev, flush, clean):
     a.steps = 40
     v = timed("C5_serving", lambda: serving_line(a))
     res["C5_serving"] = {k: v[k] for k in ("value", "unit", "plain_queries_per_s", "speedup_vs_plain",
-                                           "results_equal_alone_and_in_mix", "poisson", "config", "server_stats")}
+                                           "decoded_gb_per_s_saturated", "results_equal_alone_and_in_mix", "poisson",
+                                           "config", "server_stats")}
     time.sleep(0.2)
     sampler.stop()
     for key, (t0, t1) in spans.items():
@@ -629,14 +630,17 @@ def serving_line(args):
     t0 = time.perf_counter()
     plain = E.run_plain(decs, plain_reqs)
     plain_qps = len(plain_reqs) / (time.perf_counter() - t0)
-    srv = E.Server(decs, slots=4, max_queries=4096, max_chunks=1 << 21, max_items=1 << 22)
+    caps = {"slots": 4, "max_queries": 16384, "max_chunks": 1 << 23, "max_items": 1 << 23}
+    srv = E.Server(decs, **caps)
     srv.replay(plain_reqs[:50])  # warm-up
     # saturated throughput: a full queue (the plain requests first, then more), all submitted at once;
     # the plain requests' answers in the mix are compared bit for bit with their plain answers
-    sat_reqs = plain_reqs + make_requests(max(0, 2000 - len(plain_reqs)))
+    sat_reqs = plain_reqs + make_requests(max(0, 4000 - len(plain_reqs)))
     t0 = time.perf_counter()
     mixed = srv.replay(sat_reqs)
-    sat_qps = len(sat_reqs) / (time.perf_counter() - t0)
+    sat_s = time.perf_counter() - t0
+    sat_qps = len(sat_reqs) / sat_s
+    sat_rows = sum(meta[i][1] for ids, _, _ in sat_reqs for i in ids)
     mixed = mixed[: len(plain_reqs)]
     equal = all((a["count"] == b["count"]) and all(
         (a[f] == b[f]) or (np.isnan(a[f]) and np.isnan(b[f])) for f in ("sum", "min", "max"))
@@ -662,9 +666,11 @@ def serving_line(args):
             "config": {"workload": "serving: resident columns of log-uniform length 256K..16M f64, codecs uniform over "
                                    "Gorilla/Chimp128/BUFF/RLE; requests: random range + one of sum/min/max over 1..8 columns",
                        "columns": n_cols, "scale": args.scale, "rows": sum(m[1] for m in meta),
-                       "column_bytes": sum(m[2] for m in meta), "slots": 4},
+                       "column_bytes": sum(m[2] for m in meta), **caps,
+                       "tiling": "server default: 8 BUFF tiles, 8 RLE chunks, 16 Gorilla chunks per work item"},
             "saturated_requests": len(sat_reqs), "plain_requests": len(plain_reqs),
             "plain_queries_per_s": round(plain_qps, 1), "speedup_vs_plain": round(sat_qps / plain_qps, 2),
+            "decoded_gb_per_s_saturated": round(8.0 * sat_rows / sat_s / 1e9, 1),
             "results_equal_alone_and_in_mix": bool(equal), "poisson": rates, "server_stats": st}
     for d in decs:
         d.close()

@@ -71,6 +71,32 @@ __global__ void __launch_bounds__(kTileThreads) buff_count_kernel(QueryParams q,
 constexpr int kMatStage = 32 * 33;  // entries per warp
 constexpr size_t kMatSmem = size_t(kTileWarps) * kMatStage * sizeof(unsigned long long);
 
+// The warp's run: staged entry j (padded position j + j / 32) becomes output
+// wbase + j.  SMALL: every fixed value of the chunk fits an int32.
+template <bool SMALL, typename D>
+__device__ __forceinline__ void mat_write(const QueryParams& q, const BuffCtx& k, const D* st,
+                                          unsigned long long wbase, unsigned int wcount, int lane) {
+    const unsigned long long base = static_cast<unsigned long long>(k.base);
+    auto value = [&](D delta) -> double {
+        if constexpr (SMALL)
+            return fixed32_to_f64(static_cast<int32_t>(static_cast<uint32_t>(base) + static_cast<uint32_t>(delta)), k.frac);
+        else
+            return fixed_to_f64(static_cast<long long>(base + static_cast<unsigned long long>(delta)), k.frac, k.scale);
+    };
+    if (wcount == 1024 && wbase + 1024 <= q.out_cap) {
+        double* o = q.out_vals + wbase + lane;
+        const D* sp = st + lane;
+#pragma unroll 8
+        for (int it = 0; it < 32; ++it) o[32 * it] = value(sp[33 * it]);
+        return;
+    }
+#pragma unroll 4
+    for (unsigned int j = lane; j < wcount; j += 32) {
+        const unsigned long long pos = wbase + j;
+        if (pos < q.out_cap) q.out_vals[pos] = value(st[j + (j >> 5)]);
+    }
+}
+
 template <int TB, typename D>
 __device__ void buff_mat_tile(const QueryParams& q, const BuffCtx& k, uint32_t begin,
                               const unsigned long long* tile_offsets, unsigned long long base_row,
@@ -85,45 +111,53 @@ __device__ void buff_mat_tile(const QueryParams& q, const BuffCtx& k, uint32_t b
         sel = has_mask ? (mask_word(q.in_mask, k.row_off + r0, q.n_records) & valid) : valid;
         if (sel) load_deltas<TB, D>(k, r0, k.np_load, k.np, k.load_tail, d);
     }
-    // block-exclusive prefix of the per-thread counts
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const unsigned int cnt = __popc(sel);
-    unsigned int inc = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned int y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += y;
-    }
-    if (lane == 31) warp_tot[wid] = inc;
-    __syncthreads();
-    const unsigned int wcount = __shfl_sync(0xffffffffu, inc, 31);
-    if (wcount == 0) return;  // warp-uniform
+    unsigned int wcount, off;
     unsigned long long wbase;
     if (has_mask) {
+        // block-exclusive prefix of the per-thread counts (has_mask is the same for the whole block)
+        const unsigned int cnt = __popc(sel);
+        unsigned int inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) warp_tot[wid] = inc;
+        __syncthreads();
+        wcount = __shfl_sync(0xffffffffu, inc, 31);
+        if (wcount == 0) return;  // warp-uniform
         unsigned int before = 0;
         for (int w = 0; w < wid; ++w) before += warp_tot[w];
         wbase = tile_offsets[blockIdx.x] + before;
+        off = inc - cnt;
     } else {
-        // lane 0 holds rows, so every lane before the last holding any is full
-        wbase = k.row_off + begin + uint32_t(wid) * 1024u - base_row;
+        // every row of the warp's 1,024 inside the chunk, in order: lanes before
+        // the last holding rows are full
+        const uint32_t w0 = begin + uint32_t(wid) * 1024u;
+        wcount = k.ok && w0 < k.n ? (k.n - w0 < 1024u ? k.n - w0 : 1024u) : 0u;
+        if (wcount == 0) return;  // warp-uniform
+        wbase = k.row_off + w0 - base_row;
+        off = uint32_t(lane) * 32u;
     }
     D* st = reinterpret_cast<D*>(stage) + wid * kMatStage;
-    unsigned int off = inc - cnt;
+    if (sel == ~0u && off == uint32_t(lane) * 32u) {
+        // a full lane at its own place: rows lane*32 + i go to entries lane*33 + i
+        D* p = st + lane * 33;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
-        if ((sel >> i) & 1u) {
-            st[off + (off >> 5)] = d[i];
-            ++off;
+        for (int i = 0; i < 32; ++i) p[i] = d[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            if ((sel >> i) & 1u) {
+                st[off + (off >> 5)] = d[i];
+                ++off;
+            }
         }
     }
     __syncwarp();
-    const unsigned long long base = static_cast<unsigned long long>(k.base);
-#pragma unroll 4
-    for (unsigned int j = lane; j < wcount; j += 32) {
-        const unsigned long long pos = wbase + j;
-        const long long fixed = static_cast<long long>(base + static_cast<unsigned long long>(st[j + (j >> 5)]));
-        if (pos < q.out_cap) q.out_vals[pos] = fixed_to_f64(fixed, k.frac, k.scale);
-    }
+    if (k.fits32 && sizeof(D) == 4) mat_write<true, D>(q, k, st, wbase, wcount, lane);
+    else mat_write<false, D>(q, k, st, wbase, wcount, lane);
 }
 
 template <typename D>

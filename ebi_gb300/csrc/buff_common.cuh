@@ -54,6 +54,20 @@ __device__ __forceinline__ double fixed_to_f64(long long fixed, uint32_t frac, d
     return __longlong_as_double(static_cast<long long>(sign | (ex << 52) | (mant & 0xfffffffffffffull)));
 }
 
+// fixed_to_f64 for a value that fits an int32 with frac <= 1022: exact (at most
+// 32 significant bits) and normal, so only the leading-zero count, one shift
+// and the exponent remain, in 32-bit arithmetic.
+__device__ __forceinline__ double fixed32_to_f64(int32_t fixed, uint32_t frac) {
+    const uint32_t s = static_cast<uint32_t>(fixed >> 31);     // 0 or all ones
+    const uint32_t m = (static_cast<uint32_t>(fixed) ^ s) - s;  // |fixed|
+    const int lz = __clz(static_cast<int>(m));                  // m in [2^(31 - lz), 2^(32 - lz))
+    // significand with its leading one at bit 52, plus the biased exponent minus one
+    const unsigned long long mant = static_cast<unsigned long long>(m) << (lz + 21);
+    const uint32_t hi = static_cast<uint32_t>(mant >> 32) + (static_cast<uint32_t>(1053 - lz - static_cast<int>(frac)) << 20);
+    const uint32_t lo = static_cast<uint32_t>(mant);
+    return m ? __hiloint2double(static_cast<int>(hi | (s & 0x80000000u)), static_cast<int>(lo)) : 0.0;
+}
+
 enum : uint32_t { SIDE_ABSENT = 0, SIDE_ALL = 1, SIDE_NONE = 2, SIDE_CMP = 3 };
 
 // Predicate compiled into the delta domain of one chunk, exactly as the

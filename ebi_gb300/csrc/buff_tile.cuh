@@ -27,6 +27,7 @@ struct BuffCtx {
     uint32_t n, bits, frac, np, tb;
     uint32_t np_load, load_tail;  // planes / tail read when materializing
     uint32_t ok;                  // selected and readable
+    uint32_t fits32;              // every row's fixed value fits an int32 and frac <= 1022
     uint32_t selected;
     // predicate compiled into the delta domain
     uint32_t lmode, rmode, lincl, rincl, emode;
@@ -61,6 +62,8 @@ __device__ void buff_setup(const QueryParams& q, uint32_t c, bool has_mask, Buff
     k.scale = k.frac <= 1023 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 + k.frac) << 52))
                              : __longlong_as_double(0x7ff0000000000000ll);
     k.inv_scale = k.frac <= 1022 ? __longlong_as_double(static_cast<long long>(uint64_t(1023 - k.frac) << 52)) : 0.0;
+    k.fits32 = k.frac <= 1022 && k.bits <= 31 && k.base >= -2147483648ll &&
+               k.base + ((1ll << k.bits) - 1) <= 2147483647ll;
 
     // controlled precision (buff/controlled_precision.rs:5-75)
     k.np_load = k.np;
