@@ -357,7 +357,8 @@ def materialize_config(dec, data, dev, steps, warmup, flush, clean):
     n = dec.n_records
     out = torch.empty(n, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
-    ts = []
+    dec.set_timing(True)
+    ts, ks = [], []
     for i in range(warmup + steps):
         flush.fill_(i & 0xFF)
         clean.sum()
@@ -369,7 +370,9 @@ def materialize_config(dec, data, dev, steps, warmup, flush, clean):
         e1.synchronize()
         if i >= warmup:
             ts.append(e0.elapsed_time(e1) / 1e3)
+            ks.append(dec.segmented_execution_times()["scan_ms"] / 1e3)
     t = statistics.median(ts)
+    kt = statistics.median(ks)
     want = O.Decoder(data, threads=os.cpu_count() or 1).materialize()
     same = bool(np.array_equal(out.cpu().numpy().view(np.uint64), want.view(np.uint64)))
     col = sum(dec.chunk_info(c)[1] for c in range(dec.n_chunks))
@@ -377,9 +380,11 @@ def materialize_config(dec, data, dev, steps, warmup, flush, clean):
     peak, _ = measured_peak()
     return {"workload": "C2 full materialize: every value of the headline column written to a device array",
             "rows": n, "value": round(8.0 * n / t / 1e9, 3), "unit": UNIT, "ms_per_step": round(1e3 * t, 4),
+            "kernel": "buff_materialize_kernel<false> (32-bit deltas)", "kernel_ms": round(1e3 * kt, 4),
             "roofline": {"bound": "hbm", "algorithmic_bytes_per_launch": alg, "read_bytes": col, "write_bytes": 8 * n,
                          "achieved": round(alg / t / 1e9, 1), "peak": peak, "frac": round(alg / t / 1e9 / peak, 4),
-                         "scope": "whole call (decode + write)"},
+                         "scope": "whole call (decode + write)",
+                         "kernel_achieved": round(alg / kt / 1e9, 1), "kernel_frac": round(alg / kt / 1e9 / peak, 4)},
             "parity_check": {"values_bit_exact": same}}
 
 
@@ -856,6 +861,8 @@ def main():
                                                                "batched", "serving", "tpch_q6", "tpch_q1"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="batched / serving: fraction of the configuration's columns to build")
+    ap.add_argument("--materialize", action="store_true",
+                    help="BUFF workload: measure only the full materialize of the column (C2's second leg)")
     ap.add_argument("--no-configs", action="store_true",
                     help="headline only: skip the other configurations (C1, C2 materialize, C3a, C3b, C4, C5)")
     args = ap.parse_args()
@@ -910,6 +917,10 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MiB > 129 MB L2
     clean = torch.zeros(32 << 20, dtype=torch.float64, device=dev)  # another 256 MiB, read after the write
     alg_bytes = sum(dec.chunk_info(c)[1] for c in range(dec.n_chunks)) + 8 * dec.mask_words
+    if args.materialize:
+        if rank == 0:
+            print(json.dumps(materialize_config(dec, data, dev, args.steps, args.warmup, flush, clean)), flush=True)
+        return
 
     def one_step(i):
         flush.fill_(i & 0xFF)  # evicts the column from L2 (not timed)

@@ -33,6 +33,17 @@ static_assert(kBatchThreads == kXorThreads && kBatchThreads == kRleThreads, "cod
 
 // One function per item kind, kept out of line so that each gets its own
 // register allocation (the kernel's is the largest, not the sum of all paths).
+// One tile with 32-bit or 64-bit deltas, each out of line with its own
+// register allocation (the 64-bit form needs twice the delta registers).
+__device__ __noinline__ void buff_tile32(const QueryParams& q, const BuffCtx& k, uint32_t chunk, uint32_t tile,
+                                         uint32_t begin, BlockRed& red) {
+    buff_query_dispatch<uint32_t>(q, k, chunk, tile, begin, red);
+}
+__device__ __noinline__ void buff_tile64(const QueryParams& q, const BuffCtx& k, uint32_t chunk, uint32_t tile,
+                                         uint32_t begin, BlockRed& red) {
+    buff_query_dispatch<unsigned long long>(q, k, chunk, tile, begin, red);
+}
+
 // Tiles [unit, unit + count) of one query's column; the chunk context is set
 // up again only when the chunk changes.
 __device__ __noinline__ void item_buff_tile(const QueryParams& q, const BatchItem& it, BuffCtx& k, BlockRed& red) {
@@ -46,8 +57,8 @@ __device__ __noinline__ void item_buff_tile(const QueryParams& q, const BatchIte
             __syncthreads();
             chunk = t.chunk;
         }
-        if (k.ok && k.bits > 32) buff_query_dispatch<unsigned long long>(q, k, t.chunk, tile, t.begin, red);
-        else buff_query_dispatch<uint32_t>(q, k, t.chunk, tile, t.begin, red);
+        if (k.ok && k.bits > 32) buff_tile64(q, k, t.chunk, tile, t.begin, red);
+        else buff_tile32(q, k, t.chunk, tile, t.begin, red);
     }
 }
 __device__ __noinline__ void item_raw(const QueryParams& q, const BatchItem& it) {
@@ -62,12 +73,23 @@ __device__ __noinline__ void item_rle(const QueryParams& q, const BatchItem& it)
         rle_chunk(q, it.unit + j, it.unit + j, VAL_SCAN, nullptr);
     }
 }
-// Chunks [unit, unit + chunks): warp w walks chunks w, w + 8, ...
+// Chunks [unit, unit + chunks): warp w walks chunks w, w + 8, ...  Up to
+// kGorillaShare queries keep their state in registers; more (up to
+// kGorillaShareWide) keep it in the warp's share of the dynamic shared memory.
+static_assert(kGorillaShareWide <= kSharedSinkQueries, "shared-memory walk state");
+static_assert((kBatchThreads / 32) * sizeof(SharedSinkState) <= xor_smem_bytes(CODEC_CHIMP128),
+              "the batch kernel's dynamic shared memory holds one walk state per warp");
 __device__ __noinline__ void item_gorilla(const QueryParams& q, const BatchItem& it) {
     const uint32_t warp = threadIdx.x >> 5, chunks = it.count & 0xffu;
     const uint32_t nq = it.count >> 8 ? it.count >> 8 : 1u;  // queries it.query .. + nq: one column
-    for (uint32_t w = warp; w < chunks; w += kBatchThreads / 32)
-        gorilla_chunk_l1<kGorillaShare>(&q, nq, it.unit + w, it.unit + w, VAL_SCAN, nullptr);
+    if (nq <= kGorillaShare) {
+        for (uint32_t w = warp; w < chunks; w += kBatchThreads / 32)
+            gorilla_chunk_l1<kGorillaShare>(&q, nq, it.unit + w, it.unit + w, VAL_SCAN, nullptr);
+        return;
+    }
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    SharedSinkState* st = reinterpret_cast<SharedSinkState*>(smem_raw) + warp;
+    for (uint32_t w = warp; w < chunks; w += kBatchThreads / 32) gorilla_chunk_l1_shared(&q, nq, it.unit + w, st);
 }
 __device__ __noinline__ void item_chimp(const QueryParams& q, const BatchItem& it) {
     xor_chunk<CODEC_CHIMP>(&q, it.count, it.unit, it.unit, VAL_SCAN, nullptr);  // queries it.query .. + count: one column

@@ -1,55 +1,128 @@
-// gorilla.cu -- kernel and launcher of the Gorilla chunk pass (gorilla_dev.cuh):
-// one warp per chunk, the chunk staged in shared memory by one bulk copy
-// (cp.async.bulk, completed on an mbarrier with a bounded wait); chunks above
-// the staging size are read through L1 from the resident file instead.
+// gorilla.cu -- kernel and launcher of the Gorilla chunk pass (gorilla_dev.cuh).
+//
+// One CTA of two warps per chunk: warp 0 brings the chunk into shared memory
+// by one bulk copy (cp.async.bulk, completed on an mbarrier with a bounded
+// wait; chunks above the staging size are read through L1 from the resident
+// file instead) and parses the stream; each parse step's values (up to 32,
+// one per lane) go through a ring of kRing slots in shared memory to warp 1,
+// which applies the query to them.  The parse no longer waits for the query's
+// work (predicate, bitmask word, compensated sums) between its steps.  Warp 1
+// gives step values to lanes exactly as the one-warp walk does (value i of a
+// step to lane i), so every per-lane running sum, and the result, is the same
+// as the batched path's walk.  Slots are handed over with full / empty
+// mbarriers (32 arrivals each: every lane releases its own writes); every wait
+// is bounded and a wait that runs out ends the chunk with EBI_E_CUDA.
 #include "internal.h"
 #include "gorilla_dev.cuh"
 
 namespace ebi {
 namespace {
 
-constexpr int kWarpsPerCta = 1;  // one chunk (and its staged bytes) per CTA
+constexpr int kRing = 8;
+constexpr uint32_t kEnd = 1u << 8;  // meta: the parse is over; status in bits 16..
 
-__global__ void __launch_bounds__(kWarpsPerCta * 32) gorilla_kernel(QueryParams q, uint32_t chunk_base, uint32_t n_chunks,
-                                                                    int mode, const unsigned long long* chunk_offsets) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t li = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
-    if (li >= n_chunks) return;  // whole warps; the kernel has no block barriers
+struct __align__(16) GorillaRing {
+    uint64_t full[kRing];
+    uint64_t empty[kRing];
+    uint32_t meta[kRing];  // k | kEnd | status << 16
+    uint32_t ok;           // the chunk is read by this pass
+    uint32_t pad[3];
+    uint64_t vals[kRing][32];
+};
+constexpr size_t kRingOff = 16;  // after the bulk copy's mbarrier
+constexpr size_t kStageOff = kRingOff + sizeof(GorillaRing);
+static_assert(kStageOff % 16 == 0, "bulk copies land on 16-byte boundaries");
+
+__global__ void __launch_bounds__(64) gorilla_kernel(QueryParams q, uint32_t chunk_base, int mode,
+                                                     const unsigned long long* chunk_offsets) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t li = blockIdx.x;
     const uint32_t c = chunk_base + li;
-    if (!gorilla_begin(q, li, c, mode, chunk_offsets)) return;
-    const ChunkDesc cd = q.chunks[c];
-    ChunkAcc* acc = q.acc + c;
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-    const uint32_t* stage = reinterpret_cast<const uint32_t*>(smem + 16);
-    const uint64_t span = stage_span(cd.byte_off, cd.byte_len);
-    if (span <= q.stage_bytes) {
-        const uint8_t* src = q.file + (cd.byte_off & ~uint64_t(15));
+    GorillaRing* R = reinterpret_cast<GorillaRing*>(smem + kRingOff);
+    if (warp == 0) {
+        const bool ok = gorilla_begin(q, li, c, mode, chunk_offsets);  // warp-collective
         if (lane == 0) {
+            R->ok = ok ? 1u : 0u;
+            for (int i = 0; i < kRing; ++i) {
+                mbar_init(&R->full[i], 32);
+                mbar_init(&R->empty[i], 32);
+            }
             mbar_init(bar, 1);
             fence_mbar_init();
-            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(span));
-            bulk_g2s(smem + 16, src, static_cast<uint32_t>(span), bar);
         }
-        __syncwarp();
-        bool arrived = mbar_wait(bar, 0, q.copy_wait);
-        if (!__all_sync(kFull, arrived)) {
-            // give the copy a second wait (full limit) before the CTA leaves, then report it
-            mbar_wait(bar, 0);
-            if (lane == 0) {
-                set_status(acc, EBI_E_CUDA);
-                if (mode == VAL_COUNT) q.tile_counts[li] = 0;
-            }
-            return;
-        }
-        const uint64_t bit0 = (cd.byte_off & 15) * 8;
-        walk<1>(&q, 1, 1u, cd, c, li, mode, chunk_offsets,
-                [stage, bit0](uint64_t p) { return peek64_le_smem(stage, bit0 + p); });
-    } else {
-        const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
-        const uint64_t bit0 = cd.byte_off * 8;
-        walk<1>(&q, 1, 1u, cd, c, li, mode, chunk_offsets, [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); });
     }
+    __syncthreads();
+    if (!R->ok) return;
+    const ChunkDesc cd = q.chunks[c];
+
+    if (warp == 0) {
+        // ---- parse: each step into the next ring slot ----------------------
+        uint32_t n = 0;       // slots put
+        bool broken = false;  // a wait for a free slot ran out: the rest is dropped
+        auto put = [&](uint32_t k, uint64_t v, uint32_t flags) {
+            if (broken) return;
+            const uint32_t s = n % kRing;
+            if (n >= kRing && !__all_sync(kFull, mbar_wait(&R->empty[s], ((n / kRing) - 1) & 1))) {
+                broken = true;
+                if (lane == 0) set_status(q.acc + c, EBI_E_CUDA);
+                return;
+            }
+            R->vals[s][lane] = v;
+            if (lane == 0) R->meta[s] = k | flags;
+            mbar_arrive(&R->full[s]);
+            ++n;
+        };
+        const uint64_t span = stage_span(cd.byte_off, cd.byte_len);
+        uint32_t status;
+        if (span <= q.stage_bytes) {
+            const uint8_t* src = q.file + (cd.byte_off & ~uint64_t(15));
+            if (lane == 0) {
+                mbar_arrive_expect_tx(bar, static_cast<uint32_t>(span));
+                bulk_g2s(smem + kStageOff, src, static_cast<uint32_t>(span), bar);
+            }
+            __syncwarp();
+            if (!__all_sync(kFull, mbar_wait(bar, 0, q.copy_wait))) {
+                mbar_wait(bar, 0);  // a second wait (full limit) before the CTA leaves
+                status = EBI_E_CUDA;
+            } else {
+                const uint32_t* stage = reinterpret_cast<const uint32_t*>(smem + kStageOff);
+                const uint64_t bit0 = (cd.byte_off & 15) * 8;
+                status = parse_stream(cd.byte_len * 8, [stage, bit0](uint64_t p) { return peek64_le_smem(stage, bit0 + p); },
+                                      [&](uint32_t k, uint64_t v) { put(k, v, 0u); });
+            }
+        } else {
+            const uint32_t* fw = reinterpret_cast<const uint32_t*>(q.file);
+            const uint64_t bit0 = cd.byte_off * 8;
+            status = parse_stream(cd.byte_len * 8, [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); },
+                                  [&](uint32_t k, uint64_t v) { put(k, v, 0u); });
+        }
+        put(0u, 0ull, kEnd | (status << 16));
+        return;
+    }
+
+    // ---- query: the ring's steps in order -------------------------------------
+    WalkSink<1> sink;
+    sink.init(&q, 1, 1u, cd, li, mode, chunk_offsets);
+    uint32_t status = 0;
+    for (uint32_t n = 0;; ++n) {
+        const uint32_t s = n % kRing;
+        if (!__all_sync(kFull, mbar_wait(&R->full[s], (n / kRing) & 1))) {
+            status = EBI_E_CUDA;
+            break;
+        }
+        const uint32_t meta = R->meta[s];
+        const uint64_t v = R->vals[s][lane];
+        mbar_arrive(&R->empty[s]);
+        if (meta & kEnd) {
+            status = meta >> 16;
+            break;
+        }
+        sink.apply(meta & 0xffu, v);
+    }
+    if (status) sink.fail(c, li, status);
+    else sink.finish(c, li);
 }
 
 }  // namespace
@@ -67,11 +140,10 @@ uint32_t gorilla_stage_bytes(const ChunkDesc* chunks, uint64_t n) {
 cudaError_t launch_gorilla(const QueryParams& q, uint32_t chunk_begin, uint32_t n_chunks, int mode,
                            const unsigned long long* chunk_offsets, cudaStream_t s) {
     if (n_chunks == 0) return cudaSuccess;
-    const uint32_t grid = (n_chunks + kWarpsPerCta - 1) / kWarpsPerCta;
-    const size_t smem = q.stage_bytes ? 16 + size_t(q.stage_bytes) : 16;
+    const size_t smem = kStageOff + size_t(q.stage_bytes);
     const cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(gorilla_kernel), smem);
     if (e != cudaSuccess) return e;
-    gorilla_kernel<<<grid, kWarpsPerCta * 32, smem, s>>>(q, chunk_begin, n_chunks, mode, chunk_offsets);
+    gorilla_kernel<<<n_chunks, 64, smem, s>>>(q, chunk_begin, mode, chunk_offsets);
     count_launch();
     return cudaGetLastError();
 }

@@ -50,37 +50,43 @@ __host__ __device__ __forceinline__ uint64_t stage_span(uint64_t byte_off, uint6
     return ((byte_off + byte_len + 15) & ~uint64_t(15)) + 16 - (byte_off & ~uint64_t(15));
 }
 
-// Decodes chunk cd and runs the query over its values (one warp).
-// The walk of one chunk for up to MaxQ queries over the same column at once
-// (qs[0 .. nq), those with bit j of okm set): the stream is parsed once and
-// each emitted run of values goes through every query's bitmask, predicate
-// and aggregates.  Materialize and count passes take one query.
-template <int MaxQ, typename Peek>
-__device__ __forceinline__ void walk(const QueryParams* qs, uint32_t nq, uint32_t okm, const ChunkDesc& cd, uint32_t c,
-                                     uint32_t li, int mode, const unsigned long long* chunk_offsets, Peek peek) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t B = cd.byte_len * 8;
+// The query side of a chunk walk: up to MaxQ queries over the same column
+// (qs[0 .. nq), those with bit j of okm set), each with its predicate and
+// per-lane running aggregates in registers.  Each emitted run of values (lanes
+// [0, k) hold chunk rows idx .. idx + k - 1) goes through every query's
+// bitmask, predicate and aggregates.  Materialize and count passes take one
+// query.
+template <int MaxQ>
+struct WalkSink {
+    const QueryParams* qs;
+    uint32_t nq, okm;
+    int mode;
+    uint64_t row_off;
     KeyPred kp[MaxQ];
     ValAgg agg[MaxQ];
-#pragma unroll
-    for (int j = 0; j < MaxQ; ++j) {
-        const QueryParams& q = qs[j < static_cast<int>(nq) ? j : 0];
-        kp[j] = key_pred(q.pred);
-        agg[j] = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
-    }
-    unsigned long long out_pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull;
-    uint64_t idx = 0;  // chunk row of the next value
+    unsigned long long out_pos;
+    uint64_t idx;  // chunk row of the next value
 
-    // Lanes [0, k) hold the values (bits) of rows idx + lane.  Applies the end
-    // marker and the queries; returns true when the stream ended here.
-    auto emit = [&](uint32_t k, uint64_t vbits) -> bool {
-        const uint32_t nanm = __ballot_sync(kFull, static_cast<uint32_t>(lane) < k && vbits == kNanBits);
-        bool ended = false;
-        if (nanm) {
-            k = __ffs(nanm) - 1;
-            ended = true;
+    __device__ __forceinline__ void init(const QueryParams* qs_, uint32_t nq_, uint32_t okm_, const ChunkDesc& cd,
+                                         uint32_t li, int mode_, const unsigned long long* chunk_offsets) {
+        qs = qs_;
+        nq = nq_;
+        okm = okm_;
+        mode = mode_;
+        row_off = cd.row_off;
+#pragma unroll
+        for (int j = 0; j < MaxQ; ++j) {
+            const QueryParams& q = qs[j < static_cast<int>(nq) ? j : 0];
+            kp[j] = key_pred(q.pred);
+            agg[j] = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
         }
-        const uint64_t g = cd.row_off + idx + lane;
+        out_pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0ull;
+        idx = 0;
+    }
+
+    __device__ __forceinline__ void apply(uint32_t k, uint64_t vbits) {
+        const int lane = threadIdx.x & 31;
+        const uint64_t g = row_off + idx + lane;
 #pragma unroll
         for (int j = 0; j < MaxQ; ++j) {
             if (j >= static_cast<int>(nq) || !((okm >> j) & 1u)) continue;  // the same for every lane
@@ -98,7 +104,7 @@ __device__ __forceinline__ void walk(const QueryParams* qs, uint32_t nq, uint32_
             } else {
                 if (mode == VAL_SCAN && pred_on && q.out_mask != nullptr) {
                     const uint32_t word = __ballot_sync(kFull, pass && g < q.n_records);
-                    if (lane == 0 && word) store_mask_word(q.out_mask, cd.row_off + idx, word, true);
+                    if (lane == 0 && word) store_mask_word(q.out_mask, row_off + idx, word, true);
                 }
                 if (pass) {
                     if (mode == VAL_COUNT) ++agg[j].cnt;
@@ -107,90 +113,205 @@ __device__ __forceinline__ void walk(const QueryParams* qs, uint32_t nq, uint32_
             }
         }
         idx += k;
-        return ended;
-    };
-
-    uint32_t status = 0;
-    if (B < 64) {
-        status = EBI_E_UNEXPECTED_END;
-    } else {
-        uint64_t carry = peek(0);  // the previous value
-        uint64_t p = 64;
-        uint32_t lead = 0, trail = 0;
-        bool done = emit(1, carry);
-        while (!done) {
-            if (p + 1 > B) { status = EBI_E_UNEXPECTED_END; break; }
-            const uint64_t x = peek(p);
-            if (!(x >> 63)) {
-                // '0' run: one repeat per zero bit inside the chunk
-                uint64_t z = x ? static_cast<uint64_t>(__clzll(static_cast<long long>(x))) : 64;
-                if (z > B - p) z = B - p;
-                const uint32_t k = z < 32 ? static_cast<uint32_t>(z) : 32u;
-                done = emit(k, carry);
-                p += k;
-                continue;
-            }
-            if (p + 2 > B) { status = EBI_E_UNEXPECTED_END; break; }
-            if (!((x >> 62) & 1)) {
-                // '10' run at stride 2 + sig
-                const uint32_t sig = 64 - lead - trail;  // 1..64
-                const uint64_t L = 2 + sig;
-                const uint64_t qi = p + static_cast<uint64_t>(lane) * L;
-                bool fits = qi + L <= B;
-                uint64_t y = 0;
-                if (fits) {
-                    y = peek(qi);
-                    fits = (y >> 62) == 2;
-                }
-                const uint32_t m = __ballot_sync(kFull, fits);
-                const uint32_t k = ~m ? static_cast<uint32_t>(__ffs(~m) - 1) : 32u;
-                if (k == 0) { status = EBI_E_UNEXPECTED_END; break; }  // the record at p does not fit
-                uint64_t d = 0;
-                if (static_cast<uint32_t>(lane) < k) {
-                    const uint64_t w = sig <= 62 ? (y << 2) : peek(qi + 2);
-                    d = (w >> (64 - sig)) << trail;
-                }
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint64_t t = __shfl_up_sync(kFull, d, o);
-                    if (lane >= o) d ^= t;
-                }
-                const uint64_t v = carry ^ d;
-                carry = __shfl_sync(kFull, v, k - 1);
-                p += k * L;
-                done = emit(k, v);
-                continue;
-            }
-            // '11': a new window
-            if (p + 13 > B) { status = EBI_E_UNEXPECTED_END; break; }
-            const uint32_t l = static_cast<uint32_t>(x >> 57) & 31u;
-            const uint32_t sg = (static_cast<uint32_t>(x >> 51) & 63u) + 1;
-            if (l + sg > 64) { status = EBI_E_CORRUPT; break; }
-            if (p + 13 + sg > B) { status = EBI_E_UNEXPECTED_END; break; }
-            lead = l;
-            trail = 64 - l - sg;
-            carry ^= (peek(p + 13) >> (64 - sg)) << trail;
-            p += 13 + sg;
-            done = emit(1, carry);
-        }
     }
-    if (status) {
-        if (lane == 0) {
+
+    __device__ __forceinline__ void fail(uint32_t c, uint32_t li, uint32_t status) {
+        if ((threadIdx.x & 31) == 0) {
             for (uint32_t j = 0; j < nq; ++j)
                 if ((okm >> j) & 1u) set_status(qs[j].acc + c, status);
             if (mode == VAL_COUNT) qs[0].tile_counts[li] = 0;
         }
-        return;
     }
-    if (mode == VAL_MATERIALIZE) return;
+
+    __device__ __forceinline__ void finish(uint32_t c, uint32_t li) {
+        const int lane = threadIdx.x & 31;
+        if (mode == VAL_MATERIALIZE) return;
 #pragma unroll
-    for (int j = 0; j < MaxQ; ++j) {
-        if (j >= static_cast<int>(nq) || !((okm >> j) & 1u)) continue;  // the same for every lane
-        const ValAgg a = val_agg_warp(agg[j]);
-        if (lane != 0) continue;
-        if (mode == VAL_COUNT) qs[j].tile_counts[li] = a.cnt;
-        else val_agg_store(qs[j].acc + c, a);
+        for (int j = 0; j < MaxQ; ++j) {
+            if (j >= static_cast<int>(nq) || !((okm >> j) & 1u)) continue;  // the same for every lane
+            const ValAgg a = val_agg_warp(agg[j]);
+            if (lane != 0) continue;
+            if (mode == VAL_COUNT) qs[j].tile_counts[li] = a.cnt;
+            else val_agg_store(qs[j].acc + c, a);
+        }
     }
+};
+
+// WalkSink with its per-query state in shared memory instead of registers, so
+// that one walk serves up to kSharedSinkQueries queries (a batch item's share
+// of the CTA's dynamic shared memory per warp).  Every lane runs the same
+// aggregate updates in the same order as WalkSink's (value i of a step to lane
+// i), so results are identical.  Scan passes only (no count / materialize).
+constexpr uint32_t kSharedSinkQueries = 8;
+struct SharedSinkState {
+    KeyPred kp[kSharedSinkQueries];
+    uint32_t want[kSharedSinkQueries];
+    double hi[kSharedSinkQueries][32], lo[kSharedSinkQueries][32];
+    unsigned long long mnk[kSharedSinkQueries][32], mxk[kSharedSinkQueries][32], cnt[kSharedSinkQueries][32];
+};
+
+struct SharedSink {
+    const QueryParams* qs;
+    uint32_t nq, okm;
+    uint64_t row_off;
+    uint64_t idx;
+    SharedSinkState* st;
+
+    __device__ __forceinline__ void init(const QueryParams* qs_, uint32_t nq_, uint32_t okm_, const ChunkDesc& cd,
+                                         SharedSinkState* st_) {
+        const int lane = threadIdx.x & 31;
+        qs = qs_;
+        nq = nq_;
+        okm = okm_;
+        row_off = cd.row_off;
+        idx = 0;
+        st = st_;
+        for (uint32_t j = 0; j < nq; ++j) {
+            const QueryParams& q = qs[j];
+            const ValAgg a = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
+            if (lane == 0) {
+                st->kp[j] = key_pred(q.pred);
+                st->want[j] = a.want;
+            }
+            st->hi[j][lane] = a.hi;
+            st->lo[j][lane] = a.lo;
+            st->mnk[j][lane] = a.mnk;
+            st->mxk[j][lane] = a.mxk;
+            st->cnt[j][lane] = a.cnt;
+        }
+        __syncwarp();
+    }
+
+    __device__ __forceinline__ void apply(uint32_t k, uint64_t vbits) {
+        const int lane = threadIdx.x & 31;
+        const uint64_t g = row_off + idx + lane;
+        for (uint32_t j = 0; j < nq; ++j) {
+            if (!((okm >> j) & 1u)) continue;  // the same for every lane
+            const QueryParams& q = qs[j];
+            const bool pred_on = q.pred_on != 0;
+            const bool in = static_cast<uint32_t>(lane) < k && (!q.in_mask || mask_row(q.in_mask, q.n_records, g));
+            const bool pass = in && (!pred_on || st->kp[j].pass(vbits));
+            if (pred_on && q.out_mask != nullptr) {
+                const uint32_t word = __ballot_sync(kFull, pass && g < q.n_records);
+                if (lane == 0 && word) store_mask_word(q.out_mask, row_off + idx, word, true);
+            }
+            if (pass) {
+                ValAgg a{st->hi[j][lane], st->lo[j][lane], st->mnk[j][lane], st->mxk[j][lane], st->cnt[j][lane],
+                         st->want[j]};
+                val_agg_add1(a, vbits);
+                st->hi[j][lane] = a.hi;
+                st->lo[j][lane] = a.lo;
+                st->mnk[j][lane] = a.mnk;
+                st->mxk[j][lane] = a.mxk;
+                st->cnt[j][lane] = a.cnt;
+            }
+        }
+        idx += k;
+    }
+
+    __device__ __forceinline__ void fail(uint32_t c, uint32_t status) {
+        if ((threadIdx.x & 31) == 0)
+            for (uint32_t j = 0; j < nq; ++j)
+                if ((okm >> j) & 1u) set_status(qs[j].acc + c, status);
+    }
+
+    __device__ __forceinline__ void finish(uint32_t c) {
+        const int lane = threadIdx.x & 31;
+        for (uint32_t j = 0; j < nq; ++j) {
+            if (!((okm >> j) & 1u)) continue;  // the same for every lane
+            ValAgg a{st->hi[j][lane], st->lo[j][lane], st->mnk[j][lane], st->mxk[j][lane], st->cnt[j][lane], st->want[j]};
+            a = val_agg_warp(a);
+            if (lane == 0) val_agg_store(qs[j].acc + c, a);
+        }
+    }
+};
+
+// The parse side of a chunk walk (one warp): follows the stream of B bits and
+// calls emit(k, vbits) for each step's values, lanes [0, k) holding them (the
+// end marker already cut off: k may be 0 on the last step).  Returns 0 when
+// the stream ended at its marker, else the chunk's error status.
+template <typename Peek, typename Emit>
+__device__ __forceinline__ uint32_t parse_stream(uint64_t B, Peek peek, Emit emit) {
+    const int lane = threadIdx.x & 31;
+    // applies the end marker to a step: true when the stream ended in it
+    auto step = [&](uint32_t k, uint64_t vbits) -> bool {
+        const uint32_t nanm = __ballot_sync(kFull, static_cast<uint32_t>(lane) < k && vbits == kNanBits);
+        const bool ended = nanm != 0;
+        emit(ended ? static_cast<uint32_t>(__ffs(nanm) - 1) : k, vbits);
+        return ended;
+    };
+    if (B < 64) return EBI_E_UNEXPECTED_END;
+    uint64_t carry = peek(0);  // the previous value
+    uint64_t p = 64;
+    uint32_t lead = 0, trail = 0;
+    if (step(1, carry)) return 0;
+    for (;;) {
+        if (p + 1 > B) return EBI_E_UNEXPECTED_END;
+        const uint64_t x = peek(p);
+        if (!(x >> 63)) {
+            // '0' run: one repeat per zero bit inside the chunk
+            uint64_t z = x ? static_cast<uint64_t>(__clzll(static_cast<long long>(x))) : 64;
+            if (z > B - p) z = B - p;
+            const uint32_t k = z < 32 ? static_cast<uint32_t>(z) : 32u;
+            p += k;
+            if (step(k, carry)) return 0;
+            continue;
+        }
+        if (p + 2 > B) return EBI_E_UNEXPECTED_END;
+        if (!((x >> 62) & 1)) {
+            // '10' run at stride 2 + sig
+            const uint32_t sig = 64 - lead - trail;  // 1..64
+            const uint64_t L = 2 + sig;
+            const uint64_t qi = p + static_cast<uint64_t>(lane) * L;
+            bool fits = qi + L <= B;
+            uint64_t y = 0;
+            if (fits) {
+                y = peek(qi);
+                fits = (y >> 62) == 2;
+            }
+            const uint32_t m = __ballot_sync(kFull, fits);
+            const uint32_t k = ~m ? static_cast<uint32_t>(__ffs(~m) - 1) : 32u;
+            if (k == 0) return EBI_E_UNEXPECTED_END;  // the record at p does not fit
+            uint64_t d = 0;
+            if (static_cast<uint32_t>(lane) < k) {
+                const uint64_t w = sig <= 62 ? (y << 2) : peek(qi + 2);
+                d = (w >> (64 - sig)) << trail;
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t t = __shfl_up_sync(kFull, d, o);
+                if (lane >= o) d ^= t;
+            }
+            const uint64_t v = carry ^ d;
+            carry = __shfl_sync(kFull, v, k - 1);
+            p += k * L;
+            if (step(k, v)) return 0;
+            continue;
+        }
+        // '11': a new window
+        if (p + 13 > B) return EBI_E_UNEXPECTED_END;
+        const uint32_t l = static_cast<uint32_t>(x >> 57) & 31u;
+        const uint32_t sg = (static_cast<uint32_t>(x >> 51) & 63u) + 1;
+        if (l + sg > 64) return EBI_E_CORRUPT;
+        if (p + 13 + sg > B) return EBI_E_UNEXPECTED_END;
+        lead = l;
+        trail = 64 - l - sg;
+        carry ^= (peek(p + 13) >> (64 - sg)) << trail;
+        p += 13 + sg;
+        if (step(1, carry)) return 0;
+    }
+}
+
+// Decodes chunk cd and runs up to MaxQ queries over its values (one warp: the
+// walk parses the stream once and applies each step to every query).
+template <int MaxQ, typename Peek>
+__device__ __forceinline__ void walk(const QueryParams* qs, uint32_t nq, uint32_t okm, const ChunkDesc& cd, uint32_t c,
+                                     uint32_t li, int mode, const unsigned long long* chunk_offsets, Peek peek) {
+    WalkSink<MaxQ> sink;
+    sink.init(qs, nq, okm, cd, li, mode, chunk_offsets);
+    const uint32_t status = parse_stream(cd.byte_len * 8, peek, [&](uint32_t k, uint64_t v) { sink.apply(k, v); });
+    if (status) sink.fail(c, li, status);
+    else sink.finish(c, li);
 }
 
 // Chunk selection and geometry checks of one Gorilla chunk (warp-uniform
@@ -243,6 +364,25 @@ __device__ __forceinline__ void gorilla_chunk_l1(const QueryParams* qs, uint32_t
     const uint64_t bit0 = cd.byte_off * 8;
     walk<MaxQ>(qs, nq, okm, cd, c, li, mode, chunk_offsets,
                [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); });
+}
+
+// One Gorilla chunk by one warp for nq <= kSharedSinkQueries scan queries over
+// the same column, their state in `st` (this warp's shared memory).
+__device__ __forceinline__ void gorilla_chunk_l1_shared(const QueryParams* qs, uint32_t nq, uint32_t c,
+                                                        SharedSinkState* st) {
+    uint32_t okm = 0;
+    for (uint32_t j = 0; j < nq; ++j)  // the same for every lane
+        if (gorilla_begin(qs[j], c, c, VAL_SCAN, nullptr)) okm |= 1u << j;
+    if (!okm) return;
+    const ChunkDesc cd = qs[0].chunks[c];
+    const uint32_t* fw = reinterpret_cast<const uint32_t*>(qs[0].file);
+    const uint64_t bit0 = cd.byte_off * 8;
+    SharedSink sink;
+    sink.init(qs, nq, okm, cd, st);
+    const uint32_t status = parse_stream(cd.byte_len * 8, [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); },
+                                         [&](uint32_t k, uint64_t v) { sink.apply(k, v); });
+    if (status) sink.fail(c, status);
+    else sink.finish(c);
 }
 
 }  // namespace

@@ -136,8 +136,11 @@ struct BatchItem {
     // Chimp family: queries sharing the chunk; Gorilla: chunks | (queries sharing them) << 8
     uint32_t count;
 };
-// Queries over one Gorilla column that one batch item serves at once.
+// Queries over one Gorilla column that one batch item serves at once: up to
+// kGorillaShare with the walk's state in registers, up to kGorillaShareWide
+// with it in shared memory.
 constexpr uint32_t kGorillaShare = 3;
+constexpr uint32_t kGorillaShareWide = 8;
 
 // Work-item tiling of a batch, per codec family and column-size bucket
 // (size_bucket): how many 8,192-row BUFF tiles, Uncompressed / RLE chunks and

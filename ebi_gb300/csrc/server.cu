@@ -103,7 +103,7 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
     // The batch's queries in column order, so that the queries on one column
     // are consecutive: a Chimp-family chunk is then decoded once for all of
     // them (items naming up to 32 consecutive queries), a group of Gorilla
-    // chunks once for up to kGorillaShare.
+    // chunks once for up to kGorillaShareWide.
     struct Ent { uint32_t col, req, k; };
     std::vector<Ent> ents;
     std::vector<uint32_t> base(sl.reqs.size() + 1, 0);
@@ -148,11 +148,11 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
                 for (size_t i = first; i < items.size(); ++i) items[i].count = std::min<uint32_t>(32, h - q0);
             }
         } else if (c->scheme == EBI_GORILLA) {
-            // a group of chunks is parsed once for up to kGorillaShare queries
-            for (uint32_t q0 = g; q0 < h; q0 += kGorillaShare) {
+            // a group of chunks is parsed once for up to kGorillaShareWide queries
+            for (uint32_t q0 = g; q0 < h; q0 += kGorillaShareWide) {
                 const size_t first = items.size();
                 column_items(c->scheme, c->n_chunks, tiles, c->n_records, s->tiling, q0, items);
-                const uint32_t share = std::min<uint32_t>(kGorillaShare, h - q0);
+                const uint32_t share = std::min<uint32_t>(kGorillaShareWide, h - q0);
                 for (size_t i = first; i < items.size(); ++i) items[i].count |= share << 8;
             }
         } else {

@@ -92,7 +92,8 @@ def test_results_equal_alone_and_in_the_mix(rate):
 def test_shared_decodes_match_oracle(codecs):
     # Three columns and 300 requests queued at once: every batch holds many queries per
     # column, so a Chimp-family chunk is decoded once for up to 32 of them and a Gorilla
-    # chunk group is walked once for up to 3.  Each answer is checked against the oracle.
+    # chunk group is walked once for up to 8 (up to 3 with the walk's state in registers,
+    # more with it in shared memory).  Each answer is checked against the oracle.
     rng = np.random.default_rng(17)
     cols = columns(rng, 3, codecs=codecs, lo=30_000, hi=120_000)
     decs = [d for d, _, _ in cols]
