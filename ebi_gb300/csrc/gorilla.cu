@@ -1,39 +1,46 @@
 // gorilla.cu -- kernel and launcher of the Gorilla chunk pass (gorilla_dev.cuh).
 //
-// One CTA of two warps per chunk: warp 0 brings the chunk into shared memory
-// by one bulk copy (cp.async.bulk, completed on an mbarrier with a bounded
-// wait; chunks above the staging size are read through L1 from the resident
-// file instead) and parses the stream; each parse step's values (up to 32,
-// one per lane) go through a ring of kRing slots in shared memory to warp 1,
-// which applies the query to them.  The parse no longer waits for the query's
-// work (predicate, bitmask word, compensated sums) between its steps.  Warp 1
-// gives step values to lanes exactly as the one-warp walk does (value i of a
-// step to lane i), so every per-lane running sum, and the result, is the same
-// as the batched path's walk.  Slots are handed over with full / empty
-// mbarriers (32 arrivals each: every lane releases its own writes); every wait
-// is bounded and a wait that runs out ends the chunk with EBI_E_CUDA.
+// One CTA of three warps per chunk.  Warp 0 brings the chunk into shared
+// memory by one bulk copy (cp.async.bulk, completed on an mbarrier with a
+// bounded wait; chunks above the staging size are read through L1 from the
+// resident file instead) and parses the stream; its parse steps' values (up
+// to 32 per step, one per lane) go, kSub steps per slot, through a ring of
+// kRing slots in shared memory to warps 1 and 2, which apply the query: warp 1
+// the bitmask, counts, min / max and materialized values, warp 2 the
+// compensated sums.  Neither the parse nor the FP64 sums wait for the rest of
+// the query's work.  Both query warps give step values to lanes exactly as the
+// one-warp walk does (value i of a step to lane i) and warp 1 takes warp 2's
+// per-lane sums before the warp reduction, so every per-lane running value,
+// and the result, is the same as the batched path's walk.  Slots are handed
+// over with full / empty mbarriers (every lane arrives: each releases its own
+// writes or reads); every wait is bounded and a wait that runs out ends the
+// chunk with EBI_E_CUDA.
 #include "internal.h"
 #include "gorilla_dev.cuh"
 
 namespace ebi {
 namespace {
 
-constexpr int kRing = 8;
+constexpr int kRing = 4;
+constexpr int kSub = 8;             // parse steps per slot
 constexpr uint32_t kEnd = 1u << 8;  // meta: the parse is over; status in bits 16..
 
 struct __align__(16) GorillaRing {
     uint64_t full[kRing];
     uint64_t empty[kRing];
-    uint32_t meta[kRing];  // k | kEnd | status << 16
-    uint32_t ok;           // the chunk is read by this pass
+    uint64_t sums_ready;         // warp 2's per-lane sums are in hi / lo
+    double hi[32], lo[32];
+    uint32_t meta[kRing][kSub];  // k | kEnd | status << 16
+    uint32_t nsub[kRing];        // steps in the slot
+    uint32_t ok;                 // the chunk is read by this pass
     uint32_t pad[3];
-    uint64_t vals[kRing][32];
+    uint64_t vals[kRing][kSub][32];
 };
 constexpr size_t kRingOff = 16;  // after the bulk copy's mbarrier
 constexpr size_t kStageOff = kRingOff + sizeof(GorillaRing);
 static_assert(kStageOff % 16 == 0, "bulk copies land on 16-byte boundaries");
 
-__global__ void __launch_bounds__(64) gorilla_kernel(QueryParams q, uint32_t chunk_base, int mode,
+__global__ void __launch_bounds__(96) gorilla_kernel(QueryParams q, uint32_t chunk_base, int mode,
                                                      const unsigned long long* chunk_offsets) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t li = blockIdx.x;
@@ -47,8 +54,9 @@ __global__ void __launch_bounds__(64) gorilla_kernel(QueryParams q, uint32_t chu
             R->ok = ok ? 1u : 0u;
             for (int i = 0; i < kRing; ++i) {
                 mbar_init(&R->full[i], 32);
-                mbar_init(&R->empty[i], 32);
+                mbar_init(&R->empty[i], 64);
             }
+            mbar_init(&R->sums_ready, 32);
             mbar_init(bar, 1);
             fence_mbar_init();
         }
@@ -58,21 +66,29 @@ __global__ void __launch_bounds__(64) gorilla_kernel(QueryParams q, uint32_t chu
     const ChunkDesc cd = q.chunks[c];
 
     if (warp == 0) {
-        // ---- parse: each step into the next ring slot ----------------------
-        uint32_t n = 0;       // slots put
+        // ---- parse: kSub steps into each ring slot ---------------------------
+        uint32_t n = 0;       // slots published
+        uint32_t sub = 0;     // steps in the slot being filled
+        uint32_t s = 0;       // that slot
         bool broken = false;  // a wait for a free slot ran out: the rest is dropped
         auto put = [&](uint32_t k, uint64_t v, uint32_t flags) {
             if (broken) return;
-            const uint32_t s = n % kRing;
-            if (n >= kRing && !__all_sync(kFull, mbar_wait(&R->empty[s], ((n / kRing) - 1) & 1))) {
-                broken = true;
-                if (lane == 0) set_status(q.acc + c, EBI_E_CUDA);
-                return;
+            if (sub == 0) {
+                s = n % kRing;
+                if (n >= kRing && !__all_sync(kFull, mbar_wait(&R->empty[s], ((n / kRing) - 1) & 1))) {
+                    broken = true;
+                    if (lane == 0) set_status(q.acc + c, EBI_E_CUDA);
+                    return;
+                }
             }
-            R->vals[s][lane] = v;
-            if (lane == 0) R->meta[s] = k | flags;
-            mbar_arrive(&R->full[s]);
-            ++n;
+            R->vals[s][sub][lane] = v;
+            if (lane == 0) R->meta[s][sub] = k | flags;
+            if (++sub == kSub || (flags & kEnd)) {
+                if (lane == 0) R->nsub[s] = sub;
+                mbar_arrive(&R->full[s]);
+                ++n;
+                sub = 0;
+            }
         };
         const uint64_t span = stage_span(cd.byte_off, cd.byte_len);
         uint32_t status;
@@ -102,9 +118,12 @@ __global__ void __launch_bounds__(64) gorilla_kernel(QueryParams q, uint32_t chu
         return;
     }
 
-    // ---- query: the ring's steps in order -------------------------------------
-    WalkSink<1> sink;
-    sink.init(&q, 1, 1u, cd, li, mode, chunk_offsets);
+    // ---- query: the ring's steps in order (warp 1: all but the sums; warp 2: the sums)
+    const bool sums = warp == 2;
+    WalkSink<1, kPartNoSum> sink;
+    WalkSink<1, kPartSum> sum_sink;
+    if (sums) sum_sink.init(&q, 1, 1u, cd, li, mode, chunk_offsets);
+    else sink.init(&q, 1, 1u, cd, li, mode, chunk_offsets);
     uint32_t status = 0;
     for (uint32_t n = 0;; ++n) {
         const uint32_t s = n % kRing;
@@ -112,14 +131,46 @@ __global__ void __launch_bounds__(64) gorilla_kernel(QueryParams q, uint32_t chu
             status = EBI_E_CUDA;
             break;
         }
-        const uint32_t meta = R->meta[s];
-        const uint64_t v = R->vals[s][lane];
-        mbar_arrive(&R->empty[s]);
-        if (meta & kEnd) {
-            status = meta >> 16;
-            break;
+        // the slot's steps into registers, then the slot goes back to the parse
+        const uint32_t ns = R->nsub[s];
+        uint32_t meta[kSub];
+        uint64_t v[kSub];
+#pragma unroll
+        for (int j = 0; j < kSub; ++j) {
+            meta[j] = R->meta[s][j];
+            v[j] = R->vals[s][j][lane];
         }
-        sink.apply(meta & 0xffu, v);
+        mbar_arrive(&R->empty[s]);
+        bool end = false;
+#pragma unroll
+        for (int j = 0; j < kSub; ++j) {
+            if (end || static_cast<uint32_t>(j) >= ns) break;
+            if (meta[j] & kEnd) {
+                status = meta[j] >> 16;
+                end = true;
+                break;
+            }
+            if (sums) sum_sink.apply(meta[j] & 0xffu, v[j]);
+            else sink.apply(meta[j] & 0xffu, v[j]);
+        }
+        if (end) break;
+    }
+    if (sums) {
+        // hand the per-lane sums to warp 1 (nothing to hand over after a failure)
+        if (!status) {
+            R->hi[lane] = sum_sink.agg[0].hi;
+            R->lo[lane] = sum_sink.agg[0].lo;
+            mbar_arrive(&R->sums_ready);
+        }
+        return;
+    }
+    if (!status && mode == VAL_SCAN) {
+        if (__all_sync(kFull, mbar_wait(&R->sums_ready, 0))) {
+            sink.agg[0].hi = R->hi[lane];
+            sink.agg[0].lo = R->lo[lane];
+        } else {
+            status = EBI_E_CUDA;
+        }
     }
     if (status) sink.fail(c, li, status);
     else sink.finish(c, li);
@@ -143,7 +194,7 @@ cudaError_t launch_gorilla(const QueryParams& q, uint32_t chunk_begin, uint32_t 
     const size_t smem = kStageOff + size_t(q.stage_bytes);
     const cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void*>(gorilla_kernel), smem);
     if (e != cudaSuccess) return e;
-    gorilla_kernel<<<n_chunks, 64, smem, s>>>(q, chunk_begin, mode, chunk_offsets);
+    gorilla_kernel<<<n_chunks, 96, smem, s>>>(q, chunk_begin, mode, chunk_offsets);
     count_launch();
     return cudaGetLastError();
 }

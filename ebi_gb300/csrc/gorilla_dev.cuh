@@ -55,8 +55,10 @@ __host__ __device__ __forceinline__ uint64_t stage_span(uint64_t byte_off, uint6
 // per-lane running aggregates in registers.  Each emitted run of values (lanes
 // [0, k) hold chunk rows idx .. idx + k - 1) goes through every query's
 // bitmask, predicate and aggregates.  Materialize and count passes take one
-// query.
-template <int MaxQ>
+// query.  Part splits the work between two sinks fed the same steps: 0 does
+// everything; 1 everything but the compensated sums; 2 only the sums.
+enum : int { kPartAll = 0, kPartNoSum = 1, kPartSum = 2 };
+template <int MaxQ, int Part = kPartAll>
 struct WalkSink {
     const QueryParams* qs;
     uint32_t nq, okm;
@@ -94,6 +96,11 @@ struct WalkSink {
             const bool pred_on = q.pred_on != 0;
             const bool in = static_cast<uint32_t>(lane) < k && (!q.in_mask || mask_row(q.in_mask, q.n_records, g));
             const bool pass = in && (!pred_on || kp[j].pass(vbits));
+            if (Part == kPartSum) {
+                if (mode == VAL_SCAN && pass && (agg[j].want & AGG_SUM))
+                    neumaier_add(agg[j].hi, agg[j].lo, __longlong_as_double(static_cast<long long>(vbits)));
+                continue;
+            }
             if (mode == VAL_MATERIALIZE) {
                 const uint32_t bal = __ballot_sync(kFull, pass);
                 if (pass) {
@@ -107,8 +114,14 @@ struct WalkSink {
                     if (lane == 0 && word) store_mask_word(q.out_mask, row_off + idx, word, true);
                 }
                 if (pass) {
-                    if (mode == VAL_COUNT) ++agg[j].cnt;
-                    else val_agg_add1(agg[j], vbits);
+                    if (mode == VAL_COUNT) {
+                        ++agg[j].cnt;
+                    } else if (Part == kPartNoSum) {
+                        ++agg[j].cnt;
+                        val_agg_minmax(agg[j], vbits);
+                    } else {
+                        val_agg_add1(agg[j], vbits);
+                    }
                 }
             }
         }
