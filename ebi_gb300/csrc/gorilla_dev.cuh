@@ -1,4 +1,4 @@
-// gorilla_dev.cuh -- Gorilla chunks decoded and queried by one warp per chunk.
+// gorilla_dev.cuh -- Gorilla chunks parsed by one warp per chunk and queried.
 //
 // Format (decoder/chunk_reader/gorilla.rs:90-157; encoder compressor/gorilla.rs:118-190):
 // 64 raw bits, then per value '0' (repeat), '10' + payload in the inherited
@@ -8,22 +8,29 @@
 //
 // The warp follows the stream exactly, several records per step:
 //   * a '0' run: the count of leading zero bits at the cursor is the number of
-//     consecutive repeats (up to 32 per step);
+//     consecutive repeats (up to 32 per step); the step's remaining lanes
+//     check the '10' records that follow, as below;
 //   * a '10' run: with the window fixed, records sit at a fixed stride of
 //     2 + significant bits.  Lane i checks that record i of the stride still
 //     starts with '10' and fits in the chunk; the ballot's leading ones say how
 //     many records are confirmed, each lane extracts its payload and a
 //     warp-shuffle prefix XOR (seeded with the previous value) gives the values;
-//   * a '11' record (new window) is one step.
-// On the bench series over 99 % of the records are '10' in a handful of
-// windows, so an 8,192-value chunk takes a few hundred warp steps.  Each
-// step's values go straight to the query: NaN end check, bitmask ballot,
-// per-lane compensated sums, materialize positions from the ballot.
+//   * a '11' record (new window) opens a step: lane 0 takes it and lanes 1..31
+//     check the '10' records that follow it in the new window, as above.
+// On the bench series over 98 % of the records are '10', so an 8,192-value
+// chunk takes a few hundred warp steps.  The parse (parse_stream) cuts each
+// step at the NaN end marker and hands it to a query sink: value i of the step
+// to lane i, which runs the bitmask ballot, the per-lane compensated sums,
+// min / max, or the materialize positions.  WalkSink keeps up to a few queries'
+// state in registers, SharedSink up to 8 in shared memory; both, and the
+// single-column pass that feeds a sink from another warp, see the same steps,
+// so every path gives the same per-lane sums and the same results.
 //
-// Every step's read depends on the previous step's position, so the chunk is
-// first brought into shared memory by one bulk copy (cp.async.bulk, completed
-// on an mbarrier with a bounded wait); chunks above the staging size are read
-// through L1 from the resident file instead.
+// Every step's read depends on the previous step's position, so the
+// single-column pass first brings the chunk into shared memory by one bulk
+// copy (cp.async.bulk, completed on an mbarrier with a bounded wait); chunks
+// above the staging size, and the batched walk, read through L1 from the
+// resident file instead.
 #pragma once
 
 #include "bitstream.cuh"
@@ -261,57 +268,60 @@ __device__ __forceinline__ uint32_t parse_stream(uint64_t B, Peek peek, Emit emi
     for (;;) {
         if (p + 1 > B) return EBI_E_UNEXPECTED_END;
         const uint64_t x = peek(p);
+        uint32_t first;  // lanes before it hold a value already (repeats, or this step's '11' record)
+        uint64_t d = 0;  // each lane's XOR delta against the previous value
+        uint64_t p0;     // the run's first record
         if (!(x >> 63)) {
-            // '0' run: one repeat per zero bit inside the chunk
+            // '0' run: one repeat (delta 0) per zero bit inside the chunk, then in
+            // the same step the '10' run that may follow it
             uint64_t z = x ? static_cast<uint64_t>(__clzll(static_cast<long long>(x))) : 64;
             if (z > B - p) z = B - p;
-            const uint32_t k = z < 32 ? static_cast<uint32_t>(z) : 32u;
-            p += k;
-            if (step(k, carry)) return 0;
-            continue;
+            first = z < 32 ? static_cast<uint32_t>(z) : 32u;
+            p0 = p + first;
+        } else if (p + 2 > B) {
+            return EBI_E_UNEXPECTED_END;
+        } else if (!((x >> 62) & 1)) {
+            first = 0;
+            p0 = p;
+        } else {
+            // '11': a new window, then in the same step the '10' run that follows it
+            if (p + 13 > B) return EBI_E_UNEXPECTED_END;
+            const uint32_t l = static_cast<uint32_t>(x >> 57) & 31u;
+            const uint32_t sg = (static_cast<uint32_t>(x >> 51) & 63u) + 1;
+            if (l + sg > 64) return EBI_E_CORRUPT;
+            if (p + 13 + sg > B) return EBI_E_UNEXPECTED_END;
+            lead = l;
+            trail = 64 - l - sg;
+            if (lane == 0) d = (peek(p + 13) >> (64 - sg)) << trail;
+            first = 1;
+            p0 = p + 13 + sg;
         }
-        if (p + 2 > B) return EBI_E_UNEXPECTED_END;
-        if (!((x >> 62) & 1)) {
-            // '10' run at stride 2 + sig
-            const uint32_t sig = 64 - lead - trail;  // 1..64
-            const uint64_t L = 2 + sig;
-            const uint64_t qi = p + static_cast<uint64_t>(lane) * L;
-            bool fits = qi + L <= B;
-            uint64_t y = 0;
-            if (fits) {
-                y = peek(qi);
-                fits = (y >> 62) == 2;
-            }
-            const uint32_t m = __ballot_sync(kFull, fits);
-            const uint32_t k = ~m ? static_cast<uint32_t>(__ffs(~m) - 1) : 32u;
-            if (k == 0) return EBI_E_UNEXPECTED_END;  // the record at p does not fit
-            uint64_t d = 0;
-            if (static_cast<uint32_t>(lane) < k) {
-                const uint64_t w = sig <= 62 ? (y << 2) : peek(qi + 2);
-                d = (w >> (64 - sig)) << trail;
-            }
+        // '10' records at stride 2 + sig from p0, one per lane from lane `first`
+        const uint32_t sig = 64 - lead - trail;  // 1..64
+        const uint64_t L = 2 + sig;
+        const uint64_t qi = p0 + static_cast<uint64_t>(static_cast<uint32_t>(lane) - first) * L;
+        bool fits = static_cast<uint32_t>(lane) < first;
+        uint64_t y = 0;
+        if (!fits && qi + L <= B) {
+            y = peek(qi);
+            fits = (y >> 62) == 2;
+        }
+        const uint32_t m = __ballot_sync(kFull, fits);
+        const uint32_t k = ~m ? static_cast<uint32_t>(__ffs(~m) - 1) : 32u;
+        if (k == 0) return EBI_E_UNEXPECTED_END;  // the '10' record at p does not fit
+        if (static_cast<uint32_t>(lane) >= first && static_cast<uint32_t>(lane) < k) {
+            const uint64_t w = sig <= 62 ? (y << 2) : peek(qi + 2);
+            d = (w >> (64 - sig)) << trail;
+        }
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint64_t t = __shfl_up_sync(kFull, d, o);
-                if (lane >= o) d ^= t;
-            }
-            const uint64_t v = carry ^ d;
-            carry = __shfl_sync(kFull, v, k - 1);
-            p += k * L;
-            if (step(k, v)) return 0;
-            continue;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t t = __shfl_up_sync(kFull, d, o);
+            if (lane >= o) d ^= t;
         }
-        // '11': a new window
-        if (p + 13 > B) return EBI_E_UNEXPECTED_END;
-        const uint32_t l = static_cast<uint32_t>(x >> 57) & 31u;
-        const uint32_t sg = (static_cast<uint32_t>(x >> 51) & 63u) + 1;
-        if (l + sg > 64) return EBI_E_CORRUPT;
-        if (p + 13 + sg > B) return EBI_E_UNEXPECTED_END;
-        lead = l;
-        trail = 64 - l - sg;
-        carry ^= (peek(p + 13) >> (64 - sg)) << trail;
-        p += 13 + sg;
-        if (step(1, carry)) return 0;
+        const uint64_t v = carry ^ d;
+        carry = __shfl_sync(kFull, v, k - 1);
+        p = p0 + (k - first) * L;
+        if (step(k, v)) return 0;
     }
 }
 
