@@ -1,7 +1,7 @@
 // buff_stream.cu -- host side of the register-streaming BUFF scan
 // (buff_stream.cuh): the unit list of a column and the launch, which picks the
 // kernel built for the column's most common chunk width (buff_stream_np0..4.cu;
-// up to two byte planes: three CTAs per SM, else two).
+// up to two byte planes: four CTAs per SM, else two).
 #include "internal.h"
 
 namespace ebi {
@@ -49,7 +49,7 @@ cudaError_t launch_buff_stream(const QueryParams& q, const BuffChunkInfo* info, 
     constexpr uint32_t kWarps = 8;  // per CTA
     const uint32_t np = bits / 8, tb = bits % 8;
     const uint32_t max_grid = (n_units + kWarps - 1) / kWarps;
-    const uint32_t grid = sms * (np <= 2 ? 3 : 2);
+    const uint32_t grid = sms * (np <= 2 ? 4 : 2);
     const uint32_t g = grid < max_grid ? grid : (max_grid ? max_grid : 1);
     if (g > kScanSlots) return cudaErrorInvalidConfiguration;
     switch (np) {

@@ -323,9 +323,10 @@ __device__ __forceinline__ uint32_t run_chunk_any(const QueryParams& q, const St
 // The kernel built for chunks of NP byte planes and TB tail bits (NP = 0:
 // tail-only chunks of 1..7 bits; the
 // column's most common width); chunks of other widths take run_chunk_any.
-// Narrow widths keep fewer registers and fit three CTAs per SM.
+// Narrow widths keep fewer registers and fit four CTAs per SM (64 registers:
+// a few spilled words, measured faster than three CTAs at 80 registers).
 template <int NP, int TB>
-__global__ void __launch_bounds__(kStreamThreads, NP <= 2 ? 3 : 2)
+__global__ void __launch_bounds__(kStreamThreads, NP <= 2 ? 4 : 2)
 buff_stream_kernel(QueryParams q, const BuffChunkInfo* info, const uint2* __restrict__ units, uint32_t unit_base,
                    uint32_t n_units, uint32_t upc, ScanTotals* T, QueryResult* res, uint32_t frac, uint32_t fold) {
     __shared__ WarpTot wtot[kStreamWarps];
