@@ -69,7 +69,8 @@ __global__ void __launch_bounds__(kTileThreads) buff_count_kernel(QueryParams q,
 // delta into its double and writes the run as consecutive doubles, 256 bytes
 // per store instruction.
 constexpr int kMatStage = 32 * 33;  // entries per warp
-constexpr size_t kMatSmem = size_t(kTileWarps) * kMatStage * sizeof(unsigned long long);
+// stage bytes: 64-bit deltas (WIDE) or 32-bit
+constexpr size_t mat_smem(bool wide) { return size_t(kTileWarps) * kMatStage * (wide ? 8 : 4); }
 
 // The warp's run: staged entry j (padded position j + j / 32) becomes output
 // wbase + j.  SMALL: every fixed value of the chunk fits an int32.
@@ -177,11 +178,12 @@ __device__ void buff_mat_dispatch(const QueryParams& q, const BuffCtx& k, uint32
 }
 
 // WIDE: some readable chunk of the column is more than 32 bits wide (64-bit
-// deltas); the narrow build keeps 32-bit deltas and fits three CTAs per SM.
+// deltas); the narrow build stages 32-bit deltas (33 KB a CTA) and fits four
+// CTAs per SM.
 // quiet: no chunk the pass reads can raise, so the chunks' accumulators are
 // left untouched and no fold follows.
 template <bool WIDE>
-__global__ void __launch_bounds__(kTileThreads, WIDE ? 2 : 3) buff_materialize_kernel(
+__global__ void __launch_bounds__(kTileThreads, WIDE ? 2 : 4) buff_materialize_kernel(
     QueryParams q, uint32_t tile_base, const unsigned long long* tile_offsets, unsigned long long base_row,
     bool quiet) {
     extern __shared__ unsigned long long mat_stage[];
@@ -241,10 +243,11 @@ cudaError_t launch_buff_materialize(const QueryParams& q, uint32_t tile_begin, u
     if (n_tiles == 0) return cudaSuccess;
     const void* fn = wide ? reinterpret_cast<const void*>(buff_materialize_kernel<true>)
                           : reinterpret_cast<const void*>(buff_materialize_kernel<false>);
-    const cudaError_t e = allow_dynamic_smem(fn, kMatSmem);
+    const size_t smem = mat_smem(wide);
+    const cudaError_t e = allow_dynamic_smem(fn, smem);
     if (e != cudaSuccess) return e;
-    if (wide) buff_materialize_kernel<true><<<n_tiles, kTileThreads, kMatSmem, s>>>(q, tile_begin, tile_offsets, base_row, quiet);
-    else buff_materialize_kernel<false><<<n_tiles, kTileThreads, kMatSmem, s>>>(q, tile_begin, tile_offsets, base_row, quiet);
+    if (wide) buff_materialize_kernel<true><<<n_tiles, kTileThreads, smem, s>>>(q, tile_begin, tile_offsets, base_row, quiet);
+    else buff_materialize_kernel<false><<<n_tiles, kTileThreads, smem, s>>>(q, tile_begin, tile_offsets, base_row, quiet);
     count_launch();
     return cudaGetLastError();
 }
