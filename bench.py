@@ -299,6 +299,11 @@ def cpu_figures(data: bytes, wl, threads: int, n_all: int = 9, n_one: int = 3):
                       f"{len(one)} queries on one thread; two_call: {len(two)} queries as the reference's two calls"}
 
 
+def same_bits(a, b):
+    """Two f64 results with the same bits (NaN results compare equal)."""
+    return np.float64(a).view(np.uint64) == np.float64(b).view(np.uint64) or (np.isnan(a) and np.isnan(b))
+
+
 def value_config(name, dev, steps, warmup, flush, clean):
     """One of the other single-column configurations, measured as the headline is: each step one
     fused filter + aggregate query with L2 flushed before it; the median device time of the query
@@ -333,6 +338,22 @@ def value_config(name, dev, steps, warmup, flush, clean):
     exact = wl.codec == "buff"
     same = (np.array_equal(mask.cpu().numpy().view(np.uint64)[: len(om)], om) and (mn, mx) == (omn, omx)
             and (s == os_ if exact else abs(s - os_) <= 1e-12 * max(abs(os_), 1e-300)))
+    # the unfiltered aggregates (decode + sum / min / max, one call each, as the reference's Decoder)
+    unfiltered = {}
+    for a in wl.aggregates:
+        ks_a = []
+        for i in range(warmup + max(5, steps // 2)):
+            flush.fill_(i & 0xFF)
+            clean.sum()
+            torch.cuda._sleep(1_000_000)
+            got = getattr(dec, a)()
+            if i >= warmup:
+                ks_a.append(dec.segmented_execution_times()["total_ms"])
+        want = getattr(o, a)()
+        ok = same_bits(got, want) if a != "sum" else (got == want if exact else abs(got - want) <= 1e-12 * max(abs(want), 1e-300))
+        unfiltered[a] = {"ms": round(statistics.median(ks_a), 4),
+                         "decoded_gb_per_s": round(8.0 * wl.rows / (statistics.median(ks_a) / 1e3) / 1e9, 3),
+                         "equal_to_oracle": bool(ok)}
     peak, _ = measured_peak()
     ks, ts = statistics.median(scan) / 1e3, statistics.median(total) / 1e3
     cpu = cpu_figures(data, wl, os.cpu_count() or 1, n_all=5, n_one=0)
@@ -344,6 +365,7 @@ def value_config(name, dev, steps, warmup, flush, clean):
                          "achieved": round(alg / ks / 1e9, 1), "peak": peak, "frac": round(alg / ks / 1e9 / peak, 4)},
             "parity_check": {"bitmask_min_max_bit_exact_sum_within_tolerance": bool(same),
                              "sum_rel_diff": abs(s - os_) / max(abs(os_), 1e-300), "rows_selected": int(cnt)},
+            "unfiltered": unfiltered,
             "cpu_baseline": {k: cpu[k] for k in ("value", "cores", "kind")}}
 
 
