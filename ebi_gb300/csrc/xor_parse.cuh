@@ -111,53 +111,43 @@ XOR_HD uint32_t parse_rec(Peek peek, uint64_t B, PState& s, Rec& r) {
         s.pos = q + n;
         return 0;
     } else {
+        // Chimp / Chimp128, without branches on the flag: the lanes of a warp
+        // parse different records, and a branch per flag would run every
+        // lane through all four paths.  Every field is computed for every
+        // flag and selected; the reader's error checks, in its order, run only
+        // when one of them fails.
         if (p + 2 > B) return EBI_E_UNEXPECTED_END;
         const uint64_t x = peek(p);
         const uint32_t flag = static_cast<uint32_t>(x >> 62);
-        if (flag == 0) {
-            r.delta = 0;
-            if (CODEC == CODEC_CHIMP128) {
-                if (p + 9 > B) return EBI_E_UNEXPECTED_END;
-                r.ring = static_cast<uint32_t>(x >> 55) & 127u;
-                r.nan_ok = false;  // chimp_n.rs: the '00' copy is not checked against NaN
-                s.pos = p + 9;
-            } else {
-                s.pos = p + 2;
-            }
-            return 0;
-        }
-        if (flag == 3 || flag == 2) {
-            uint32_t lead = s.win;
-            uint64_t q = p + 2;
-            if (flag == 3) {
-                if (p + 5 > B) return EBI_E_UNEXPECTED_END;
-                lead = lead_decode(static_cast<uint32_t>(x >> 59) & 7u);
-                q = p + 5;
-            } else if (lead > 64) {
-                return EBI_E_CORRUPT;  // '10' before any leading count was stored
-            }
-            const uint32_t n = 64 - lead;  // 40..64 bits
-            if (q + n > B) return EBI_E_UNEXPECTED_END;
-            r.delta = n == 64 ? peek(q) : peek(q) >> (64 - n);
-            s.win = lead;
-            s.pos = q + n;
-            return 0;
-        }
-        // flag 1
-        const uint32_t hdr = CODEC == CODEC_CHIMP128 ? 16u : 9u;
-        if (p + 2 + hdr > B) return EBI_E_UNEXPECTED_END;
+        constexpr uint32_t hdr = CODEC == CODEC_CHIMP128 ? 16u : 9u;  // '01' header after the flag
         const uint32_t t = static_cast<uint32_t>(x >> (62 - hdr)) & ((1u << hdr) - 1u);
-        if (CODEC == CODEC_CHIMP128) r.ring = (t >> 9) & 127u;
-        const uint32_t lead = lead_decode((t >> 6) & 7u);
-        uint32_t sig = t & 63u;
-        if (sig == 0) sig = 64;
-        if (sig + lead > 64) return EBI_E_CORRUPT;
-        const uint32_t trail = 64 - sig - lead;
-        const uint64_t q = p + 2 + hdr;
-        if (q + sig > B) return EBI_E_UNEXPECTED_END;
-        r.delta = (sig == 64 ? peek(q) : peek(q) >> (64 - sig)) << trail;
+        const uint32_t lead1 = lead_decode((t >> 6) & 7u), lead3 = lead_decode(static_cast<uint32_t>(x >> 59) & 7u);
+        const uint32_t sig1 = (t & 63u) ? (t & 63u) : 64u;
+        const uint32_t lead = flag == 1 ? lead1 : flag == 3 ? lead3 : s.win;  // '00' and '10' keep the stored count
+        const uint32_t hl = flag == 0 ? (CODEC == CODEC_CHIMP128 ? 9u : 2u) : flag == 1 ? 2u + hdr : flag == 2 ? 2u : 5u;
+        const uint32_t n = flag == 0 ? 0u : flag == 1 ? sig1 : 64u - (lead > 64u ? 64u : lead);
+        const uint64_t q = p + hl;
+        const bool bad = (flag == 2 && s.win > 64u) || (flag == 1 && sig1 + lead1 > 64u) || q + n > B;
+        if (bad) {
+            if (flag == 0) return EBI_E_UNEXPECTED_END;  // p + 9 (Chimp128) past the chunk
+            if (flag == 1) {
+                if (p + 2 + hdr > B) return EBI_E_UNEXPECTED_END;
+                if (sig1 + lead1 > 64u) return EBI_E_CORRUPT;
+                return EBI_E_UNEXPECTED_END;
+            }
+            if (flag == 3) return EBI_E_UNEXPECTED_END;  // p + 5 or the payload past the chunk
+            if (s.win > 64u) return EBI_E_CORRUPT;        // '10' before any leading count was stored
+            return EBI_E_UNEXPECTED_END;
+        }
+        const uint32_t trail = flag == 1 ? 64u - sig1 - lead1 : 0u;
+        const uint64_t y = n ? peek(q) : 0ull;
+        r.delta = (n == 64u ? y : n ? (y >> (64u - n)) : 0ull) << trail;
+        if (CODEC == CODEC_CHIMP128) {
+            r.ring = flag == 0 ? static_cast<uint32_t>(x >> 55) & 127u : flag == 1 ? (t >> 9) & 127u : kRefPrev;
+            r.nan_ok = flag != 0;  // chimp_n.rs: the '00' copy is not checked against NaN
+        }
         s.win = lead;
-        s.pos = q + sig;
+        s.pos = q + n;
         return 0;
     }
 }
