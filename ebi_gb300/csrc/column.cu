@@ -117,6 +117,45 @@ class PinnedSlots {
 static PinnedSlots<QueryResult> g_pinned;
 static PinnedSlots<ScanTotals> g_pinned_tot;
 
+// Pinned staging for the small tables a column open uploads (chunk table,
+// tiles, units, repack segments, chunk headers), one per host thread, grown on
+// demand and kept: copies from it are asynchronous, so none of them holds the
+// host, and they queue behind the column's own bytes without delaying them.
+class TableStage {
+  public:
+    ~TableStage() {
+        if (p_) cudaFreeHost(p_);
+    }
+    // Room for `bytes` (16-byte aligned pieces); false when pinned memory runs out.
+    bool reserve(size_t bytes) {
+        used_ = 0;
+        if (bytes <= cap_) return true;
+        if (p_) cudaFreeHost(p_);
+        p_ = nullptr;
+        cap_ = 0;
+        void* q = nullptr;
+        if (cudaMallocHost(&q, bytes * 2) != cudaSuccess) return false;
+        p_ = static_cast<uint8_t*>(q);
+        cap_ = bytes * 2;
+        return true;
+    }
+    // Copies n bytes into the stage and returns their pinned address (null
+    // when they do not fit the room reserved).
+    const void* put(const void* src, size_t n) {
+        const size_t step = (n + 15) & ~size_t(15);
+        if (step > cap_ - used_) return nullptr;
+        uint8_t* d = p_ + used_;
+        std::memcpy(d, src, n);
+        used_ += step;
+        return d;
+    }
+
+  private:
+    uint8_t* p_ = nullptr;
+    size_t cap_ = 0, used_ = 0;
+};
+static thread_local TableStage t_stage;
+
 // (double)x / 2^frac as the device's fold_scale rounds it (one conversion, one
 // exact power-of-two scaling).
 static double host_fold_scale(long long x, uint32_t frac) {
@@ -632,6 +671,33 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     RepackSeg* d_segs = nullptr;
     if (!st && c->scheme == EBI_BUFF && !src) st = dev_alloc(&raw, len + kFilePad, s);
     if (!st && c->scheme == EBI_BUFF) st = dev_alloc(&d_segs, segs.size(), s);
+    static const ScanTotals kRest = {0, 0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0, 0};
+    // every table the open uploads (units: at most one per 2,048 rows of a chunk), 16-byte pieces
+    const size_t table_bytes = segs.size() * sizeof(RepackSeg) + c->n_chunks * sizeof(ChunkDesc) +
+                               c->tiles.tiles.size() * sizeof(Tile) + binfo.size() * sizeof(BuffChunkInfo) +
+                               size_t(c->n_records / kBuffUnitRows + c->n_chunks + 1) * sizeof(uint2) +
+                               2 * sizeof(ScanTotals) + 8 * 16;
+    if (!st && !t_stage.reserve(table_bytes)) st = fail(EBI_E_OOM, "pinned allocation failed");
+    cudaError_t e = cudaSuccess;
+    // the column's bytes first: the link is the long pole of an open
+    if (!st) {
+        if (!src) {
+            uint8_t* dst = raw ? raw : c->d_file;
+            e = cudaMemcpyAsync(dst, file, len, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(dst + len, 0, kFilePad, s);
+            if (raw) src = raw;
+        }
+        if (e == cudaSuccess && c->scheme == EBI_BUFF) {
+            e = cudaMemsetAsync(c->d_file + dev_len, 0, kFilePad, s);
+            if (e == cudaSuccess && !segs.empty()) {
+                const void* h = t_stage.put(segs.data(), segs.size() * sizeof(RepackSeg));
+                e = h ? cudaMemcpyAsync(d_segs, h, segs.size() * sizeof(RepackSeg), cudaMemcpyHostToDevice, s)
+                      : cudaErrorMemoryAllocation;
+            }
+            if (e == cudaSuccess) e = launch_buff_repack(src, c->d_file, d_segs, static_cast<uint32_t>(segs.size()), s);
+        }
+    }
+    // the rest of the column's tables, built while the bytes cross the link
     std::vector<uint2> units;
     if (c->scheme == EBI_BUFF) {
         units = buff_units(c->chunks, c->first_unit);
@@ -649,41 +715,22 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st && !(c->h_res = g_pinned.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st && !(c->h_tot = g_pinned_tot.take())) st = fail(EBI_E_OOM, "pinned allocation failed");
     if (!st) {
-        cudaError_t e = cudaSuccess;
-        if (!src) {
-            uint8_t* dst = raw ? raw : c->d_file;
-            e = cudaMemcpyAsync(dst, file, len, cudaMemcpyHostToDevice, s);
-            if (e == cudaSuccess) e = cudaMemsetAsync(dst + len, 0, kFilePad, s);
-            if (raw) src = raw;
-        }
-        // the small tables first: a copy from pageable memory may hold the
-        // host until the stream reaches it, which must not wait for the repack
-        if (e == cudaSuccess && c->scheme == EBI_BUFF) {
-            e = cudaMemsetAsync(c->d_file + dev_len, 0, kFilePad, s);
-            if (e == cudaSuccess && !segs.empty())
-                e = cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(RepackSeg), cudaMemcpyHostToDevice, s);
-            if (e == cudaSuccess && !units.empty())
-                e = cudaMemcpyAsync(c->d_units, units.data(), units.size() * sizeof(uint2), cudaMemcpyHostToDevice, s);
-        }
-        if (e == cudaSuccess && c->n_chunks)
-            e = cudaMemcpyAsync(c->d_chunks, c->chunks.data(), c->n_chunks * sizeof(ChunkDesc), cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess && !c->tiles.tiles.empty())
-            e = cudaMemcpyAsync(c->d_tiles, c->tiles.tiles.data(), c->tiles.tiles.size() * sizeof(Tile),
-                                cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess && !binfo.empty())
-            e = cudaMemcpyAsync(c->d_buff, binfo.data(), binfo.size() * sizeof(BuffChunkInfo), cudaMemcpyHostToDevice, s);
-        static const ScanTotals kRest = {0, 0, 0, LLONG_MIN, LLONG_MAX, 0, 0xffffffffu, 0, 0, 0};
-        if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_tot, &kRest, sizeof kRest, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(c->d_tot) + kScanTotalsBytes, &kRest, sizeof kRest,
-                                cudaMemcpyHostToDevice, s);
+        auto up = [&](void* dst, const void* host, size_t n) {
+            if (e != cudaSuccess || !n) return;
+            const void* h = t_stage.put(host, n);
+            e = h ? cudaMemcpyAsync(dst, h, n, cudaMemcpyHostToDevice, s) : cudaErrorMemoryAllocation;
+        };
+        if (c->scheme == EBI_BUFF) up(c->d_units, units.data(), units.size() * sizeof(uint2));
+        up(c->d_chunks, c->chunks.data(), c->n_chunks * sizeof(ChunkDesc));
+        up(c->d_tiles, c->tiles.tiles.data(), c->tiles.tiles.size() * sizeof(Tile));
+        up(c->d_buff, binfo.data(), binfo.size() * sizeof(BuffChunkInfo));
+        up(c->d_tot, &kRest, sizeof kRest);
+        up(reinterpret_cast<uint8_t*>(c->d_tot) + kScanTotalsBytes, &kRest, sizeof kRest);
         if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
-        if (e == cudaSuccess && c->scheme == EBI_BUFF)
-            e = launch_buff_repack(src, c->d_file, d_segs, static_cast<uint32_t>(segs.size()), s);
-        // host sources (chunk table, tiles, segments) must stay alive until the copies ran
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) st = cuda_fail(e, "ebi_column_open upload");
     }
+    // the staged tables must stay until the copies ran
+    if (cudaError_t e2 = cudaStreamSynchronize(s); e == cudaSuccess) e = e2;
+    if (!st && e != cudaSuccess) st = cuda_fail(e, "ebi_column_open upload");
     if (raw) cudaFreeAsync(raw, s);
     if (d_segs) cudaFreeAsync(d_segs, s);
     if (st) { ebi_column_close(c); return st; }
