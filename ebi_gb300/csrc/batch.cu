@@ -51,8 +51,10 @@ __device__ __noinline__ void item_buff_tile(const QueryParams& q, const BatchIte
     for (uint32_t j = 0; j < it.count; ++j) {
         const uint32_t tile = it.unit + j;
         const Tile t = q.tiles[tile];
+        // thread 0 has read the previous tile's block reduction (and every
+        // thread is done with k) before any warp writes the next one
+        if (j) __syncthreads();
         if (t.chunk != chunk) {
-            __syncthreads();  // the previous tile is done with k
             if (threadIdx.x == 0) buff_setup(q, t.chunk, q.in_mask != nullptr, k);
             __syncthreads();
             chunk = t.chunk;

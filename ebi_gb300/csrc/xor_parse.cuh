@@ -117,7 +117,11 @@ XOR_HD uint32_t parse_rec(Peek peek, uint64_t B, PState& s, Rec& r) {
         // flag and selected; the reader's error checks, in its order, run only
         // when one of them fails.
         if (p + 2 > B) return EBI_E_UNEXPECTED_END;
+        // the record's first 128 bits in two reads that do not wait on each
+        // other (a record is at most 2 + 16 + 64 bits); the second only when
+        // the chunk goes on past the first
         const uint64_t x = peek(p);
+        const uint64_t x2 = p + 64 < B ? peek(p + 64) : 0ull;
         const uint32_t flag = static_cast<uint32_t>(x >> 62);
         constexpr uint32_t hdr = CODEC == CODEC_CHIMP128 ? 16u : 9u;  // '01' header after the flag
         const uint32_t t = static_cast<uint32_t>(x >> (62 - hdr)) & ((1u << hdr) - 1u);
@@ -140,7 +144,7 @@ XOR_HD uint32_t parse_rec(Peek peek, uint64_t B, PState& s, Rec& r) {
             return EBI_E_UNEXPECTED_END;
         }
         const uint32_t trail = flag == 1 ? 64u - sig1 - lead1 : 0u;
-        const uint64_t y = n ? peek(q) : 0ull;
+        const uint64_t y = (x << hl) | (x2 >> (64u - hl));  // the 64 bits at q (hl is 2..18)
         r.delta = (n == 64u ? y : n ? (y >> (64u - n)) : 0ull) << trail;
         if (CODEC == CODEC_CHIMP128) {
             r.ring = flag == 0 ? static_cast<uint32_t>(x >> 55) & 127u : flag == 1 ? (t >> 9) & 127u : kRefPrev;
