@@ -663,9 +663,10 @@ def serving_line(args):
     caps = {"slots": 4, "max_queries": 16384, "max_chunks": 1 << 23, "max_items": 1 << 23}
     srv = E.Server(decs, **caps)
     srv.replay(plain_reqs[:50])  # warm-up
-    # saturated throughput: a full queue (the plain requests first, then more), all submitted at once;
+    # saturated throughput: a full queue of 10,000 requests (the plain requests first, then more), all
+    # submitted at once, so that several batches run back to back;
     # the plain requests' answers in the mix are compared bit for bit with their plain answers
-    sat_reqs = plain_reqs + make_requests(max(0, 4000 - len(plain_reqs)))
+    sat_reqs = plain_reqs + make_requests(max(0, 10_000 - len(plain_reqs)))
     t0 = time.perf_counter()
     mixed = srv.replay(sat_reqs)
     sat_s = time.perf_counter() - t0
