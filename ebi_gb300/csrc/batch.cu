@@ -194,6 +194,28 @@ void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_re
     }
 }
 
+void shared_column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& t,
+                         uint32_t first, uint32_t n, std::vector<BatchItem>& out) {
+    const bool chimp = scheme == EBI_CHIMP || scheme == EBI_CHIMP128 || scheme == EBI_ELF_ON_CHIMP || scheme == EBI_ELF;
+    const uint32_t end = first + n;
+    if (chimp) {
+        for (uint32_t q0 = first; q0 < end; q0 += 32) {
+            const size_t i0 = out.size();
+            column_items(scheme, n_chunks, n_tiles, n_records, t, q0, out);
+            for (size_t i = i0; i < out.size(); ++i) out[i].count = std::min<uint32_t>(32, end - q0);
+        }
+    } else if (scheme == EBI_GORILLA) {
+        for (uint32_t q0 = first; q0 < end; q0 += kGorillaShareWide) {
+            const size_t i0 = out.size();
+            column_items(scheme, n_chunks, n_tiles, n_records, t, q0, out);
+            const uint32_t share = std::min<uint32_t>(kGorillaShareWide, end - q0);
+            for (size_t i = i0; i < out.size(); ++i) out[i].count |= share << 8;
+        }
+    } else {
+        for (uint32_t qi = first; qi < end; ++qi) column_items(scheme, n_chunks, n_tiles, n_records, t, qi, out);
+    }
+}
+
 uint64_t column_item_count(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& tl) {
     const int b = size_bucket(n_records);
     auto per = [](uint32_t v, uint32_t hi) -> uint64_t { return v < 1 ? 1u : v > hi ? hi : v; };

@@ -134,7 +134,11 @@ void save_cache_locked() {
 }  // namespace
 
 struct ebi_batch {
-    std::vector<ebi_batch_query> queries;
+    std::vector<ebi_batch_query> queries;  // in the caller's order
+    // device order: queries on one column consecutive (first appearance order),
+    // so that a Chimp-family chunk or a Gorilla chunk group is decoded once for
+    // several of them; order[pos] = caller index, slot[caller index] = pos
+    std::vector<uint32_t> order, slot;
     uint64_t n_chunks = 0;
     uint64_t max_items = 0;  // the most items any candidate tiling makes
     int sms = 1;
@@ -163,13 +167,18 @@ struct ebi_batch {
 
 namespace {
 
-// The work items of configuration c (query order, then cost order if asked).
+// The work items of configuration c (device order: the queries on one column
+// share their decodes; then cost order if asked).
 void build_items(const ebi_batch* b, const Config& c, std::vector<BatchItem>& items) {
     items.clear();
-    for (size_t i = 0; i < b->queries.size(); ++i) {
-        const ebi_column* col = b->queries[i].col;
-        column_items(col->scheme, col->n_chunks, static_cast<uint32_t>(col->tiles.tiles.size()), col->n_records,
-                     c.tiling, static_cast<uint32_t>(i), items);
+    const uint32_t n = static_cast<uint32_t>(b->order.size());
+    for (uint32_t g = 0; g < n;) {
+        const ebi_column* col = b->queries[b->order[g]].col;
+        uint32_t h = g + 1;
+        while (h < n && b->queries[b->order[h]].col == col) ++h;
+        shared_column_items(col->scheme, col->n_chunks, static_cast<uint32_t>(col->tiles.tiles.size()), col->n_records,
+                            c.tiling, g, h - g, items);
+        g = h;
     }
     if (kShapes[c.shape].order == 0) order_by_cost(items);
 }
@@ -333,11 +342,23 @@ int ebi_batch_create(const ebi_batch_query* queries, uint64_t n, void* stream, e
     ebi_batch* b = new (std::nothrow) ebi_batch();
     if (!b) return bfail(EBI_E_OOM, "host allocation failed");
     b->queries.assign(queries, queries + n);
-    std::vector<QueryParams> qp(n);
+    {
+        // device order: by column, columns in order of first appearance, queries stable
+        std::map<const ebi_column*, uint32_t> first_seen;
+        std::vector<uint32_t> key(n);
+        for (uint64_t i = 0; i < n; ++i)
+            key[i] = first_seen.emplace(queries[i].col, static_cast<uint32_t>(first_seen.size())).first->second;
+        b->order.resize(n);
+        for (uint64_t i = 0; i < n; ++i) b->order[i] = static_cast<uint32_t>(i);
+        std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t x, uint32_t y) { return key[x] < key[y]; });
+        b->slot.resize(n);
+        for (uint64_t p = 0; p < n; ++p) b->slot[b->order[p]] = static_cast<uint32_t>(p);
+    }
+    std::vector<QueryParams> qp(n);  // device order
     std::vector<uint64_t> acc_off(n);
     std::map<int, uint64_t> shape_count;  // scheme * buckets + bucket -> queries
     for (uint64_t i = 0; i < n; ++i) {
-        const ebi_batch_query& bq = queries[i];
+        const ebi_batch_query& bq = queries[b->order[i]];  // position i of the device order
         if (!bq.col) { delete b; return bfail(EBI_E_INVALID, "query without a column"); }
         const ebi_predicate& p = bq.pred;
         if (p.kind < EBI_PRED_EQ || p.kind > EBI_PRED_RANGE ||
@@ -418,7 +439,7 @@ int ebi_batch_run(ebi_batch* b, const ebi_predicate* preds, ebi_batch_result* re
         for (size_t i = 0; i < n; ++i) {
             const ebi_predicate& p = preds[i];
             if (p.kind < EBI_PRED_EQ || p.kind > EBI_PRED_RANGE) return bfail(EBI_E_INVALID, "bad predicate kind");
-            b->h_qp[i].pred = p;
+            b->h_qp[b->slot[i]].pred = p;
             b->queries[i].pred = p;
         }
     }
@@ -432,7 +453,7 @@ int ebi_batch_run(ebi_batch* b, const ebi_predicate* preds, ebi_batch_result* re
     BCK(cudaStreamSynchronize(s));
     int first_err = EBI_OK;
     for (size_t i = 0; i < n; ++i) {
-        const QueryResult& r = b->h_res[i];
+        const QueryResult& r = b->h_res[b->slot[i]];
         if (results) {
             results[i].sum = r.sum;
             results[i].min = r.min;

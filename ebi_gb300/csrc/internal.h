@@ -160,6 +160,12 @@ BatchTiling default_tiling();
 // chunk count in the low byte of count (callers add a sharing count above it).
 void column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& t,
                   uint32_t query, std::vector<BatchItem>& out);
+// The items of queries [first, first + n) of a batch, all over one column:
+// a Chimp-family chunk is decoded once for up to 32 of them, a Gorilla chunk
+// group walked once for up to kGorillaShareWide; other codecs get one set of
+// items per query.
+void shared_column_items(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& t,
+                         uint32_t first, uint32_t n, std::vector<BatchItem>& out);
 // How many items column_items appends for such a column.
 uint64_t column_item_count(int scheme, uint64_t n_chunks, uint32_t n_tiles, uint64_t n_records, const BatchTiling& t);
 // Relative cost of one item (device time of the 8,192-row units it covers,

@@ -138,26 +138,8 @@ cudaError_t launch_slot(ebi_server* s, Slot& sl) {
         uint32_t h = g;
         while (h < nq && ents[h].col == ents[g].col) ++h;  // queries g .. h - 1: one column
         const ebi_column* c = s->cols[ents[g].col];
-        const uint32_t tiles = static_cast<uint32_t>(c->tiles.tiles.size());
-        const bool shared = c->scheme == EBI_CHIMP || c->scheme == EBI_CHIMP128 || c->scheme == EBI_ELF_ON_CHIMP ||
-                            c->scheme == EBI_ELF;
-        if (shared) {
-            for (uint32_t q0 = g; q0 < h; q0 += 32) {
-                const size_t first = items.size();
-                column_items(c->scheme, c->n_chunks, tiles, c->n_records, s->tiling, q0, items);
-                for (size_t i = first; i < items.size(); ++i) items[i].count = std::min<uint32_t>(32, h - q0);
-            }
-        } else if (c->scheme == EBI_GORILLA) {
-            // a group of chunks is parsed once for up to kGorillaShareWide queries
-            for (uint32_t q0 = g; q0 < h; q0 += kGorillaShareWide) {
-                const size_t first = items.size();
-                column_items(c->scheme, c->n_chunks, tiles, c->n_records, s->tiling, q0, items);
-                const uint32_t share = std::min<uint32_t>(kGorillaShareWide, h - q0);
-                for (size_t i = first; i < items.size(); ++i) items[i].count |= share << 8;
-            }
-        } else {
-            for (uint32_t qi = g; qi < h; ++qi) column_items(c->scheme, c->n_chunks, tiles, c->n_records, s->tiling, qi, items);
-        }
+        shared_column_items(c->scheme, c->n_chunks, static_cast<uint32_t>(c->tiles.tiles.size()), c->n_records,
+                            s->tiling, g, h - g, items);
         g = h;
     }
     order_by_cost(items);

@@ -197,7 +197,9 @@ int ebi_rows_from_mask(const uint64_t* d_mask, uint64_t n_records, uint32_t* d_r
  * chunks one work item covers; the fastest is kept (and, with a tuning cache
  * set, stored under the batch's column shape for later batches).  Results
  * equal the single-column calls (ebi_filter_agg) bit for bit whatever the
- * tiling.  The columns must stay open while the batch exists; runs of one
+ * tiling.  Queries over the same column run together: a Chimp-family chunk
+ * is decoded once for up to 32 of them and a Gorilla chunk group walked once
+ * for up to 8.  The columns must stay open while the batch exists; runs of one
  * batch must not overlap. */
 enum { EBI_AGG_SUM = 1, EBI_AGG_MIN = 2, EBI_AGG_MAX = 4 };
 typedef struct {

@@ -152,3 +152,49 @@ def test_tiling_is_tuned_cached_and_exact(tmp_path):
         b2.close()
     finally:
         E.Batch.set_tuning_cache(None)
+
+
+def test_queries_on_one_column_share_decodes():
+    # Twelve queries on each of four columns, interleaved: the batch runs them grouped by
+    # column, so a Chimp128 chunk is decoded once for all twelve and a Gorilla chunk group is
+    # walked twice (8 + 4 queries); results come back in the caller's order and equal the
+    # oracle and the queries run alone, also after new predicates are set.
+    rng = np.random.default_rng(12)
+    cols = []
+    for codec in ("chimp128", "gorilla", "buff", "rle"):
+        n = 70_000
+        if codec == "buff":
+            v = np.round(rng.uniform(-1000, 1000, n), 3) + 0.0
+            data = E.encode(v, "buff", ("record_count", 65536), 1000)
+        elif codec == "rle":
+            v = np.repeat(np.round(rng.normal(0, 5, n // 30 + 1), 1), 30)[:n] + 0.0
+            data = E.encode(v, "rle", ("record_count", 8192))
+        else:
+            v = np.round(30 + np.cumsum(rng.normal(0, 0.5, n)), 2) + 0.0
+            data = E.encode(v, codec, ("record_count", 8192))
+        cols.append((E.Decoder(data), v, O.Decoder(data), codec))
+    queries = []
+    for k in range(48):
+        d, v, _, _ = cols[k % 4]
+        queries.append((d, random_preds(v, rng, k=1)[0], [("sum", "min", "max"), ("sum",), ("min",), ("max",)][k % 4]))
+    b = E.Batch(queries)
+    for rnd in range(2):
+        if rnd == 1:
+            preds = [random_preds(cols[k % 4][1], rng, k=1)[0] for k in range(48)]
+            queries = [(d, p, a) for (d, _, a), p in zip(queries, preds)]
+            got = b.run(preds)
+        else:
+            got = b.run()
+        for k, (d, p, aggs) in enumerate(queries):
+            m, s, mn, mx, n = alone(d, p, aggs)
+            gs, gmn, gmx, gn = got[k]
+            om, os_, omn, omx, on, sel = oracle_filter_agg(cols[k % 4][2], p)
+            assert gn == on == n, k
+            assert same(gs, s) and same(gmn, mn) and same(gmx, mx), k
+            if "sum" in aggs:
+                assert sum_ok(gs, os_, cols[k % 4][3] == "buff", sel), k
+            if "min" in aggs:
+                assert same_scalar(gmn, omn), k
+            if "max" in aggs:
+                assert same_scalar(gmx, omx), k
+    b.close()
