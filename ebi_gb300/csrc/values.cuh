@@ -2,7 +2,7 @@
 // (decoder/query.rs:14-154), shared by the codecs that decode to values before
 // querying them (RLE, Uncompressed, Gorilla, Chimp, Chimp128).
 //
-// Per chunk, rows are judged as the default operators do: a row counts when
+// Per chunk, rows are decided as the default operators do: a row counts when
 // it is in the input bitmask (or there is none) and, for a filter, when the
 // predicate holds.  The chunk's sum is compensated, min/max are NaN-ignoring
 // (f64::min/max).  Partial results are combined in a fixed order, so a query
