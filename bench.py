@@ -442,7 +442,7 @@ def config_results(args, dec, data, dev, flush, clean):
     a.steps = 40
     v = timed("C5_serving", lambda: serving_line(a))
     res["C5_serving"] = {k: v[k] for k in ("value", "unit", "plain_queries_per_s", "plain_statistic",
-                                           "plain_queries_per_s_median", "speedup_vs_plain",
+                                           "plain_queries_per_s_runs", "plain_queries_per_s_median", "speedup_vs_plain",
                                            "decoded_gb_per_s_saturated", "results_equal_alone_and_in_mix", "poisson",
                                            "config", "server_stats")}
     time.sleep(0.2)
@@ -656,9 +656,13 @@ def serving_line(args):
     # column (first-use allocations out of the timing)
     E.run_plain(decs, [([i], column_range(meta[i][0], rng), ("sum",)) for i in range(n_cols)])
     plain_reqs = make_requests(max(20, args.steps))
-    t0 = time.perf_counter()
-    plain = E.run_plain(decs, plain_reqs)
-    plain_qps = len(plain_reqs) / (time.perf_counter() - t0)
+    plain_rates, plain = [], None
+    for _ in range(3):  # best of three: the host's other work can stretch single runs
+        t0 = time.perf_counter()
+        got = E.run_plain(decs, plain_reqs)
+        plain_rates.append(len(plain_reqs) / (time.perf_counter() - t0))
+        plain = plain if plain is not None else got
+    plain_qps = max(plain_rates)
     plain_median_qps = 1e9 / float(np.median([r["done_ns"] - r["submit_ns"] for r in plain]))
     caps = {"slots": 4, "max_queries": 16384, "max_chunks": 1 << 23, "max_items": 1 << 23}
     srv = E.Server(decs, **caps)
@@ -700,7 +704,9 @@ def serving_line(args):
                        "column_bytes": sum(m[2] for m in meta), **caps,
                        "tiling": "server default: 8 BUFF tiles, 8 RLE chunks, 16 Gorilla chunks per work item"},
             "saturated_requests": len(sat_reqs), "plain_requests": len(plain_reqs),
-            "plain_queries_per_s": round(plain_qps, 1), "plain_statistic": "requests / wall time, one at a time",
+            "plain_queries_per_s": round(plain_qps, 1),
+            "plain_statistic": "requests / wall time, one at a time, best of three runs",
+            "plain_queries_per_s_runs": [round(x, 1) for x in plain_rates],
             "plain_queries_per_s_median": round(plain_median_qps, 1), "speedup_vs_plain": round(sat_qps / plain_qps, 2),
             "decoded_gb_per_s_saturated": round(8.0 * sat_rows / sat_s / 1e9, 1),
             "results_equal_alone_and_in_mix": bool(equal), "poisson": rates, "server_stats": st}
