@@ -172,7 +172,7 @@ class Workload:
 DEFAULT_ROWS = {"buff": N_ROWS, "gorilla": 1_048_576, "chimp128": 16_777_216, "rle": 16_777_216,
                 "elf": 16_777_216, "elf_on_chimp": 16_777_216}
 KERNELS = {"buff": "buff_stream_kernel<2,6> (register-streaming decode + range filter + bitmask + sum)",
-           "gorilla": "gorilla_kernel (one warp per chunk: decode + filter + bitmask + sum/min/max)",
+           "gorilla": "gorilla_kernel (three warps per chunk: parse, bitmask + min/max, sums)",
            "chimp128": "xor_kernel<Chimp128> (segment-parallel decode + filter + bitmask + max)",
            "elf": "xor_kernel<Elf> (segment-parallel decode + decimal restore + filter + bitmask + max)",
            "elf_on_chimp": "xor_kernel<ElfOnChimp> (segment-parallel decode + decimal restore + filter + bitmask + max)",

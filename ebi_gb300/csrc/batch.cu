@@ -136,7 +136,9 @@ batch_kernel(const QueryParams* __restrict__ qp, const BatchItem* __restrict__ i
 
 __global__ void __launch_bounds__(kFinThreads) batch_finalize_kernel(const QueryParams* __restrict__ qp,
                                                                      QueryResult* res) {
-    finalize_chunks(qp[blockIdx.x], res + blockIdx.x);
+    const QueryParams& q = qp[blockIdx.x];
+    if (q.scheme == EBI_BUFF) finalize_chunks(q, res + blockIdx.x);
+    else fold_values_cta(q, res + blockIdx.x);
 }
 
 }  // namespace

@@ -387,7 +387,7 @@ int finish(ebi_column* c, const QueryParams& q, cudaStream_t s) {
         }
     }
     if (!done) {
-        if (!c->fused_pending) CK(launch_finalize(q, c->d_res, s));
+        if (!c->fused_pending) CK(launch_finalize(q, c->d_res, c->d_parts, s));
         c->fused_pending = false;
         if (c->timing) CK(cudaEventRecord(c->ev[2], s));
         folded = true;
@@ -708,6 +708,8 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st) st = col_alloc(c, &c->d_tiles, c->tiles.tiles.size(), s);
     if (!st) st = col_alloc(c, &c->d_acc, c->n_chunks, s);
     if (!st) st = col_alloc(c, &c->d_res, 1, s);
+    if (!st && c->scheme != EBI_BUFF)
+        st = col_alloc(c, &c->d_parts, value_slices(static_cast<uint32_t>(c->n_chunks)) + 1, s);
     if (!st && !binfo.empty()) st = col_alloc(c, &c->d_buff, binfo.size(), s);
     // the scan totals and, behind them, one slot per CTA of a scan launch
     // two totals blocks (totals-only queries alternate between them)
@@ -726,6 +728,8 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
         up(c->d_buff, binfo.data(), binfo.size() * sizeof(BuffChunkInfo));
         up(c->d_tot, &kRest, sizeof kRest);
         up(reinterpret_cast<uint8_t*>(c->d_tot) + kScanTotalsBytes, &kRest, sizeof kRest);
+        if (e == cudaSuccess && c->d_parts)
+            e = cudaMemsetAsync(c->d_parts, 0, (value_slices(static_cast<uint32_t>(c->n_chunks)) + 1) * sizeof(ValPart), s);
         if (e == cudaSuccess) e = launch_acc_init(c->d_acc, static_cast<uint32_t>(c->n_chunks), s);
     }
     // the staged tables must stay until the copies ran
@@ -781,7 +785,7 @@ int ebi_column_close(ebi_column* c) {
     cudaStream_t s = c->stream;
     for (cudaEvent_t e : c->ev) if (e) cudaEventDestroy(e);
     void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
-                    c->d_scratch_mask, c->d_buff, c->d_tot, c->d_units};
+                    c->d_scratch_mask, c->d_buff, c->d_tot, c->d_units, c->d_parts};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
     if (c->h_res || c->h_tot) {
         cudaStreamSynchronize(s);  // no copy into the slots is pending when they are recycled

@@ -120,6 +120,21 @@ struct QueryResult {
     unsigned long long count;  // rows selected / values written
 };
 
+// A partial fold of the non-BUFF codecs' chunk results over a range of
+// chunks: double-double sum, min / max, rows, and the lowest failing chunk.
+// One per slice of kSliceChunks chunks in the column's fold scratch, whose
+// last entry's first word is the fold's CTA counter (rest 0).
+struct ValPart {
+    double hi, lo, mn, mx;
+    unsigned long long cnt;
+    uint32_t bad;     // lowest chunk index with an error status (0xffffffff: none)
+    uint32_t bad_st;  // its status
+};
+constexpr uint32_t kSliceChunks = 64;
+__host__ __device__ inline uint32_t value_slices(uint32_t n_chunks) {
+    return (n_chunks + kSliceChunks - 1) / kSliceChunks;
+}
+
 enum Op : int {
     OP_FILTER = 0,      // bitmask only
     OP_FILTER_AGG = 1,  // bitmask + sum/min/max/count of the selected rows

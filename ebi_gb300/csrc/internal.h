@@ -192,7 +192,9 @@ cudaError_t launch_select_chunks(const QueryParams& q, cudaStream_t s);
 cudaError_t launch_tile_scan(const unsigned long long* counts, unsigned long long* offsets, uint32_t n,
                              cudaStream_t s);
 // Folds the per-chunk partials in chunk order into *res and re-arms acc.
-cudaError_t launch_finalize(const QueryParams& q, QueryResult* res, cudaStream_t s);
+// Codecs other than BUFF fold over a grid through `parts`: value_slices(n_chunks)
+// ValParts and a counter behind them (at rest 0).
+cudaError_t launch_finalize(const QueryParams& q, QueryResult* res, ValPart* parts, cudaStream_t s);
 // Sets acc to its rest values (once, at open).
 cudaError_t launch_acc_init(ChunkAcc* acc, uint32_t n, cudaStream_t s);
 

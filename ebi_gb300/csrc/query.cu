@@ -85,6 +85,49 @@ __global__ void __launch_bounds__(kFinThreads) finalize_kernel(QueryParams q, Qu
     finalize_chunks(q, res);
 }
 
+// The non-BUFF fold over a grid: warp w of CTA b folds slice 8b + w into
+// parts[slice]; the last CTA to finish (a ticket in the counter behind the
+// slices) folds the slices into *res and puts the counter back to 0.
+constexpr int kSliceWarps = 8;
+__global__ void __launch_bounds__(kSliceWarps * 32) fold_values_kernel(QueryParams q, ValPart* parts,
+                                                                       QueryResult* res) {
+    __shared__ uint32_t last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t S = value_slices(q.n_chunks);
+    unsigned int* counter = reinterpret_cast<unsigned int*>(parts + S);
+    const uint32_t s = blockIdx.x * kSliceWarps + wid;
+    if (s < S) {
+        const ValPart p = slice_fold(q, s);
+        if (lane == 0) {
+            parts[s] = p;
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last || wid) return;
+    __threadfence();
+    ValPart acc = val_part_rest();
+    for (uint32_t i = lane; i < S; i += 32) {
+        const ValPart* p = parts + i;
+        ValPart b;
+        b.hi = __ldcg(&p->hi);
+        b.lo = __ldcg(&p->lo);
+        b.mn = __ldcg(&p->mn);
+        b.mx = __ldcg(&p->mx);
+        b.cnt = __ldcg(&p->cnt);
+        b.bad = __ldcg(&p->bad);
+        b.bad_st = __ldcg(&p->bad_st);
+        val_part_add(acc, b);
+    }
+    const ValPart r = val_part_warp(acc);
+    if (lane == 0) {
+        *res = val_part_result(r);
+        *counter = 0;
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_acc_init(ChunkAcc* acc, uint32_t n, cudaStream_t s) {
@@ -109,8 +152,15 @@ cudaError_t launch_tile_scan(const unsigned long long* counts, unsigned long lon
     return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(const QueryParams& q, QueryResult* res, cudaStream_t s) {
-    finalize_kernel<<<1, kFinThreads, 0, s>>>(q, res);
+cudaError_t launch_finalize(const QueryParams& q, QueryResult* res, ValPart* parts, cudaStream_t s) {
+    if (q.scheme == EBI_BUFF) {
+        finalize_kernel<<<1, kFinThreads, 0, s>>>(q, res);
+    } else {
+        if (!parts) return cudaErrorInvalidValue;
+        const uint32_t S = value_slices(q.n_chunks);
+        const uint32_t grid = S ? (S + kSliceWarps - 1) / kSliceWarps : 1;
+        fold_values_kernel<<<grid, kSliceWarps * 32, 0, s>>>(q, parts, res);
+    }
     count_launch();
     return cudaGetLastError();
 }
