@@ -120,16 +120,21 @@ struct QueryResult {
     unsigned long long count;  // rows selected / values written
 };
 
-// A partial fold of the non-BUFF codecs' chunk results over a range of
-// chunks: double-double sum, min / max, rows, and the lowest failing chunk.
-// One per slice of kSliceChunks chunks in the column's fold scratch, whose
-// last entry's first word is the fold's CTA counter (rest 0).
-struct ValPart {
-    double hi, lo, mn, mx;
+// A partial fold of the non-BUFF codecs' chunk results over one slice of
+// kSliceChunks chunks (finalize.cuh): the signed 192-bit fixed-point sum of
+// the chunks' compensated sums, min / max as ordered keys, rows, and the
+// lowest failing chunk.  The column's fold scratch holds one per slice; the
+// first word after the last one is the fold's CTA counter (rest 0).
+struct alignas(16) ValPart {
+    unsigned long long w0, w1, w2;  // the sum, two's complement, in units of 2^(top - 1172)
+    unsigned long long mn, mx;      // ordered keys (rest: +inf / -inf)
     unsigned long long cnt;
-    uint32_t bad;     // lowest chunk index with an error status (0xffffffff: none)
-    uint32_t bad_st;  // its status
+    uint32_t top;      // largest exponent field of the slice's finite nonzero terms (0: none)
+    uint32_t special;  // 1: a NaN term, 2: +inf, 4: -inf
+    uint32_t bad;      // lowest chunk index with an error status (0xffffffff: none)
+    uint32_t bad_st;   // its status
 };
+static_assert(sizeof(ValPart) == 64, "four 16-byte words per slice");
 constexpr uint32_t kSliceChunks = 64;
 __host__ __device__ inline uint32_t value_slices(uint32_t n_chunks) {
     return (n_chunks + kSliceChunks - 1) / kSliceChunks;

@@ -87,8 +87,27 @@ __global__ void __launch_bounds__(kFinThreads) finalize_kernel(QueryParams q, Qu
 
 // The non-BUFF fold over a grid: warp w of CTA b folds slice 8b + w into
 // parts[slice]; the last CTA to finish (a ticket in the counter behind the
-// slices) folds the slices into *res and puts the counter back to 0.
+// slices) sums the slices into *res and puts the counter back to 0.
 constexpr int kSliceWarps = 8;
+
+__device__ __forceinline__ ValPart load_part(const ValPart* p) {
+    const ulonglong2* v = reinterpret_cast<const ulonglong2*>(p);
+    const ulonglong2 a = __ldcg(v), b = __ldcg(v + 1), c = __ldcg(v + 2);
+    const uint4 d = __ldcg(reinterpret_cast<const uint4*>(p) + 3);
+    ValPart r;
+    r.w0 = a.x;
+    r.w1 = a.y;
+    r.w2 = b.x;
+    r.mn = b.y;
+    r.mx = c.x;
+    r.cnt = c.y;
+    r.top = d.x;
+    r.special = d.y;
+    r.bad = d.z;
+    r.bad_st = d.w;
+    return r;
+}
+
 __global__ void __launch_bounds__(kSliceWarps * 32) fold_values_kernel(QueryParams q, ValPart* parts,
                                                                        QueryResult* res) {
     __shared__ uint32_t last;
@@ -108,22 +127,14 @@ __global__ void __launch_bounds__(kSliceWarps * 32) fold_values_kernel(QueryPara
     __syncthreads();
     if (!last || wid) return;
     __threadfence();
-    ValPart acc = val_part_rest();
-    for (uint32_t i = lane; i < S; i += 32) {
-        const ValPart* p = parts + i;
-        ValPart b;
-        b.hi = __ldcg(&p->hi);
-        b.lo = __ldcg(&p->lo);
-        b.mn = __ldcg(&p->mn);
-        b.mx = __ldcg(&p->mx);
-        b.cnt = __ldcg(&p->cnt);
-        b.bad = __ldcg(&p->bad);
-        b.bad_st = __ldcg(&p->bad_st);
-        val_part_add(acc, b);
-    }
-    const ValPart r = val_part_warp(acc);
+    uint32_t tq = 0;
+    for (uint32_t i = lane; i < S; i += 32) tq = max(tq, __ldcg(&parts[i].top));
+    tq = __reduce_max_sync(0xffffffffu, tq);
+    ValTotal t = val_total_rest();
+    for (uint32_t i = lane; i < S; i += 32) val_total_add(t, load_part(parts + i), tq);
+    t = val_total_warp(t);
     if (lane == 0) {
-        *res = val_part_result(r);
+        *res = val_total_result(t, tq);
         *counter = 0;
     }
 }
