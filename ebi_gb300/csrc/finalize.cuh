@@ -187,6 +187,18 @@ __device__ __forceinline__ void chunk_terms(const ChunkAcc& a, unsigned long lon
 __device__ __forceinline__ unsigned long long u64_min(unsigned long long a, unsigned long long b) { return a < b ? a : b; }
 __device__ __forceinline__ unsigned long long u64_max(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
 
+// A chunk's accumulator through L2 (other CTAs of the same launch wrote it).
+__device__ __forceinline__ ChunkAcc load_acc_cg(const ChunkAcc* p) {
+    static_assert(sizeof(ChunkAcc) == 80, "five 16-byte words per chunk");
+    const uint4* v = reinterpret_cast<const uint4*>(p);
+    uint4 w[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) w[i] = __ldcg(v + i);
+    ChunkAcc a;
+    memcpy(&a, w, sizeof a);
+    return a;
+}
+
 // Slice s of query q by one warp (every lane returns the slice's part); re-arms its chunks.
 __device__ __forceinline__ ValPart slice_fold(const QueryParams& q, uint32_t s) {
     const int lane = threadIdx.x & 31;
@@ -198,7 +210,7 @@ __device__ __forceinline__ ValPart slice_fold(const QueryParams& q, uint32_t s) 
     for (int k = 0; k < 2; ++k) {
         const uint32_t c = s * kSliceChunks + 2 * lane + k;
         if (c < q.n_chunks) {
-            const ChunkAcc a = q.acc[c];
+            const ChunkAcc a = load_acc_cg(q.acc + c);
             if (a.status && bad == 0xffffffffu) { bad = c; bad_st = a.status; }
             if (chunk_included(q, a)) {
                 chunk_terms(a, t[2 * k], t[2 * k + 1], special);
@@ -337,6 +349,41 @@ __device__ inline void fold_values_cta(const QueryParams& q, QueryResult* res) {
         for (int w = 1; w < kWarps; ++w) val_total_merge(t, s_tot[w]);
         *res = val_total_result(t, tq);
     }
+}
+
+// ---- the grid fold's scratch: slice parts, then the CTA counter --------------
+__device__ __forceinline__ unsigned int* fold_counters(ValPart* parts, uint32_t S) {
+    return reinterpret_cast<unsigned int*>(parts + S);
+}
+
+__device__ __forceinline__ ValPart load_part(const ValPart* p) {
+    const ulonglong2* v = reinterpret_cast<const ulonglong2*>(p);
+    const ulonglong2 a = __ldcg(v), b = __ldcg(v + 1), c = __ldcg(v + 2);
+    const uint4 d = __ldcg(reinterpret_cast<const uint4*>(p) + 3);
+    ValPart r;
+    r.w0 = a.x;
+    r.w1 = a.y;
+    r.w2 = b.x;
+    r.mn = b.y;
+    r.mx = c.x;
+    r.cnt = c.y;
+    r.top = d.x;
+    r.special = d.y;
+    r.bad = d.z;
+    r.bad_st = d.w;
+    return r;
+}
+
+// One warp sums the S slice parts (written by other CTAs: read through L2) into *res.
+__device__ inline void fold_parts_warp(const ValPart* parts, uint32_t S, QueryResult* res) {
+    const int lane = threadIdx.x & 31;
+    uint32_t tq = 0;
+    for (uint32_t i = lane; i < S; i += 32) tq = max(tq, __ldcg(&parts[i].top));
+    tq = __reduce_max_sync(0xffffffffu, tq);
+    ValTotal t = val_total_rest();
+    for (uint32_t i = lane; i < S; i += 32) val_total_add(t, load_part(parts + i), tq);
+    t = val_total_warp(t);
+    if (lane == 0) *res = val_total_result(t, tq);
 }
 
 // Folds BUFF query q's per-chunk partials in chunk order into *res and

@@ -85,35 +85,17 @@ __global__ void __launch_bounds__(kFinThreads) finalize_kernel(QueryParams q, Qu
     finalize_chunks(q, res);
 }
 
-// The non-BUFF fold over a grid: warp w of CTA b folds slice 8b + w into
+// The non-BUFF fold over a grid (more than eight slices): warp w of CTA b folds slice 8b + w into
 // parts[slice]; the last CTA to finish (a ticket in the counter behind the
 // slices) sums the slices into *res and puts the counter back to 0.
 constexpr int kSliceWarps = 8;
-
-__device__ __forceinline__ ValPart load_part(const ValPart* p) {
-    const ulonglong2* v = reinterpret_cast<const ulonglong2*>(p);
-    const ulonglong2 a = __ldcg(v), b = __ldcg(v + 1), c = __ldcg(v + 2);
-    const uint4 d = __ldcg(reinterpret_cast<const uint4*>(p) + 3);
-    ValPart r;
-    r.w0 = a.x;
-    r.w1 = a.y;
-    r.w2 = b.x;
-    r.mn = b.y;
-    r.mx = c.x;
-    r.cnt = c.y;
-    r.top = d.x;
-    r.special = d.y;
-    r.bad = d.z;
-    r.bad_st = d.w;
-    return r;
-}
 
 __global__ void __launch_bounds__(kSliceWarps * 32) fold_values_kernel(QueryParams q, ValPart* parts,
                                                                        QueryResult* res) {
     __shared__ uint32_t last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t S = value_slices(q.n_chunks);
-    unsigned int* counter = reinterpret_cast<unsigned int*>(parts + S);
+    unsigned int* counter = fold_counters(parts, S);
     const uint32_t s = blockIdx.x * kSliceWarps + wid;
     if (s < S) {
         const ValPart p = slice_fold(q, s);
@@ -127,16 +109,8 @@ __global__ void __launch_bounds__(kSliceWarps * 32) fold_values_kernel(QueryPara
     __syncthreads();
     if (!last || wid) return;
     __threadfence();
-    uint32_t tq = 0;
-    for (uint32_t i = lane; i < S; i += 32) tq = max(tq, __ldcg(&parts[i].top));
-    tq = __reduce_max_sync(0xffffffffu, tq);
-    ValTotal t = val_total_rest();
-    for (uint32_t i = lane; i < S; i += 32) val_total_add(t, load_part(parts + i), tq);
-    t = val_total_warp(t);
-    if (lane == 0) {
-        *res = val_total_result(t, tq);
-        *counter = 0;
-    }
+    fold_parts_warp(parts, S, res);
+    if (lane == 0) *counter = 0;
 }
 
 }  // namespace
@@ -163,12 +137,36 @@ cudaError_t launch_tile_scan(const unsigned long long* counts, unsigned long lon
     return cudaGetLastError();
 }
 
+// Up to 8 slices: one CTA, a warp per slice, the slices summed through
+// shared memory (no global round trips between the two steps).  More slices
+// take the grid: one SM folding 32 slices measured slower than four.
+constexpr uint32_t kCtaSlices = 8;
+__global__ void __launch_bounds__(kCtaSlices * 32) fold_values_cta_kernel(QueryParams q, QueryResult* res) {
+    __shared__ ValPart sp[kCtaSlices];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t S = value_slices(q.n_chunks);
+    if (static_cast<uint32_t>(wid) < S) {
+        const ValPart p = slice_fold(q, wid);
+        if (lane == 0) sp[wid] = p;
+    }
+    __syncthreads();
+    if (wid) return;
+    const bool have = static_cast<uint32_t>(lane) < S;
+    const uint32_t tq = __reduce_max_sync(0xffffffffu, have ? sp[lane].top : 0u);
+    ValTotal t = val_total_rest();
+    if (have) val_total_add(t, sp[lane], tq);
+    t = val_total_warp(t);
+    if (lane == 0) *res = val_total_result(t, tq);
+}
+
 cudaError_t launch_finalize(const QueryParams& q, QueryResult* res, ValPart* parts, cudaStream_t s) {
+    const uint32_t S = value_slices(q.n_chunks);
     if (q.scheme == EBI_BUFF) {
         finalize_kernel<<<1, kFinThreads, 0, s>>>(q, res);
+    } else if (S <= kCtaSlices) {
+        fold_values_cta_kernel<<<1, S ? S * 32 : 32, 0, s>>>(q, res);
     } else {
         if (!parts) return cudaErrorInvalidValue;
-        const uint32_t S = value_slices(q.n_chunks);
         const uint32_t grid = S ? (S + kSliceWarps - 1) / kSliceWarps : 1;
         fold_values_kernel<<<grid, kSliceWarps * 32, 0, s>>>(q, parts, res);
     }

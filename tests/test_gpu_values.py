@@ -1,8 +1,8 @@
 """RLE, Uncompressed, Gorilla, Chimp, Chimp128, Elf and ElfOnChimp on the GPU
 against the oracle.
 
-Values, bitmasks and min/max are bit-exact; sums are compensated (double-double)
-and checked against the oracle's sequential sum (relative 1e-12 of the sum of
+Values, bitmasks and min/max are bit-exact; sums are compensated within each
+chunk and combined exactly across chunks, and checked against the oracle's sequential sum (relative 1e-12 of the sum of
 magnitudes) and against math.fsum of the same values (2 ulps).
 """
 import numpy as np
@@ -167,6 +167,32 @@ def test_many_small_chunks(codec, kind):
     assert n_chunks >= 1024
     check_query_suite(data, random_preds(v, rng, k=2), masks=(None, random_mask(n, 0.3, rng)),
                       chunk_ids=(None, int(rng.integers(n_chunks))))
+
+
+@pytest.mark.parametrize("codec", ["uncompressed", "rle", "gorilla", "chimp128"])
+@pytest.mark.parametrize("corrupt", [False, True])
+def test_fold_over_many_slices(codec, corrupt):
+    # 2,344 chunks of 64 values: more than 32 slices of 64 chunks, so the
+    # single-column fold runs over a grid of CTAs (and the batch over one CTA)
+    rng = np.random.default_rng(23)
+    n = 150_000
+    v = columns(rng, n)["walk"]
+    data = bytearray(E.encode(v, codec, ("record_count", 64)))
+    d = O.Decoder(bytes(data))
+    assert d.n_chunks > 32 * 64
+    if corrupt:
+        for c in (1500, 2100, 2300):  # failing chunks in different slices and CTAs
+            phys, size, _, _ = d.chunk_info(c)
+            data[phys + size // 2] ^= 0x10
+    preds = random_preds(v, rng, k=2)
+    check_query_suite(bytes(data), preds, masks=(None, random_mask(n, 0.3, rng)))
+    if not corrupt:
+        # the batch folds the same slices in one CTA per query: the same bits
+        g = E.Decoder(bytes(data))
+        got = E.Batch([(g, p, ("sum", "min", "max")) for p in preds]).run()
+        for p, (s, mn, mx, cnt) in zip(preds, got):
+            _, s1, mn1, mx1, cnt1 = g.filter_agg(p)
+            assert same_f64(np.array([s, mn, mx]), np.array([s1, mn1, mx1])) and cnt == cnt1, (p, s, s1)
 
 
 @pytest.mark.parametrize("codec", ["chimp", "chimp128", "elf_on_chimp", "elf"])
