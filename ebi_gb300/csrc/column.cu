@@ -215,6 +215,7 @@ int parse_file(const uint8_t* d, uint64_t len, ebi_column* c) {
         if (nphys < phys || phys > len || nphys > len) { cd.flags |= kChunkBadGeometry; cd.byte_len = 0; }
         if (nlogi < logi || nlogi - logi > 0xffffffffull || nlogi > nrec) { cd.flags |= kChunkBadGeometry; cd.n_rows = 0; }
         if (logi % 32) c->rows_aligned32 = false;
+        if (i > 0 && logi < c->chunks[i - 1].row_off) c->rows_in_order = false;
         c->chunks[i] = cd;
     }
     return EBI_OK;
@@ -429,8 +430,11 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
     uint32_t tb, tn;
     tile_range(c, chunk_id, &tb, &tn);
     if (c->scheme != EBI_BUFF) {
-        // value codecs OR their rows into a zeroed output (decoded runs may start on any row)
-        if (d_out_mask) CK(cudaMemsetAsync(d_out_mask, 0, c->mask_words * 8, s));
+        // Value codecs OR their rows into a zeroed output (decoded runs may
+        // start on any row).  When every chunk is scanned and chunks start on
+        // 32-row boundaries in row order, each chunk's CTA zeroes its own words.
+        q.zero_out = d_out_mask && tn > 0 && tn == c->n_chunks && c->rows_aligned32 && c->rows_in_order;
+        if (d_out_mask && !q.zero_out) CK(cudaMemsetAsync(d_out_mask, 0, c->mask_words * 8, s));
         if (d_mask) CK(launch_select_chunks(q, s));
         if (int st = mark_scan(c, s)) return st;
         CK(launch_values(c, q, tb, tn, VAL_SCAN, nullptr, s));

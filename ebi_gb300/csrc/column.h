@@ -19,6 +19,7 @@ struct ebi_column {
     std::vector<ChunkDesc> chunks;
     TileMap tiles;
     bool rows_aligned32 = true;
+    bool rows_in_order = true;  // chunk row offsets never decrease (a well-formed footer)
     int32_t precision = -1;
     uint8_t* d_file = nullptr;
     ChunkDesc* d_chunks = nullptr;

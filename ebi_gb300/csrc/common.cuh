@@ -174,6 +174,7 @@ struct QueryParams {
     uint32_t stage_bytes;      // Gorilla: shared-memory staging size per chunk (0: read through L1)
     const double* dec_tab;     // Elf / ElfOnChimp: decimal tables of elf_dev.cuh (device memory)
     long long copy_wait;       // limit (SM clocks) of a kernel's waits for its bulk copies to land; <= 0: one look
+    int zero_out;              // value codecs: each chunk's CTA zeroes its own out_mask words first (no memset)
 };
 
 // Passes of the value-codec kernels (one CTA per chunk).
@@ -242,6 +243,19 @@ __device__ __forceinline__ void store_mask_word(uint32_t* m, uint64_t r, uint32_
 }
 
 __device__ __forceinline__ void set_status(ChunkAcc* a, uint32_t code) { atomicCAS(&a->status, 0u, code); }
+
+// With q.zero_out (a value-codec scan over every chunk of a column whose
+// chunks start on 32-row boundaries, in row order), chunk c's words of the
+// output bitmask belong to its CTA alone: every thread of the CTA calls this
+// before the CTA's first barrier, and the chunk's ORs follow that barrier.
+// The last chunk also zeroes the rest of the mask's last u64 word.
+__device__ __forceinline__ void zero_chunk_words(const QueryParams& q, const ChunkDesc& cd, uint32_t c) {
+    if (!q.zero_out) return;
+    const uint64_t end = ((q.n_records + 63) >> 6) * 2;  // u32 words of the mask
+    const uint64_t w0 = min(cd.row_off >> 5, end);
+    const uint64_t w1 = c + 1 == q.n_chunks ? end : min((cd.row_off + cd.n_rows + 31) >> 5, end);
+    for (uint64_t w = w0 + threadIdx.x; w < w1; w += blockDim.x) q.out_mask[w] = 0u;
+}
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {

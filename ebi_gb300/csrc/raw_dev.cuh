@@ -48,6 +48,7 @@ __device__ __forceinline__ void raw_chunk(const QueryParams& q, uint32_t li, uin
         }
         s_ok = ok;
     }
+    zero_chunk_words(q, cd, c);
     __syncthreads();
     if (!s_ok) {
         if (mode == VAL_COUNT && threadIdx.x == 0) q.tile_counts[li] = 0;

@@ -61,6 +61,7 @@ __device__ __forceinline__ void rle_chunk(const QueryParams& q, uint32_t li, uin
         s_ok = ok;
         if (mode == VAL_COUNT && !ok) q.tile_counts[li] = 0;
     }
+    zero_chunk_words(q, cd, c);
     __syncthreads();
     if (!s_ok) return;
     const uint8_t* base = q.file + cd.byte_off;

@@ -195,6 +195,31 @@ def test_fold_over_many_slices(codec, corrupt):
             assert same_f64(np.array([s, mn, mx]), np.array([s1, mn1, mx1])) and cnt == cnt1, (p, s, s1)
 
 
+@pytest.mark.parametrize("codec", VALUE_CODECS)
+@pytest.mark.parametrize("chunk", [512, 1000])
+def test_output_mask_fully_written(codec, chunk):
+    # the output bitmask starts as all ones: every word, the padding past the
+    # last row included, must come back as the oracle's (512-row chunks: each
+    # chunk's CTA zeroes its own words; 1,000-row chunks share words: a memset)
+    rng = np.random.default_rng(31)
+    n = 32 * 937 - 5  # an odd number of u32 words: the last u64 word's upper half holds no row
+    v = columns(rng, n)["walk"]
+    data = E.encode(v, codec, ("record_count", chunk))
+    g, o = E.Decoder(data), O.Decoder(data)
+    p = E.Predicate.range(E.RangeValue.inclusive(25.0), E.RangeValue.inclusive(35.0))
+    op = O.rng(O.BOUND_INCLUSIVE, 25.0, O.BOUND_INCLUSIVE, 35.0)
+    for m in (None, random_mask(n, 0.2, rng)):
+        out = g.new_mask()
+        out.fill_(-1)
+        g.filter(p, m, out=out)
+        want = o.filter(op, m)
+        got = mask_np(out)
+        assert np.array_equal(got[: len(want)], want) and not got[len(want):].any()
+        out.fill_(-1)
+        g.filter_agg(p, m, out=out)
+        assert np.array_equal(mask_np(out)[: len(want)], want)
+
+
 @pytest.mark.parametrize("codec", ["chimp", "chimp128", "elf_on_chimp", "elf"])
 def test_many_small_chunks_corrupt(codec):
     rng = np.random.default_rng(9)
