@@ -29,7 +29,7 @@ namespace ebi {
 namespace {
 
 constexpr int kBatchThreads = 256;
-static_assert(kBatchThreads == kXorThreads && kBatchThreads == kRleThreads, "codec CTA shapes");
+static_assert(kBatchThreads == kXorThreads, "codec CTA shapes");
 
 // One function per item kind, kept out of line so that each gets its own
 // register allocation (the kernel's is the largest, not the sum of all paths).
@@ -69,11 +69,15 @@ __device__ __noinline__ void item_raw(const QueryParams& q, const BatchItem& it)
         raw_chunk<kBatchThreads>(q, it.unit + j, it.unit + j, VAL_SCAN, nullptr);
     }
 }
+// Chunks [unit, unit + count): warp w takes chunks w, w + 8, ... with its
+// share of the dynamic shared memory.
+static_assert((kBatchThreads / 32) * sizeof(RleWarpSmem) <= xor_smem_bytes(CODEC_CHIMP128),
+              "the batch kernel's dynamic shared memory holds one RLE stage per warp");
 __device__ __noinline__ void item_rle(const QueryParams& q, const BatchItem& it) {
-    for (uint32_t j = 0; j < it.count; ++j) {
-        if (j) __syncthreads();  // the previous chunk is done with shared memory
-        rle_chunk(q, it.unit + j, it.unit + j, VAL_SCAN, nullptr);
-    }
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    RleWarpSmem* sm = reinterpret_cast<RleWarpSmem*>(smem_raw) + (threadIdx.x >> 5);
+    for (uint32_t j = threadIdx.x >> 5; j < it.count; j += kBatchThreads / 32)
+        rle_chunk_warp(q, it.unit + j, it.unit + j, VAL_SCAN, nullptr, sm);
 }
 // Chunks [unit, unit + chunks): warp w walks chunks w, w + 8, ...  Up to
 // kGorillaShare queries keep their state in registers; more (up to

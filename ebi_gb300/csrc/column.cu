@@ -218,6 +218,23 @@ int parse_file(const uint8_t* d, uint64_t len, ebi_column* c) {
         if (i > 0 && logi < c->chunks[i - 1].row_off) c->rows_in_order = false;
         c->chunks[i] = cd;
     }
+    // Uncompressed chunks decode exactly their rows; an RLE chunk decodes the
+    // sum of its run lengths (decoder/chunk_reader/run_length.rs:68-91), read
+    // here for every chunk whose field table fits (the others fail when read).
+    c->rows_bounded = scheme == EBI_UNCOMPRESSED;
+    if (scheme == EBI_RLE) {
+        c->rows_bounded = true;
+        for (uint64_t i = 0; i < nch && c->rows_bounded; ++i) {
+            const ChunkDesc& cd = c->chunks[i];
+            if ((cd.flags & kChunkBadGeometry) || cd.byte_len < 8) continue;
+            const uint8_t* p = d + cd.byte_off;
+            const uint64_t nf = rd64(p);
+            if (nf > (cd.byte_len - 8) / 9) continue;
+            uint64_t rows = 0;
+            for (uint64_t k = 0; k < nf; ++k) rows += p[8 + 9 * k];
+            if (rows > cd.n_rows) c->rows_bounded = false;
+        }
+    }
     return EBI_OK;
 }
 
@@ -431,9 +448,12 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
     tile_range(c, chunk_id, &tb, &tn);
     if (c->scheme != EBI_BUFF) {
         // Value codecs OR their rows into a zeroed output (decoded runs may
-        // start on any row).  When every chunk is scanned and chunks start on
-        // 32-row boundaries in row order, each chunk's CTA zeroes its own words.
-        q.zero_out = d_out_mask && tn > 0 && tn == c->n_chunks && c->rows_aligned32 && c->rows_in_order;
+        // start on any row).  When every chunk is scanned, chunks start on
+        // 32-row boundaries in row order and none decodes rows past its range
+        // (whose bits would land in the next chunk's words), each chunk's CTA
+        // zeroes its own words.
+        q.own_words = c->rows_aligned32 && c->rows_in_order && c->rows_bounded;
+        q.zero_out = d_out_mask && tn > 0 && tn == c->n_chunks && q.own_words;
         if (d_out_mask && !q.zero_out) CK(cudaMemsetAsync(d_out_mask, 0, c->mask_words * 8, s));
         if (d_mask) CK(launch_select_chunks(q, s));
         if (int st = mark_scan(c, s)) return st;

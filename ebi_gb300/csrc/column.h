@@ -20,6 +20,7 @@ struct ebi_column {
     TileMap tiles;
     bool rows_aligned32 = true;
     bool rows_in_order = true;  // chunk row offsets never decrease (a well-formed footer)
+    bool rows_bounded = false;  // no chunk decodes rows past its range (Uncompressed; RLE with run totals checked)
     int32_t precision = -1;
     uint8_t* d_file = nullptr;
     ChunkDesc* d_chunks = nullptr;

@@ -174,7 +174,8 @@ struct QueryParams {
     uint32_t stage_bytes;      // Gorilla: shared-memory staging size per chunk (0: read through L1)
     const double* dec_tab;     // Elf / ElfOnChimp: decimal tables of elf_dev.cuh (device memory)
     long long copy_wait;       // limit (SM clocks) of a kernel's waits for its bulk copies to land; <= 0: one look
-    int zero_out;              // value codecs: each chunk's CTA zeroes its own out_mask words first (no memset)
+    int zero_out;              // Uncompressed / RLE: each chunk's CTA zeroes its own out_mask words first (no memset)
+    int own_words;             // chunks start on 32-row boundaries in row order and decode no row past their range
 };
 
 // Passes of the value-codec kernels (one CTA per chunk).
@@ -244,11 +245,12 @@ __device__ __forceinline__ void store_mask_word(uint32_t* m, uint64_t r, uint32_
 
 __device__ __forceinline__ void set_status(ChunkAcc* a, uint32_t code) { atomicCAS(&a->status, 0u, code); }
 
-// With q.zero_out (a value-codec scan over every chunk of a column whose
-// chunks start on 32-row boundaries, in row order), chunk c's words of the
-// output bitmask belong to its CTA alone: every thread of the CTA calls this
-// before the CTA's first barrier, and the chunk's ORs follow that barrier.
-// The last chunk also zeroes the rest of the mask's last u64 word.
+// With q.zero_out (an Uncompressed or RLE scan over every chunk of a column
+// whose chunks start on 32-row boundaries, in row order, and decode no more
+// rows than their range), chunk c's words of the output bitmask belong to its
+// CTA alone: every thread of the CTA calls this before the CTA's first
+// barrier, and the chunk's ORs follow that barrier.  The last chunk also
+// zeroes the rest of the mask's last u64 word.
 __device__ __forceinline__ void zero_chunk_words(const QueryParams& q, const ChunkDesc& cd, uint32_t c) {
     if (!q.zero_out) return;
     const uint64_t end = ((q.n_records + 63) >> 6) * 2;  // u32 words of the mask

@@ -61,10 +61,9 @@ __global__ void __launch_bounds__(96) gorilla_kernel(QueryParams q, uint32_t chu
             fence_mbar_init();
         }
     }
-    const ChunkDesc cd = q.chunks[c];
-    zero_chunk_words(q, cd, c);
     __syncthreads();
     if (!R->ok) return;
+    const ChunkDesc cd = q.chunks[c];
 
     if (warp == 0) {
         // ---- parse: kSub steps into each ring slot ---------------------------

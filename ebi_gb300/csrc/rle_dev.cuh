@@ -4,10 +4,9 @@
 // row i of the chunk is global row logical_offset + i, and the default
 // operators (decoder/query.rs:14-154) run over the expanded rows.
 //
-// One CTA per chunk walks its fields in batches of 1024 (4 per thread): a
-// block scan of the run lengths gives every field's first row; each field
-// then evaluates the predicate once for its whole run and sets the run's
-// bitmask bits with at most ceil(255 / 32) + 1 word operations.
+// One warp per chunk (rle_chunk_warp); the field bytes of each step are
+// staged in shared memory by coalesced 16-byte loads first (9-byte fields read
+// in place would touch ~18 sectors per warp load).
 #pragma once
 
 #include "values.cuh"
@@ -15,26 +14,34 @@
 namespace ebi {
 namespace {
 
-constexpr int kRleThreads = 256;
 constexpr int kRlePer = 4;
+constexpr uint32_t kRleStep = 32 * kRlePer;  // fields per warp step
+constexpr uint32_t kRleWords = 256;          // bitmap words per warp: chunks up to 8,192 rows
 
-__device__ __forceinline__ double field_value(const uint8_t* f) {
-    return __longlong_as_double(static_cast<long long>(load_u64_unaligned(f + 1)));
-}
+// A warp's shared memory: the chunk's bitmap and one step's field bytes (the
+// 16-byte words that cover them, plus slack for the last value's second word).
+struct RleWarpSmem {
+    uint32_t bits[kRleWords];
+    alignas(16) uint8_t stage[(kRleStep * 9 + 30) / 16 * 16 + 16];
+};
 
-// One RLE chunk c by a CTA of kRleThreads threads; li indexes the pass's
-// per-chunk counts / offsets.
-__device__ __forceinline__ void rle_chunk(const QueryParams& q, uint32_t li, uint32_t c, int mode,
-                                          const unsigned long long* chunk_offsets) {
-    constexpr int kThreads = kRleThreads;
-    __shared__ uint32_t sh_scan[kThreads / 32];
-    __shared__ ValAgg sh_agg[kThreads / 32];
-    __shared__ int s_ok;
+// One RLE chunk c by one warp; li indexes the pass's per-chunk counts /
+// offsets.  Fields go 32 * kRlePer at a time (kRlePer consecutive fields per
+// lane): a warp scan of the run lengths gives every field's first row; each
+// field evaluates the predicate once for its run and sets the run's bitmask
+// bits with at most ceil(255 / 32) + 1 word operations, into the warp's
+// bitmap in shared memory (kRleWords words) when the chunk owns its words
+// (q.own_words) and fits, which then go out as whole words; else into the
+// output by atomicOr.  A warp per chunk keeps every step on shuffles: no
+// CTA barrier, and as many chunks in flight as warps fit.
+__device__ __forceinline__ void rle_chunk_warp(const QueryParams& q, uint32_t li, uint32_t c, int mode,
+                                               const unsigned long long* chunk_offsets, RleWarpSmem* sm) {
+    const int lane = threadIdx.x & 31;
     const ChunkDesc cd = q.chunks[c];
     const bool has_mask = q.in_mask != nullptr;
     ChunkAcc* acc = q.acc + c;
-    if (threadIdx.x == 0) {
-        int ok = 1;
+    int ok = 1;
+    if (lane == 0) {
         if (mode == VAL_SCAN) {
             ok = has_mask ? acc->selected != 0 : (q.chunk_id < 0 || static_cast<uint64_t>(q.chunk_id) == c);
             if (ok && !has_mask) acc->selected = 1;
@@ -58,36 +65,71 @@ __device__ __forceinline__ void rle_chunk(const QueryParams& q, uint32_t li, uin
                 ok = 0;
             }
         }
-        s_ok = ok;
         if (mode == VAL_COUNT && !ok) q.tile_counts[li] = 0;
     }
-    zero_chunk_words(q, cd, c);
-    __syncthreads();
-    if (!s_ok) return;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    const bool pred_on = q.pred_on != 0;
+    const bool store = mode == VAL_SCAN && pred_on && q.out_mask;
+    // the chunk's words of the output bitmask (the last chunk's run to the mask's end)
+    const uint64_t mend = ((q.n_records + 63) >> 6) * 2;
+    const uint64_t gw0 = min(cd.row_off >> 5, mend);
+    const uint64_t gw1 = c + 1 == q.n_chunks ? mend : min((cd.row_off + cd.n_rows + 31) >> 5, mend);
+    uint32_t* sbits = sm->bits;
+    const bool local = ok && store && q.own_words && gw1 - gw0 <= kRleWords;
+    if (q.zero_out && !local) {
+        for (uint64_t w = gw0 + lane; w < gw1; w += 32) q.out_mask[w] = 0u;
+        __syncwarp();  // before this warp's ORs into the same words
+    }
+    if (!ok) return;
+    if (local) {
+        for (uint32_t w = lane; w < kRleWords; w += 32) sbits[w] = 0u;
+        __syncwarp();
+    }
     const uint8_t* base = q.file + cd.byte_off;
     const uint64_t nf = load_u64_unaligned(base);
     const uint8_t* fields = base + 8;
-    const bool pred_on = q.pred_on != 0;
-    const bool store = mode == VAL_SCAN && pred_on && q.out_mask;
     const KeyPred kp = key_pred(q.pred);
     ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
     unsigned long long out_pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0;
     uint64_t carry_row = 0;
-    for (uint64_t b0 = 0; b0 < nf; b0 += (kRleThreads * kRlePer)) {
-        const uint64_t f0 = b0 + uint64_t(threadIdx.x) * kRlePer;
+    for (uint64_t b0 = 0; b0 < nf; b0 += kRleStep) {
+        // the step's fields [b0, b0 + kRleStep) into shared memory (the file
+        // allocation is 16-byte aligned and padded past its end)
+        const uint8_t* s0 = fields + 9 * b0;
+        const uint64_t nb = 9 * min(uint64_t(kRleStep), nf - b0);
+        const uint8_t* a0 = reinterpret_cast<const uint8_t*>(reinterpret_cast<uintptr_t>(s0) & ~uintptr_t(15));
+        const uint32_t skew = static_cast<uint32_t>(s0 - a0);
+        const uint32_t n16 = static_cast<uint32_t>((skew + nb + 15) >> 4);
+        __syncwarp();  // the previous step's fields are read
+        for (uint32_t i = lane; i < n16; i += 32)
+            reinterpret_cast<uint4*>(sm->stage)[i] = ldg16(a0 + 16 * i);
+        __syncwarp();
+        const uint64_t f0 = b0 + uint64_t(lane) * kRlePer;
         uint32_t run[kRlePer];
         double val[kRlePer];
         uint32_t rows = 0;
 #pragma unroll
         for (int k = 0; k < kRlePer; ++k) {
             const bool in = f0 + k < nf;
-            run[k] = in ? fields[9 * (f0 + k)] : 0u;
-            val[k] = in ? field_value(fields + 9 * (f0 + k)) : 0.0;
+            const uint32_t o = skew + 9 * (lane * kRlePer + k);  // the field's byte in the stage
+            run[k] = in ? sm->stage[o] : 0u;
+            uint64_t vb = 0;
+            if (in) {
+                const uint32_t p = o + 1, sh = (p & 7) * 8;
+                const uint64_t* w = reinterpret_cast<const uint64_t*>(sm->stage + (p & ~7u));
+                vb = sh ? (w[0] >> sh) | (w[1] << (64 - sh)) : w[0];
+            }
+            val[k] = __longlong_as_double(static_cast<long long>(vb));
             rows += run[k];
         }
-        uint32_t total;
-        const uint32_t first = block_excl_scan_u32<kThreads>(rows, sh_scan, &total);
-        uint64_t r = carry_row + first;  // chunk row of this thread's first field
+        uint32_t incl = rows;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint64_t r = carry_row + (incl - rows);  // chunk row of this lane's first field
         uint32_t sel_rows[kRlePer];
 #pragma unroll
         for (int k = 0; k < kRlePer; ++k) {
@@ -109,7 +151,11 @@ __device__ __forceinline__ void rle_chunk(const QueryParams& q, uint32_t li, uin
                             if (bits) bits &= q.in_mask[w];
                             n_sel += __popc(bits);
                         }
-                        if (store && bits) atomicOr(&q.out_mask[w], bits);
+                        if (store && bits) {
+                            // a chunk that owns its words decodes no row past them
+                            if (local && w >= gw0 && w - gw0 < kRleWords) atomicOr(&sbits[w - gw0], bits);
+                            else atomicOr(&q.out_mask[w], bits);
+                        }
                         g = wend;
                     }
                 }
@@ -123,22 +169,29 @@ __device__ __forceinline__ void rle_chunk(const QueryParams& q, uint32_t li, uin
             uint32_t mine = 0;
 #pragma unroll
             for (int k = 0; k < kRlePer; ++k) mine += sel_rows[k];
-            uint32_t btotal;
-            const uint32_t before = block_excl_scan_u32<kThreads>(mine, sh_scan, &btotal);
-            unsigned long long pos = out_pos + before;
+            uint32_t mi = mine;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, mi, o);
+                if (lane >= o) mi += y;
+            }
+            unsigned long long pos = out_pos + (mi - mine);
 #pragma unroll
             for (int k = 0; k < kRlePer; ++k) {
                 for (uint32_t i = 0; i < sel_rows[k]; ++i, ++pos)
                     if (pos < q.out_cap) q.out_vals[pos] = val[k];
             }
-            out_pos += btotal;
+            out_pos += __shfl_sync(0xffffffffu, mi, 31);
         }
         carry_row += total;
-        __syncthreads();
+    }
+    if (local) {
+        __syncwarp();
+        for (uint64_t w = gw0 + lane; w < gw1; w += 32) q.out_mask[w] = sbits[w - gw0];
     }
     if (mode == VAL_MATERIALIZE) return;
-    const ValAgg a = val_agg_block(agg, sh_agg);
-    if (threadIdx.x != 0) return;
+    const ValAgg a = val_agg_warp(agg);
+    if (lane != 0) return;
     if (mode == VAL_COUNT) q.tile_counts[li] = a.cnt;
     else val_agg_store(acc, a);
 }

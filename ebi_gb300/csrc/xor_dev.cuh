@@ -244,7 +244,6 @@ __device__ __forceinline__ void xor_chunk(const QueryParams* qs, uint32_t nq, ui
         s_ok = okm;
         s_status = 0;
     }
-    zero_chunk_words(q, cd, c);
     __syncthreads();
     const uint32_t okm = s_ok;
     if (!okm) return;

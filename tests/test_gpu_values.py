@@ -204,11 +204,15 @@ def test_output_mask_fully_written(codec, chunk):
     rng = np.random.default_rng(31)
     n = 32 * 937 - 5  # an odd number of u32 words: the last u64 word's upper half holds no row
     v = columns(rng, n)["walk"]
-    data = E.encode(v, codec, ("record_count", chunk))
+    check_mask_words(E.encode(v, codec, ("record_count", chunk)), (None, random_mask(n, 0.2, rng)))
+
+
+def check_mask_words(data, masks, lo=25.0, hi=35.0):
+    """filter / filter_agg into an all-ones output equal the oracle's bitmask in every word."""
     g, o = E.Decoder(data), O.Decoder(data)
-    p = E.Predicate.range(E.RangeValue.inclusive(25.0), E.RangeValue.inclusive(35.0))
-    op = O.rng(O.BOUND_INCLUSIVE, 25.0, O.BOUND_INCLUSIVE, 35.0)
-    for m in (None, random_mask(n, 0.2, rng)):
+    p = E.Predicate.range(E.RangeValue.inclusive(lo), E.RangeValue.inclusive(hi))
+    op = O.rng(O.BOUND_INCLUSIVE, lo, O.BOUND_INCLUSIVE, hi)
+    for m in masks:
         out = g.new_mask()
         out.fill_(-1)
         g.filter(p, m, out=out)
@@ -218,6 +222,19 @@ def test_output_mask_fully_written(codec, chunk):
         out.fill_(-1)
         g.filter_agg(p, m, out=out)
         assert np.array_equal(mask_np(out)[: len(want)], want)
+
+
+def test_rle_runs_past_chunk_rows():
+    # a chunk whose run lengths add up to more than its rows: the extra rows
+    # take the next chunk's row ids, in the bitmask too, as the reader's do
+    rng = np.random.default_rng(37)
+    n = 4096
+    v = np.repeat(np.round(rng.uniform(20, 40, n // 16), 1), 16)[:n] + 0.0
+    data = bytearray(E.encode(v, "rle", ("record_count", 512)))
+    d = O.Decoder(bytes(data))
+    phys, _, _, _ = d.chunk_info(2)
+    data[phys + 8] = 200  # the chunk's first run: 16 -> 200 rows
+    check_mask_words(bytes(data), (None, random_mask(n, 0.5, rng)))
 
 
 @pytest.mark.parametrize("codec", ["chimp", "chimp128", "elf_on_chimp", "elf"])
