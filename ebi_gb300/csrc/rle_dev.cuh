@@ -92,6 +92,13 @@ __device__ __forceinline__ void rle_chunk_warp(const QueryParams& q, uint32_t li
     ValAgg agg = val_agg_init(q.op == OP_FILTER_AGG || q.op == OP_AGG ? q.agg : 0u);
     unsigned long long out_pos = mode == VAL_MATERIALIZE ? chunk_offsets[li] : 0;
     uint64_t carry_row = 0;
+    // Without an input bitmask, a chunk that owns its words marks only where
+    // the predicate's outcome changes: a toggle bit at the first row of every
+    // run whose outcome differs from the last non-empty run before it (and at
+    // the end of the chunk's rows if the last one passes); a prefix XOR over
+    // the words then gives the bitmask.
+    const bool toggles = local && !has_mask;
+    uint32_t prev_pass = 0;  // outcome of the last non-empty run so far (warp-uniform)
     for (uint64_t b0 = 0; b0 < nf; b0 += kRleStep) {
         // the step's fields [b0, b0 + kRleStep) into shared memory (the file
         // allocation is 16-byte aligned and padded past its end)
@@ -131,14 +138,36 @@ __device__ __forceinline__ void rle_chunk_warp(const QueryParams& q, uint32_t li
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
         uint64_t r = carry_row + (incl - rows);  // chunk row of this lane's first field
         uint32_t sel_rows[kRlePer];
+        uint32_t e = prev_pass;  // toggles: the outcome before this lane's first field
+        if (toggles) {
+            // last non-empty run among this lane's fields, then among the lanes before it
+            uint32_t hv = 0;  // bit 1: a non-empty run, bit 0: its outcome
+#pragma unroll
+            for (int k = 0; k < kRlePer; ++k)
+                if (run[k]) hv = 2u | (!pred_on || kp.pass(static_cast<uint64_t>(__double_as_longlong(val[k]))) ? 1u : 0u);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, hv, o);
+                if (lane >= o && !(hv & 2u)) hv = y;
+            }
+            const uint32_t before = __shfl_up_sync(0xffffffffu, hv, 1);
+            if (lane > 0 && (before & 2u)) e = before & 1u;
+            const uint32_t last = __shfl_sync(0xffffffffu, hv, 31);
+            if (last & 2u) prev_pass = last & 1u;
+        }
 #pragma unroll
         for (int k = 0; k < kRlePer; ++k) {
             const uint64_t g0 = cd.row_off + r;  // global rows [g0, g0 + run)
             const bool pass = !pred_on || kp.pass(static_cast<uint64_t>(__double_as_longlong(val[k])));
             uint32_t n_sel = 0;
+            if (toggles && run[k]) {
+                if ((pass ? 1u : 0u) != e && r < 32u * kRleWords)
+                    atomicXor(&sbits[r >> 5], 1u << (r & 31));
+                e = pass ? 1u : 0u;
+            }
             if (run[k] && pass) {
                 if (!has_mask) n_sel = run[k];
-                if (has_mask || store) {
+                if (has_mask || (store && !toggles)) {
                     for (uint64_t g = g0; g < g0 + run[k];) {
                         const uint64_t w = g >> 5;
                         const uint64_t wend = (w + 1) << 5;
@@ -184,6 +213,39 @@ __device__ __forceinline__ void rle_chunk_warp(const QueryParams& q, uint32_t li
             out_pos += __shfl_sync(0xffffffffu, mi, 31);
         }
         carry_row += total;
+    }
+    if (toggles) {
+        // the last run's outcome ends at the chunk's last decoded row
+        if (lane == 0 && prev_pass && carry_row < 32u * kRleWords)
+            atomicXor(&sbits[carry_row >> 5], 1u << (carry_row & 31));
+        __syncwarp();
+        // prefix XOR: lane l takes words [8l, 8l + 8), the carry in is the
+        // parity of every toggle in the words before them
+        uint32_t x[kRleWords / 32], par = 0;
+#pragma unroll
+        for (int j = 0; j < int(kRleWords / 32); ++j) {
+            x[j] = sbits[(kRleWords / 32) * lane + j];
+            par ^= __popc(x[j]) & 1u;
+        }
+        uint32_t pi = par;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, pi, o);
+            if (lane >= o) pi ^= y;
+        }
+        uint32_t carry = pi ^ par;
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < int(kRleWords / 32); ++j) {
+            uint32_t y = x[j];
+            y ^= y << 1;
+            y ^= y << 2;
+            y ^= y << 4;
+            y ^= y << 8;
+            y ^= y << 16;
+            sbits[(kRleWords / 32) * lane + j] = carry ? ~y : y;
+            carry ^= __popc(x[j]) & 1u;
+        }
     }
     if (local) {
         __syncwarp();
