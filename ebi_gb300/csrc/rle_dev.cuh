@@ -14,7 +14,7 @@
 namespace ebi {
 namespace {
 
-constexpr int kRlePer = 4;
+constexpr int kRlePer = 6;
 constexpr uint32_t kRleStep = 32 * kRlePer;  // fields per warp step
 constexpr uint32_t kRleWords = 256;          // bitmap words per warp: chunks up to 8,192 rows
 
