@@ -171,11 +171,12 @@ def test_many_small_chunks(codec, kind):
 
 @pytest.mark.parametrize("codec", ["uncompressed", "rle", "gorilla", "chimp128"])
 @pytest.mark.parametrize("corrupt", [False, True])
-def test_fold_over_many_slices(codec, corrupt):
-    # 2,344 chunks of 64 values: more than 32 slices of 64 chunks, so the
-    # single-column fold runs over a grid of CTAs (and the batch over one CTA)
+@pytest.mark.parametrize("n", [150_000, 300_000])
+def test_fold_over_many_slices(codec, corrupt, n):
+    # 2,344 / 4,688 chunks of 64 values: 37 / 74 slices of 64 chunks, so the
+    # single-column fold runs over a grid of CTAs with a ticket (and the batch
+    # in one CTA)
     rng = np.random.default_rng(23)
-    n = 150_000
     v = columns(rng, n)["walk"]
     data = bytearray(E.encode(v, codec, ("record_count", 64)))
     d = O.Decoder(bytes(data))
