@@ -72,7 +72,7 @@ static uint32_t rd32(const uint8_t* p) {
 static uint64_t rd64(const uint8_t* p) { return uint64_t(rd32(p)) | (uint64_t(rd32(p + 4)) << 32); }
 
 // The device's default stream-ordered pool keeps freed memory for reuse, so
-// reopening columns of similar size does not go back to the driver.
+// reopening columns of similar size does not go back to the CUDA driver for memory.
 static void tune_pool_once() {
     static std::once_flag once;
     std::call_once(once, [] {
