@@ -122,7 +122,9 @@ __device__ __forceinline__ void val_agg_add(ValAgg& a, double v, uint32_t k) {
     val_agg_minmax(a, b);
     if (a.want & AGG_SUM) {
         const double kd = static_cast<double>(k);
-        const double p = v * kd;
+        // rounded on its own (never fused into the add that follows): every
+        // kernel that adds runs gets the same bits, whatever the compiler fuses
+        const double p = __dmul_rn(v, kd);
         neumaier_add(a.hi, a.lo, p);
         const uint64_t pb = static_cast<uint64_t>(__double_as_longlong(p));
         if ((pb & kAbsMask) < 0x7ff0000000000000ull) a.lo += fma(v, kd, -p);
