@@ -14,7 +14,7 @@ __device__ __forceinline__ double fold_pow2(int e) {  // 2^e for -1022 <= e <= 1
 // (double)x / 2^frac exactly as `x as f64 / 2.0f64.powi(frac)` rounds it.
 __device__ __forceinline__ double fold_scale(long long x, uint32_t frac) {
     const double v = static_cast<double>(x);
-    if (frac <= 1022) return v * fold_pow2(-static_cast<int>(frac));
+    if (frac <= 1022) return __dmul_rn(v, fold_pow2(-static_cast<int>(frac)));
     return v / (frac <= 1023 ? fold_pow2(1023) : __longlong_as_double(0x7ff0000000000000ll));
 }
 
@@ -50,7 +50,8 @@ __device__ inline BuffVal buff_value(const QueryParams& q, uint32_t c, const Chu
 }
 __device__ inline double buff_chunk_sum_f64(const BuffVal& v, uint32_t c, const QueryParams& q) {
     const BuffChunkInfo ci = q.binfo[c];
-    if (ci.bits == 0) return fold_scale(ci.base, ci.frac) * static_cast<double>(ci.n);
+    // rounded on its own: never fused into the reference's `result += chunk` that follows
+    if (ci.bits == 0) return __dmul_rn(fold_scale(ci.base, ci.frac), static_cast<double>(ci.n));
     return fold_scale(v.sum_fixed, v.frac);
 }
 
