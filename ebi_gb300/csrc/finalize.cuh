@@ -1,7 +1,9 @@
-// finalize.cuh -- the chunk-ordered fold of per-chunk results (Decoder's
-// `result += chunk`, `result = result.min(chunk)`, `result = result.max(chunk)`,
-// api/decoder.rs:323-439), shared by the single-query finalize (query.cu) and
-// the batched launch (batch.cu).
+// finalize.cuh -- the fold of per-chunk results into the query's result
+// (Decoder's `result += chunk`, `result = result.min(chunk)`,
+// `result = result.max(chunk)`, api/decoder.rs:323-439): BUFF in chunk order
+// on exact integers, the other codecs as an exact fixed-point sum (the same in
+// any order); shared by the single-query folds (query.cu) and the batched
+// launch (batch.cu).
 #pragma once
 
 #include <climits>
