@@ -6,8 +6,8 @@
 // fetch_footer do (decoder.rs:131-220, format/deserialize.rs:117-300), the
 // chunk table (GeneralChunkHandle geometry, decoder.rs:283-352) is built once,
 // and the unmodified file bytes are copied to HBM where they stay.  Every
-// query then runs the codec's kernel over the chunk table and one
-// finalize_kernel that folds the per-chunk results in chunk order.
+// query then runs the codec's kernel over the chunk table and a fold of the
+// per-chunk results (query.cu; the fused BUFF scans fold in their last CTA).
 #include <algorithm>
 #include <atomic>
 #include <climits>

@@ -1,7 +1,7 @@
 // query.cu -- kernels shared by every codec: chunk selection, tile scans and
-// the chunk-ordered fold of per-chunk results (Decoder's `result += chunk`,
-// `result = result.min(chunk)`, `result = result.max(chunk)`,
-// api/decoder.rs:323-439).
+// the folds of per-chunk results into the query's result (Decoder's
+// `result += chunk`, `result = result.min(chunk)`, `result = result.max(chunk)`,
+// api/decoder.rs:323-439; finalize.cuh).
 #include <climits>
 
 #include "internal.h"
