@@ -453,6 +453,7 @@ int run_scan(ebi_column* c, int op, const ebi_predicate* pred, const uint64_t* d
         // (whose bits would land in the next chunk's words), each chunk's CTA
         // zeroes its own words.
         q.own_words = c->rows_aligned32 && c->rows_in_order && c->rows_bounded;
+        q.segs = c->d_segs;
         q.zero_out = d_out_mask && tn > 0 && tn == c->n_chunks && q.own_words;
         if (d_out_mask && !q.zero_out) CK(cudaMemsetAsync(d_out_mask, 0, c->mask_words * 8, s));
         if (d_mask) CK(launch_select_chunks(q, s));
@@ -734,6 +735,13 @@ int ebi_column_open(const uint8_t* file, uint64_t len, void* stream, ebi_column*
     if (!st) st = col_alloc(c, &c->d_res, 1, s);
     if (!st && c->scheme != EBI_BUFF)
         st = col_alloc(c, &c->d_parts, value_slices(static_cast<uint32_t>(c->n_chunks)) + 1, s);
+    // the XOR chunk pass's segment starts, converged ahead of it by a separate
+    // kernel; not for columns of chunks so small that the scratch would exceed
+    // a quarter of the file (their chunks converge in a round or two anyway)
+    const bool xor_segs = c->scheme == EBI_CHIMP || c->scheme == EBI_CHIMP128 || c->scheme == EBI_ELF ||
+                          c->scheme == EBI_ELF_ON_CHIMP;
+    if (!st && xor_segs && c->n_chunks * kSegsPerChunk * sizeof(SegState) <= c->file_len / 4)
+        st = col_alloc(c, &c->d_segs, c->n_chunks * kSegsPerChunk, s);
     if (!st && !binfo.empty()) st = col_alloc(c, &c->d_buff, binfo.size(), s);
     // the scan totals and, behind them, one slot per CTA of a scan launch
     // two totals blocks (totals-only queries alternate between them)
@@ -809,7 +817,7 @@ int ebi_column_close(ebi_column* c) {
     cudaStream_t s = c->stream;
     for (cudaEvent_t e : c->ev) if (e) cudaEventDestroy(e);
     void* ptrs[] = {c->d_file, c->d_chunks, c->d_tiles, c->d_acc, c->d_res, c->d_tile_counts, c->d_tile_offsets,
-                    c->d_scratch_mask, c->d_buff, c->d_tot, c->d_units, c->d_parts};
+                    c->d_scratch_mask, c->d_buff, c->d_tot, c->d_units, c->d_parts, c->d_segs};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, s);
     if (c->h_res || c->h_tot) {
         cudaStreamSynchronize(s);  // no copy into the slots is pending when they are recycled

@@ -28,6 +28,7 @@ struct ebi_column {
     ChunkAcc* d_acc = nullptr;
     QueryResult* d_res = nullptr;
     ValPart* d_parts = nullptr;  // codecs other than BUFF: the fold's slice partials and counter
+    SegState* d_segs = nullptr;  // Chimp / Chimp128 / Elf / ElfOnChimp: converged segment starts (or null)
     QueryResult* h_res = nullptr;
     unsigned long long* d_tile_counts = nullptr;   // n_tiles
     unsigned long long* d_tile_offsets = nullptr;  // n_tiles + 1

@@ -176,7 +176,20 @@ struct QueryParams {
     long long copy_wait;       // limit (SM clocks) of a kernel's waits for its bulk copies to land; <= 0: one look
     int zero_out;              // Uncompressed / RLE: each chunk's CTA zeroes its own out_mask words first (no memset)
     int own_words;             // chunks start on 32-row boundaries in row order and decode no row past their range
+    // Chimp / Chimp128 / Elf / ElfOnChimp single-column scans: the segment
+    // starts of every launched chunk are converged by a separate kernel into
+    // this scratch (kSegsPerChunk per chunk, by launch index); null: in the
+    // chunk's own kernel
+    struct SegState* segs;
 };
+
+// One segment of an XOR chunk's control parse after convergence: its start
+// state (PState packed), and the records and first error of its parse from there.
+struct SegState {
+    unsigned long long in;
+    uint32_t n, fail;
+};
+constexpr uint32_t kSegsPerChunk = 256;
 
 // Passes of the value-codec kernels (one CTA per chunk).
 //   VAL_SCAN         filter / filter+agg / agg into the output bitmask and acc

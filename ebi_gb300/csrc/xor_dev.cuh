@@ -191,6 +191,47 @@ __device__ __noinline__ void elf_restore(Smem sm, uint32_t end, const double* __
     __syncthreads();
 }
 
+// The control parse of a chunk of B bits by a CTA of kXorThreads threads:
+// thread t's segment of the bits starts at a guess (thread 0 at the true first
+// record), and each round a thread whose start differs from its predecessor's
+// end adopts that end and parses again, until no start up to the first
+// failing segment changes.  Out: this thread's converged start, its records
+// and first error from there, and the first failing segment (kXorThreads:
+// none).  s_in / s_out: kXorThreads words each, s_red: the block reductions'.
+template <int CODEC, typename Peek>
+__device__ __forceinline__ void converge_segments(Peek peek, uint64_t B, uint64_t* s_in, uint64_t* s_out,
+                                                  uint32_t* s_red, PState& in, uint32_t& n, uint32_t& fail,
+                                                  uint32_t& first_fail) {
+    const int tid = threadIdx.x;
+    constexpr uint64_t kFirst = is_elf(CODEC) ? 0 : 64;  // bits before the first parsed record
+    const uint64_t span = B - kFirst;
+    const uint64_t seg = (span + kXorThreads - 1) / kXorThreads;
+    const uint64_t sbeg = kFirst + seg * tid;
+    const uint64_t send =
+        tid == kXorThreads - 1 ? B : (kFirst + seg * (tid + 1) < B ? kFirst + seg * (tid + 1) : B);
+    const bool last = tid == kXorThreads - 1;
+    const uint32_t win0 = CODEC == CODEC_GORILLA ? 0u : CODEC == CODEC_ELF ? kNoWin : kNoLead;
+    in = PState{tid == 0 ? kFirst : (sbeg < B ? sbeg : B), tid == 0 ? win0 : 0u};
+    PState out = parse_segment<CODEC>(peek, B, in, send, last, &n, &fail);
+    s_in[tid] = pack_state(in);
+    s_out[tid] = pack_state(out);
+    first_fail = kXorThreads;
+    for (int round = 0; round < kXorThreads; ++round) {
+        __syncthreads();
+        first_fail = block_min_u32(fail ? static_cast<uint32_t>(tid) : kXorThreads, s_red);
+        const bool stale = tid > 0 && s_in[tid] != s_out[tid - 1];
+        const uint64_t want = tid > 0 ? s_out[tid - 1] : 0;
+        if (!__syncthreads_or(stale && static_cast<uint32_t>(tid) <= first_fail)) break;
+        if (stale) {
+            in = unpack_state(want);
+            out = parse_segment<CODEC>(peek, B, in, send, last, &n, &fail);
+            s_in[tid] = want;
+            s_out[tid] = pack_state(out);
+        }
+    }
+}
+
+
 // One Chimp / Chimp128 chunk c by a CTA of kXorThreads threads with
 // xor_smem_bytes(CODEC) bytes of dynamic shared memory; li indexes the pass's
 // per-chunk counts / offsets.  qs[0, nq) (nq <= 32) are queries over the same
@@ -199,7 +240,8 @@ __device__ __noinline__ void elf_restore(Smem sm, uint32_t end, const double* __
 // share the decode).
 template <int CODEC>
 __device__ __forceinline__ void xor_chunk(const QueryParams* qs, uint32_t nq, uint32_t li, uint32_t c, int mode,
-                                          const unsigned long long* chunk_offsets) {
+                                          const unsigned long long* chunk_offsets, const SegState* segs = nullptr) {
+    static_assert(kSegsPerChunk == kXorThreads, "one converged segment per thread");
     const QueryParams& q = qs[0];  // the column (file, chunk table, tables) of every query
     extern __shared__ __align__(16) uint8_t smem_raw[];
     Smem sm;
@@ -260,56 +302,38 @@ __device__ __forceinline__ void xor_chunk(const QueryParams* qs, uint32_t nq, ui
     bool serial = !parallel;
     if (parallel) {
         auto peek = [fw, bit0](uint64_t p) { return peek64_file(fw, bit0 + p); };
-        // The convergence rounds re-read the chunk and each read depends on the
-        // previous one: stage the chunk's words (big-endian) in the values
-        // array, unused until the extraction, when it fits; else warm L2.
-        const uint64_t w0 = cd.byte_off >> 2;
-        const uint64_t nwords = ((cd.byte_off + cd.byte_len + 3) >> 2) - w0 + 3;
-        const bool staged = nwords <= uint64_t(kRcap) * 2;
-        uint32_t* stage = reinterpret_cast<uint32_t*>(sm.vals);
-        if (staged) {
-            for (uint64_t i = tid; i < nwords; i += kXorThreads) stage[i] = bswap32(__ldg(fw + w0 + i));
-            __syncthreads();
-        } else {
-            for (uint64_t a = (cd.byte_off & ~uint64_t(127)) + uint64_t(tid) * 128; a < cd.byte_off + cd.byte_len;
-                 a += uint64_t(kXorThreads) * 128)
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(q.file + a));
-        }
-        const uint64_t sbit0 = (cd.byte_off & 3) * 8;
-        auto peek_staged = [stage, sbit0](uint64_t p) { return peek64_be(stage, sbit0 + p); };
-
-        // ---- 1. control parse: segments converge to the sequential parse ---
-        const uint64_t span = B - kFirst;
-        const uint64_t seg = (span + kXorThreads - 1) / kXorThreads;
-        const uint64_t sbeg = kFirst + seg * tid;
-        const uint64_t send =
-            tid == kXorThreads - 1 ? B : (kFirst + seg * (tid + 1) < B ? kFirst + seg * (tid + 1) : B);
-        const bool last = tid == kXorThreads - 1;
-        const uint32_t win0 = CODEC == CODEC_GORILLA ? 0u : CODEC == CODEC_ELF ? kNoWin : kNoLead;
-        PState in{tid == 0 ? kFirst : (sbeg < B ? sbeg : B), tid == 0 ? win0 : 0u};
-        uint32_t n, fail;
-        auto parse = [&](PState from, uint32_t* n_out, uint32_t* fail_out) {
-            return staged ? parse_segment<CODEC>(peek_staged, B, from, send, last, n_out, fail_out)
-                          : parse_segment<CODEC>(peek, B, from, send, last, n_out, fail_out);
-        };
-        PState out = parse(in, &n, &fail);
-        s_in[tid] = pack_state(in);
-        s_out[tid] = pack_state(out);
-        uint32_t first_fail = kXorThreads;
-        for (int round = 0; round < kXorThreads; ++round) {
-            __syncthreads();
+        PState in;
+        uint32_t n, fail, first_fail;
+        if (segs) {
+            // converged by xor_converge_kernel (the same rounds, run ahead at high occupancy)
+            const SegState g = segs[uint64_t(li) * kSegsPerChunk + tid];
+            in = unpack_state(g.in);
+            n = g.n;
+            fail = g.fail;
             first_fail = block_min_u32(fail ? static_cast<uint32_t>(tid) : kXorThreads, s_red);
-            const bool stale = tid > 0 && s_in[tid] != s_out[tid - 1];
-            const uint64_t want = tid > 0 ? s_out[tid - 1] : 0;
-            if (!__syncthreads_or(stale && static_cast<uint32_t>(tid) <= first_fail)) break;
-            if (stale) {
-                in = unpack_state(want);
-                out = parse(in, &n, &fail);
-                s_in[tid] = want;
-                s_out[tid] = pack_state(out);
+        } else {
+            // The convergence rounds re-read the chunk and each read depends on the
+            // previous one: stage the chunk's words (big-endian) in the values
+            // array, unused until the extraction, when it fits; else warm L2.
+            const uint64_t w0 = cd.byte_off >> 2;
+            const uint64_t nwords = ((cd.byte_off + cd.byte_len + 3) >> 2) - w0 + 3;
+            const bool staged = nwords <= uint64_t(kRcap) * 2;
+            uint32_t* stage = reinterpret_cast<uint32_t*>(sm.vals);
+            if (staged) {
+                for (uint64_t i = tid; i < nwords; i += kXorThreads) stage[i] = bswap32(__ldg(fw + w0 + i));
+                __syncthreads();
+            } else {
+                for (uint64_t a = (cd.byte_off & ~uint64_t(127)) + uint64_t(tid) * 128; a < cd.byte_off + cd.byte_len;
+                     a += uint64_t(kXorThreads) * 128)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(q.file + a));
             }
+            const uint64_t sbit0 = (cd.byte_off & 3) * 8;
+            auto peek_staged = [stage, sbit0](uint64_t p) { return peek64_be(stage, sbit0 + p); };
+            // ---- 1. control parse: segments converge to the sequential parse ---
+            if (staged) converge_segments<CODEC>(peek_staged, B, s_in, s_out, s_red, in, n, fail, first_fail);
+            else converge_segments<CODEC>(peek, B, s_in, s_out, s_red, in, n, fail, first_fail);
+            __syncthreads();  // the staged words are overwritten by the extraction
         }
-        __syncthreads();  // the staged words are overwritten by the extraction
         // Segments past the first failure hold no records of the stream.
         if (static_cast<uint32_t>(tid) > first_fail) n = 0;
         uint32_t total;
