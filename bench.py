@@ -173,9 +173,12 @@ DEFAULT_ROWS = {"buff": N_ROWS, "gorilla": 1_048_576, "chimp128": 16_777_216, "r
                 "elf": 16_777_216, "elf_on_chimp": 16_777_216}
 KERNELS = {"buff": "buff_stream_kernel<2,6> (register-streaming decode + range filter + bitmask + sum)",
            "gorilla": "gorilla_kernel (three warps per chunk: parse, bitmask + min/max, sums)",
-           "chimp128": "xor_kernel<Chimp128> (segment-parallel decode + filter + bitmask + max)",
-           "elf": "xor_kernel<Elf> (segment-parallel decode + decimal restore + filter + bitmask + max)",
-           "elf_on_chimp": "xor_kernel<ElfOnChimp> (segment-parallel decode + decimal restore + filter + bitmask + max)",
+           "chimp128": "xor_converge_kernel + xor_kernel<Chimp128> (segment control parse, then extraction + ring "
+                       "resolution + filter + bitmask + max)",
+           "elf": "xor_converge_kernel + xor_kernel<Elf> (segment control parse, then extraction + decimal restore "
+                  "+ filter + bitmask + max)",
+           "elf_on_chimp": "xor_converge_kernel + xor_kernel<ElfOnChimp> (segment control parse, then extraction + "
+                           "decimal restore + filter + bitmask + max)",
            "rle": "rle_kernel (run expansion + filter + bitmask + max)"}
 
 
